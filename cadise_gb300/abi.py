@@ -1,0 +1,208 @@
+"""ctypes mirror of ``include/cadise_gpu.h`` and scene flattening.
+
+:func:`flatten` turns a :class:`cadise_gb300.scenes.SceneSpec` into the flat,
+caller-owned arrays of ``cgpu_scene_desc`` (primitives in the reference's
+creation order: one per rectangle, one per mesh triangle - the order
+``instantiator::makePrimitive`` appends intersectors in,
+``source/core/instantiator/primitiveInstantiator.cpp:92-129``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from typing import Dict, List
+
+import numpy as np
+
+from . import scenes as S
+
+CGPU_PRIM_TRIANGLE = 0
+CGPU_PRIM_RECTANGLE = 1
+
+CGPU_BSDF_LAMBERTIAN = 0
+CGPU_BSDF_CONDUCTOR_GGX = 1
+CGPU_BSDF_GLASS = 2
+CGPU_BSDF_ABSORBER = 3
+CGPU_BSDF_DIELECTRIC_GGX = 4
+
+CGPU_MODE_MEGAKERNEL = 0
+CGPU_MODE_WAVEFRONT = 1
+
+BSDF_OF_TYPE = {
+    S.LAMBERT: CGPU_BSDF_LAMBERTIAN,
+    S.CONDUCTOR: CGPU_BSDF_CONDUCTOR_GGX,
+    S.GLASS: CGPU_BSDF_GLASS,
+    S.ROUGH_DIELECTRIC: CGPU_BSDF_DIELECTRIC_GGX,
+    "absorb": CGPU_BSDF_ABSORBER,
+}
+
+STATUS_NAMES = {0: "CGPU_OK", 1: "CGPU_ERR_INVALID_ARGUMENT", 2: "CGPU_ERR_CUDA",
+                3: "CGPU_ERR_OUT_OF_MEMORY", 4: "CGPU_ERR_TIMEOUT", 5: "CGPU_ERR_UNSUPPORTED",
+                6: "CGPU_ERR_NOT_FOUND", 7: "CGPU_ERR_PARSE", 8: "CGPU_ERR_NO_DEVICE"}
+
+
+class cgpu_material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("albedo_texture", C.c_int32), ("albedo", C.c_float * 3),
+                ("f0", C.c_float * 3), ("roughness", C.c_float), ("ior_outer", C.c_float),
+                ("ior_inner", C.c_float), ("reserved", C.c_float)]
+
+
+class cgpu_texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("texels", C.POINTER(C.c_float))]
+
+
+class cgpu_area_light(C.Structure):
+    _fields_ = [("primitive", C.c_int32), ("color", C.c_float * 3), ("watt", C.c_float),
+                ("back_face_emit", C.c_int32)]
+
+
+class cgpu_scene_desc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32),
+                ("cam_position", C.c_float * 3), ("cam_direction", C.c_float * 3), ("cam_up", C.c_float * 3),
+                ("fov_degrees", C.c_float), ("sensor_width_mm", C.c_float),
+                ("max_depth", C.c_int32), ("spp", C.c_int32),
+                ("num_primitives", C.c_uint32), ("prim_kind", C.POINTER(C.c_int32)),
+                ("prim_vertices", C.POINTER(C.c_float)), ("prim_normals", C.POINTER(C.c_float)),
+                ("prim_uvws", C.POINTER(C.c_float)), ("prim_material", C.POINTER(C.c_int32)),
+                ("num_materials", C.c_uint32), ("materials", C.POINTER(cgpu_material)),
+                ("num_textures", C.c_uint32), ("textures", C.POINTER(cgpu_texture)),
+                ("num_lights", C.c_uint32), ("lights", C.POINTER(cgpu_area_light))]
+
+
+class cgpu_scene_info(C.Structure):
+    _fields_ = [("num_primitives", C.c_uint32), ("num_triangles", C.c_uint32),
+                ("num_bvh_nodes", C.c_uint32), ("num_lights", C.c_uint32),
+                ("device_bytes", C.c_uint64), ("build_ms", C.c_double),
+                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3)]
+
+
+class cgpu_options(C.Structure):
+    _fields_ = [("device", C.c_int32), ("stream", C.c_void_p), ("max_paths", C.c_uint32),
+                ("flags", C.c_int32)]
+
+
+class cgpu_ray(C.Structure):
+    _fields_ = [("org", C.c_float * 3), ("t_min", C.c_float), ("dir", C.c_float * 3), ("t_max", C.c_float)]
+
+
+class cgpu_hit(C.Structure):
+    _fields_ = [("t", C.c_float), ("primitive", C.c_int32), ("u", C.c_float), ("v", C.c_float)]
+
+
+class cgpu_render_params(C.Structure):
+    _fields_ = [("scenes", C.POINTER(C.c_int32)), ("num_scenes", C.c_uint32),
+                ("first_sample", C.c_uint32), ("num_samples", C.c_uint32), ("seed", C.c_uint64),
+                ("mode", C.c_int32), ("use_graph", C.c_int32)]
+
+
+class cgpu_render_stats(C.Structure):
+    _fields_ = [("paths", C.c_uint64), ("closest_rays", C.c_uint64), ("any_rays", C.c_uint64),
+                ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64),
+                ("kernel_launches", C.c_uint32), ("timeouts", C.c_uint32)]
+
+
+def _fptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _iptr(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+@dataclass
+class FlatScene:
+    """Owns the numpy arrays a ``cgpu_scene_desc`` points into."""
+    desc: cgpu_scene_desc
+    kind: np.ndarray
+    vertices: np.ndarray
+    material: np.ndarray
+    normals: object
+    uvws: object
+    materials: object
+    lights: object
+    textures: object
+    texture_arrays: list
+    prim_names: Dict[str, int]
+    material_names: Dict[str, int]
+
+    @property
+    def ptr(self):
+        return C.byref(self.desc)
+
+
+def flatten(spec: "S.SceneSpec") -> FlatScene:
+    mat_index = {m.name: i for i, m in enumerate(spec.materials)}
+    tex_index = {t.name: i for i, t in enumerate(spec.textures)}
+    n = spec.num_primitives()
+    kind = np.zeros(n, dtype=np.int32)
+    verts = np.zeros((n, 9), dtype=np.float32)
+    mat = np.zeros(n, dtype=np.int32)
+    has_normals = any(isinstance(p, S.TriangleMesh) and p.normals is not None for p in spec.primitives)
+    has_uvws = any(isinstance(p, S.TriangleMesh) and p.uvws is not None for p in spec.primitives)
+    normals = np.zeros((n, 9), dtype=np.float32) if has_normals else None
+    uvws = None
+    if has_uvws:
+        uvws = np.tile(np.array([0, 0, 0, 1, 0, 0, 0, 1, 0], dtype=np.float32), (n, 1))
+    names: Dict[str, int] = {}
+    i = 0
+    for p in spec.primitives:
+        if isinstance(p, S.Rectangle):
+            kind[i] = CGPU_PRIM_RECTANGLE
+            verts[i] = np.array([*p.v1, *p.v2, *p.v3], dtype=np.float32)
+            mat[i] = mat_index[p.material]
+            names.setdefault(p.name, i)
+            i += 1
+        else:
+            m = p.positions.shape[0]
+            kind[i:i + m] = CGPU_PRIM_TRIANGLE
+            verts[i:i + m] = p.positions.reshape(m, 9)
+            mat[i:i + m] = mat_index[p.material]
+            if normals is not None and p.normals is not None:
+                normals[i:i + m] = p.normals.reshape(m, 9)
+            if uvws is not None and p.uvws is not None:
+                uvws[i:i + m] = p.uvws.reshape(m, 9)
+            # the reference's name map keeps the first triangle of a mesh
+            names.setdefault(p.name, i)
+            i += m
+    mats = (cgpu_material * max(1, len(spec.materials)))()
+    for j, m in enumerate(spec.materials):
+        mats[j].type = BSDF_OF_TYPE[m.type]
+        mats[j].albedo_texture = tex_index[m.albedo_texture] if m.albedo_texture else -1
+        mats[j].albedo[:] = [float(x) for x in m.albedo]
+        mats[j].f0[:] = [float(x) for x in m.f0]
+        mats[j].roughness = float(m.roughness)
+        mats[j].ior_outer = float(m.ior_outer)
+        mats[j].ior_inner = float(m.ior_inner)
+    lights = (cgpu_area_light * max(1, len(spec.lights)))()
+    for j, lt in enumerate(spec.lights):
+        lights[j].primitive = names[lt.primitive]
+        lights[j].color[:] = [float(x) for x in lt.color]
+        lights[j].watt = float(lt.watt)
+        lights[j].back_face_emit = 1 if lt.back_face_emit else 0
+    tex_arrays = [np.ascontiguousarray(t.texels, dtype=np.float32) for t in spec.textures]
+    texs = (cgpu_texture * max(1, len(spec.textures)))()
+    for j, a in enumerate(tex_arrays):
+        texs[j].height, texs[j].width = int(a.shape[0]), int(a.shape[1])
+        texs[j].texels = _fptr(a)
+    d = cgpu_scene_desc()
+    d.width, d.height = spec.width, spec.height
+    d.cam_position[:] = [float(x) for x in spec.cam_position]
+    d.cam_direction[:] = [float(x) for x in spec.cam_direction]
+    d.cam_up[:] = [float(x) for x in spec.cam_up]
+    d.fov_degrees = float(spec.fov)
+    d.sensor_width_mm = float(spec.sensor_width_mm)
+    d.max_depth = spec.max_depth
+    d.spp = spec.spp
+    d.num_primitives = n
+    d.prim_kind = _iptr(kind)
+    d.prim_vertices = _fptr(verts)
+    d.prim_normals = _fptr(normals) if normals is not None else None
+    d.prim_uvws = _fptr(uvws) if uvws is not None else None
+    d.prim_material = _iptr(mat)
+    d.num_materials = len(spec.materials)
+    d.materials = mats
+    d.num_textures = len(spec.textures)
+    d.textures = texs
+    d.num_lights = len(spec.lights)
+    d.lights = lights
+    return FlatScene(d, kind, verts, mat, normals, uvws, mats, lights, texs, tex_arrays, names, mat_index)

@@ -1,0 +1,335 @@
+"""Seeded procedural scenes in the reference's scene vocabulary.
+
+A :class:`SceneSpec` holds exactly what a CRSD file holds (film, camera,
+renderer, accelerator, light cluster, materials, primitives, lights) and can be
+written out as CRSD text (``to_crsd``), the scene format parsed by the
+reference (``source/file-io/scene-description/sdParser.cpp:19-35``,
+``tokenizer.cpp:12-43``).  Large meshes are kept as numpy arrays so the same
+scene can also be handed to the C-ABI as flat arrays without a text round trip.
+
+Workloads
+---------
+* :func:`cornell_box` - the 5-wall Cornell box: 556-unit box with one quad per
+  wall, a 165^3 box rotated -18 deg and a 165x330x165 box rotated 15 deg
+  (12 triangles each), a 130x105 ceiling quad light with emission (17, 12, 4),
+  white/red/green Lambert albedos, 40 deg pinhole, 256^2, 16 spp, depth 6.
+* :func:`icosphere_field` - displaced icospheres over a 2-triangle ground plane
+  with Lambert / GGX conductor / dielectric materials and quad area lights.
+  With ``n_spheres=200, subdivision=4`` it is the 1,024,000-triangle field
+  rendered at 1920x1080, 64 spp, depth 12.
+
+Area-light mapping: an emission RGB ``E`` on a quad of area ``A`` is written as
+``color "E"`` and ``watt = sum(E) * A * pi``, because the reference sets
+``L = color / sum(color) * watt / (A * pi)``
+(``source/core/light/category/singleAreaLight.cpp:32-36``).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+
+# Material kinds understood by the CUDA library (and by the reference where a
+# CRSD type exists for them).
+LAMBERT = "matte-lambertian"
+CONDUCTOR = "conductor-microfacet"
+GLASS = "glass"
+# Rough (GGX) dielectric after Walter et al. 2007.  The reference has no rough
+# dielectric, so this type exists only in this library.
+ROUGH_DIELECTRIC = "dielectric-microfacet"
+
+
+@dataclass
+class Material:
+    name: str
+    type: str
+    albedo: tuple = (0.5, 0.5, 0.5)
+    roughness: float = 0.0
+    f0: tuple = (1.0, 1.0, 1.0)
+    ior_outer: float = 1.0
+    ior_inner: float = 1.5
+    albedo_texture: Optional[str] = None  # name of a texture-spectrum block
+
+
+@dataclass
+class Rectangle:
+    name: str
+    material: str
+    v1: tuple
+    v2: tuple
+    v3: tuple
+
+
+@dataclass
+class TriangleMesh:
+    name: str
+    material: str
+    positions: np.ndarray  # (n_tri, 3, 3) float32
+    normals: Optional[np.ndarray] = None  # (n_tri, 3, 3)
+    uvws: Optional[np.ndarray] = None  # (n_tri, 3, 3)
+
+
+@dataclass
+class AreaLight:
+    primitive: str
+    color: tuple
+    watt: float
+    back_face_emit: bool = False
+
+
+@dataclass
+class ImageTexture:
+    """RGB float texture, nearest lookup with repeat wrap."""
+    name: str
+    texels: np.ndarray  # (h, w, 3) float32
+
+
+@dataclass
+class SceneSpec:
+    width: int
+    height: int
+    spp: int
+    max_depth: int
+    cam_position: tuple
+    cam_direction: tuple
+    cam_up: tuple
+    fov: float
+    sensor_width_mm: float = 36.0
+    materials: List[Material] = field(default_factory=list)
+    # primitives in CRSD order: Rectangle or TriangleMesh objects
+    primitives: List[object] = field(default_factory=list)
+    lights: List[AreaLight] = field(default_factory=list)
+    textures: List[ImageTexture] = field(default_factory=list)
+
+    # ------------------------------------------------------------------ sizes
+    def num_primitives(self) -> int:
+        """Primitive count in the reference's sense (one per rectangle, one per
+        mesh triangle), i.e. the length of its intersector list."""
+        n = 0
+        for p in self.primitives:
+            n += 1 if isinstance(p, Rectangle) else int(p.positions.shape[0])
+        return n
+
+    def num_triangles(self) -> int:
+        """Triangles after splitting every rectangle in two."""
+        n = 0
+        for p in self.primitives:
+            n += 2 if isinstance(p, Rectangle) else int(p.positions.shape[0])
+        return n
+
+    # ------------------------------------------------------------------- CRSD
+    def to_crsd(self, with_header: bool = True) -> str:
+        out: List[str] = []
+        w = out.append
+
+        def v3(v):
+            return "%.9g %.9g %.9g" % (float(v[0]), float(v[1]), float(v[2]))
+
+        w("film {\n    [image-width int32 \"%d\"]\n    [image-height int32 \"%d\"]\n"
+          "    [filter string \"box\"]\n}\n" % (self.width, self.height))
+        w("camera {\n    [type string \"perspective-pinhole\"]\n"
+          "    [position vector3r \"%s\"]\n    [direction vector3r \"%s\"]\n"
+          "    [up vector3r \"%s\"]\n    [fov real \"%.9g\"]\n"
+          "    [sensor-width-mm real \"%.9g\"]\n}\n"
+          % (v3(self.cam_position), v3(self.cam_direction), v3(self.cam_up),
+             self.fov, self.sensor_width_mm))
+        w("renderer {\n    [type string \"sampling\"]\n    [sample-number int32 \"%d\"]\n"
+          "    [sampler string \"stratified\"]\n    [estimator string \"pt\"]\n"
+          "    [max-depth int32 \"%d\"]\n}\n" % (self.spp, self.max_depth))
+        w("accelerator {\n    [type string \"bvh\"]\n}\n")
+        w("light-cluster {\n    [type string \"uniform\"]\n}\n")
+        for m in self.materials:
+            w("material {\n    [type string \"%s\"]\n    [name string \"%s\"]\n" % (m.type, m.name))
+            if m.type == LAMBERT:
+                if m.albedo_texture:
+                    w("    [albedo texture \"%s\"]\n" % m.albedo_texture)
+                else:
+                    w("    [albedo rgb \"%s\"]\n" % v3(m.albedo))
+            elif m.type == CONDUCTOR:
+                w("    [microfacet-type string \"ggx\"]\n    [fresnel-type string \"schlick\"]\n"
+                  "    [f0 rgb \"%s\"]\n    [roughness real \"%.9g\"]\n" % (v3(m.f0), m.roughness))
+            elif m.type in (GLASS, ROUGH_DIELECTRIC):
+                w("    [albedo rgb \"%s\"]\n    [ior-outer real \"%.9g\"]\n    [ior-inner real \"%.9g\"]\n"
+                  % (v3(m.albedo), m.ior_outer, m.ior_inner))
+                if m.type == ROUGH_DIELECTRIC:
+                    w("    [roughness real \"%.9g\"]\n" % m.roughness)
+            w("}\n")
+        for p in self.primitives:
+            if isinstance(p, Rectangle):
+                w("primitive {\n    [type string \"rectangle\"]\n    [name string \"%s\"]\n"
+                  "    [bsdf material \"%s\"]\n    [v1 vector3r \"%s\"]\n    [v2 vector3r \"%s\"]\n"
+                  "    [v3 vector3r \"%s\"]\n}\n" % (p.name, p.material, v3(p.v1), v3(p.v2), v3(p.v3)))
+            else:
+                pos = p.positions.reshape(-1, 3)
+                w("primitive {\n    [type string \"triangle-mesh\"]\n    [name string \"%s\"]\n"
+                  "    [bsdf material \"%s\"]\n" % (p.name, p.material))
+                w("    [positions vector3r-array \"%s\"]\n" % ", ".join(v3(v) for v in pos))
+                if p.normals is not None:
+                    w("    [normals vector3r-array \"%s\"]\n"
+                      % ", ".join(v3(v) for v in p.normals.reshape(-1, 3)))
+                if p.uvws is not None:
+                    w("    [uvws vector3r-array \"%s\"]\n"
+                      % ", ".join(v3(v) for v in p.uvws.reshape(-1, 3)))
+                w("}\n")
+        for lt in self.lights:
+            w("light {\n    [type string \"area\"]\n    [primitive primitive \"%s\"]\n"
+              "    [color rgb \"%s\"]\n    [watt real \"%.9g\"]\n"
+              "    [is-back-face-emit bool \"%s\"]\n}\n"
+              % (lt.primitive, v3(lt.color), lt.watt, "true" if lt.back_face_emit else "false"))
+        return "".join(out)
+
+
+# --------------------------------------------------------------------------
+# geometry helpers
+# --------------------------------------------------------------------------
+
+def _box_triangles(size, center_xz, angle_deg, y0=0.0) -> np.ndarray:
+    """12 outward-wound triangles of an axis-aligned box rotated about +y."""
+    sx, sy, sz = size
+    hx, hz = sx * 0.5, sz * 0.5
+    corners = np.array([[x, y, z] for y in (y0, y0 + sy) for z in (-hz, hz) for x in (-hx, hx)],
+                       dtype=np.float64)
+    a = math.radians(angle_deg)
+    ca, sa = math.cos(a), math.sin(a)
+    rot = np.array([[ca, 0.0, sa], [0.0, 1.0, 0.0], [-sa, 0.0, ca]])
+    corners = corners @ rot.T
+    corners[:, 0] += center_xz[0]
+    corners[:, 2] += center_xz[1]
+    # corner index = x + 2*z + 4*y
+    quads = [(0, 1, 3, 2),  # bottom (y0)
+             (4, 6, 7, 5),  # top
+             (0, 4, 5, 1),  # z = -hz
+             (2, 3, 7, 6),  # z = +hz
+             (0, 2, 6, 4),  # x = -hx
+             (1, 5, 7, 3)]  # x = +hx
+    tris = []
+    for a0, a1, a2, a3 in quads:
+        tris.append([corners[a0], corners[a1], corners[a2]])
+        tris.append([corners[a0], corners[a2], corners[a3]])
+    return np.asarray(tris, dtype=np.float32)
+
+
+def _quad_light_watt(emission, area) -> float:
+    return float(sum(emission)) * float(area) * math.pi
+
+
+def cornell_box(width: int = 256, height: int = 256, spp: int = 16, max_depth: int = 6) -> SceneSpec:
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(278.0, 278.0, -800.0), cam_direction=(0.0, 0.0, 1.0),
+                  cam_up=(0.0, 1.0, 0.0), fov=40.0)
+    s.materials = [Material("white", LAMBERT, albedo=(0.725, 0.71, 0.68)),
+                   Material("red", LAMBERT, albedo=(0.63, 0.065, 0.05)),
+                   Material("green", LAMBERT, albedo=(0.14, 0.45, 0.091))]
+    L = 556.0
+    s.primitives = [
+        Rectangle("floor", "white", (L, 0, 0), (0, 0, 0), (0, 0, L)),
+        Rectangle("ceiling", "white", (0, L, 0), (L, L, 0), (L, L, L)),
+        Rectangle("back", "white", (0, 0, L), (L, 0, L), (L, L, L)),
+        Rectangle("left", "green", (0, 0, 0), (0, 0, L), (0, L, L)),
+        Rectangle("right", "red", (L, 0, L), (L, 0, 0), (L, L, 0)),
+        TriangleMesh("shortBox", "white", _box_triangles((165, 165, 165), (185.5, 169.0), -18.0)),
+        TriangleMesh("tallBox", "white", _box_triangles((165, 330, 165), (368.5, 351.0), 15.0)),
+        Rectangle("light", "white", (343.0, 555.0, 225.5), (213.0, 555.0, 225.5), (213.0, 555.0, 330.5)),
+    ]
+    emission = (17.0, 12.0, 4.0)
+    s.lights = [AreaLight("light", emission, _quad_light_watt(emission, 130.0 * 105.0))]
+    return s
+
+
+def icosphere(subdivision: int) -> np.ndarray:
+    """Unit icosphere triangles, (20 * 4**subdivision, 3, 3) float64."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    verts = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t),
+             (0, -1, -t), (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+             (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+             (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    v = np.asarray(verts, dtype=np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    tris = v[np.asarray(faces)]
+    for _ in range(subdivision):
+        a, b, c = tris[:, 0], tris[:, 1], tris[:, 2]
+        ab = a + b
+        bc = b + c
+        ca = c + a
+        ab /= np.linalg.norm(ab, axis=1, keepdims=True)
+        bc /= np.linalg.norm(bc, axis=1, keepdims=True)
+        ca /= np.linalg.norm(ca, axis=1, keepdims=True)
+        tris = np.stack([np.stack([a, ab, ca], 1), np.stack([ab, b, bc], 1),
+                         np.stack([ca, bc, c], 1), np.stack([ab, bc, ca], 1)], 1).reshape(-1, 3, 3)
+    return tris
+
+
+def _value_noise(p: np.ndarray, lattice: np.ndarray, freq: float) -> np.ndarray:
+    """Trilinear smoothstep value noise in [-1, 1] from a periodic lattice."""
+    n = lattice.shape[0]
+    q = p * freq
+    i0 = np.floor(q).astype(np.int64)
+    f = q - i0
+    f = f * f * (3.0 - 2.0 * f)
+    out = np.zeros(p.shape[0])
+    for dx in (0, 1):
+        for dy in (0, 1):
+            for dz in (0, 1):
+                w = ((f[:, 0] if dx else 1 - f[:, 0]) * (f[:, 1] if dy else 1 - f[:, 1])
+                     * (f[:, 2] if dz else 1 - f[:, 2]))
+                ix = (i0[:, 0] + dx) % n
+                iy = (i0[:, 1] + dy) % n
+                iz = (i0[:, 2] + dz) % n
+                out += w * lattice[ix, iy, iz]
+    return out
+
+
+def icosphere_field(n_spheres: int = 200, subdivision: int = 4, n_lights: int = 8, seed: int = 2,
+                    width: int = 1920, height: int = 1080, spp: int = 64, max_depth: int = 12,
+                    dielectric: str = ROUGH_DIELECTRIC, box: float = 100.0,
+                    radius_range=(3.0, 8.0), displacement: float = 0.10) -> SceneSpec:
+    """Displaced icospheres with centres uniform in a ``box``^3 cube over a
+    2-triangle ground plane; materials drawn uniformly from Lambert
+    (albedo U[0.05,0.9]^3), GGX conductor (roughness U[0.05,0.6], F0
+    U[0.5,1]^3) and dielectric (IOR U[1.3,1.7]); quad lights with emission
+    log-uniform in [1, 50]."""
+    rng = np.random.default_rng(seed)
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(0.5 * box, 0.75 * box, -0.95 * box),
+                  cam_direction=(0.0, -0.35, 1.0), cam_up=(0.0, 1.0, 0.0), fov=55.0)
+    s.materials.append(Material("ground", LAMBERT, albedo=(0.5, 0.5, 0.5)))
+    g = 2.0 * box
+    y0 = -1.0
+    ground = np.array([[[-g, y0, -g], [g, y0, g], [g, y0, -g]],
+                       [[-g, y0, -g], [-g, y0, g], [g, y0, g]]], dtype=np.float32)
+    s.primitives.append(TriangleMesh("ground", "ground", ground))
+    unit = icosphere(subdivision)
+    flat = unit.reshape(-1, 3)
+    for i in range(n_spheres):
+        kind = int(rng.integers(0, 3))
+        name = "m%d" % i
+        if kind == 0:
+            s.materials.append(Material(name, LAMBERT, albedo=tuple(rng.uniform(0.05, 0.9, 3))))
+        elif kind == 1:
+            s.materials.append(Material(name, CONDUCTOR, roughness=float(rng.uniform(0.05, 0.6)),
+                                        f0=tuple(rng.uniform(0.5, 1.0, 3))))
+        else:
+            s.materials.append(Material(name, dielectric, albedo=(1.0, 1.0, 1.0),
+                                        roughness=float(rng.uniform(0.05, 0.3)),
+                                        ior_inner=float(rng.uniform(1.3, 1.7))))
+        centre = rng.uniform(0.0, box, 3)
+        radius = float(rng.uniform(*radius_range))
+        lattice = rng.uniform(-1.0, 1.0, (8, 8, 8))
+        disp = 1.0 + displacement * _value_noise(flat + 1.0, lattice, 1.7)
+        pos = (flat * (radius * disp)[:, None] + centre).astype(np.float32).reshape(-1, 3, 3)
+        s.primitives.append(TriangleMesh("sphere%d" % i, name, pos))
+    s.materials.append(Material("lightBase", LAMBERT, albedo=(0.5, 0.5, 0.5)))
+    side = 0.15 * box
+    for j in range(n_lights):
+        cx, cz = rng.uniform(0.0, box, 2)
+        y = 1.3 * box
+        e = float(math.exp(rng.uniform(math.log(1.0), math.log(50.0))))
+        name = "quadLight%d" % j
+        # v1 - v2 = +x edge, v3 - v2 = +z edge: normal (+x) x (+z) = -y (down)
+        s.primitives.append(Rectangle(name, "lightBase", (cx + side / 2, y, cz - side / 2),
+                                      (cx - side / 2, y, cz - side / 2), (cx - side / 2, y, cz + side / 2)))
+        s.lights.append(AreaLight(name, (e, e, e), _quad_light_watt((e, e, e), side * side)))
+    return s

@@ -1,0 +1,243 @@
+/*
+ * cadise_gpu.h - C ABI of the GB300 (sm_103a) path tracer.
+ *
+ * Plain C types only: host pointers, sizes and status codes.  Every function
+ * returns a cgpu_status and never aborts; cgpu_last_error() gives the message
+ * of the last failure on a context.  One context owns one CUDA stream and is
+ * used from one host thread at a time.
+ *
+ * What each entry point replaces in the reference renderer (paths relative to
+ * the reference project):
+ *
+ *   cgpu_create / cgpu_destroy     RenderDatabase::prepareRender wiring
+ *                                  (source/core/renderDatabase.cpp:78-131)
+ *   cgpu_scene_upload              makePrimitive / makeBsdf / makeLight /
+ *                                  makeLightCluster + Scene ctor
+ *                                  (source/core/instantiator/primitiveInstantiator.cpp:92-129,
+ *                                   bsdfInstantiator.cpp:177-221, lightInstantiator.cpp:80-103,
+ *                                   source/core/scene.cpp:13-22)
+ *                                  and the BVH build of makeAccelerator
+ *                                  (source/core/instantiator/acceleratorInstantiator.cpp:57-80,
+ *                                   source/core/intersector/accelerator/bvh/bvhAccelerator.cpp:10-32)
+ *   cgpu_trace_closest             Accelerator::isIntersecting / Scene::isIntersecting
+ *                                  (source/core/intersector/accelerator/accelerator.h:7-13,
+ *                                   bvh/bvhAccelerator.cpp:40-97, source/core/scene.cpp:30-65)
+ *   cgpu_trace_any                 Accelerator::isOccluded / Scene::isOccluded
+ *                                  (bvh/bvhAccelerator.cpp:99-156, source/core/scene.cpp:67-77)
+ *   cgpu_camera_rays               Camera::spawnPrimaryRay
+ *                                  (source/core/camera/perspectivePinholeCamera.cpp:52-73)
+ *   cgpu_path_radiance             EnergyEstimator::estimate of PtEstimator
+ *                                  (source/core/estimator/energyEstimator.h:12-30,
+ *                                   source/core/estimator/ptEstimator.cpp:25-123)
+ *   cgpu_render                    Renderer::render of SamplingRenderer
+ *                                  (source/core/renderer/renderer.h:11-29,
+ *                                   source/core/renderer/sampling/samplingRenderer.cpp:33-68,
+ *                                   render-work/estimatorTileWork.cpp:32-61)
+ *   cgpu_film_read / _clear        Film::mergeWithFilmTile / Film::save accumulation
+ *                                  (source/core/film/film.cpp:79-99,159-196)
+ *   cgpu_adjoint_*                 no counterpart in the reference (it has no
+ *                                  differentiable rendering)
+ */
+#ifndef CADISE_GPU_H
+#define CADISE_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CGPU_ABI_VERSION 1
+
+typedef enum cgpu_status {
+    CGPU_OK = 0,
+    CGPU_ERR_INVALID_ARGUMENT = 1,
+    CGPU_ERR_CUDA = 2,
+    CGPU_ERR_OUT_OF_MEMORY = 3,
+    CGPU_ERR_TIMEOUT = 4, /* a device-side iteration budget ran out */
+    CGPU_ERR_UNSUPPORTED = 5,
+    CGPU_ERR_NOT_FOUND = 6,
+    CGPU_ERR_PARSE = 7,
+    CGPU_ERR_NO_DEVICE = 8
+} cgpu_status;
+
+typedef struct cgpu_ctx cgpu_ctx;
+
+/* ---------------------------------------------------------------- scene -- */
+
+/* Primitive kinds, one per reference intersector (primitiveInstantiator.cpp:92-129). */
+enum { CGPU_PRIM_TRIANGLE = 0, CGPU_PRIM_RECTANGLE = 1 };
+
+/* BSDF kinds keyed like the reference's CRSD material types (bsdfInstantiator.cpp:177-221). */
+enum {
+    CGPU_BSDF_LAMBERTIAN = 0,       /* "matte-lambertian"      lambertianDiffuse.cpp        */
+    CGPU_BSDF_CONDUCTOR_GGX = 1,    /* "conductor-microfacet"  conductorMicrofacet.cpp      */
+    CGPU_BSDF_GLASS = 2,            /* "glass"                 specularDielectric.cpp       */
+    CGPU_BSDF_ABSORBER = 3,         /* "absorb"                absorberBsdf.cpp             */
+    CGPU_BSDF_DIELECTRIC_GGX = 4    /* "dielectric-microfacet" (no reference counterpart)   */
+};
+
+typedef struct cgpu_material {
+    int32_t type;            /* CGPU_BSDF_* */
+    int32_t albedo_texture;  /* index into cgpu_scene_desc.textures, or -1 for constant albedo */
+    float albedo[3];
+    float f0[3];             /* Schlick F0 of the conductor */
+    float roughness;         /* CRSD "roughness"; alpha = max(max(r, 1e-3)^2, 1e-3) */
+    float ior_outer;
+    float ior_inner;
+    float reserved;
+} cgpu_material;
+
+/* RGB float texture, nearest texel with repeat wrap (rgbImageTexture.cpp:8-15). */
+typedef struct cgpu_texture {
+    int32_t width;
+    int32_t height;
+    const float* texels; /* width * height * 3, row-major, row 0 first */
+} cgpu_texture;
+
+/* One-sided area emitter on a primitive (singleAreaLight.cpp:20-37):
+ * L = color / sum(color) * watt / (area * pi). */
+typedef struct cgpu_area_light {
+    int32_t primitive;       /* index into the primitive arrays */
+    float color[3];
+    float watt;
+    int32_t back_face_emit;
+} cgpu_area_light;
+
+typedef struct cgpu_scene_desc {
+    /* film + camera (filmInstantiator.cpp:13-30, cameraInstantiator.cpp:27-45) */
+    int32_t width;
+    int32_t height;
+    float cam_position[3];
+    float cam_direction[3];
+    float cam_up[3];
+    float fov_degrees;       /* horizontal FOV over the sensor width */
+    float sensor_width_mm;   /* reference default 36 */
+    /* estimator (estimatorInstantiator.cpp:18-24) */
+    int32_t max_depth;
+    int32_t spp;             /* sample count of one full render (strata layout) */
+
+    /* primitives in the reference's creation order */
+    uint32_t num_primitives;
+    const int32_t* prim_kind;      /* CGPU_PRIM_*; NULL means every primitive is a triangle */
+    const float* prim_vertices;    /* 9 floats per primitive: triangle vA vB vC, rectangle v1 v2 v3 */
+    const float* prim_normals;     /* optional, 9 per primitive (triangle vertex normals) */
+    const float* prim_uvws;        /* optional, 9 per primitive (triangle vertex uvw) */
+    const int32_t* prim_material;  /* one material index per primitive */
+
+    uint32_t num_materials;
+    const cgpu_material* materials;
+    uint32_t num_textures;
+    const cgpu_texture* textures;
+    uint32_t num_lights;
+    const cgpu_area_light* lights;
+} cgpu_scene_desc;
+
+typedef struct cgpu_scene_info {
+    uint32_t num_primitives;
+    uint32_t num_triangles;   /* rectangles count twice */
+    uint32_t num_bvh_nodes;   /* 4-wide nodes of 128 B */
+    uint32_t num_lights;
+    uint64_t device_bytes;    /* scene + BVH bytes resident on the device */
+    double build_ms;          /* host BVH build time */
+    float bounds_min[3];
+    float bounds_max[3];
+} cgpu_scene_info;
+
+/* -------------------------------------------------------------- context -- */
+
+typedef struct cgpu_options {
+    int32_t device;             /* CUDA device ordinal */
+    void* stream;               /* cudaStream_t to launch on; NULL: the library creates one */
+    uint32_t max_paths;         /* paths in flight per wavefront batch; 0 = automatic */
+    int32_t flags;              /* reserved, 0 */
+} cgpu_options;
+
+cgpu_status cgpu_create(cgpu_ctx** out_ctx, const cgpu_options* options);
+void cgpu_destroy(cgpu_ctx* ctx);
+const char* cgpu_last_error(const cgpu_ctx* ctx);
+const char* cgpu_status_string(cgpu_status status);
+int32_t cgpu_abi_version(void);
+cgpu_status cgpu_synchronize(cgpu_ctx* ctx);
+
+cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* desc, int32_t* out_scene);
+cgpu_status cgpu_scene_release(cgpu_ctx* ctx, int32_t scene);
+cgpu_status cgpu_scene_info_get(cgpu_ctx* ctx, int32_t scene, cgpu_scene_info* out_info);
+
+/* ------------------------------------------------------------ ray queries -- */
+
+/* 32-byte ray: origin, t_min, direction (normalised), t_max. */
+typedef struct cgpu_ray {
+    float org[3];
+    float t_min;
+    float dir[3];
+    float t_max;
+} cgpu_ray;
+
+/* Closest hit: primitive = -1 on a miss; u, v barycentrics of vB and vC. */
+typedef struct cgpu_hit {
+    float t;
+    int32_t primitive;
+    float u;
+    float v;
+} cgpu_hit;
+
+/* Host buffers in and out; copies are made on the context stream. */
+cgpu_status cgpu_trace_closest(cgpu_ctx* ctx, int32_t scene, const cgpu_ray* rays, uint32_t n, cgpu_hit* hits);
+cgpu_status cgpu_trace_any(cgpu_ctx* ctx, int32_t scene, const cgpu_ray* rays, uint32_t n, uint8_t* occluded);
+/* Device buffers (already resident); asynchronous on the context stream. */
+cgpu_status cgpu_trace_closest_device(cgpu_ctx* ctx, int32_t scene, const cgpu_ray* d_rays, uint32_t n, cgpu_hit* d_hits);
+cgpu_status cgpu_trace_any_device(cgpu_ctx* ctx, int32_t scene, const cgpu_ray* d_rays, uint32_t n, uint8_t* d_occluded);
+
+/* Primary rays for film positions (x right, y down, in pixels): 6 floats (org, dir) each. */
+cgpu_status cgpu_camera_rays(cgpu_ctx* ctx, int32_t scene, const double* film_xy, uint32_t n, float* out_rays);
+
+/* --------------------------------------------------------------- render -- */
+
+enum { CGPU_MODE_MEGAKERNEL = 0, CGPU_MODE_WAVEFRONT = 1 };
+
+typedef struct cgpu_render_params {
+    const int32_t* scenes;     /* scene ids rendered together (one launch sequence) */
+    uint32_t num_scenes;
+    uint32_t first_sample;     /* samples [first_sample, first_sample + num_samples) */
+    uint32_t num_samples;      /* per pixel */
+    uint64_t seed;
+    int32_t mode;              /* CGPU_MODE_* */
+    int32_t use_graph;         /* wavefront: replay a captured CUDA graph per pass */
+} cgpu_render_params;
+
+/* Accumulates into each scene's FP64 film on the device (asynchronous). */
+cgpu_status cgpu_render(cgpu_ctx* ctx, const cgpu_render_params* params);
+cgpu_status cgpu_film_clear(cgpu_ctx* ctx, int32_t scene);
+/* Film read-back: each pointer may be NULL; sizes width*height*3 / *3 / *1 doubles. */
+cgpu_status cgpu_film_read(cgpu_ctx* ctx, int32_t scene, double* sum_rgb, double* sum_sq_rgb, double* count);
+
+/* Per-path estimate for given film positions and path keys (path stream starts
+ * at draw 0 with the estimator).  out_rgb: 3 floats per path. */
+cgpu_status cgpu_path_radiance(cgpu_ctx* ctx, int32_t scene, int32_t mode, const double* film_xy,
+                               const uint64_t* keys, uint32_t n, float* out_rgb);
+/* Per-path radiance of a render pass layout: pixel-major within each sample,
+ * out_rgb: num_samples * width * height * 3 floats (does not touch the film). */
+cgpu_status cgpu_render_paths(cgpu_ctx* ctx, int32_t scene, int32_t mode, uint32_t first_sample,
+                              uint32_t num_samples, uint64_t seed, float* out_rgb);
+
+/* Device-side counters of the last render (for throughput and roofline). */
+typedef struct cgpu_render_stats {
+    uint64_t paths;
+    uint64_t closest_rays;
+    uint64_t any_rays;
+    uint64_t node_visits;      /* 4-wide nodes fetched (counting builds only, else 0) */
+    uint64_t triangle_tests;
+    uint32_t kernel_launches;  /* kernels this library launched in the last cgpu_render */
+    uint32_t timeouts;
+} cgpu_render_stats;
+cgpu_status cgpu_render_stats_get(cgpu_ctx* ctx, cgpu_render_stats* out_stats);
+/* Count rays, node fetches and triangle tests in every following render (slower). */
+cgpu_status cgpu_set_counting(cgpu_ctx* ctx, int32_t enabled);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CADISE_GPU_H */

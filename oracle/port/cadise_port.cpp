@@ -1,0 +1,985 @@
+// CPU restatement of the reference's unidirectional path tracer.
+//
+// TEST INFRASTRUCTURE ONLY.  This is the oracle: only tests/, the smoke check
+// and bench.py's CPU-baseline leg load it, and only as the checker / the timed
+// CPU baseline.  The product library never links it.
+//
+// It restates, function by function and in the reference's floating-point
+// evaluation order, the path the reference takes for one path sample, so
+// that with the same per-path random stream (oracle_rng.h) it reproduces the
+// reference harness's radiance bit-for-bit on x86 (pinned by
+// tests/test_oracle_pin.py against tests/golden/).  Citations are to the
+// reference project's files.
+//
+// Scene input is the C-ABI scene description (include/cadise_gpu.h), so the
+// CUDA library and this oracle consume the very same arrays.
+
+#include "../../include/cadise_gpu.h"
+#include "../oracle_rng.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <thread>
+#include <vector>
+
+namespace port {
+
+// ---------------------------------------------------------------- math ----
+// source/math/tVector.ipp: dot/lengthSquared accumulate left to right,
+// normalize multiplies by 1/length, scalar division multiplies by 1/s.
+struct V3 {
+    float x = 0, y = 0, z = 0;
+    V3() = default;
+    V3(float a, float b, float c) : x(a), y(b), z(c) {}
+    explicit V3(float s) : x(s), y(s), z(s) {}
+    float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+    float& operator[](int i) { return i == 0 ? x : (i == 1 ? y : z); }
+    V3 operator-() const { return V3(-x, -y, -z); }
+    V3 operator+(const V3& o) const { return V3(x + o.x, y + o.y, z + o.z); }
+    V3 operator-(const V3& o) const { return V3(x - o.x, y - o.y, z - o.z); }
+    V3 operator*(const V3& o) const { return V3(x * o.x, y * o.y, z * o.z); }
+    V3 operator*(float s) const { return V3(x * s, y * s, z * s); }
+    V3 operator/(float s) const { const float inv = 1.0f / s; return V3(x * inv, y * inv, z * inv); }
+    V3 operator+(float s) const { return V3(x + s, y + s, z + s); }
+    V3 operator-(float s) const { return V3(x - s, y - s, z - s); }
+    V3& operator+=(const V3& o) { x += o.x; y += o.y; z += o.z; return *this; }
+    V3& operator*=(const V3& o) { x *= o.x; y *= o.y; z *= o.z; return *this; }
+    V3& operator*=(float s) { x *= s; y *= s; z *= s; return *this; }
+    float dot(const V3& o) const { float r = 0; r += x * o.x; r += y * o.y; r += z * o.z; return r; }
+    float absDot(const V3& o) const { return std::abs(dot(o)); }
+    float lengthSquared() const { float r = 0; r += x * x; r += y * y; r += z * z; return r; }
+    float length() const { return std::sqrt(lengthSquared()); }
+    V3 normalize() const { const float inv = 1.0f / length(); return *this * inv; }
+    V3 cross(const V3& v) const { return V3(y * v.z - z * v.y, z * v.x - x * v.z, x * v.y - y * v.x); }
+    bool isZero() const { return x == 0.0f && y == 0.0f && z == 0.0f; }
+    float sum() const { float r = 0; r += x; r += y; r += z; return r; }
+    float average() const { return sum() / 3.0f; }
+    float maxComponent() const { float m = x; if (y > m) m = y; if (z > m) m = z; return m; }
+    V3 complement() const { return V3(1.0f) - *this; }
+    V3 reciprocal() const { return V3(1.0f / x, 1.0f / y, 1.0f / z); }
+    // tVector.ipp:462-465
+    V3 reflect(const V3& n) const { const V3 r = n * (2.0f * absDot(n)); return r - *this; }
+    bool finite() const { return std::isfinite(x) && std::isfinite(y) && std::isfinite(z); }
+};
+inline V3 operator*(float s, const V3& v) { return v * s; }
+
+constexpr float kPi = 3.1415926535897932f;
+constexpr float kTwoPi = 6.2831853071795864f;
+constexpr float kInvPi = 0.3183098861837906f;
+constexpr float kRayEps = 0.001f;  // constant::ray_epsilon (math/constant.h:9-11)
+
+// math.cpp:36-58
+void buildCoordinateSystem(const V3& y, V3* z, V3* x) {
+    if (std::abs(y.x) > std::abs(y.y)) {
+        V3 zz(-y.z, 0.0f, y.x);
+        const float inv = 1.0f / std::sqrt(y.x * y.x + y.z * y.z);
+        zz *= inv;
+        *z = zz;
+    } else {
+        V3 zz(0.0f, y.z, -y.y);
+        const float inv = 1.0f / std::sqrt(y.y * y.y + y.z * y.z);
+        zz *= inv;
+        *z = zz;
+    }
+    *x = y.cross(*z);
+}
+
+struct Rng {
+    oracle_rng::Stream s;
+    float next() { return s.next(); }
+    // The reference builds 2-D samples as Vector2R(Random::nextReal(),
+    // Random::nextReal()) (lambertianDiffuse.cpp:62, conductorMicrofacet.cpp:88,
+    // triangle.cpp:165).  C++ leaves the order of argument evaluation
+    // unspecified; GCC evaluates right to left, so the first draw becomes .y
+    // and the second .x.  Kept so paths replay exactly.
+    void next2(float* x, float* y) { *y = next(); *x = next(); }
+    // random.cpp:21-26
+    std::size_t index(std::size_t lo, std::size_t hi) {
+        const std::size_t interval = hi - lo;
+        const std::size_t idx = static_cast<std::size_t>(lo + next() * interval);
+        return std::min(std::max(idx, lo), hi - 1);
+    }
+};
+
+// ---------------------------------------------------------------- scene ---
+struct Ray {
+    V3 o, d;
+    float minT = kRayEps, maxT = std::numeric_limits<float>::max();
+};
+
+struct Triangle {  // triangle.cpp:14-42
+    V3 a, b, c, eAB, eAC, nA, nB, nC, uA, uB, uC;
+};
+struct Rectangle {  // rectangle.cpp:14-35
+    V3 vA, vB, vC, vD, eA, eB;
+};
+struct Material {
+    int type;
+    V3 albedo, f0;
+    float roughness, iorOuter, iorInner;
+};
+struct Light {
+    int prim;
+    V3 radiance;
+    bool backFace;
+};
+struct Prim {
+    int kind, material, light, slot;  // slot: index into tris or rects
+};
+
+struct Scene {
+    std::vector<Prim> prims;
+    std::vector<Triangle> tris;
+    std::vector<Rectangle> rects;
+    std::vector<Material> mats;
+    std::vector<Light> lights;
+    // reference BVH (bvhBuilder.cpp / bvhLinearNode.h): binary, 1-primitive leaves
+    struct Node { V3 lo, hi; int second; int prim; int count; int axis; };
+    std::vector<Node> nodes;
+    std::vector<int> order;
+    // camera (perspectivePinholeCamera.cpp:32-50)
+    int W = 0, H = 0, maxDepth = 0, spp = 1;
+    V3 camPos, camX, camY, camZ;
+    float sx = 0, sy = 0, tx = 0, ty = 0, offset = 0;
+};
+
+// ------------------------------------------------------------ primitives --
+V3 triNormal(const Triangle& t) {
+    V3 n = t.eAB.cross(t.eAC);
+    return n.isZero() ? V3(0.0f, 1.0f, 0.0f) : n.normalize();
+}
+V3 rectNormal(const Rectangle& r) {
+    V3 n = r.eA.cross(r.eB);
+    return n.isZero() ? V3(0.0f, 1.0f, 0.0f) : n.normalize();
+}
+float triArea(const Triangle& t) { return 0.5f * t.eAB.cross(t.eAC).length(); }  // triangle.cpp:199-201
+float rectArea(const Rectangle& r) { return r.eA.length() * r.eB.length(); }      // rectangle.cpp:175-177
+
+// triangle.cpp:54-89 (and :91-123 for the occlusion variant)
+bool triHit(const Triangle& tr, const Ray& ray, float* tOut) {
+    V3 eAB = tr.eAB, eAC = tr.eAC;
+    const V3& D = ray.d;
+    if (D.dot(eAB.cross(eAC)) > 0.0f) std::swap(eAB, eAC);
+    const V3 T = ray.o - tr.a;
+    const V3 Q = T.cross(eAB);
+    const V3 P = D.cross(eAC);
+    const float den = P.dot(eAB);
+    if (den == 0.0f) return false;
+    const float inv = 1.0f / den;
+    const float t = Q.dot(eAC) * inv;
+    const float u = P.dot(T) * inv;
+    const float v = Q.dot(D) * inv;
+    if (u < 0.0f || v < 0.0f || u + v > 1.0f) return false;
+    if (t < ray.minT || t > ray.maxT) return false;
+    *tOut = t;
+    return true;
+}
+
+// rectangle.cpp:49-75
+bool rectHit(const Rectangle& r, const Ray& ray, float* tOut) {
+    V3 eA = r.eA, eB = r.eB;
+    if (ray.d.dot(eA.cross(eB)) > 0.0f) std::swap(eA, eB);
+    const V3 n = eA.cross(eB).normalize();
+    const float t = n.dot(r.vB - ray.o) / n.dot(ray.d);
+    if (t < ray.minT || t > ray.maxT) return false;
+    const V3 onPlane = (ray.o + ray.d * t) - r.vB;
+    const float p1 = onPlane.dot(r.eA.normalize());
+    const float p2 = onPlane.dot(r.eB.normalize());
+    if (p1 < 0.0f || p1 > r.eA.length() || p2 < 0.0f || p2 > r.eB.length()) return false;
+    *tOut = t;
+    return true;
+}
+
+bool primHit(const Scene& s, int p, const Ray& ray, float* t) {
+    const Prim& pr = s.prims[p];
+    return pr.kind == CGPU_PRIM_TRIANGLE ? triHit(s.tris[pr.slot], ray, t) : rectHit(s.rects[pr.slot], ray, t);
+}
+
+void primBound(const Scene& s, int p, V3* lo, V3* hi) {
+    const Prim& pr = s.prims[p];
+    V3 vs[4];
+    int n = 3;
+    if (pr.kind == CGPU_PRIM_TRIANGLE) {
+        const Triangle& t = s.tris[pr.slot];
+        vs[0] = t.a; vs[1] = t.b; vs[2] = t.c;
+    } else {
+        const Rectangle& r = s.rects[pr.slot];
+        vs[0] = r.vA; vs[1] = r.vB; vs[2] = r.vC; vs[3] = r.vD; n = 4;
+    }
+    *lo = vs[0]; *hi = vs[0];
+    for (int i = 1; i < n; ++i)
+        for (int k = 0; k < 3; ++k) {
+            (*lo)[k] = std::min((*lo)[k], vs[i][k]);
+            (*hi)[k] = std::max((*hi)[k], vs[i][k]);
+        }
+    *lo = *lo - 0.0001f;  // expand(0.0001) triangle.cpp:45-52, rectangle.cpp:37-44
+    *hi = *hi + 0.0001f;
+}
+
+// ------------------------------------------------------------------ BVH ---
+// bvhBuilder.cpp:59-169 + :251-358: SAH over 12 buckets along the largest
+// centroid extent (traversal 0.125, intersection 1), equal split for <= 2
+// primitives, leaf of 1 primitive, depth-first layout with the first child
+// adjacent.
+struct BuildItem { V3 lo, hi, c; int idx; };
+
+void boxUnion(V3& lo, V3& hi, const V3& l2, const V3& h2) {
+    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], l2[k]); hi[k] = std::max(hi[k], h2[k]); }
+}
+float halfArea(const V3& lo, const V3& hi) {
+    const V3 e = hi - lo;
+    return e.x * e.y + e.y * e.z + e.z * e.x;
+}
+
+int buildRec(Scene& s, std::vector<BuildItem>& items, int begin, int end) {
+    const int nodeIndex = static_cast<int>(s.nodes.size());
+    s.nodes.push_back({});
+    // An empty TAABB starts at (FLT_MAX, FLT_MIN) with FLT_MIN the smallest
+    // positive float (tAabb.ipp:13-17), so every bound the reference unions
+    // up reaches at least 0 on its upper side; kept for the same tree.
+    V3 lo(std::numeric_limits<float>::max()), hi(std::numeric_limits<float>::min());
+    V3 clo = lo, chi = hi;
+    for (int i = begin; i < end; ++i) {
+        boxUnion(lo, hi, items[i].lo, items[i].hi);
+        boxUnion(clo, chi, items[i].c, items[i].c);
+    }
+    auto makeLeaf = [&]() {
+        Scene::Node& n = s.nodes[nodeIndex];
+        n.lo = lo; n.hi = hi; n.second = -1; n.prim = static_cast<int>(s.order.size()); n.count = end - begin; n.axis = 0;
+        for (int i = begin; i < end; ++i) s.order.push_back(items[i].idx);
+        return nodeIndex;
+    };
+    const int count = end - begin;
+    if (count <= 1) return makeLeaf();
+    const V3 ext = chi - clo;
+    int axis = 0;
+    if (ext.y > ext[axis]) axis = 1;
+    if (ext.z > ext[axis]) axis = 2;
+    if (clo[axis] == chi[axis]) return makeLeaf();
+    int mid;
+    if (count <= 2) {  // bvhBuilder.cpp:212-249
+        mid = begin + (count + 1) / 2;
+        std::nth_element(items.begin() + begin, items.begin() + mid, items.begin() + end,
+                         [axis](const BuildItem& a, const BuildItem& b) { return a.c[axis] < b.c[axis]; });
+    } else {
+        constexpr int NB = 12;
+        const float invExt = 1.0f / ext[axis];
+        int bc[NB] = {0};
+        V3 blo[NB], bhi[NB];
+        for (int b = 0; b < NB; ++b) { blo[b] = V3(std::numeric_limits<float>::max()); bhi[b] = V3(std::numeric_limits<float>::min()); }
+        auto bucketOf = [&](const BuildItem& it) {
+            int b = static_cast<int>((it.c[axis] - clo[axis]) * invExt * NB);
+            return b >= NB ? NB - 1 : b;
+        };
+        for (int i = begin; i < end; ++i) {
+            const int b = bucketOf(items[i]);
+            bc[b]++;
+            boxUnion(blo[b], bhi[b], items[i].lo, items[i].hi);
+        }
+        const float invArea = 1.0f / halfArea(lo, hi);
+        float best = std::numeric_limits<float>::max();
+        int bestSplit = -1;
+        for (int split = 0; split < NB - 1; ++split) {
+            V3 alo(std::numeric_limits<float>::max()), ahi(std::numeric_limits<float>::min()), b2lo = alo, b2hi = ahi;
+            int ca = 0, cb = 0;
+            for (int i = 0; i <= split; ++i) if (bc[i]) { boxUnion(alo, ahi, blo[i], bhi[i]); ca += bc[i]; }
+            for (int i = split + 1; i < NB; ++i) if (bc[i]) { boxUnion(b2lo, b2hi, blo[i], bhi[i]); cb += bc[i]; }
+            const float pa = ca ? halfArea(alo, ahi) * invArea : 0.0f;
+            const float pb = cb ? halfArea(b2lo, b2hi) * invArea : 0.0f;
+            const float cost = 0.125f + (pa * ca + pb * cb);
+            if (cost < best) { best = cost; bestSplit = split; }
+        }
+        if (best >= static_cast<float>(count)) return makeLeaf();
+        auto midIt = std::partition(items.begin() + begin, items.begin() + end,
+                                    [&](const BuildItem& it) { return bucketOf(it) <= bestSplit; });
+        mid = static_cast<int>(midIt - items.begin());
+        if (mid == begin || mid == end) return makeLeaf();
+    }
+    buildRec(s, items, begin, mid);
+    const int second = buildRec(s, items, mid, end);
+    Scene::Node& n = s.nodes[nodeIndex];
+    n.lo = lo; n.hi = hi; n.second = second; n.prim = -1; n.count = 0; n.axis = axis;
+    return nodeIndex;
+}
+
+// tAabb.ipp:68-127
+bool slab(const Scene::Node& n, const V3& o, const V3& inv, float minT, float maxT) {
+    const V3 nearT = (n.lo - o) * inv;
+    const V3 farT = (n.hi - o) * inv;
+    for (int k = 0; k < 3; ++k) {
+        if (inv[k] > 0.0f) { minT = std::max(minT, nearT[k]); maxT = std::min(maxT, farT[k]); }
+        else { minT = std::max(minT, farT[k]); maxT = std::min(maxT, nearT[k]); }
+    }
+    return !(minT > maxT);
+}
+
+// bvhAccelerator.cpp:40-97 (closest) and :99-156 (any)
+int traverse(const Scene& s, Ray& ray, bool anyHit) {
+    const V3 inv = ray.d.reciprocal();
+    const int neg[3] = {inv.x < 0.0f, inv.y < 0.0f, inv.z < 0.0f};
+    int stack[64];
+    int sp = 0, cur = 0, hit = -1;
+    for (;;) {
+        const Scene::Node& n = s.nodes[cur];
+        if (slab(n, ray.o, inv, ray.minT, ray.maxT)) {
+            if (n.second < 0) {
+                for (int i = 0; i < n.count; ++i) {
+                    const int p = s.order[n.prim + i];
+                    float t;
+                    if (primHit(s, p, ray, &t)) {
+                        if (anyHit) return p;
+                        ray.maxT = t;
+                        hit = p;
+                    }
+                }
+                if (sp == 0) break;
+                cur = stack[--sp];
+            } else if (neg[n.axis]) {
+                stack[sp++] = cur + 1;
+                cur = n.second;
+            } else {
+                stack[sp++] = n.second;
+                cur = cur + 1;
+            }
+        } else {
+            if (sp == 0) break;
+            cur = stack[--sp];
+        }
+    }
+    return hit;
+}
+
+// ----------------------------------------------------- surface details ---
+struct Surface {
+    int prim = -1;
+    V3 P, Ng, Ns, uvw, wi;
+};
+
+// triangle.cpp:233-262
+V3 barycentric(const Triangle& t, const V3& p) {
+    const V3 v0 = t.b - t.a, v1 = t.c - t.a, v2 = p - t.a;
+    const float d00 = v0.dot(v0), d01 = v0.dot(v1), d11 = v1.dot(v1), d20 = v2.dot(v0), d21 = v2.dot(v1);
+    const float den = d00 * d11 - d01 * d01;
+    if (den == 0.0f) return V3(0.0f);
+    const float inv = 1.0f / den;
+    const float u = (d11 * d20 - d01 * d21) * inv;
+    const float v = (d00 * d21 - d01 * d20) * inv;
+    return V3(1.0f - u - v, u, v);
+}
+
+// scene.cpp:30-65 + triangle.cpp:125-160 + rectangle.cpp:102-132
+bool intersect(const Scene& s, Ray& ray, Surface* si) {
+    const int p = traverse(s, ray, false);
+    if (p < 0) return false;
+    si->prim = p;
+    si->wi = -ray.d;
+    si->P = ray.o + ray.d * ray.maxT;
+    const Prim& pr = s.prims[p];
+    if (pr.kind == CGPU_PRIM_TRIANGLE) {
+        const Triangle& t = s.tris[pr.slot];
+        const V3 Ng = triNormal(t);
+        const V3 b = barycentric(t, si->P);
+        si->uvw = b.x * t.uA + b.y * t.uB + b.z * t.uC;
+        V3 Ns = b.x * t.nA + b.y * t.nB + b.z * t.nC;
+        Ns = Ns.isZero() ? Ng : Ns.normalize();
+        si->Ng = Ng;
+        si->Ns = Ns;
+    } else {
+        const Rectangle& r = s.rects[pr.slot];
+        const V3 N = rectNormal(r);
+        si->Ng = N;
+        si->Ns = N;
+        const V3 onPlane = si->P - r.vB;
+        // rectangle.cpp:122-129 (both projections divide by |eA|, as there)
+        const float p1 = onPlane.dot(r.eA.normalize()) / r.eA.length();
+        const float p2 = onPlane.dot(r.eB.normalize()) / r.eA.length();
+        auto lerp = [](const V3& a, const V3& b, float t) {
+            const float c = 1.0f - t;
+            return V3(c * a.x + t * b.x, c * a.y + t * b.y, c * a.z + t * b.z);
+        };
+        const V3 uA(1, 0, 0), uB(0, 0, 0), uC(0, 1, 0), uD(1, 1, 0);
+        si->uvw = lerp(lerp(uB, uC, p2), lerp(uA, uD, p2), p1);
+    }
+    return true;
+}
+
+bool occluded(const Scene& s, Ray ray) { return traverse(s, ray, true) >= 0; }
+
+// ----------------------------------------------------------------- BSDF ---
+struct BsdfSample { V3 f, L; float pdf = 0.0f; bool valid() const { return !f.isZero() && pdf > 0.0f; } };
+
+bool isSpecular(int type) { return type == CGPU_BSDF_GLASS; }
+
+// tRoughnessMapper.h:18-40 (SQUARE)
+float roughnessToAlpha(float r) {
+    const float safe = std::max(r, 0.001f);
+    return std::max(safe * safe, 0.001f);
+}
+// isotropicGgx.cpp:11-34
+float ggxD(float alpha, const V3& N, const V3& H) {
+    const float NdotH = N.dot(H);
+    if (NdotH <= 0.0f) return 0.0f;
+    const float a2 = alpha * alpha, c2 = NdotH * NdotH, c4 = c2 * c2;
+    const float tan2 = (1.0f - c2) / c2;
+    return a2 / (kPi * c4 * (a2 + tan2) * (a2 + tan2));
+}
+// microfacet.cpp:11-23 + isotropicGgx.cpp:36-69
+float ggxG(float alpha, const V3& V, const V3& L, const V3& N, const V3& H) {
+    const float VdotH = V.dot(H), VdotN = V.dot(N), LdotH = L.dot(H), LdotN = L.dot(N);
+    if (!((VdotH * VdotN > 0.0f) && (LdotH * LdotN > 0.0f))) return 0.0f;
+    const float a2 = alpha * alpha;
+    const float v2 = VdotN * VdotN;
+    const float g1v = 2.0f / (1.0f + std::sqrt(1.0f + a2 * ((1.0f - v2) / v2)));
+    const float l2 = LdotN * LdotN;
+    const float g1l = 2.0f / (1.0f + std::sqrt(1.0f + a2 * ((1.0f - l2) / l2)));
+    return g1v * g1l;
+}
+// isotropicGgx.cpp:71-100
+V3 ggxSampleH(float alpha, float u0, float u1) {
+    const float s0 = std::min(std::max(u0, 0.0f), 0.9999f);
+    const float s1 = std::min(std::max(u1, 0.0f), 0.9999f);
+    const float phi = kTwoPi * s0;
+    const float theta = std::atan(alpha * std::sqrt(s1 / (1.0f - s1)));
+    if (!std::isfinite(theta)) return V3(0.0f, 1.0f, 0.0f);
+    const float c = std::cos(theta);
+    const float sn = std::sqrt(1.0f - c * c);
+    return V3(std::sin(phi) * sn, c, std::cos(phi) * sn);
+}
+// schlickConductorFresnel.cpp:28-41
+V3 schlick(const V3& f0, float cosI) {
+    const float c = 1.0f - std::abs(cosI);
+    const V3 comp = f0.complement();
+    return f0 + comp * c * (c * c) * (c * c);
+}
+// vanillaDielectricFresnel.cpp:17-48
+float dielectricFresnel(float etaI, float etaT, float cosI) {
+    if (cosI < 0.0f) { std::swap(etaI, etaT); cosI *= -1.0f; }
+    const float ratio = etaI / etaT;
+    const float sinT2 = ratio * ratio * (1.0f - cosI * cosI);
+    if (sinT2 >= 1.0f) return 1.0f;
+    const float cosT = std::sqrt(1.0f - sinT2);
+    const float rPar = (etaT * cosI - etaI * cosT) / (etaT * cosI + etaI * cosT);
+    const float rPer = (etaI * cosI - etaT * cosT) / (etaI * cosI + etaT * cosT);
+    return 0.5f * (rPar * rPar + rPer * rPer);
+}
+// tVector.ipp:468-503
+bool canRefract(const V3& v, const V3& n, float etaI, float etaT, V3* out) {
+    float sign = 1.0f;
+    const float cosI = v.dot(n);
+    if (cosI < 0.0f) { std::swap(etaI, etaT); sign = -1.0f; }
+    const float ratio = etaI / etaT;
+    const float sinT2 = ratio * ratio * (1.0f - cosI * cosI);
+    if (sinT2 >= 1.0f) return false;
+    const float cosT = std::sqrt(1.0f - sinT2);
+    V3 r = v * (-ratio);
+    r += n * ((ratio * sign * cosI - cosT) * sign);
+    *out = r.normalize();
+    return true;
+}
+
+// lambertianDiffuse.cpp:27-44 / conductorMicrofacet.cpp:32-66
+V3 bsdfEval(const Material& m, const Surface& si, const V3& L) {
+    const V3& Ns = si.Ns;
+    const V3& V = si.wi;
+    if (m.type == CGPU_BSDF_LAMBERTIAN) {
+        if (V.dot(Ns) * L.dot(Ns) <= 0.0f) return V3(0.0f);
+        return m.albedo * kInvPi;
+    }
+    if (m.type == CGPU_BSDF_CONDUCTOR_GGX) {
+        const float VdotN = V.dot(Ns), LdotN = L.dot(Ns);
+        if (VdotN * LdotN <= 0.0f) return V3(0.0f);
+        const float sgn = static_cast<float>((0.0f < VdotN) - (VdotN < 0.0f));
+        V3 H = (V + L) * sgn;
+        if (H.isZero()) return V3(0.0f);
+        H = H.normalize();
+        const float alpha = roughnessToAlpha(m.roughness);
+        const V3 F = schlick(m.f0, L.dot(H));
+        const float D = ggxD(alpha, Ns, H);
+        const float G = ggxG(alpha, V, L, Ns, H);
+        return F * G * D / (4.0f * std::abs(VdotN * LdotN));
+    }
+    return V3(0.0f);
+}
+
+// lambertianDiffuse.cpp:83-96 / conductorMicrofacet.cpp:126-163
+float bsdfPdf(const Material& m, const Surface& si, const V3& L) {
+    const V3& Ns = si.Ns;
+    const V3& V = si.wi;
+    if (m.type == CGPU_BSDF_LAMBERTIAN) {
+        if (V.dot(Ns) * L.dot(Ns) <= 0.0f) return 0.0f;
+        return L.absDot(Ns) * kInvPi;
+    }
+    if (m.type == CGPU_BSDF_CONDUCTOR_GGX) {
+        const float VdotN = V.dot(Ns), LdotN = L.dot(Ns);
+        if (VdotN * LdotN <= 0.0f) return 0.0f;
+        const float sgn = static_cast<float>((0.0f < VdotN) - (VdotN < 0.0f));
+        V3 H = (V + L) * sgn;
+        if (H.isZero()) return 0.0f;
+        H = H.normalize();
+        const float alpha = roughnessToAlpha(m.roughness);
+        const float D = ggxD(alpha, Ns, H);
+        const float pdfH = std::abs(D * Ns.dot(H));
+        const float pdfL = std::abs(pdfH / (4.0f * L.dot(H)));
+        return std::isfinite(pdfL) ? pdfL : 0.0f;
+    }
+    return 0.0f;
+}
+
+BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng) {
+    BsdfSample out;
+    const V3& Ns = si.Ns;
+    const V3& V = si.wi;
+    if (m.type == CGPU_BSDF_LAMBERTIAN) {  // lambertianDiffuse.cpp:46-81
+        V3 z, x;
+        buildCoordinateSystem(Ns, &z, &x);
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        // hemisphere.cpp:30-48
+        const float phi = kTwoPi * u0;
+        const float theta = std::acos(1.0f - 2.0f * u1) * 0.5f;
+        const float c = std::cos(theta);
+        const float sn = std::sqrt(1.0f - c * c);
+        V3 L(std::sin(phi) * sn, c, std::cos(phi) * sn);
+        const float pdf = c * kInvPi;
+        L = x * L.x + Ns * L.y + z * L.z;
+        L = L.normalize();
+        if (V.dot(Ns) <= 0.0f) L = -L;
+        out.f = m.albedo * kInvPi;
+        out.L = L;
+        out.pdf = pdf;
+        return out;
+    }
+    if (m.type == CGPU_BSDF_CONDUCTOR_GGX) {  // conductorMicrofacet.cpp:68-124
+        const float nf = V.dot(Ns) > 0.0f ? 1.0f : -1.0f;
+        const float alpha = roughnessToAlpha(m.roughness);
+        V3 z, x;
+        buildCoordinateSystem(Ns, &z, &x);
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        V3 H = ggxSampleH(alpha, u0, u1);
+        H = x * H.x + Ns * H.y + z * H.z;
+        H = H.normalize();
+        const V3 L = V.reflect(H * nf);
+        const float VdotN = V.dot(Ns), LdotN = L.dot(Ns), LdotH = L.dot(H), NdotH = Ns.dot(H);
+        if (VdotN * LdotN <= 0.0f) return out;
+        const V3 F = schlick(m.f0, LdotH);
+        const float D = ggxD(alpha, Ns, H);
+        const float G = ggxG(alpha, V, L, Ns, H);
+        const float pdfH = std::abs(D * NdotH);
+        const float pdfL = std::abs(pdfH / (4.0f * LdotH));
+        if (!std::isfinite(pdfL)) return out;
+        out.f = F * G * D / (4.0f * std::abs(VdotN * LdotN));
+        out.L = L;
+        out.pdf = pdfL;
+        return out;
+    }
+    if (m.type == CGPU_BSDF_GLASS) {  // specularDielectric.cpp:35-127
+        const float VdotN = V.dot(Ns);
+        const float R = dielectricFresnel(m.iorOuter, m.iorInner, VdotN);
+        const V3 reflectance(R);
+        const float pr = reflectance.average();
+        const float u = rng.next();
+        if (u < pr) {
+            const float nf = VdotN > 0.0f ? 1.0f : -1.0f;
+            const V3 L = V.reflect(Ns * nf);
+            const float LdotN = L.absDot(Ns);
+            out.f = m.albedo * reflectance / LdotN;
+            out.L = L;
+            out.pdf = pr;
+        } else {
+            float etaI = m.iorOuter, etaT = m.iorInner;
+            V3 L;
+            if (!canRefract(V, Ns, etaI, etaT, &L)) return out;
+            const float cosI = L.dot(Ns);
+            const V3 Rt(dielectricFresnel(m.iorOuter, m.iorInner, cosI));
+            if (cosI < 0.0f) std::swap(etaI, etaT);
+            const float btdf = (etaT * etaT) / (etaI * etaI);
+            const float LdotN = std::abs(cosI);
+            const V3 trans = Rt.complement();
+            out.f = m.albedo * trans * btdf / LdotN;
+            out.L = L;
+            out.pdf = 1.0f - pr;
+        }
+        return out;
+    }
+    return out;  // absorber: invalid (absorberBsdf.cpp)
+}
+
+// ---------------------------------------------------------------- lights ---
+struct LightSample { V3 pos, N, radiance; float pdfW = 0.0f; bool valid() const { return !radiance.isZero() && pdfW > 0.0f; } };
+
+bool canEmit(const Light& l, const V3& dir, const V3& N) { return (dir.dot(N) >= 0.0f) != l.backFace; }  // areaLight.cpp:24-28
+
+// singleAreaLight.cpp:54-85 with the position samplers of
+// triangle.cpp:162-193 (sampleWarp.cpp:10-19) and rectangle.cpp:134-169.
+LightSample lightSample(const Scene& s, const Light& l, const V3& target, Rng& rng) {
+    LightSample out;
+    const Prim& pr = s.prims[l.prim];
+    V3 P, Ns;
+    float pdfA;
+    if (pr.kind == CGPU_PRIM_TRIANGLE) {
+        const Triangle& t = s.tris[pr.slot];
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        const float sa = std::sqrt(u0);
+        const float ss = 1.0f - sa, st = sa * u1;
+        P = t.a + t.eAB * ss + t.eAC * st;
+        const V3 b = barycentric(t, P);
+        const V3 Ng = triNormal(t);
+        V3 n = b.x * t.nA + b.y * t.nB + b.z * t.nC;
+        Ns = n.isZero() ? Ng : n;
+        pdfA = 1.0f / triArea(t);
+    } else {
+        const Rectangle& r = s.rects[pr.slot];
+        V3 eA = r.eA, eB = r.eB;
+        if (eA.length() < eB.length()) std::swap(eA, eB);
+        const float longW = eA.length(), shortW = eB.length();
+        float a, b;
+        do {
+            a = rng.next();
+            b = rng.next();
+        } while (b > shortW / longW);
+        P = r.vB + eA * a + eB.normalize() * (b * eA.length());
+        Ns = rectNormal(r);
+        pdfA = 1.0f / rectArea(r);
+    }
+    if (!(pdfA > 0.0f)) return out;
+    const V3 emitVec = target - P;
+    if (!canEmit(l, emitVec, Ns)) return out;
+    const float d2 = emitVec.lengthSquared();
+    const float cosE = (emitVec / std::sqrt(d2)).absDot(Ns);
+    if (cosE <= 0.0f) return out;
+    out.pos = P;
+    out.N = Ns;
+    out.pdfW = pdfA * d2 / cosE;
+    out.radiance = l.radiance;
+    return out;
+}
+
+float lightArea(const Scene& s, const Light& l) {
+    const Prim& pr = s.prims[l.prim];
+    return pr.kind == CGPU_PRIM_TRIANGLE ? triArea(s.tris[pr.slot]) : rectArea(s.rects[pr.slot]);
+}
+
+// singleAreaLight.cpp:39-52
+V3 emittance(const Light& l, const Surface& si) {
+    if (!canEmit(l, si.wi, si.Ns)) return V3(0.0f);
+    return l.radiance;
+}
+// singleAreaLight.cpp:87-109
+float lightPdfW(const Scene& s, const Light& l, const Surface& si, const V3& target) {
+    const V3 emitVec = target - si.P;
+    if (!canEmit(l, si.wi, si.Ns)) return 0.0f;
+    const float c = si.wi.absDot(si.Ns);
+    if (c <= 0.0f) return 0.0f;
+    const float pdfA = 1.0f / lightArea(s, l);
+    return pdfA * emitVec.lengthSquared() / c;
+}
+
+float misPower(float a, float b) {  // tMis.h:21-47
+    const float a2 = a * a, b2 = b * b;
+    return a2 / (a2 + b2);
+}
+
+// directLightEvaluator.cpp:18-109
+V3 directLight(const Scene& s, const Surface& si, const Material& m, int lightIndex, Rng& rng) {
+    V3 result(0.0f);
+    if (m.type == CGPU_BSDF_ABSORBER) return result;
+    const Light& l = s.lights[lightIndex];
+    const V3 P = si.P, Ns = si.Ns;
+    {
+        const LightSample ls = lightSample(s, l, P, rng);
+        if (ls.valid()) {
+            const V3 Lv = ls.pos - P;
+            const float dist = Lv.length();
+            const V3 L = Lv / dist;
+            Ray shadow;
+            shadow.o = P;
+            shadow.d = L.normalize();
+            shadow.maxT = dist - kRayEps;
+            if (!occluded(s, shadow)) {
+                const V3 f = bsdfEval(m, si, L);
+                const V3 factor = f * L.absDot(Ns);
+                const float bp = bsdfPdf(m, si, L);
+                const float w = misPower(ls.pdfW, bp);
+                result += w * ls.radiance * factor / ls.pdfW;
+            }
+        }
+    }
+    {
+        const BsdfSample bs = bsdfSample(m, si, rng);
+        if (bs.valid()) {
+            Ray r;
+            r.o = P;
+            r.d = bs.L.normalize();
+            Surface hit;
+            if (intersect(s, r, &hit)) {
+                if (s.prims[hit.prim].light == lightIndex) {
+                    const V3 factor = bs.f * bs.L.absDot(Ns);
+                    const V3 rad = emittance(l, hit);
+                    const float lp = lightPdfW(s, l, hit, P);
+                    const float w = misPower(bs.pdf, lp);
+                    result += w * rad * factor / bs.pdf;
+                }
+            }
+        }
+    }
+    return result;
+}
+
+// ptEstimator.cpp:25-123
+V3 estimate(const Scene& s, Ray ray, Rng& rng) {
+    V3 L(0.0f), T(1.0f);
+    bool countEmission = true;
+    for (int bounce = 0; bounce < s.maxDepth; ++bounce) {
+        Surface si;
+        if (!intersect(s, ray, &si)) break;
+        const Prim& pr = s.prims[si.prim];
+        const Material& m = s.mats[pr.material];
+        if (pr.light >= 0 && countEmission) {
+            L += T * emittance(s.lights[pr.light], si);
+        }
+        if (!isSpecular(m.type)) {
+            countEmission = false;
+            const std::size_t li = rng.index(0, s.lights.size());
+            const float pick = 1.0f / static_cast<float>(s.lights.size());
+            const V3 direct = directLight(s, si, m, static_cast<int>(li), rng) / pick;
+            L += T * direct;
+        } else {
+            countEmission = true;
+        }
+        const BsdfSample bs = bsdfSample(m, si, rng);
+        if (!bs.valid()) break;
+        const float LdotN = bs.L.absDot(si.Ns);
+        T *= bs.f * LdotN / bs.pdf;
+        if (bounce > 2) {  // russianRoulette.cpp:9-28
+            const float q = std::min(std::max(1.0f - T.maxComponent(), 0.05f), 1.0f);
+            const float u = rng.next();
+            if (u > q) T = T * (1.0f / (1.0f - q));
+            else break;
+        }
+        if (T.isZero()) break;
+        ray = Ray();
+        ray.o = si.P;
+        ray.d = bs.L.normalize();
+    }
+    return L;
+}
+
+// perspectivePinholeCamera.cpp:52-73 with the film->camera transform of :32-50
+// and the camera->world lookAt of tMatrix4.ipp:47-60.
+Ray cameraRay(const Scene& s, double fx, double fy) {
+    const float x = static_cast<float>(fx), y = static_cast<float>(fy);
+    const float cx = s.sx * x + s.tx;
+    const float cy = s.sy * y + s.ty;
+    const float cz = -s.offset;
+    V3 d(s.camX.x * cx + s.camY.x * cy + s.camZ.x * cz,
+         s.camX.y * cx + s.camY.y * cy + s.camZ.y * cz,
+         s.camX.z * cx + s.camY.z * cy + s.camZ.z * cz);
+    Ray r;
+    r.o = s.camPos;
+    r.d = d.normalize();
+    return r;
+}
+
+// Sample layout shared with the CUDA library: sample `si` of a pixel takes
+// stratum si of the floor(sqrt(spp))^2 grid (strata beyond it are uniform),
+// jittered by the first two draws of the path stream.  This is the set the
+// reference's StratifiedSampler produces (stratifiedSampler.cpp:38-73) without
+// its shuffle, which only reorders samples within a pixel.
+void jitter(int spp, uint32_t si, Rng& rng, float* jx, float* jy) {
+    const int base = static_cast<int>(std::floor(std::sqrt(static_cast<float>(spp))));
+    const float u0 = rng.next(), u1 = rng.next();
+    if (static_cast<int>(si) < base * base) {
+        const float inv = 1.0f / static_cast<float>(base);
+        *jx = (static_cast<float>(si % base) + u0) * inv;
+        *jy = (static_cast<float>(si / base) + u1) * inv;
+    } else {
+        *jx = u0;
+        *jy = u1;
+    }
+}
+
+V3 vload(const float* p) { return V3(p[0], p[1], p[2]); }
+
+Scene* create(const cgpu_scene_desc* d) {
+    auto s = std::make_unique<Scene>();
+    s->W = d->width; s->H = d->height; s->maxDepth = d->max_depth; s->spp = d->spp > 0 ? d->spp : 1;
+    for (uint32_t i = 0; i < d->num_materials; ++i) {
+        const cgpu_material& m = d->materials[i];
+        s->mats.push_back({m.type, vload(m.albedo), vload(m.f0), m.roughness, m.ior_outer, m.ior_inner});
+    }
+    for (uint32_t i = 0; i < d->num_primitives; ++i) {
+        const int kind = d->prim_kind ? d->prim_kind[i] : CGPU_PRIM_TRIANGLE;
+        const float* v = d->prim_vertices + 9 * static_cast<std::size_t>(i);
+        Prim p{kind, d->prim_material[i], -1, 0};
+        if (kind == CGPU_PRIM_TRIANGLE) {
+            Triangle t;
+            t.a = vload(v); t.b = vload(v + 3); t.c = vload(v + 6);
+            t.eAB = t.b - t.a; t.eAC = t.c - t.a;
+            const V3 N0 = t.eAB.cross(t.eAC);
+            const V3 N = N0.isZero() ? V3(0.0f, 1.0f, 0.0f) : N0.normalize();
+            t.nA = t.nB = t.nC = N;
+            if (d->prim_normals) {  // triangleMesh.cpp:24-28 (setN* ignores zero normals)
+                const float* n = d->prim_normals + 9 * static_cast<std::size_t>(i);
+                if (!vload(n).isZero()) t.nA = vload(n);
+                if (!vload(n + 3).isZero()) t.nB = vload(n + 3);
+                if (!vload(n + 6).isZero()) t.nC = vload(n + 6);
+            }
+            t.uA = V3(0, 0, 0); t.uB = V3(1, 0, 0); t.uC = V3(0, 1, 0);
+            if (d->prim_uvws) {
+                const float* u = d->prim_uvws + 9 * static_cast<std::size_t>(i);
+                t.uA = vload(u); t.uB = vload(u + 3); t.uC = vload(u + 6);
+            }
+            p.slot = static_cast<int>(s->tris.size());
+            s->tris.push_back(t);
+        } else {
+            Rectangle r;
+            r.vA = vload(v); r.vB = vload(v + 3); r.vC = vload(v + 6);
+            r.eA = r.vA - r.vB; r.eB = r.vC - r.vB;
+            r.vD = r.vB + r.eA + r.eB;
+            p.slot = static_cast<int>(s->rects.size());
+            s->rects.push_back(r);
+        }
+        s->prims.push_back(p);
+    }
+    for (uint32_t i = 0; i < d->num_lights; ++i) {
+        const cgpu_area_light& l = d->lights[i];
+        Light L;
+        L.prim = l.primitive;
+        L.backFace = l.back_face_emit != 0;
+        const V3 color = vload(l.color);
+        const V3 unit = color / color.sum();
+        const V3 total = unit * l.watt;
+        s->lights.push_back(L);
+        const float area = lightArea(*s, s->lights.back());
+        s->lights.back().radiance = total / area * kInvPi;  // singleAreaLight.cpp:32-36
+        s->prims[l.primitive].light = static_cast<int>(i);
+    }
+    std::vector<BuildItem> items(s->prims.size());
+    for (std::size_t i = 0; i < s->prims.size(); ++i) {
+        primBound(*s, static_cast<int>(i), &items[i].lo, &items[i].hi);
+        items[i].c = (items[i].lo + items[i].hi) * 0.5f;
+        items[i].idx = static_cast<int>(i);
+    }
+    if (!items.empty()) buildRec(*s, items, 0, static_cast<int>(items.size()));
+    // camera
+    const V3 pos = vload(d->cam_position), dir = vload(d->cam_direction), up = vload(d->cam_up);
+    s->camPos = pos;
+    s->camZ = (-dir).normalize();
+    s->camX = up.cross(s->camZ).normalize();
+    s->camY = s->camZ.cross(s->camX);
+    const double sw = d->sensor_width_mm > 0 ? d->sensor_width_mm : 36.0;
+    const double aspect = static_cast<double>(d->width) / static_cast<double>(d->height);
+    const double sh = sw / aspect;
+    const float halfFovRad = static_cast<float>(d->fov_degrees * 0.5) * 0.0174532925199432f;
+    s->offset = static_cast<float>((sw * 0.5) / std::tan(halfFovRad));
+    s->sx = static_cast<float>(sw / d->width);
+    s->sy = static_cast<float>(-sh / d->height);
+    s->tx = static_cast<float>(-(sw * 0.5));
+    s->ty = static_cast<float>(sh * 0.5);
+    return s.release();
+}
+
+}  // namespace port
+
+extern "C" {
+
+void* port_scene_create(const cgpu_scene_desc* desc) { return port::create(desc); }
+void port_scene_destroy(void* s) { delete static_cast<port::Scene*>(s); }
+int port_num_bvh_nodes(void* s) { return static_cast<int>(static_cast<port::Scene*>(s)->nodes.size()); }
+
+void port_camera_rays(void* sp, const double* xy, uint32_t n, float* out) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    for (uint32_t i = 0; i < n; ++i) {
+        const port::Ray r = port::cameraRay(s, xy[2 * i], xy[2 * i + 1]);
+        float* o = out + 6 * static_cast<std::size_t>(i);
+        o[0] = r.o.x; o[1] = r.o.y; o[2] = r.o.z; o[3] = r.d.x; o[4] = r.d.y; o[5] = r.d.z;
+    }
+}
+
+// rays: 8 floats each (org, t_min, dir, t_max)
+void port_trace(void* sp, const float* rays, uint32_t n, int32_t* prim, float* t, int32_t* occ) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float* r = rays + 8 * static_cast<std::size_t>(i);
+        port::Ray ray;
+        ray.o = port::V3(r[0], r[1], r[2]);
+        ray.d = port::V3(r[4], r[5], r[6]).normalize();  // Ray ctor normalises (ray.cpp:19-30)
+        ray.minT = r[3];
+        ray.maxT = r[7];
+        port::Ray a = ray;
+        const int p = port::traverse(s, a, false);
+        prim[i] = p;
+        t[i] = p >= 0 ? a.maxT : 0.0f;
+        if (occ) occ[i] = port::occluded(s, ray) ? 1 : 0;
+    }
+}
+
+void port_paths(void* sp, const double* xy, const uint64_t* keys, uint32_t n, float* rgb, uint32_t* draws) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    for (uint32_t i = 0; i < n; ++i) {
+        port::Rng rng;
+        rng.s.key = keys[i];
+        rng.s.counter = 0;
+        const port::Ray r = port::cameraRay(s, xy[2 * i], xy[2 * i + 1]);
+        const port::V3 L = port::estimate(s, r, rng);
+        rgb[3 * i] = L.x; rgb[3 * i + 1] = L.y; rgb[3 * i + 2] = L.z;
+        if (draws) draws[i] = rng.s.counter;
+    }
+}
+
+// Renders samples [first, first + count) of rows [row0, row1) with `threads`
+// host threads.  film: W*H*7 doubles (sum rgb, sum sq rgb, accepted count);
+// path_rgb (optional): count*W*H*3 floats, sample-major.
+void port_render(void* sp, uint64_t seed, uint32_t scene_index, uint32_t first, uint32_t count,
+                 int32_t row0, int32_t row1, int32_t threads, double* film, float* path_rgb) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    std::atomic<int> next{row0};
+    auto worker = [&]() {
+        for (;;) {
+            const int iy = next.fetch_add(1);
+            if (iy >= row1) break;
+            for (int ix = 0; ix < s.W; ++ix) {
+                const uint32_t pixel = static_cast<uint32_t>(iy * s.W + ix);
+                for (uint32_t k = 0; k < count; ++k) {
+                    const uint32_t si = first + k;
+                    port::Rng rng;
+                    rng.s.key = oracle_rng::path_key(seed, scene_index, pixel, si);
+                    rng.s.counter = 0;
+                    float jx, jy;
+                    port::jitter(s.spp, si, rng, &jx, &jy);
+                    const float fx = static_cast<float>(ix) + jx, fy = static_cast<float>(iy) + jy;
+                    const port::Ray r = port::cameraRay(s, fx, fy);
+                    const port::V3 L = port::estimate(s, r, rng);
+                    if (path_rgb) {
+                        float* o = path_rgb + 3 * (static_cast<std::size_t>(k) * s.W * s.H + pixel);
+                        o[0] = L.x; o[1] = L.y; o[2] = L.z;
+                    }
+                    if (film && L.finite()) {  // filmTile.cpp:21-28 drops NaN / Inf samples
+                        double* px = film + 7 * static_cast<std::size_t>(pixel);
+                        px[0] += L.x; px[1] += L.y; px[2] += L.z;
+                        px[3] += static_cast<double>(L.x) * L.x;
+                        px[4] += static_cast<double>(L.y) * L.y;
+                        px[5] += static_cast<double>(L.z) * L.z;
+                        px[6] += 1.0;
+                    }
+                }
+            }
+        }
+    };
+    if (threads <= 1) {
+        worker();
+    } else {
+        std::vector<std::thread> pool;
+        for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+        for (auto& t : pool) t.join();
+    }
+}
+
+}  // extern "C"

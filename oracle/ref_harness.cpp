@@ -1,0 +1,344 @@
+// Reference harness: drives the reference renderer's OWN object files.
+//
+// Test infrastructure only.  oracle/Makefile compiles every reference source
+// except source/cadise/cadise.cpp (its main) and source/math/random.cpp (its
+// RNG) and links them with this file.  Nothing here re-implements reference
+// behaviour; it loads a CRSD scene through the reference's own tokenizer and
+// factories and calls:
+//
+//   Camera::spawnPrimaryRay        core/camera/perspectivePinholeCamera.cpp:52-73
+//   Accelerator::isIntersecting    core/intersector/accelerator/bvh/bvhAccelerator.cpp:40-97
+//   Accelerator::isOccluded        core/intersector/accelerator/bvh/bvhAccelerator.cpp:99-156
+//   BruteForceAccelerator          core/intersector/accelerator/bruteForceAccelerator.cpp:26-43
+//   EnergyEstimator::estimate      core/estimator/ptEstimator.cpp:25-123
+//   Sampler::requestSample2D       core/sampler/category/stratifiedSampler.cpp:38-73
+//
+// cadise::Random (source/math/random.h) is interposed with the seeded
+// per-path stream of oracle_rng.h so that a render is reproducible.
+//
+// Commands (binary little-endian I/O, see tests/golden/make_golden.py):
+//   camera <scene.crsd> <in: N x {f64 fx, f64 fy}>           <out: N x 6 f32 (o, d)>
+//   trace  <scene.crsd> <in: N x 8 f32 {o, tmin, d, tmax}>    <out: N x {i32 bvh_prim, f32 bvh_t, i32 bf_prim, f32 bf_t, i32 occluded}>
+//   paths  <scene.crsd> <in: N x {f64 fx, f64 fy, u64 key}>   <out: N x {f32 r, g, b, u32 draws}>
+//   render <scene.crsd> <out: H x W x 7 f64> <spp> <seed> <threads>
+//          (sum r,g,b, sum of squares r,g,b, accepted sample count)
+
+#include "core/camera/camera.h"
+#include "core/estimator/energyEstimator.h"
+#include "core/film/film.h"
+#include "core/instantiator/instantiator.h"
+#include "core/intersector/accelerator/accelerator.h"
+#include "core/intersector/accelerator/bruteForceAccelerator.h"
+#include "core/intersector/intersector.h"
+#include "core/intersector/primitive/primitive.h"
+#include "core/intersector/primitiveInfo.h"
+#include "core/light/cluster/lightCluster.h"
+#include "core/light/light.h"
+#include "core/ray.h"
+#include "core/sampler/sampleRecord2D.h"
+#include "core/sampler/sampler.h"
+#include "core/scene.h"
+#include "core/spectrum/spectrum.h"
+#include "core/surface/bsdf/bsdf.h"
+#include "core/texture/tTexture.h"
+#include "file-io/scene-description/eSdClassType.h"
+#include "file-io/scene-description/sdData.h"
+#include "file-io/scene-description/tokenizer.h"
+#include "math/random.h"
+#include "math/type/mapType.h"
+
+#include "oracle_rng.h"
+
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <limits>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace cadise {
+
+static thread_local oracle_rng::Stream g_stream;
+
+// Interposed: same signature as source/math/random.h.
+real Random::nextReal() { return g_stream.next(); }
+
+// Interposed: the index formula of source/math/random.cpp:21-26 over the
+// interposed stream (min + u * (max - min), clamped into [min, max - 1]).
+std::size_t Random::nextIndex(const std::size_t minIndex, const std::size_t maxIndex) {
+    const std::size_t interval = maxIndex - minIndex;
+    const std::size_t idx = static_cast<std::size_t>(minIndex + nextReal() * interval);
+    if (idx < minIndex) return minIndex;
+    if (idx > maxIndex - 1) return maxIndex - 1;
+    return idx;
+}
+
+}  // namespace cadise
+
+using namespace cadise;
+
+namespace {
+
+struct LoadedScene {
+    std::string text;  // SdData keeps string_views into this buffer
+    std::vector<std::shared_ptr<SdData>> blocks;
+    std::shared_ptr<SdData> film, camera, renderer, accel, cluster;
+    StringKeyMap<TTexture<real>> realTextures;
+    StringKeyMap<TTexture<Spectrum>> spectrumTextures;
+    StringKeyMap<Bsdf> bsdfs;
+    StringKeyMap<Primitive> primitives;
+    std::vector<std::shared_ptr<Intersector>> intersectors;
+    std::vector<std::shared_ptr<Light>> lights;
+    std::shared_ptr<Primitive> background;
+    std::shared_ptr<Accelerator> accelerator;
+    std::shared_ptr<Accelerator> bruteForce;
+    std::shared_ptr<LightCluster> lightCluster;
+    std::shared_ptr<Scene> scene;
+    std::shared_ptr<Camera> cam;
+    std::shared_ptr<EnergyEstimator> estimator;
+    std::shared_ptr<Sampler> sampler;
+    std::map<const void*, int> primIndex;  // Primitive* -> CRSD creation order
+    int width = 0, height = 0;
+};
+
+std::string readStripped(const char* path) {
+    FILE* f = std::fopen(path, "r");
+    if (!f) {
+        std::fprintf(stderr, "cannot open %s\n", path);
+        std::exit(2);
+    }
+    std::string s;
+    int ch;
+    while ((ch = std::fgetc(f)) != EOF) {
+        if (ch == '#') {
+            while ((ch = std::fgetc(f)) != EOF && ch != '\n') {
+            }
+        } else {
+            s.push_back(static_cast<char>(ch));
+        }
+    }
+    std::fclose(f);
+    return s;
+}
+
+std::unique_ptr<LoadedScene> load(const char* path) {
+    auto ls = std::make_unique<LoadedScene>();
+    ls->text = readStripped(path);
+    std::string_view view(ls->text);
+    Tokenizer tok;
+    std::size_t start = 0, end = 0;
+    while ((end = view.find_first_of('}', start)) != std::string_view::npos) {
+        auto data = tok.tokenize(view.substr(start, end - start + 1));
+        ls->blocks.push_back(data);
+        switch (data->classType()) {
+            case ESdClassType::FILM: ls->film = data; break;
+            case ESdClassType::CAMERA: ls->camera = data; break;
+            case ESdClassType::RENDERER: ls->renderer = data; break;
+            case ESdClassType::ACCELERATOR: ls->accel = data; break;
+            case ESdClassType::LIGHT_CLUSTER: ls->cluster = data; break;
+            case ESdClassType::TEXTURE_REAL:
+                ls->realTextures.insert({std::string(data->findString("name")),
+                                         instantiator::makeRealTexture(data, ls->realTextures, ls->spectrumTextures)});
+                break;
+            case ESdClassType::TEXTURE_SPECTRUM:
+                ls->spectrumTextures.insert({std::string(data->findString("name")),
+                                             instantiator::makeSpectrumTexture(data, ls->realTextures, ls->spectrumTextures)});
+                break;
+            case ESdClassType::MATERIAL:
+                ls->bsdfs.insert({std::string(data->findString("name")),
+                                  instantiator::makeBsdf(data, ls->realTextures, ls->spectrumTextures, ls->bsdfs)});
+                break;
+            case ESdClassType::LIGHT: {
+                auto light = instantiator::makeLight(data, ls->primitives, ls->background);
+                ls->lights.push_back(light);
+                break;
+            }
+            case ESdClassType::PRIMITIVE: {
+                const std::size_t before = ls->intersectors.size();
+                instantiator::makePrimitive(data, ls->bsdfs, &ls->intersectors, &ls->primitives);
+                for (std::size_t i = before; i < ls->intersectors.size(); ++i) {
+                    const Primitive* p = dynamic_cast<const Primitive*>(ls->intersectors[i].get());
+                    ls->primIndex[p] = static_cast<int>(i);
+                }
+                break;
+            }
+            default: break;
+        }
+        start = end + 1;
+    }
+    ls->accelerator = instantiator::makeAccelerator(ls->accel, ls->intersectors);
+    ls->bruteForce = std::make_shared<BruteForceAccelerator>(ls->intersectors);
+    ls->lightCluster = instantiator::makeLightCluster(ls->cluster, ls->lights);
+    ls->scene = std::make_shared<Scene>(ls->accelerator, ls->lightCluster);
+    if (ls->background) ls->scene->setBackgroundSphere(ls->background.get());
+    ls->cam = instantiator::makeCamera(ls->camera);
+    ls->width = ls->film->findInt32("image-width", 1024);
+    ls->height = ls->film->findInt32("image-height", 768);
+    ls->cam->setResolution(Vector2S(static_cast<std::size_t>(ls->width), static_cast<std::size_t>(ls->height)));
+    ls->cam->updateTransform();
+    ls->estimator = instantiator::makeEstimator(ls->renderer);
+    ls->sampler = instantiator::makeSampler(ls->renderer);
+    return ls;
+}
+
+template <typename T>
+std::vector<T> readAll(const char* path) {
+    std::ifstream f(path, std::ios::binary);
+    std::vector<char> bytes((std::istreambuf_iterator<char>(f)), std::istreambuf_iterator<char>());
+    std::vector<T> out(bytes.size() / sizeof(T));
+    std::memcpy(out.data(), bytes.data(), out.size() * sizeof(T));
+    return out;
+}
+
+void writeAll(const char* path, const void* data, std::size_t bytes) {
+    std::ofstream f(path, std::ios::binary);
+    f.write(static_cast<const char*>(data), static_cast<std::streamsize>(bytes));
+}
+
+int primOf(const LoadedScene& ls, const PrimitiveInfo& info) {
+    auto it = ls.primIndex.find(info.primitive());
+    return it == ls.primIndex.end() ? -2 : it->second;
+}
+
+int cmdCamera(const LoadedScene& ls, const char* in, const char* out) {
+    const auto xy = readAll<double>(in);
+    const std::size_t n = xy.size() / 2;
+    std::vector<float> res(n * 6);
+    for (std::size_t i = 0; i < n; ++i) {
+        Ray r;
+        ls.cam->spawnPrimaryRay(Vector2D(xy[2 * i], xy[2 * i + 1]), &r);
+        for (int k = 0; k < 3; ++k) {
+            res[6 * i + k] = r.origin()[k];
+            res[6 * i + 3 + k] = r.direction()[k];
+        }
+    }
+    writeAll(out, res.data(), res.size() * sizeof(float));
+    return 0;
+}
+
+int cmdTrace(const LoadedScene& ls, const char* in, const char* out) {
+    const auto rays = readAll<float>(in);
+    const std::size_t n = rays.size() / 8;
+    struct Rec { int32_t bvhPrim; float bvhT; int32_t bfPrim; float bfT; int32_t occluded; };
+    std::vector<Rec> res(n);
+    for (std::size_t i = 0; i < n; ++i) {
+        const float* r = &rays[8 * i];
+        const Vector3R o(r[0], r[1], r[2]), d(r[4], r[5], r[6]);
+        Ray a(o, d, r[3], r[7]);
+        PrimitiveInfo pa;
+        Rec rec{-1, 0.0f, -1, 0.0f, 0};
+        if (ls.accelerator->isIntersecting(a, pa)) {
+            rec.bvhPrim = primOf(ls, pa);
+            rec.bvhT = a.maxT();
+        }
+        Ray b(o, d, r[3], r[7]);
+        PrimitiveInfo pb;
+        if (ls.bruteForce->isIntersecting(b, pb)) {
+            rec.bfPrim = primOf(ls, pb);
+            rec.bfT = b.maxT();
+        }
+        Ray c(o, d, r[3], r[7]);
+        rec.occluded = ls.accelerator->isOccluded(c) ? 1 : 0;
+        res[i] = rec;
+    }
+    writeAll(out, res.data(), res.size() * sizeof(Rec));
+    return 0;
+}
+
+int cmdPaths(const LoadedScene& ls, const char* in, const char* out) {
+    struct Q { double fx, fy; uint64_t key; };
+    const auto qs = readAll<Q>(in);
+    struct R { float r, g, b; uint32_t draws; };
+    std::vector<R> res(qs.size());
+    for (std::size_t i = 0; i < qs.size(); ++i) {
+        g_stream.key = qs[i].key;
+        g_stream.counter = 0;
+        Ray primary;
+        ls.cam->spawnPrimaryRay(Vector2D(qs[i].fx, qs[i].fy), &primary);
+        Spectrum radiance;
+        ls.estimator->estimate(*ls.scene, primary, &radiance);
+        Vector3R rgb;
+        radiance.transformToRgb(&rgb);
+        res[i] = R{rgb[0], rgb[1], rgb[2], g_stream.counter};
+    }
+    writeAll(out, res.data(), res.size() * sizeof(R));
+    return 0;
+}
+
+// The reference tile loop (core/renderer/render-work/estimatorTileWork.cpp:32-61)
+// with an FP64 box-filtered film in place of the FP32 FilmTile: per pixel the
+// reference sampler draws its stratified 2-D set from a per-pixel stream, then
+// every sample runs the reference estimator on its own path stream.
+int cmdRender(const LoadedScene& ls, const char* out, int spp, uint64_t seed, int threads) {
+    const int W = ls.width, H = ls.height;
+    std::vector<double> film(static_cast<std::size_t>(W) * H * 7, 0.0);
+    std::atomic<int> nextRow{0};
+    auto worker = [&]() {
+        for (;;) {
+            const int iy = nextRow.fetch_add(1);
+            if (iy >= H) break;
+            for (int ix = 0; ix < W; ++ix) {
+                const uint32_t pixel = static_cast<uint32_t>(iy * W + ix);
+                g_stream.key = oracle_rng::path_key(seed, 0, pixel, 0xFFFFFFFFu);
+                g_stream.counter = 0;
+                auto s = ls.sampler->clone(static_cast<std::size_t>(spp));
+                auto rec = s->requestSample2D();
+                double* px = &film[static_cast<std::size_t>(pixel) * 7];
+                for (int si = 0; si < spp; ++si) {
+                    const Vector2R jitter = rec->nextSample();
+                    const double fx = ix + static_cast<double>(jitter.x());
+                    const double fy = iy + static_cast<double>(jitter.y());
+                    const uint64_t pixelKey = g_stream.key;
+                    const uint32_t pixelCtr = g_stream.counter;
+                    g_stream.key = oracle_rng::path_key(seed, 0, pixel, static_cast<uint32_t>(si));
+                    g_stream.counter = 0;
+                    Ray primary;
+                    ls.cam->spawnPrimaryRay(Vector2D(fx, fy), &primary);
+                    Spectrum radiance;
+                    ls.estimator->estimate(*ls.scene, primary, &radiance);
+                    g_stream.key = pixelKey;
+                    g_stream.counter = pixelCtr;
+                    Vector3R rgb;
+                    radiance.transformToRgb(&rgb);
+                    if (!(std::isfinite(rgb[0]) && std::isfinite(rgb[1]) && std::isfinite(rgb[2]))) continue;
+                    for (int k = 0; k < 3; ++k) {
+                        px[k] += rgb[k];
+                        px[3 + k] += static_cast<double>(rgb[k]) * rgb[k];
+                    }
+                    px[6] += 1.0;
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    writeAll(out, film.data(), film.size() * sizeof(double));
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: ref_harness <camera|trace|paths|render> <scene.crsd> ...\n");
+        return 2;
+    }
+    const std::string cmd = argv[1];
+    auto ls = load(argv[2]);
+    if (cmd == "camera" && argc >= 5) return cmdCamera(*ls, argv[3], argv[4]);
+    if (cmd == "trace" && argc >= 5) return cmdTrace(*ls, argv[3], argv[4]);
+    if (cmd == "paths" && argc >= 5) return cmdPaths(*ls, argv[3], argv[4]);
+    if (cmd == "render" && argc >= 7) {
+        return cmdRender(*ls, argv[3], std::atoi(argv[4]), std::strtoull(argv[5], nullptr, 10), std::atoi(argv[6]));
+    }
+    std::fprintf(stderr, "bad command\n");
+    return 2;
+}
