@@ -1,0 +1,332 @@
+"""Benchmark: wavefront path samples/s on the 1,024,000-triangle icosphere
+field (1920x1080, 64 spp, depth 12, NEE + MIS, Lambert / GGX conductor /
+GGX dielectric, 8 quad lights) on one GB300, next to the FP32 megakernel
+on the same GPU and the oracle CPU path on the host cores.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+A step is one full 64-spp render of the frame (132.7 M path samples)
+through the C ABI, scene resident in HBM.  Prints one JSON line (rank 0).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "path samples/s at equal relMSE (wavefront vs megakernel, 1 GB300)"
+UNIT = "samples/s"
+WORKLOAD = "icosphere-field-1M-tris-1920x1080-64spp-depth12"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--spp", type=int, default=64)
+    ap.add_argument("--quick", action="store_true", help="small frame for a fast check (not a bench number)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_scene(args):
+    from cadise_gb300 import scenes
+    if args.quick:
+        return scenes.icosphere_field(n_spheres=40, subdivision=3, width=640, height=360, spp=args.spp)
+    return scenes.icosphere_field(spp=args.spp)
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    """nvidia-smi clock / throttle samples during the timed region (read only)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        rows = []
+        with open(self.file.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.file.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for k, n in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+# ------------------------------------------------------------- CPU oracle --
+def cpu_rate(flat, seconds: float = 12.0, threads: int = 0):
+    """The oracle's CPU path tracer (a restatement of the reference's, run on
+    all host cores) on a bounded sample of the same frame: whole rows at
+    1 spp from the middle of the image until ~`seconds` of CPU work."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    ps = oracle.PortScene(flat)
+    h, w = flat.desc.height, flat.desc.width
+    mid = h // 2
+    t0 = time.perf_counter()
+    ps.render(seed=1, first=0, count=1, rows=(mid, mid + 1), threads=threads)
+    one = max(time.perf_counter() - t0, 1e-3)
+    rows = int(max(1, min(h - mid, seconds / one)))
+    t0 = time.perf_counter()
+    ps.render(seed=1, first=0, count=1, rows=(mid - rows // 2, mid - rows // 2 + rows), threads=threads)
+    dt = time.perf_counter() - t0
+    samples = rows * w
+    return samples / dt, threads, "%d rows x %d px x 1 spp (%d path samples) of the same frame" % (rows, w, samples)
+
+
+# ---------------------------------------------------------------- GPU arm --
+def run_gpu(args, rank, world, local):
+    import numpy as np
+    import torch
+
+    import cadise_gb300 as cg
+    from cadise_gb300 import abi
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.Stream()
+    ctx = cg.Context(device=local, stream=stream.cuda_stream)
+    spec = make_scene(args)
+    flat = abi.flatten(spec)
+    sid = ctx.upload(flat)
+    info = ctx.info(sid)
+    npix = spec.width * spec.height
+    spp = spec.spp
+    # weak scaling: every rank renders its own disjoint sample range of the frame
+    first = rank * spp
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    def render(mode, graph=True):
+        ctx.render([sid], first, spp, seed=2024, mode=mode, graph=graph, sync=False)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            flush.fill_(1)
+            render(cg.CGPU_MODE_WAVEFRONT)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        clocks = ClockSampler(local)
+        clocks.start()
+        torch.cuda.synchronize()
+        starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+        launches = 0
+        wall0 = time.perf_counter()
+        for i in range(args.steps):
+            flush.fill_(1)
+            starts[i].record(stream)
+            render(cg.CGPU_MODE_WAVEFRONT)
+            ends[i].record(stream)
+            launches += ctx.stats().kernel_launches
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+        if world > 1:
+            torch.distributed.barrier()
+        clk = clocks.stop()
+        step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+        total_ms = sum(step_ms)
+        if world > 1:
+            t = torch.tensor([total_ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(t.item())
+        samples_all = float(npix) * spp * args.steps * world
+        value = samples_all / (total_ms / 1e3)
+
+        # megakernel on the same frame and samples (equal estimator => equal relMSE)
+        mk_steps = max(1, min(2, args.steps))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        flush.fill_(1)
+        e0.record(stream)
+        for _ in range(mk_steps):
+            render(cg.CGPU_MODE_MEGAKERNEL)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        mk_value = float(npix) * spp * mk_steps / (e0.elapsed_time(e1) / 1e3)
+
+        # counting replay (same seeds, counters on) and per-kernel event timing
+        ctx.set_counting(True)
+        ctx.render([sid], first, 1, seed=2024, mode=cg.CGPU_MODE_WAVEFRONT, graph=False, sync=True)
+        st = ctx.stats()
+        ctx.set_counting(False)
+        ctx.set_profiling(True)
+        ctx.render([sid], first, 1, seed=2024, mode=cg.CGPU_MODE_WAVEFRONT, graph=False, sync=True)
+        kt = ctx.kernel_times()
+        ctx.set_profiling(False)
+
+        # end to end through the public API: render + film read-back into pinned host memory
+        film = torch.empty(npix * 7, dtype=torch.float64, pin_memory=True)
+        fs = film.numpy()
+        e2e_t = []
+        h2d = 0
+        for i in range(max(1, min(3, args.steps))):
+            t0 = time.perf_counter()
+            ctx.film_clear(sid)
+            ctx.render([sid], first, spp, seed=2024 + i, mode=cg.CGPU_MODE_WAVEFRONT, sync=False)
+            h2d = ctx.stats().h2d_bytes
+            ctx.film_read_into(sid, fs[:3 * npix], fs[3 * npix:6 * npix], fs[6 * npix:])
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_value = float(npix) * spp * world / statistics.mean(e2e_t)
+
+    # roofline of the dominant kernel (closest-hit traversal), algorithmic bytes:
+    # 32 B per 4-wide-node child slot (128 B node) + 48 B per triangle record + 64 B ray/hit queue I/O
+    ext_bytes = 128.0 * st.node_visits + 48.0 * st.triangle_tests + 64.0 * st.closest_rays
+    ext_ms, ext_launches = kt["extend"]
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = ext_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "extend_traffic.json")) as f:
+            tr = json.load(f)
+        # scale the captured per-launch traffic to this frame by closest rays
+        traffic = tr["dram_bytes_per_closest_ray"] * st.closest_rays / max(1, ext_launches)
+    except Exception:
+        pass
+    rays_per_sample = (st.closest_rays + st.any_rays) / float(npix)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        rate, cores, sample = cpu_rate(flat)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": spec.width,
+                   "height": spec.height, "spp": spp, "max_depth": spec.max_depth,
+                   "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
+                   "schedule": "wavefront, CUDA graph per batch", "l2": "256 MB buffer written between steps",
+                   "parallelism": "replicas" if world > 1 else "single"},
+        "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value},
+        "rays": {"closest_per_sample": st.closest_rays / float(npix), "any_per_sample": st.any_rays / float(npix),
+                 "mrays_per_s": value * rays_per_sample / 1e6},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_wf_extend (closest-hit traversal)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s"},
+        "kernel_ms_per_pass": {k: v[0] for k, v in kt.items()},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": npix * 7 * 8,
+                "path": "cgpu_film_clear + cgpu_render + cgpu_film_read into pinned host buffers"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "cpu_baseline": cpu,
+        "wall_s_timed": wall,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ---------------------------------------------------------- reference arm --
+def run_reference(args, rank, world, local):
+    """The reference's CPU path (its algorithm restated by the oracle, run
+    with every host thread) on bounded samples of the same frame."""
+    if rank != 0:
+        return
+    from cadise_gb300 import abi
+    import oracle
+    spec = make_scene(args)
+    flat = abi.flatten(spec)
+    threads = os.cpu_count() or 1
+    ps = oracle.PortScene(flat)
+    w, h = spec.width, spec.height
+    rows = 4
+    mid = h // 2
+    for i in range(args.warmup):
+        ps.render(seed=i, first=0, count=1, rows=(mid, mid + 1), threads=threads)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        r0 = (mid + i * rows) % (h - rows)
+        ps.render(seed=100 + i, first=i, count=1, rows=(r0, r0 + rows), threads=threads)
+    dt = time.perf_counter() - t0
+    samples = rows * w * args.steps
+    value = samples / dt
+    sample = "%d steps x %d rows x %d px x 1 spp of the frame" % (args.steps, rows, w)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": w, "height": h,
+                   "spp": spec.spp, "max_depth": spec.max_depth},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

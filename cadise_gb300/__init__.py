@@ -1,0 +1,239 @@
+"""cadise_gb300 - the reference renderer's unidirectional path tracer on GB300.
+
+The product is the C-ABI shared library ``_build/libcadise_gpu.so`` (header
+``include/cadise_gpu.h``): hand-written sm_103a kernels for BVH traversal,
+the NEE + MIS path estimator (megakernel and wavefront), the FP64 film and
+the adjoint.  This package is a thin ctypes view of that ABI for tests,
+benchmarks and Python callers; it never computes radiance itself and raises
+if the library is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional, Sequence
+
+import numpy as np
+
+from . import abi
+from .abi import (CGPU_MODE_MEGAKERNEL, CGPU_MODE_WAVEFRONT, FlatScene, cgpu_hit, cgpu_options,
+                  cgpu_ray, cgpu_render_params, cgpu_render_stats, cgpu_scene_info, flatten)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libcadise_gpu.so")
+
+# Every symbol include/cadise_gpu.h declares.
+EXPORTED = [
+    "cgpu_create", "cgpu_destroy", "cgpu_last_error", "cgpu_status_string", "cgpu_abi_version",
+    "cgpu_synchronize", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
+    "cgpu_trace_closest", "cgpu_trace_any", "cgpu_trace_closest_device", "cgpu_trace_any_device",
+    "cgpu_camera_rays", "cgpu_render", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
+    "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
+    "cgpu_kernel_times_get",
+]
+
+KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel"]
+
+_lib = None
+
+
+class CgpuError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__("%s: %s" % (abi.STATUS_NAMES.get(status, str(status)), message))
+        self.status = status
+
+
+def build(verbose: bool = False) -> str:
+    from .build import build as _build
+    return _build(verbose=verbose)
+
+
+def load(path: Optional[str] = None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError("cadise_gb300: CUDA library %s is not built; run cadise_gb300.build() "
+                           "(there is no CPU fallback)" % p)
+    L = C.CDLL(p)
+    vp = C.c_void_p
+    L.cgpu_create.argtypes = [C.POINTER(vp), C.POINTER(cgpu_options)]
+    L.cgpu_destroy.argtypes = [vp]
+    L.cgpu_destroy.restype = None
+    L.cgpu_last_error.argtypes = [vp]
+    L.cgpu_last_error.restype = C.c_char_p
+    L.cgpu_status_string.argtypes = [C.c_int]
+    L.cgpu_status_string.restype = C.c_char_p
+    L.cgpu_abi_version.restype = C.c_int32
+    L.cgpu_synchronize.argtypes = [vp]
+    L.cgpu_scene_upload.argtypes = [vp, vp, C.POINTER(C.c_int32)]
+    L.cgpu_scene_release.argtypes = [vp, C.c_int32]
+    L.cgpu_scene_info_get.argtypes = [vp, C.c_int32, C.POINTER(cgpu_scene_info)]
+    L.cgpu_trace_closest.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
+    L.cgpu_trace_any.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
+    L.cgpu_trace_closest_device.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
+    L.cgpu_trace_any_device.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
+    L.cgpu_camera_rays.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
+    L.cgpu_render.argtypes = [vp, C.POINTER(cgpu_render_params)]
+    L.cgpu_film_clear.argtypes = [vp, C.c_int32]
+    L.cgpu_film_read.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.cgpu_path_radiance.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, C.c_uint32, vp]
+    L.cgpu_render_paths.argtypes = [vp, C.c_int32, C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64, vp]
+    L.cgpu_render_stats_get.argtypes = [vp, C.POINTER(cgpu_render_stats)]
+    L.cgpu_set_counting.argtypes = [vp, C.c_int32]
+    L.cgpu_set_profiling.argtypes = [vp, C.c_int32]
+    L.cgpu_kernel_times_get.argtypes = [vp, C.POINTER(abi.cgpu_kernel_times)]
+    _lib = L
+    return L
+
+
+def _p(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One library context: one CUDA stream, any number of scenes."""
+
+    def __init__(self, device: int = 0, stream: Optional[int] = None, max_paths: int = 0):
+        self.L = load()
+        opt = cgpu_options(device=device, stream=stream or None, max_paths=max_paths, flags=0)
+        h = C.c_void_p()
+        st = self.L.cgpu_create(C.byref(h), C.byref(opt))
+        if st != 0:
+            raise CgpuError(st, "cgpu_create failed")
+        self.h = h
+        self._scenes = {}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int):
+        if st != 0:
+            raise CgpuError(st, self.L.cgpu_last_error(self.h).decode())
+
+    # ---------------------------------------------------------------- scenes
+    def upload(self, scene) -> int:
+        flat = scene if isinstance(scene, FlatScene) else flatten(scene)
+        sid = C.c_int32(-1)
+        self._check(self.L.cgpu_scene_upload(self.h, C.addressof(flat.desc), C.byref(sid)))
+        self._scenes[sid.value] = flat
+        return sid.value
+
+    def release(self, sid: int):
+        self._check(self.L.cgpu_scene_release(self.h, sid))
+        self._scenes.pop(sid, None)
+
+    def info(self, sid: int) -> cgpu_scene_info:
+        out = cgpu_scene_info()
+        self._check(self.L.cgpu_scene_info_get(self.h, sid, C.byref(out)))
+        return out
+
+    # ----------------------------------------------------------- ray queries
+    def trace_closest(self, sid: int, rays: np.ndarray):
+        """rays: (n, 8) float32 (org, t_min, dir, t_max) -> (prim, t, u, v)."""
+        r = np.ascontiguousarray(rays, dtype=np.float32)
+        n = r.shape[0]
+        out = np.zeros(n, dtype=[("t", "<f4"), ("prim", "<i4"), ("u", "<f4"), ("v", "<f4")])
+        self._check(self.L.cgpu_trace_closest(self.h, sid, _p(r), n, _p(out)))
+        return out["prim"].copy(), out["t"].copy(), out["u"].copy(), out["v"].copy()
+
+    def trace_any(self, sid: int, rays: np.ndarray) -> np.ndarray:
+        r = np.ascontiguousarray(rays, dtype=np.float32)
+        occ = np.zeros(r.shape[0], dtype=np.uint8)
+        self._check(self.L.cgpu_trace_any(self.h, sid, _p(r), r.shape[0], _p(occ)))
+        return occ
+
+    def camera_rays(self, sid: int, film_xy: np.ndarray) -> np.ndarray:
+        xy = np.ascontiguousarray(film_xy, dtype=np.float64)
+        out = np.zeros((xy.shape[0], 6), dtype=np.float32)
+        self._check(self.L.cgpu_camera_rays(self.h, sid, _p(xy), xy.shape[0], _p(out)))
+        return out
+
+    # ---------------------------------------------------------------- render
+    def path_radiance(self, sid: int, film_xy: np.ndarray, keys: np.ndarray, mode: int = CGPU_MODE_MEGAKERNEL):
+        xy = np.ascontiguousarray(film_xy, dtype=np.float64)
+        k = np.ascontiguousarray(keys, dtype=np.uint64)
+        out = np.zeros((xy.shape[0], 3), dtype=np.float32)
+        self._check(self.L.cgpu_path_radiance(self.h, sid, mode, _p(xy), _p(k), xy.shape[0], _p(out)))
+        return out
+
+    def render_paths(self, sid: int, first: int, count: int, seed: int, mode: int = CGPU_MODE_WAVEFRONT):
+        flat = self._scenes[sid]
+        w, h = flat.desc.width, flat.desc.height
+        out = np.zeros((count, h, w, 3), dtype=np.float32)
+        self._check(self.L.cgpu_render_paths(self.h, sid, mode, first, count, seed, _p(out)))
+        return out
+
+    def render(self, sids: Sequence[int], first: int, count: int, seed: int,
+               mode: int = CGPU_MODE_WAVEFRONT, graph: bool = True, sync: bool = True):
+        arr = (C.c_int32 * len(sids))(*sids)
+        p = cgpu_render_params(scenes=arr, num_scenes=len(sids), first_sample=first, num_samples=count,
+                               seed=seed, mode=mode, use_graph=1 if graph else 0)
+        self._check(self.L.cgpu_render(self.h, C.byref(p)))
+        if sync:
+            self.synchronize()
+
+    def synchronize(self):
+        self._check(self.L.cgpu_synchronize(self.h))
+
+    def film_clear(self, sid: int):
+        self._check(self.L.cgpu_film_clear(self.h, sid))
+
+    def film_read(self, sid: int):
+        flat = self._scenes[sid]
+        w, h = flat.desc.width, flat.desc.height
+        s = np.zeros((h, w, 3))
+        q = np.zeros((h, w, 3))
+        n = np.zeros((h, w))
+        self._check(self.L.cgpu_film_read(self.h, sid, _p(s), _p(q), _p(n)))
+        return s, q, n
+
+    def film_read_into(self, sid: int, sum_rgb: np.ndarray, sum_sq_rgb: np.ndarray, count: np.ndarray):
+        """Film read-back into caller buffers (e.g. pinned host memory)."""
+        flat = self._scenes[sid]
+        n = flat.desc.width * flat.desc.height
+        for a, k in ((sum_rgb, 3), (sum_sq_rgb, 3), (count, 1)):
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != n * k:
+                raise ValueError("film_read_into: need contiguous float64 buffers of the film size")
+        self._check(self.L.cgpu_film_read(self.h, sid, _p(sum_rgb), _p(sum_sq_rgb), _p(count)))
+
+    def stats(self) -> cgpu_render_stats:
+        out = cgpu_render_stats()
+        self._check(self.L.cgpu_render_stats_get(self.h, C.byref(out)))
+        return out
+
+    def set_counting(self, on: bool):
+        self._check(self.L.cgpu_set_counting(self.h, 1 if on else 0))
+
+    def set_profiling(self, on: bool):
+        self._check(self.L.cgpu_set_profiling(self.h, 1 if on else 0))
+
+    def kernel_times(self):
+        """{class: (total ms, launches)} of the last render with profiling on."""
+        out = abi.cgpu_kernel_times()
+        self._check(self.L.cgpu_kernel_times_get(self.h, C.byref(out)))
+        return {name: (out.ms[i], out.launches[i]) for i, name in enumerate(KERNEL_CLASSES)}
+
+
+def gpu_available() -> bool:
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False

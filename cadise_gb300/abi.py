@@ -98,7 +98,12 @@ class cgpu_render_params(C.Structure):
 class cgpu_render_stats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("closest_rays", C.c_uint64), ("any_rays", C.c_uint64),
                 ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64),
-                ("kernel_launches", C.c_uint32), ("timeouts", C.c_uint32)]
+                ("any_node_visits", C.c_uint64), ("any_triangle_tests", C.c_uint64),
+                ("h2d_bytes", C.c_uint64), ("kernel_launches", C.c_uint32), ("batches", C.c_uint32)]
+
+
+class cgpu_kernel_times(C.Structure):
+    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint32 * 8)]
 
 
 def _fptr(a: np.ndarray):
@@ -146,8 +151,8 @@ def flatten(spec: "S.SceneSpec") -> FlatScene:
     names: Dict[str, int] = {}
     i = 0
     for p in spec.primitives:
-        if isinstance(p, S.Rectangle):
-            kind[i] = CGPU_PRIM_RECTANGLE
+        if isinstance(p, (S.Rectangle, S.Triangle)):
+            kind[i] = CGPU_PRIM_RECTANGLE if isinstance(p, S.Rectangle) else CGPU_PRIM_TRIANGLE
             verts[i] = np.array([*p.v1, *p.v2, *p.v3], dtype=np.float32)
             mat[i] = mat_index[p.material]
             names.setdefault(p.name, i)

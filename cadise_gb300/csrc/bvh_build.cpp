@@ -1,0 +1,268 @@
+// Host BVH build: binned SAH binary tree, collapsed to the 4-wide layout of
+// scene_device.cuh.
+//
+// Replaces BvhBuilder (source/core/intersector/accelerator/bvh/bvhBuilder.cpp:18-358),
+// a serial recursive SAH over 12 buckets with one primitive per leaf that
+// copies its BvhBoundInfo vectors at every level.  Here: 32 bins per axis on
+// all three axes, leaves of up to 4 triangles (8 when the SAH cannot split),
+// in-place partition of one index array, subtrees above 32k triangles built
+// on separate host threads, then a greedy collapse (open the child with the
+// largest surface area until four children) into 128-byte 4-wide nodes.
+#include "bvh_build.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <cmath>
+#include <cstring>
+#include <thread>
+
+namespace cg {
+namespace {
+
+struct Box {
+    float lo[3], hi[3];
+    void reset() {
+        for (int k = 0; k < 3; ++k) { lo[k] = FLT_MAX; hi[k] = -FLT_MAX; }
+    }
+    void grow(const Box& b) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], b.lo[k]); hi[k] = std::max(hi[k], b.hi[k]); }
+    }
+    void grow(const float* p) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
+    }
+    float half_area() const {
+        const float dx = hi[0] - lo[0], dy = hi[1] - lo[1], dz = hi[2] - lo[2];
+        if (dx < 0 || dy < 0 || dz < 0) return 0.0f;
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+struct BinNode {
+    Box box;
+    int left = -1, right = -1;
+    uint32_t first = 0, count = 0;  // leaf when left < 0
+};
+
+constexpr int kBins = 32;
+constexpr uint32_t kLeafTarget = 4;
+constexpr uint32_t kParallelMin = 32768;
+
+struct Builder {
+    const Box* boxes;
+    const float* cent;  // 3 per triangle
+    uint32_t* idx;
+    std::vector<BinNode> nodes;
+    std::atomic<int> next_node{0};
+    std::atomic<int> threads_live{0};
+    int max_threads;
+    std::atomic<int> max_depth{0};
+
+    int alloc() { return next_node.fetch_add(1); }
+
+    void build(int ni, uint32_t begin, uint32_t end, int depth) {
+        BinNode& node = nodes[ni];
+        Box box, cbox;
+        box.reset();
+        cbox.reset();
+        for (uint32_t i = begin; i < end; ++i) {
+            box.grow(boxes[idx[i]]);
+            cbox.grow(cent + 3 * size_t(idx[i]));
+        }
+        node.box = box;
+        const uint32_t n = end - begin;
+        int d = max_depth.load();
+        while (depth > d && !max_depth.compare_exchange_weak(d, depth)) {
+        }
+        auto make_leaf = [&]() {
+            node.left = node.right = -1;
+            node.first = begin;
+            node.count = n;
+        };
+        if (n <= 1) return make_leaf();
+        // binned SAH over all three axes
+        float best_cost = FLT_MAX;
+        int best_axis = -1, best_split = -1;
+        for (int ax = 0; ax < 3; ++ax) {
+            const float ext = cbox.hi[ax] - cbox.lo[ax];
+            if (!(ext > 0.0f)) continue;
+            const float scale = float(kBins) / ext;
+            Box bb[kBins];
+            uint32_t bc[kBins] = {0};
+            for (int b = 0; b < kBins; ++b) bb[b].reset();
+            for (uint32_t i = begin; i < end; ++i) {
+                const uint32_t t = idx[i];
+                int b = int((cent[3 * size_t(t) + ax] - cbox.lo[ax]) * scale);
+                b = std::min(std::max(b, 0), kBins - 1);
+                bc[b]++;
+                bb[b].grow(boxes[t]);
+            }
+            float ra[kBins];
+            uint32_t rc[kBins];
+            Box acc;
+            acc.reset();
+            uint32_t cnt = 0;
+            for (int b = kBins - 1; b > 0; --b) {
+                acc.grow(bb[b]);
+                cnt += bc[b];
+                ra[b] = acc.half_area();
+                rc[b] = cnt;
+            }
+            acc.reset();
+            cnt = 0;
+            for (int b = 0; b < kBins - 1; ++b) {
+                acc.grow(bb[b]);
+                cnt += bc[b];
+                if (cnt == 0 || rc[b + 1] == 0) continue;
+                const float cost = acc.half_area() * float(cnt) + ra[b + 1] * float(rc[b + 1]);
+                if (cost < best_cost) {
+                    best_cost = cost;
+                    best_axis = ax;
+                    best_split = b;
+                }
+            }
+        }
+        const float parent_area = box.half_area();
+        const float leaf_cost = float(n);
+        const float split_cost = parent_area > 0.0f ? 1.0f + best_cost / parent_area : FLT_MAX;
+        uint32_t mid;
+        if (best_axis < 0) {
+            // all centroids coincide: object median by index
+            if (n <= kMaxLeafTris) return make_leaf();
+            mid = begin + n / 2;
+        } else {
+            if (n <= kLeafTarget && leaf_cost <= split_cost) return make_leaf();
+            const float ext = cbox.hi[best_axis] - cbox.lo[best_axis];
+            const float scale = float(kBins) / ext;
+            uint32_t* m = std::partition(idx + begin, idx + end, [&](uint32_t t) {
+                int b = int((cent[3 * size_t(t) + best_axis] - cbox.lo[best_axis]) * scale);
+                b = std::min(std::max(b, 0), kBins - 1);
+                return b <= best_split;
+            });
+            mid = uint32_t(m - idx);
+            if (mid == begin || mid == end) mid = begin + n / 2;
+        }
+        const int l = alloc(), r = alloc();
+        node.left = l;
+        node.right = r;
+        node.count = 0;
+        const bool spawn = (mid - begin) >= kParallelMin && (end - mid) >= kParallelMin &&
+                           threads_live.fetch_add(1) < max_threads;
+        if (spawn) {
+            std::thread t([this, l, begin, mid, depth]() { build(l, begin, mid, depth + 1); });
+            build(r, mid, end, depth + 1);
+            t.join();
+            threads_live.fetch_sub(1);
+        } else {
+            if ((mid - begin) >= kParallelMin && (end - mid) >= kParallelMin) threads_live.fetch_sub(1);
+            build(l, begin, mid, depth + 1);
+            build(r, mid, end, depth + 1);
+        }
+    }
+};
+
+void set_empty(Bvh4Node& n, int i) {
+    n.lox[i] = n.loy[i] = n.loz[i] = INFINITY;
+    n.hix[i] = n.hiy[i] = n.hiz[i] = -INFINITY;
+    n.child[i] = 0;
+}
+
+}  // namespace
+
+bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, std::string* err) {
+    out->nodes.clear();
+    out->order.clear();
+    if (num_tris == 0) {
+        *err = "scene has no triangles";
+        return false;
+    }
+    if (num_tris > kMaxTriSlots) {
+        *err = "too many triangles for the 28-bit leaf encoding";
+        return false;
+    }
+    std::vector<Box> boxes(num_tris);
+    std::vector<float> cent(size_t(num_tris) * 3);
+    for (uint32_t t = 0; t < num_tris; ++t) {
+        Box b;
+        b.reset();
+        const float* v = tri_vertices + 9 * size_t(t);
+        b.grow(v);
+        b.grow(v + 3);
+        b.grow(v + 6);
+        boxes[t] = b;
+        for (int k = 0; k < 3; ++k) cent[3 * size_t(t) + k] = 0.5f * (b.lo[k] + b.hi[k]);
+    }
+    out->order.resize(num_tris);
+    for (uint32_t t = 0; t < num_tris; ++t) out->order[t] = t;
+    Builder B;
+    B.boxes = boxes.data();
+    B.cent = cent.data();
+    B.idx = out->order.data();
+    B.nodes.resize(size_t(num_tris) * 2);
+    const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+    B.max_threads = int(hw) * 2;
+    const int root = B.alloc();
+    B.build(root, 0, num_tris, 0);
+    const std::vector<BinNode>& bn = B.nodes;
+    out->binary_depth = B.max_depth.load();
+
+    // collapse into 4-wide nodes (breadth-first ids, root = 0)
+    struct Item { int bin; int wide; int depth; };
+    std::vector<Item> work;
+    out->nodes.emplace_back();
+    work.push_back({root, 0, 1});
+    size_t head = 0;
+    int wide_depth = 1;
+    while (head < work.size()) {
+        const Item it = work[head++];
+        wide_depth = std::max(wide_depth, it.depth);
+        int kids[4];
+        int nk = 0;
+        const BinNode& b = bn[it.bin];
+        if (b.left < 0) {
+            kids[nk++] = it.bin;  // a leaf root: one leaf child
+        } else {
+            kids[nk++] = b.left;
+            kids[nk++] = b.right;
+            while (nk < 4) {
+                int pick = -1;
+                float area = -1.0f;
+                for (int k = 0; k < nk; ++k) {
+                    const BinNode& c = bn[kids[k]];
+                    if (c.left >= 0 && c.box.half_area() > area) {
+                        area = c.box.half_area();
+                        pick = k;
+                    }
+                }
+                if (pick < 0) break;
+                const BinNode& c = bn[kids[pick]];
+                kids[pick] = c.left;
+                kids[nk++] = c.right;
+            }
+        }
+        Bvh4Node wn;
+        std::memset(&wn, 0, sizeof(wn));
+        for (int k = 0; k < 4; ++k) {
+            if (k >= nk) {
+                set_empty(wn, k);
+                continue;
+            }
+            const BinNode& c = bn[kids[k]];
+            wn.lox[k] = c.box.lo[0]; wn.loy[k] = c.box.lo[1]; wn.loz[k] = c.box.lo[2];
+            wn.hix[k] = c.box.hi[0]; wn.hiy[k] = c.box.hi[1]; wn.hiz[k] = c.box.hi[2];
+            if (c.left < 0) {
+                wn.child[k] = make_leaf(c.first, c.count);
+            } else {
+                const int id = int(out->nodes.size());
+                out->nodes.emplace_back();
+                work.push_back({kids[k], id, it.depth + 1});
+                wn.child[k] = uint32_t(id);
+            }
+        }
+        out->nodes[size_t(it.wide)] = wn;
+    }
+    out->wide_depth = wide_depth;
+    return true;
+}
+
+}  // namespace cg

@@ -1,0 +1,23 @@
+// Host BVH build into the 4-wide device layout (see scene_device.cuh).
+#pragma once
+
+#include "scene_device.cuh"
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+namespace cg {
+
+struct Bvh4Result {
+    std::vector<Bvh4Node> nodes;  // root at 0
+    std::vector<uint32_t> order;  // leaf order -> input triangle index
+    int binary_depth = 0;
+    int wide_depth = 0;
+};
+
+// tri_vertices: 9 floats per triangle.  Returns false (with a message) on
+// empty or oversized input.
+bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, std::string* err);
+
+}  // namespace cg

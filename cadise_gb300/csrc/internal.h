@@ -1,0 +1,137 @@
+// Library-internal state behind the C ABI (not installed, not part of the ABI).
+#pragma once
+
+#include "../../include/cadise_gpu.h"
+#include "scene_device.cuh"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+namespace cg {
+
+// One render chunk: samples [sample0, sample0 + nsamples) of every pixel of
+// one scene; its paths occupy [path_begin, path_begin + npix * nsamples) of
+// the batch, sample-major (path = path_begin + s * npix + pixel).
+struct Chunk {
+    int scene;
+    uint32_t path_begin;
+    uint32_t npix;
+    uint32_t width;
+    uint32_t sample0;
+    uint32_t nsamples;
+    uint32_t pix_begin;  // prefix over chunks of npix (film splat index space)
+    uint32_t pad;
+};
+constexpr int kMaxChunks = 256;
+
+struct BatchHeader {
+    uint32_t num_chunks;
+    uint32_t total_paths;
+    uint32_t total_pixels;
+    int max_depth;
+    uint64_t seed;
+};
+
+struct FilmD {
+    double* sum;    // 3 per pixel
+    double* sumsq;  // 3 per pixel
+    double* count;  // 1 per pixel
+};
+
+// Counters per bounce b at cnt[b * kCntStride + k]:
+//   k = 0 continuation rays to extend, 1 MIS rays to extend, 2 shadow rays,
+//   3 + kind: hits waiting for the shade kernel of that BSDF kind.
+constexpr int kCntStride = 8;
+
+struct WfBuffers {
+    float4 *ray_o, *ray_d, *hit, *thr, *L, *Ls, *mis_a, *mis_b, *mis_d, *sh_d, *sh_c;
+    uint4* meta;      // scene, pixel, sample, rng counter
+    int* q_cont[2];
+    int* q_mis[2];
+    int* q_shadow[2];
+    int* q_mat[kNumBsdfKinds];
+    int* cnt;
+    int cnt_depth;    // bounces the counter array covers
+};
+
+struct RenderArgs {
+    const SceneD* scenes;
+    const Chunk* chunks;
+    const BatchHeader* header;
+    FilmD* films;     // per scene id
+    WfBuffers wf;
+    unsigned long long* counters;  // closest rays, any rays, nodes, tris, paths
+};
+
+}  // namespace cg
+
+struct SceneSlot {
+    bool live = false;
+    cg::SceneD d{};
+    std::vector<void*> allocations;
+    cgpu_scene_info info{};
+    cg::FilmD film{};
+    int width = 0, height = 0, spp = 1, max_depth = 1;
+};
+
+struct cgpu_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t side = nullptr;  // second stream for graph branches
+    bool own_stream = false;
+    std::string last_error;
+    std::vector<SceneSlot> scenes;
+    int num_sms = 0;
+    uint32_t max_paths_opt = 0;
+    bool counting = false;
+
+    // device tables (rebuilt when the scene set changes)
+    cg::SceneD* d_scenes = nullptr;
+    cg::FilmD* d_films = nullptr;
+    int table_cap = 0;
+    bool tables_dirty = true;
+
+    // batch description
+    cg::Chunk* d_chunks = nullptr;
+    cg::BatchHeader* d_header = nullptr;
+    cg::Chunk* h_chunks = nullptr;        // pinned
+    cg::BatchHeader* h_header = nullptr;  // pinned
+
+    // per-path buffers
+    uint32_t path_cap = 0;
+    cg::WfBuffers wf{};
+    void* wf_block = nullptr;
+    unsigned long long* d_counters = nullptr;
+
+    // captured wavefront graph
+    cudaGraphExec_t graph = nullptr;
+    int graph_depth = -1;
+    uint32_t graph_paths = 0;
+
+    cgpu_render_stats stats{};
+
+    // per-kernel event timing (cgpu_set_profiling)
+    bool profiling = false;
+    struct ProfEvent { int cls; cudaEvent_t a, b; };
+    std::vector<ProfEvent> prof;
+    cgpu_kernel_times times{};
+};
+
+// implemented in render.cu
+cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p);
+cgpu_status cg_render_paths_raw(cgpu_ctx* ctx, int scene, int mode, uint32_t first, uint32_t count, uint64_t seed,
+                                float* host_rgb);
+cgpu_status cg_path_radiance(cgpu_ctx* ctx, int scene, int mode, const double* film_xy, const uint64_t* keys,
+                             uint32_t n, float* out_rgb);
+cgpu_status cg_trace(cgpu_ctx* ctx, int scene, const cgpu_ray* d_rays, uint32_t n, cgpu_hit* d_hits,
+                     uint8_t* d_occ, bool any);
+cgpu_status cg_camera(cgpu_ctx* ctx, int scene, const double* d_xy, uint32_t n, float* d_out);
+cgpu_status cg_film_clear(cgpu_ctx* ctx, int scene);
+void cg_free_render_state(cgpu_ctx* ctx);
+
+// implemented in api.cu
+cgpu_status cg_fail(cgpu_ctx* ctx, cgpu_status s, const std::string& msg);
+cgpu_status cg_cuda(cgpu_ctx* ctx, cudaError_t e, const char* what);
+cgpu_status cg_sync_tables(cgpu_ctx* ctx);

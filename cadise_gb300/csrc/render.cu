@@ -1,0 +1,804 @@
+// Render kernels: the FP32 megakernel, the wavefront stages, the FP64 film
+// splat and the batched ray-query / camera kernels behind the C ABI.
+//
+// Replaces SamplingRenderer::render + EstimatorTileWork::work
+// (source/core/renderer/sampling/samplingRenderer.cpp:33-68,
+// source/core/renderer/render-work/estimatorTileWork.cpp:32-61): instead of
+// tiles over host threads, a batch holds every path sample of one or more
+// scenes for a range of sample indices; each path is independent and owns a
+// counter-based random stream keyed by (seed, scene, pixel, sample).
+//
+// Wavefront schedule of one batch (replayed as one CUDA graph):
+//   generate -> for b in [0, max_depth): { extend(b) || shadow(b) ; shade_k(b) for each BSDF kind }
+//            -> extend(max_depth) || shadow(max_depth) -> splat
+// Queues hold path ids; per-path state lives in SoA arrays indexed by path.
+// Queue appends are warp-aggregated (ballot / match + one atomic per group).
+#include "internal.h"
+#include "shading.cuh"
+
+#include <algorithm>
+#include <cstring>
+
+namespace cg {
+
+struct PathId {
+    int scene;
+    uint32_t pixel, sample, width;
+};
+
+CG_D int find_chunk(const Chunk* ch, int n, uint32_t p) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (ch[mid].path_begin <= p) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+CG_D PathId path_id(const Chunk* chunks, int nchunks, uint32_t p) {
+    const Chunk& c = chunks[find_chunk(chunks, nchunks, p)];
+    const uint32_t local = p - c.path_begin;
+    PathId id;
+    id.scene = c.scene;
+    id.sample = c.sample0 + local / c.npix;
+    id.pixel = local % c.npix;
+    id.width = c.width;
+    return id;
+}
+
+CG_D void primary_ray(const SceneD& S, const PathId& id, uint64_t seed, Rng& rng, float3* o, float3* d) {
+    rng.key = path_key(seed, uint32_t(id.scene), id.pixel, id.sample);
+    rng.ctr = 0;
+    float jx, jy;
+    stratum_jitter(S.spp, id.sample, rng, &jx, &jy);
+    const float fx = float(id.pixel % id.width) + jx;
+    const float fy = float(id.pixel / id.width) + jy;
+    camera_ray(S.cam, fx, fy, o, d);
+}
+
+CG_D int light_of_slot(const SceneD& S, int slot) {
+    const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
+    return int(__float_as_uint(ldg4(tp + 1).w) >> 16) - 1;
+}
+CG_D int material_of_slot(const SceneD& S, int slot) {
+    const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
+    return int(__float_as_uint(ldg4(tp + 1).w) & 0xFFFFu);
+}
+
+// Counting replay: [0] closest rays, [1] any-hit rays, [2] / [3] 4-wide
+// nodes / triangles fetched by closest-hit rays, [4] / [5] by any-hit rays.
+template <bool COUNT>
+CG_D void count_flush(unsigned long long* counters, const TraceCounters& cc, const TraceCounters& ca, uint32_t closest,
+                      uint32_t any) {
+    if (!COUNT) return;
+    if (closest) atomicAdd(counters + 0, (unsigned long long)closest);
+    if (any) atomicAdd(counters + 1, (unsigned long long)any);
+    if (cc.nodes) atomicAdd(counters + 2, (unsigned long long)cc.nodes);
+    if (cc.tris) atomicAdd(counters + 3, (unsigned long long)cc.tris);
+    if (ca.nodes) atomicAdd(counters + 4, (unsigned long long)ca.nodes);
+    if (ca.tris) atomicAdd(counters + 5, (unsigned long long)ca.tris);
+}
+
+// One whole path sample (PtEstimator::estimate): the megakernel body.
+template <bool COUNT>
+CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, float3* Lsout, TraceCounters* tc,
+                  TraceCounters* ta, uint32_t* nclosest, uint32_t* nany) {
+    float3 L = splat3(0.0f), Ls = splat3(0.0f), T = splat3(1.0f);
+    bool ce = true;
+    for (int b = 0; b < S.max_depth; ++b) {
+        const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
+        HitD hit;
+        if (COUNT) ++*nclosest;
+        if (!traverse<false, COUNT>(S, r, &hit, tc)) break;
+        const SurfaceD si = surface_at(S, o, d, hit);
+        const VertexPlan pl = plan_vertex(S, si, T, ce, b, rng);
+        L += pl.emit;
+        if (pl.shadow) {
+            const RayPre sr = ray_prep(si.P, pl.sdir, kRayEps, pl.stmax);
+            HitD sh;
+            if (COUNT) ++*nany;
+            if (!traverse<true, COUNT>(S, sr, &sh, ta)) Ls += pl.scontrib;
+        }
+        if (pl.mis) {
+            const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
+            HitD mh;
+            if (COUNT) ++*nclosest;
+            if (traverse<false, COUNT>(S, mr, &mh, tc) && light_of_slot(S, mh.slot) == pl.mlight) {
+                const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
+                L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);
+            }
+        }
+        if (!pl.cont) break;
+        T = pl.T;
+        ce = pl.count_emission != 0;
+        o = si.P;
+        d = pl.cdir;
+    }
+    *Lout = L;
+    *Lsout = Ls;
+}
+
+template <bool COUNT>
+__global__ void k_megakernel(RenderArgs a) {
+    const BatchHeader h = *a.header;
+    TraceCounters tc{0, 0}, ta{0, 0};
+    uint32_t nc = 0, na = 0;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < h.total_paths; p += gridDim.x * blockDim.x) {
+        const PathId id = path_id(a.chunks, int(h.num_chunks), p);
+        const SceneD& S = a.scenes[id.scene];
+        Rng rng;
+        float3 o, d;
+        primary_ray(S, id, h.seed, rng, &o, &d);
+        float3 L, Ls;
+        mk_path<COUNT>(S, o, d, rng, &L, &Ls, &tc, &ta, &nc, &na);
+        a.wf.L[p] = make_float4(L.x, L.y, L.z, 0.0f);
+        a.wf.Ls[p] = make_float4(Ls.x, Ls.y, Ls.z, 0.0f);
+    }
+    count_flush<COUNT>(a.counters, tc, ta, nc, na);
+}
+
+// Per-path estimate for explicit film positions and keys (stream from draw 0).
+__global__ void k_paths_explicit(const SceneD* scenes, int scene, const double* xy, const uint64_t* keys, uint32_t n,
+                                 float* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const SceneD& S = scenes[scene];
+        Rng rng;
+        rng.key = keys[i];
+        rng.ctr = 0;
+        float3 o, d;
+        camera_ray(S.cam, float(xy[2 * i]), float(xy[2 * i + 1]), &o, &d);
+        float3 L, Ls;
+        TraceCounters tc{0, 0}, ta{0, 0};
+        uint32_t nc = 0, na = 0;
+        mk_path<false>(S, o, d, rng, &L, &Ls, &tc, &ta, &nc, &na);
+        out[3 * i + 0] = L.x + Ls.x;
+        out[3 * i + 1] = L.y + Ls.y;
+        out[3 * i + 2] = L.z + Ls.z;
+    }
+}
+
+// ---------------------------------------------------------------- wavefront --
+__global__ void k_wf_generate(RenderArgs a) {
+    const BatchHeader h = *a.header;
+    const WfBuffers& w = a.wf;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < h.total_paths; p += gridDim.x * blockDim.x) {
+        const PathId id = path_id(a.chunks, int(h.num_chunks), p);
+        const SceneD& S = a.scenes[id.scene];
+        Rng rng;
+        float3 o, d;
+        primary_ray(S, id, h.seed, rng, &o, &d);
+        w.ray_o[p] = make_float4(o.x, o.y, o.z, 0.0f);
+        w.ray_d[p] = make_float4(d.x, d.y, d.z, 0.0f);
+        w.thr[p] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(1));
+        w.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.Ls[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.meta[p] = make_uint4(uint32_t(id.scene), id.pixel, id.sample, rng.ctr);
+        w.q_cont[0][p] = int(p);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.cnt[0] = int(h.total_paths);
+}
+
+// Append `p` to queue `key` (key < 0: no append); one atomic per group of
+// lanes sharing a key.
+CG_D void grouped_push(int* const* queues, int* counters, int key, int p) {
+    const unsigned active = __activemask();
+    const unsigned grp = __match_any_sync(active, key);
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(grp) - 1;
+    int base = 0;
+    if (lane == leader && key >= 0) base = atomicAdd(counters + key, __popc(grp));
+    base = __shfl_sync(grp, base, leader);
+    if (key >= 0) queues[key][base + __popc(grp & ((1u << lane) - 1u))] = p;
+}
+
+template <bool COUNT>
+__global__ void k_wf_extend(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    int* cnt = w.cnt + b * kCntStride;
+    const int ncont = cnt[0], nmis = cnt[1];
+    const int n = ncont + nmis;
+    const int* qc = w.q_cont[b & 1];
+    const int* qm = w.q_mis[b & 1];
+    TraceCounters tc{0, 0};
+    uint32_t nclosest = 0;
+    int* const* qmat = w.q_mat;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        int key = -1;
+        int p;
+        if (i < ncont) {
+            p = qc[i];
+            const SceneD& S = a.scenes[w.meta[p].x];
+            const float3 o = f3(w.ray_o[p]), d = f3(w.ray_d[p]);
+            const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
+            HitD hit;
+            if (COUNT) ++nclosest;
+            if (traverse<false, COUNT>(S, r, &hit, &tc)) {
+                w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
+                key = S.materials[material_of_slot(S, hit.slot)].type;
+            }
+        } else {
+            p = qm[i - ncont];
+            const SceneD& S = a.scenes[w.meta[p].x];
+            const float3 o = f3(w.ray_o[p]);
+            const float3 md = f3(w.mis_d[p]);
+            const RayPre r = ray_prep(o, md, kRayEps, kFloatMax);
+            HitD hit;
+            if (COUNT) ++nclosest;
+            if (traverse<false, COUNT>(S, r, &hit, &tc)) {
+                const float4 mb = w.mis_b[p];
+                if (light_of_slot(S, hit.slot) == __float_as_int(mb.w)) {
+                    const SurfaceD hs = surface_at(S, o, md, hit);
+                    const float4 ma = w.mis_a[p];
+                    const float3 add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w);
+                    float4 L = w.L[p];
+                    L.x += add.x;
+                    L.y += add.y;
+                    L.z += add.z;
+                    w.L[p] = L;
+                }
+            }
+        }
+        grouped_push(qmat, cnt + 3, key, p);
+    }
+    count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
+}
+
+template <bool COUNT>
+__global__ void k_wf_shadow(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    const int n = w.cnt[b * kCntStride + 2];
+    const int* q = w.q_shadow[b & 1];
+    TraceCounters tc{0, 0};
+    uint32_t nany = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = q[i];
+        const SceneD& S = a.scenes[w.meta[p].x];
+        const float4 sd = w.sh_d[p];
+        const RayPre r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
+        HitD hit;
+        if (COUNT) ++nany;
+        if (!traverse<true, COUNT>(S, r, &hit, &tc)) {
+            const float4 c = w.sh_c[p];
+            float4 Ls = w.Ls[p];
+            Ls.x += c.x;
+            Ls.y += c.y;
+            Ls.z += c.z;
+            w.Ls[p] = Ls;
+        }
+    }
+    count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
+}
+
+template <int KIND>
+__global__ void k_wf_shade(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    const int n = w.cnt[b * kCntStride + 3 + KIND];
+    int* next = w.cnt + (b + 1) * kCntStride;
+    const int* q = w.q_mat[KIND];
+    const int nb = (b + 1) & 1;
+    const uint64_t seed = a.header->seed;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = q[i];
+        uint4 meta = w.meta[p];
+        const SceneD& S = a.scenes[meta.x];
+        const float3 o = f3(w.ray_o[p]), d = f3(w.ray_d[p]);
+        const float4 h4 = w.hit[p];
+        HitD hit;
+        hit.t = h4.x;
+        hit.slot = __float_as_int(h4.y);
+        hit.u = h4.z;
+        hit.v = h4.w;
+        const SurfaceD si = surface_at(S, o, d, hit);
+        const float4 tw = w.thr[p];
+        Rng rng;
+        rng.key = path_key(seed, meta.x, meta.y, meta.z);
+        rng.ctr = meta.w;
+        const VertexPlan pl = plan_vertex(S, si, f3(tw), (__float_as_int(tw.w) & 1) != 0, b, rng);
+        if (!is_zero(pl.emit)) {
+            float4 L = w.L[p];
+            L.x += pl.emit.x;
+            L.y += pl.emit.y;
+            L.z += pl.emit.z;
+            w.L[p] = L;
+        }
+        const bool cont = pl.cont && (b + 1 < S.max_depth);
+        if (pl.shadow || pl.mis || cont) w.ray_o[p] = make_float4(si.P.x, si.P.y, si.P.z, 0.0f);
+        if (pl.shadow) {
+            w.sh_d[p] = make_float4(pl.sdir.x, pl.sdir.y, pl.sdir.z, pl.stmax);
+            w.sh_c[p] = make_float4(pl.scontrib.x, pl.scontrib.y, pl.scontrib.z, 0.0f);
+        }
+        if (pl.mis) {
+            w.mis_d[p] = make_float4(pl.mdir.x, pl.mdir.y, pl.mdir.z, 0.0f);
+            w.mis_a[p] = make_float4(pl.mfactor.x, pl.mfactor.y, pl.mfactor.z, pl.mpdf);
+            w.mis_b[p] = make_float4(tw.x, tw.y, tw.z, __int_as_float(pl.mlight));
+        }
+        if (cont) {
+            w.ray_d[p] = make_float4(pl.cdir.x, pl.cdir.y, pl.cdir.z, 0.0f);
+            w.thr[p] = make_float4(pl.T.x, pl.T.y, pl.T.z, __int_as_float(pl.count_emission));
+        }
+        meta.w = rng.ctr;
+        w.meta[p] = meta;
+        const int s_slot = warp_append(next + 2, pl.shadow != 0);
+        if (s_slot >= 0) w.q_shadow[nb][s_slot] = p;
+        const int m_slot = warp_append(next + 1, pl.mis != 0);
+        if (m_slot >= 0) w.q_mis[nb][m_slot] = p;
+        const int c_slot = warp_append(next + 0, cont);
+        if (c_slot >= 0) w.q_cont[nb][c_slot] = p;
+    }
+}
+
+// FP64 accumulation of one batch into the scenes' films (box filter of
+// width 1: a sample at (ix + fx, iy + fy) lands in pixel (ix, iy) only);
+// NaN / Inf samples are dropped as FilmTile::addSample does
+// (source/core/film/filmTile.cpp:21-28).
+__global__ void k_splat(RenderArgs a) {
+    const BatchHeader h = *a.header;
+    for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < h.total_pixels; idx += gridDim.x * blockDim.x) {
+        int lo = 0, hi = int(h.num_chunks) - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.chunks[mid].pix_begin <= idx) lo = mid; else hi = mid - 1;
+        }
+        const Chunk c = a.chunks[lo];
+        const uint32_t pixel = idx - c.pix_begin;
+        double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0, n = 0;
+        for (uint32_t k = 0; k < c.nsamples; ++k) {
+            const uint32_t p = c.path_begin + k * c.npix + pixel;
+            const float4 L = a.wf.L[p], Ls = a.wf.Ls[p];
+            const float x = L.x + Ls.x, y = L.y + Ls.y, z = L.z + Ls.z;
+            if (!(isfinite(x) && isfinite(y) && isfinite(z))) continue;
+            s0 += x; s1 += y; s2 += z;
+            q0 += double(x) * x; q1 += double(y) * y; q2 += double(z) * z;
+            n += 1.0;
+        }
+        const FilmD f = a.films[c.scene];
+        f.sum[3 * pixel + 0] += s0;
+        f.sum[3 * pixel + 1] += s1;
+        f.sum[3 * pixel + 2] += s2;
+        f.sumsq[3 * pixel + 0] += q0;
+        f.sumsq[3 * pixel + 1] += q1;
+        f.sumsq[3 * pixel + 2] += q2;
+        f.count[pixel] += n;
+    }
+}
+
+__global__ void k_gather_paths(const float4* L, const float4* Ls, uint32_t n, float* out) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+        const float4 a = L[p], b = Ls[p];
+        out[3 * p + 0] = a.x + b.x;
+        out[3 * p + 1] = a.y + b.y;
+        out[3 * p + 2] = a.z + b.z;
+    }
+}
+
+// ------------------------------------------------------------- ray queries --
+__global__ void k_trace(const SceneD* scenes, int scene, const cgpu_ray* rays, uint32_t n, cgpu_hit* hits,
+                        uint8_t* occ) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const SceneD& S = scenes[scene];
+        const cgpu_ray r = rays[i];
+        const RayPre pr = ray_prep(mk(r.org[0], r.org[1], r.org[2]), mk(r.dir[0], r.dir[1], r.dir[2]), r.t_min, r.t_max);
+        HitD h;
+        TraceCounters tc{0, 0};
+        if (occ) {
+            occ[i] = traverse<true, false>(S, pr, &h, &tc) ? 1 : 0;
+        } else {
+            cgpu_hit out;
+            if (traverse<false, false>(S, pr, &h, &tc)) {
+                out.t = h.t;
+                out.primitive = __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + h.slot)).w);
+                out.u = h.u;
+                out.v = h.v;
+            } else {
+                out.t = 0.0f;
+                out.primitive = -1;
+                out.u = 0.0f;
+                out.v = 0.0f;
+            }
+            hits[i] = out;
+        }
+    }
+}
+
+__global__ void k_camera(const SceneD* scenes, int scene, const double* xy, uint32_t n, float* out) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float3 o, d;
+        camera_ray(scenes[scene].cam, float(xy[2 * i]), float(xy[2 * i + 1]), &o, &d);
+        out[6 * i + 0] = o.x; out[6 * i + 1] = o.y; out[6 * i + 2] = o.z;
+        out[6 * i + 3] = d.x; out[6 * i + 4] = d.y; out[6 * i + 5] = d.z;
+    }
+}
+
+}  // namespace cg
+
+// ============================================================== host side ==
+using namespace cg;
+
+namespace {
+
+constexpr int kBlock = 128;
+
+template <typename K>
+int grid_for(cgpu_ctx* ctx, K kernel, int block, uint64_t work) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    if (per_sm < 1) per_sm = 1;
+    const uint64_t full = uint64_t(ctx->num_sms) * uint64_t(per_sm);
+    const uint64_t need = (work + block - 1) / block;
+    return int(std::max<uint64_t>(1, std::min<uint64_t>(full, need)));
+}
+
+uint32_t paths_capacity(cgpu_ctx* ctx, uint32_t max_npix) {
+    uint32_t cap = ctx->max_paths_opt ? ctx->max_paths_opt : (1u << 21);
+    if (cap < max_npix) cap = max_npix;
+    return cap;
+}
+
+cgpu_status ensure_path_buffers(cgpu_ctx* ctx, uint32_t cap, int depth) {
+    if (ctx->path_cap >= cap && ctx->wf.cnt_depth >= depth + 2) return CGPU_OK;
+    cg_free_render_state(ctx);
+    const size_t P = cap;
+    const size_t n_f4 = 11, n_u4 = 1;
+    const size_t q_ints = 2 * 3 + kNumBsdfKinds;
+    const int cdepth = std::max(depth + 2, 34);
+    size_t bytes = P * 16 * (n_f4 + n_u4) + P * 4 * q_ints + size_t(cdepth) * kCntStride * 4 + 1024;
+    void* block = nullptr;
+    cudaError_t e = cudaMalloc(&block, bytes);
+    if (e != cudaSuccess) return cg_fail(ctx, CGPU_ERR_OUT_OF_MEMORY, "path buffers: " + std::string(cudaGetErrorString(e)));
+    char* c = static_cast<char*>(block);
+    auto take = [&](size_t b) { char* r = c; c += (b + 255) & ~size_t(255); return r; };
+    WfBuffers& w = ctx->wf;
+    float4** f4s[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.L, &w.Ls, &w.mis_a, &w.mis_b, &w.mis_d, &w.sh_d, &w.sh_c};
+    for (float4** f : f4s) *f = reinterpret_cast<float4*>(take(P * 16));
+    w.meta = reinterpret_cast<uint4*>(take(P * 16));
+    for (int k = 0; k < 2; ++k) {
+        w.q_cont[k] = reinterpret_cast<int*>(take(P * 4));
+        w.q_mis[k] = reinterpret_cast<int*>(take(P * 4));
+        w.q_shadow[k] = reinterpret_cast<int*>(take(P * 4));
+    }
+    for (int k = 0; k < kNumBsdfKinds; ++k) w.q_mat[k] = reinterpret_cast<int*>(take(P * 4));
+    w.cnt = reinterpret_cast<int*>(take(size_t(cdepth) * kCntStride * 4));
+    w.cnt_depth = cdepth;
+    ctx->wf_block = block;
+    ctx->path_cap = cap;
+    if (!ctx->d_counters) {
+        e = cudaMalloc(&ctx->d_counters, 8 * sizeof(unsigned long long));
+        if (e != cudaSuccess) return cg_cuda(ctx, e, "counters");
+    }
+    if (!ctx->d_chunks) {
+        if ((e = cudaMalloc(&ctx->d_chunks, sizeof(Chunk) * kMaxChunks)) != cudaSuccess) return cg_cuda(ctx, e, "chunks");
+        if ((e = cudaMalloc(&ctx->d_header, sizeof(BatchHeader))) != cudaSuccess) return cg_cuda(ctx, e, "header");
+        if ((e = cudaMallocHost(&ctx->h_chunks, sizeof(Chunk) * kMaxChunks)) != cudaSuccess) return cg_cuda(ctx, e, "chunks");
+        if ((e = cudaMallocHost(&ctx->h_header, sizeof(BatchHeader))) != cudaSuccess) return cg_cuda(ctx, e, "header");
+    }
+    return CGPU_OK;
+}
+
+RenderArgs make_args(cgpu_ctx* ctx) {
+    RenderArgs a;
+    a.scenes = ctx->d_scenes;
+    a.chunks = ctx->d_chunks;
+    a.header = ctx->d_header;
+    a.films = ctx->d_films;
+    a.wf = ctx->wf;
+    a.counters = ctx->d_counters;
+    return a;
+}
+
+// Launch wrapper: with profiling on, bracket the launch with CUDA events on
+// the stream it runs on.
+template <typename F>
+void timed(cgpu_ctx* ctx, int cls, cudaStream_t s, F&& launch) {
+    if (!ctx->profiling) {
+        launch();
+        return;
+    }
+    cgpu_ctx::ProfEvent ev{cls, nullptr, nullptr};
+    cudaEventCreate(&ev.a);
+    cudaEventCreate(&ev.b);
+    cudaEventRecord(ev.a, s);
+    launch();
+    cudaEventRecord(ev.b, s);
+    ctx->prof.push_back(ev);
+}
+
+void collect_profile(cgpu_ctx* ctx) {
+    if (ctx->prof.empty()) return;
+    cudaDeviceSynchronize();
+    for (auto& ev : ctx->prof) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, ev.a, ev.b);
+        ctx->times.ms[ev.cls] += ms;
+        ctx->times.launches[ev.cls] += 1;
+        cudaEventDestroy(ev.a);
+        cudaEventDestroy(ev.b);
+    }
+    ctx->prof.clear();
+}
+
+// Enqueue the wavefront schedule for one batch on ctx->stream.
+cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool splat, bool counting) {
+    RenderArgs a = make_args(ctx);
+    cudaStream_t s = ctx->stream, side = ctx->side;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    cudaMemsetAsync(ctx->wf.cnt, 0, size_t(depth + 2) * kCntStride * sizeof(int), s);
+    uint32_t launches = 1;
+    const int ggen = grid_for(ctx, k_wf_generate, kBlock, paths);
+    timed(ctx, CGPU_KERNEL_GENERATE, s, [&] { k_wf_generate<<<ggen, kBlock, 0, s>>>(a); });
+    auto gext = counting ? grid_for(ctx, k_wf_extend<true>, kBlock, paths) : grid_for(ctx, k_wf_extend<false>, kBlock, paths);
+    auto gsh = counting ? grid_for(ctx, k_wf_shadow<true>, kBlock, paths) : grid_for(ctx, k_wf_shadow<false>, kBlock, paths);
+    const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, kBlock, paths), grid_for(ctx, k_wf_shade<1>, kBlock, paths),
+                                    grid_for(ctx, k_wf_shade<2>, kBlock, paths), grid_for(ctx, k_wf_shade<3>, kBlock, paths),
+                                    grid_for(ctx, k_wf_shade<4>, kBlock, paths)};
+    for (int b = 0; b <= depth; ++b) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(side, fork, 0);
+        if (counting) {
+            k_wf_extend<true><<<gext, kBlock, 0, s>>>(a, b);
+            k_wf_shadow<true><<<gsh, kBlock, 0, side>>>(a, b);
+        } else {
+            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { k_wf_extend<false><<<gext, kBlock, 0, s>>>(a, b); });
+            timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { k_wf_shadow<false><<<gsh, kBlock, 0, side>>>(a, b); });
+        }
+        cudaEventRecord(join, side);
+        cudaStreamWaitEvent(s, join, 0);
+        launches += 2;
+        if (b == depth) break;
+        timed(ctx, CGPU_KERNEL_SHADE, s, [&] {
+            k_wf_shade<0><<<gsd[0], kBlock, 0, s>>>(a, b);
+            k_wf_shade<1><<<gsd[1], kBlock, 0, s>>>(a, b);
+            k_wf_shade<2><<<gsd[2], kBlock, 0, s>>>(a, b);
+            k_wf_shade<3><<<gsd[3], kBlock, 0, s>>>(a, b);
+            k_wf_shade<4><<<gsd[4], kBlock, 0, s>>>(a, b);
+        });
+        launches += kNumBsdfKinds;
+    }
+    if (splat) {
+        const int gsp = grid_for(ctx, k_splat, 256, ctx->h_header->total_pixels);
+        timed(ctx, CGPU_KERNEL_SPLAT, s, [&] { k_splat<<<gsp, 256, 0, s>>>(a); });
+        launches += 1;
+    }
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
+    ctx->stats.kernel_launches += launches;
+    return cg_cuda(ctx, cudaGetLastError(), "wavefront launch");
+}
+
+cgpu_status run_batch(cgpu_ctx* ctx, int mode, int depth, uint32_t paths, bool splat, bool use_graph) {
+    const bool counting = ctx->counting;
+    if (mode == CGPU_MODE_MEGAKERNEL) {
+        RenderArgs a = make_args(ctx);
+        if (counting) {
+            k_megakernel<true><<<grid_for(ctx, k_megakernel<true>, kBlock, paths), kBlock, 0, ctx->stream>>>(a);
+        } else {
+            const int g = grid_for(ctx, k_megakernel<false>, kBlock, paths);
+            timed(ctx, CGPU_KERNEL_MEGAKERNEL, ctx->stream, [&] { k_megakernel<false><<<g, kBlock, 0, ctx->stream>>>(a); });
+        }
+        ctx->stats.kernel_launches += 1;
+        if (splat) {
+            const int gsp = grid_for(ctx, k_splat, 256, ctx->h_header->total_pixels);
+            timed(ctx, CGPU_KERNEL_SPLAT, ctx->stream, [&] { k_splat<<<gsp, 256, 0, ctx->stream>>>(a); });
+            ctx->stats.kernel_launches += 1;
+        }
+        return cg_cuda(ctx, cudaGetLastError(), "megakernel launch");
+    }
+    if (!use_graph || counting || !splat || ctx->profiling) return enqueue_wavefront(ctx, depth, paths, splat, counting);
+    // one graph per (depth, path capacity); the batch itself lives in device memory
+    if (!ctx->graph || ctx->graph_depth != depth || ctx->graph_paths != ctx->path_cap) {
+        if (ctx->graph) {
+            cudaGraphExecDestroy(ctx->graph);
+            ctx->graph = nullptr;
+        }
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cg_cuda(ctx, e, "begin capture");
+        const uint32_t before = ctx->stats.kernel_launches;
+        // capture for the full capacity: kernels read the live path count from the header
+        cgpu_status st = enqueue_wavefront(ctx, depth, ctx->path_cap, true, false);
+        e = cudaStreamEndCapture(ctx->stream, &g);
+        if (st != CGPU_OK) return st;
+        if (e != cudaSuccess) return cg_cuda(ctx, e, "end capture");
+        e = cudaGraphInstantiate(&ctx->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cg_cuda(ctx, e, "graph instantiate");
+        ctx->graph_depth = depth;
+        ctx->graph_paths = ctx->path_cap;
+        ctx->stats.kernel_launches = before;
+    }
+    ctx->stats.kernel_launches += uint32_t(2 + (depth + 1) * 2 + depth * kNumBsdfKinds);
+    return cg_cuda(ctx, cudaGraphLaunch(ctx->graph, ctx->stream), "graph launch");
+}
+
+}  // namespace
+
+void cg_free_render_state(cgpu_ctx* ctx) {
+    if (ctx->graph) {
+        cudaGraphExecDestroy(ctx->graph);
+        ctx->graph = nullptr;
+    }
+    ctx->graph_depth = -1;
+    if (ctx->wf_block) {
+        cudaFree(ctx->wf_block);
+        ctx->wf_block = nullptr;
+    }
+    ctx->wf = WfBuffers{};
+    ctx->path_cap = 0;
+}
+
+// Split the requested samples of every scene into batches of at most
+// path_cap paths and run them.
+cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p) {
+    if (!p || !p->scenes || p->num_scenes == 0 || p->num_scenes > uint32_t(kMaxChunks))
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render: bad scene list");
+    if (p->mode != CGPU_MODE_MEGAKERNEL && p->mode != CGPU_MODE_WAVEFRONT)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render: unknown mode");
+    uint32_t max_npix = 0;
+    int depth = 1;
+    for (uint32_t i = 0; i < p->num_scenes; ++i) {
+        const int s = p->scenes[i];
+        if (s < 0 || s >= int(ctx->scenes.size()) || !ctx->scenes[s].live)
+            return cg_fail(ctx, CGPU_ERR_NOT_FOUND, "render: unknown scene id");
+        const SceneSlot& sl = ctx->scenes[s];
+        max_npix = std::max<uint32_t>(max_npix, uint32_t(sl.width) * uint32_t(sl.height));
+        depth = std::max(depth, sl.max_depth);
+    }
+    cgpu_status st = cg_sync_tables(ctx);
+    if (st != CGPU_OK) return st;
+    st = ensure_path_buffers(ctx, paths_capacity(ctx, max_npix), depth);
+    if (st != CGPU_OK) return st;
+    ctx->stats = cgpu_render_stats{};
+    ctx->times = cgpu_kernel_times{};
+    if (ctx->counting) cudaMemsetAsync(ctx->d_counters, 0, 8 * sizeof(unsigned long long), ctx->stream);
+    // remaining samples per scene
+    std::vector<uint32_t> next(p->num_scenes, p->first_sample);
+    const uint32_t end = p->first_sample + p->num_samples;
+    uint64_t total_paths = 0;
+    for (;;) {
+        uint32_t used = 0, pix = 0, nch = 0;
+        for (uint32_t i = 0; i < p->num_scenes && nch < uint32_t(kMaxChunks); ++i) {
+            if (next[i] >= end) continue;
+            const SceneSlot& sl = ctx->scenes[p->scenes[i]];
+            const uint32_t npix = uint32_t(sl.width) * uint32_t(sl.height);
+            const uint32_t room = (ctx->path_cap - used) / npix;
+            if (room == 0) continue;
+            const uint32_t k = std::min(room, end - next[i]);
+            Chunk& c = ctx->h_chunks[nch++];
+            c.scene = p->scenes[i];
+            c.path_begin = used;
+            c.npix = npix;
+            c.width = uint32_t(sl.width);
+            c.sample0 = next[i];
+            c.nsamples = k;
+            c.pix_begin = pix;
+            c.pad = 0;
+            used += k * npix;
+            pix += npix;
+            next[i] += k;
+        }
+        if (nch == 0) break;
+        BatchHeader& h = *ctx->h_header;
+        // the previous batch may still read the pinned staging copies
+        cudaStreamSynchronize(ctx->stream);
+        h.num_chunks = nch;
+        h.total_paths = used;
+        h.total_pixels = pix;
+        h.max_depth = depth;
+        h.seed = p->seed;
+        cudaMemcpyAsync(ctx->d_chunks, ctx->h_chunks, sizeof(Chunk) * nch, cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->d_header, ctx->h_header, sizeof(BatchHeader), cudaMemcpyHostToDevice, ctx->stream);
+        st = run_batch(ctx, p->mode, depth, used, true, p->use_graph != 0);
+        if (st != CGPU_OK) return st;
+        total_paths += used;
+        ctx->stats.batches += 1;
+        ctx->stats.h2d_bytes += sizeof(Chunk) * nch + sizeof(BatchHeader);
+        collect_profile(ctx);
+    }
+    ctx->stats.paths = total_paths;
+    if (ctx->counting) {
+        unsigned long long c[8];
+        cudaMemcpyAsync(c, ctx->d_counters, sizeof(c), cudaMemcpyDeviceToHost, ctx->stream);
+        cudaStreamSynchronize(ctx->stream);
+        ctx->stats.closest_rays = c[0];
+        ctx->stats.any_rays = c[1];
+        ctx->stats.node_visits = c[2];
+        ctx->stats.triangle_tests = c[3];
+        ctx->stats.any_node_visits = c[4];
+        ctx->stats.any_triangle_tests = c[5];
+    }
+    return cg_cuda(ctx, cudaGetLastError(), "render");
+}
+
+cgpu_status cg_render_paths_raw(cgpu_ctx* ctx, int scene, int mode, uint32_t first, uint32_t count, uint64_t seed,
+                                float* host_rgb) {
+    if (scene < 0 || scene >= int(ctx->scenes.size()) || !ctx->scenes[scene].live)
+        return cg_fail(ctx, CGPU_ERR_NOT_FOUND, "render_paths: unknown scene id");
+    const SceneSlot& sl = ctx->scenes[scene];
+    const uint32_t npix = uint32_t(sl.width) * uint32_t(sl.height);
+    cgpu_status st = cg_sync_tables(ctx);
+    if (st != CGPU_OK) return st;
+    st = ensure_path_buffers(ctx, paths_capacity(ctx, npix), sl.max_depth);
+    if (st != CGPU_OK) return st;
+    float* d_out = nullptr;
+    const uint32_t per = std::max<uint32_t>(1, ctx->path_cap / npix);
+    cudaError_t e = cudaMalloc(&d_out, size_t(per) * npix * 3 * sizeof(float));
+    if (e != cudaSuccess) return cg_cuda(ctx, e, "render_paths buffer");
+    for (uint32_t done = 0; done < count;) {
+        const uint32_t k = std::min(per, count - done);
+        cudaStreamSynchronize(ctx->stream);
+        Chunk& c = ctx->h_chunks[0];
+        c = Chunk{scene, 0, npix, uint32_t(sl.width), first + done, k, 0, 0};
+        BatchHeader& h = *ctx->h_header;
+        h.num_chunks = 1;
+        h.total_paths = k * npix;
+        h.total_pixels = npix;
+        h.max_depth = sl.max_depth;
+        h.seed = seed;
+        cudaMemcpyAsync(ctx->d_chunks, ctx->h_chunks, sizeof(Chunk), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->d_header, ctx->h_header, sizeof(BatchHeader), cudaMemcpyHostToDevice, ctx->stream);
+        st = run_batch(ctx, mode, sl.max_depth, k * npix, false, false);
+        if (st != CGPU_OK) break;
+        k_gather_paths<<<grid_for(ctx, k_gather_paths, 256, k * npix), 256, 0, ctx->stream>>>(ctx->wf.L, ctx->wf.Ls, k * npix, d_out);
+        cudaMemcpyAsync(host_rgb + size_t(done) * npix * 3, d_out, size_t(k) * npix * 3 * sizeof(float),
+                        cudaMemcpyDeviceToHost, ctx->stream);
+        done += k;
+    }
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_out);
+    if (st != CGPU_OK) return st;
+    return cg_cuda(ctx, cudaGetLastError(), "render_paths");
+}
+
+cgpu_status cg_path_radiance(cgpu_ctx* ctx, int scene, int mode, const double* film_xy, const uint64_t* keys,
+                             uint32_t n, float* out_rgb) {
+    (void)mode;  // one path per thread either way: both modes share plan_vertex / resolve
+    cgpu_status st = cg_sync_tables(ctx);
+    if (st != CGPU_OK) return st;
+    double* d_xy = nullptr;
+    uint64_t* d_keys = nullptr;
+    float* d_out = nullptr;
+    cudaError_t e = cudaMalloc(&d_xy, size_t(n) * 16);
+    if (e == cudaSuccess) e = cudaMalloc(&d_keys, size_t(n) * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&d_out, size_t(n) * 12);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_xy, film_xy, size_t(n) * 16, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_keys, keys, size_t(n) * 8, cudaMemcpyHostToDevice, ctx->stream);
+    if (e == cudaSuccess) {
+        k_paths_explicit<<<grid_for(ctx, k_paths_explicit, kBlock, n), kBlock, 0, ctx->stream>>>(ctx->d_scenes, scene, d_xy,
+                                                                                                d_keys, n, d_out);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out_rgb, d_out, size_t(n) * 12, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(d_xy);
+    cudaFree(d_keys);
+    cudaFree(d_out);
+    return cg_cuda(ctx, e, "path_radiance");
+}
+
+cgpu_status cg_trace(cgpu_ctx* ctx, int scene, const cgpu_ray* d_rays, uint32_t n, cgpu_hit* d_hits, uint8_t* d_occ,
+                     bool any) {
+    cgpu_status st = cg_sync_tables(ctx);
+    if (st != CGPU_OK) return st;
+    if (n == 0) return CGPU_OK;
+    k_trace<<<grid_for(ctx, k_trace, kBlock, n), kBlock, 0, ctx->stream>>>(ctx->d_scenes, scene, d_rays, n,
+                                                                        any ? nullptr : d_hits, any ? d_occ : nullptr);
+    return cg_cuda(ctx, cudaGetLastError(), "trace launch");
+}
+
+cgpu_status cg_camera(cgpu_ctx* ctx, int scene, const double* d_xy, uint32_t n, float* d_out) {
+    cgpu_status st = cg_sync_tables(ctx);
+    if (st != CGPU_OK) return st;
+    if (n == 0) return CGPU_OK;
+    k_camera<<<grid_for(ctx, k_camera, kBlock, n), kBlock, 0, ctx->stream>>>(ctx->d_scenes, scene, d_xy, n, d_out);
+    return cg_cuda(ctx, cudaGetLastError(), "camera launch");
+}
+
+cgpu_status cg_film_clear(cgpu_ctx* ctx, int scene) {
+    SceneSlot& sl = ctx->scenes[scene];
+    const size_t npix = size_t(sl.width) * sl.height;
+    cudaMemsetAsync(sl.film.sum, 0, npix * 3 * sizeof(double), ctx->stream);
+    cudaMemsetAsync(sl.film.sumsq, 0, npix * 3 * sizeof(double), ctx->stream);
+    cudaMemsetAsync(sl.film.count, 0, npix * sizeof(double), ctx->stream);
+    return cg_cuda(ctx, cudaGetLastError(), "film clear");
+}

@@ -1,0 +1,103 @@
+// Device-resident scene layout (one per uploaded scene, all in HBM).
+//
+//  * Bvh4Node, 128 B, one L2 line: four child boxes stored SoA
+//    (lo/hi x, y, z) + four 32-bit child entries.  A child entry is either an
+//    inner node index (bit 31 clear) or a leaf: bit 31 set, (count - 1) in
+//    bits 28..30, first triangle slot in bits 0..27.  Empty slots carry an
+//    inverted box (lo = +inf, hi = -inf) and never hit.
+//  * TriRecord, 48 B per triangle in leaf order: the three vertices in the
+//    primitive's own vertex order (so the geometric normal is the reference's
+//    eAB x eAC) with the primitive index, the packed material / light id and
+//    flags in the .w lanes.  A rectangle is stored as two TriRecords
+//    (vB, vA, vC) and (vA, vD, vC), both carrying the rectangle's index.
+//  * Material / Light tables and optional per-primitive shading attributes
+//    (vertex normals, vertex uvws) read only at a hit.
+#pragma once
+
+#include "common.cuh"
+
+namespace cg {
+
+struct __align__(16) Bvh4Node {
+    float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
+    uint32_t child[4];
+    uint32_t pad[4];
+};
+static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node must be one 128-byte line");
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+CG_HD bool entry_is_leaf(uint32_t e) { return (e & kLeafBit) != 0; }
+CG_HD uint32_t leaf_first(uint32_t e) { return e & 0x0FFFFFFFu; }
+CG_HD uint32_t leaf_count(uint32_t e) { return ((e >> 28) & 7u) + 1u; }
+CG_HD uint32_t make_leaf(uint32_t first, uint32_t count) { return kLeafBit | ((count - 1u) << 28) | first; }
+constexpr uint32_t kMaxLeafTris = 8;
+constexpr uint32_t kMaxTriSlots = 0x0FFFFFFFu;
+// traversal stack entries per ray; a 4-wide tree of depth D needs at most 3 D + 1
+constexpr int kStackSize = 96;
+
+struct __align__(16) TriRecord {
+    float4 v0;  // xyz = vertex A, w = primitive index (int bits)
+    float4 v1;  // xyz = vertex B, w = (material index) | ((light index + 1) << 16)
+    float4 v2;  // xyz = vertex C, w = flags (bit 0: half of a rectangle, bits 1..31: rectangle index)
+};
+static_assert(sizeof(TriRecord) == 48, "TriRecord is 48 bytes");
+
+enum : int { BSDF_LAMBERTIAN = 0, BSDF_CONDUCTOR = 1, BSDF_GLASS = 2, BSDF_ABSORBER = 3, BSDF_DIELECTRIC_GGX = 4 };
+constexpr int kNumBsdfKinds = 5;
+
+struct __align__(16) MaterialD {
+    int type;
+    int albedo_tex;   // -1 constant
+    float roughness;  // raw CRSD roughness
+    float alpha;      // max(max(r, 1e-3)^2, 1e-3)
+    float3 albedo;
+    float ior_outer;
+    float3 f0;
+    float ior_inner;
+};
+
+struct __align__(16) LightD {
+    int prim;
+    int kind;        // 0 triangle, 1 rectangle
+    int back_face;
+    float pdf_area;  // 1 / area
+    float3 radiance; // color / sum(color) * watt / (area * pi)
+    float area;
+    // triangle: p0 = vA, e0 = eAB, e1 = eAC, n = Ng, nA..nC vertex normals
+    // rectangle: p0 = vB, e0 = eA (vA - vB), e1 = eB (vC - vB), n = normalize(eA x eB)
+    float3 p0, e0, e1, n;
+    float3 nA, nB, nC;
+    int has_normals;
+    float long_len, short_len;  // rectangle rejection sampler
+    float3 long_e, short_dir;    // rectangle: longer edge, unit shorter edge
+};
+
+struct TextureD {
+    int width, height;
+    const float* texels;  // RGB float
+};
+
+// Camera in the reference's film->camera->world form (perspectivePinholeCamera.cpp:32-73).
+struct CameraD {
+    float3 pos, ax, ay, az;
+    float sx, sy, tx, ty, offset;
+};
+
+struct SceneD {
+    const Bvh4Node* nodes;
+    const TriRecord* tris;
+    const MaterialD* materials;
+    const LightD* lights;
+    const TextureD* textures;
+    const float* prim_normals;  // 9 per primitive or null
+    const float* prim_uvws;     // 9 per primitive or null
+    const float* rect_frames;   // 9 per rectangle (vB, eA, eB), indexed by the rectangle index
+    int num_lights;
+    int num_tris;
+    int width, height;
+    int max_depth;
+    int spp;
+    CameraD cam;
+};
+
+}  // namespace cg

@@ -1,0 +1,555 @@
+// Camera, surface reconstruction, BSDFs, area lights and the per-vertex
+// plan of the NEE + MIS path estimator.
+//
+// Behaviour follows the reference estimator PtEstimator::estimate
+// (source/core/estimator/ptEstimator.cpp:25-123) and its callees; each device
+// function names the reference routine it stands for.  One vertex is split
+// into `plan_vertex` (draws every random number the reference draws at that
+// vertex, in the reference's order, and emits up to three rays: the shadow
+// ray, the MIS BSDF ray and the continuation ray) and the resolve functions
+// that turn trace results into radiance.  The megakernel and the wavefront
+// scheduler both run exactly these functions, so they produce the same
+// per-path result.
+#pragma once
+
+#include "traverse.cuh"
+
+namespace cg {
+
+// ------------------------------------------------------------------ camera --
+// PerspectivePinholeCamera::spawnPrimaryRay (perspectivePinholeCamera.cpp:52-73)
+CG_D void camera_ray(const CameraD& c, float fx, float fy, float3* o, float3* d) {
+    const float cx = c.sx * fx + c.tx;
+    const float cy = c.sy * fy + c.ty;
+    const float cz = -c.offset;
+    const float3 v = mk(c.ax.x * cx + c.ay.x * cy + c.az.x * cz,
+                        c.ax.y * cx + c.ay.y * cy + c.az.y * cz,
+                        c.ax.z * cx + c.ay.z * cy + c.az.z * cz);
+    *o = c.pos;
+    *d = normalize(v);
+}
+
+// Sample `s` of a pixel: stratum s of the floor(sqrt(spp))^2 grid (uniform
+// beyond it), jittered by the first two draws of the path stream - the set
+// StratifiedSampler::requestSample2D builds (stratifiedSampler.cpp:38-73)
+// minus its in-pixel shuffle.
+CG_D void stratum_jitter(int spp, uint32_t s, Rng& rng, float* jx, float* jy) {
+    const int base = int(floorf(sqrtf(float(spp))));
+    const float u0 = rng.next(), u1 = rng.next();
+    if (int(s) < base * base) {
+        const float inv = 1.0f / float(base);
+        *jx = (float(s % uint32_t(base)) + u0) * inv;
+        *jy = (float(s / uint32_t(base)) + u1) * inv;
+    } else {
+        *jx = u0;
+        *jy = u1;
+    }
+}
+
+// ----------------------------------------------------------------- surface --
+struct SurfaceD {
+    float3 P, Ng, Ns, uvw, wi;
+    int prim, material, light;
+};
+
+// Scene::isIntersecting surface detail (scene.cpp:30-65, triangle.cpp:125-160,
+// rectangle.cpp:102-132).
+CG_D SurfaceD surface_at(const SceneD& S, float3 o, float3 d, const HitD& h) {
+    SurfaceD si;
+    const float4* tp = reinterpret_cast<const float4*>(S.tris + h.slot);
+    const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+    si.prim = __float_as_int(a.w);
+    const uint32_t packed = __float_as_uint(b.w);
+    si.material = int(packed & 0xFFFFu);
+    si.light = int(packed >> 16) - 1;
+    const uint32_t flags = __float_as_uint(c.w);
+    si.P = o + d * h.t;
+    si.wi = -d;
+    const float b1 = h.u, b2 = h.v, b0 = 1.0f - h.u - h.v;
+    if (flags & 1u) {
+        // half of a rectangle: normal and uvw from the rectangle's own frame
+        const float* fr = S.rect_frames + 9 * size_t(flags >> 1);
+        const float3 vB = mk(fr[0], fr[1], fr[2]), eA = mk(fr[3], fr[4], fr[5]), eB = mk(fr[6], fr[7], fr[8]);
+        float3 N = cross(eA, eB);
+        N = is_zero(N) ? mk(0.0f, 1.0f, 0.0f) : normalize(N);
+        si.Ng = N;
+        si.Ns = N;
+        const float3 onp = si.P - vB;
+        const float la = len(eA);
+        const float p1 = dot(onp, normalize(eA)) / la;
+        const float p2 = dot(onp, normalize(eB)) / la;  // rectangle.cpp:125 divides by |eA| too
+        si.uvw = mk(p1, p2, 0.0f);
+        return si;
+    }
+    const float3 A = f3(a), B = f3(b), C = f3(c);
+    float3 Ng = cross(B - A, C - A);
+    Ng = is_zero(Ng) ? mk(0.0f, 1.0f, 0.0f) : normalize(Ng);
+    si.Ng = Ng;
+    if (S.prim_normals) {
+        const float* n = S.prim_normals + 9 * size_t(si.prim);
+        const float3 Ns = mk(n[0], n[1], n[2]) * b0 + mk(n[3], n[4], n[5]) * b1 + mk(n[6], n[7], n[8]) * b2;
+        si.Ns = is_zero(Ns) ? Ng : normalize(Ns);
+    } else {
+        si.Ns = Ng;
+    }
+    if (S.prim_uvws) {
+        const float* u = S.prim_uvws + 9 * size_t(si.prim);
+        si.uvw = mk(u[0], u[1], u[2]) * b0 + mk(u[3], u[4], u[5]) * b1 + mk(u[6], u[7], u[8]) * b2;
+    } else {
+        si.uvw = mk(b1, b2, 0.0f);
+    }
+    return si;
+}
+
+// ------------------------------------------------------------------ texture --
+// RgbImageTexture + TNearestPixelSampler + RepeatUvwWrapper
+// (rgbImageTexture.cpp:8-15, tNearestPixelSampler.ipp:14-31, repeatUvwWrapper.cpp:9-15)
+CG_D float3 texture_rgb(const TextureD& t, float3 uvw) {
+    const float u = uvw.x - floorf(uvw.x), v = uvw.y - floorf(uvw.y);
+    int x = int(u * float(t.width)), y = int(v * float(t.height));
+    x = x < t.width ? x : x - 1;
+    y = y < t.height ? y : y - 1;
+    const float* p = t.texels + 3 * (size_t(y) * size_t(t.width) + size_t(x));
+    return mk(__ldg(p), __ldg(p + 1), __ldg(p + 2));
+}
+
+CG_D float3 albedo_of(const SceneD& S, const MaterialD& m, float3 uvw) {
+    return m.albedo_tex >= 0 ? texture_rgb(S.textures[m.albedo_tex], uvw) : m.albedo;
+}
+
+// --------------------------------------------------------------------- GGX --
+// IsotropicGgx (isotropicGgx.cpp:11-100), Microfacet::_isShadowingMaskingValid
+// (microfacet.cpp:11-23)
+CG_D float ggx_D(float alpha, float NdotH) {
+    if (NdotH <= 0.0f) return 0.0f;
+    const float a2 = alpha * alpha, c2 = NdotH * NdotH, c4 = c2 * c2;
+    const float tan2 = (1.0f - c2) / c2;
+    return a2 / (kPi * c4 * (a2 + tan2) * (a2 + tan2));
+}
+CG_D float ggx_G1(float alpha, float cosv) {
+    const float c2 = cosv * cosv;
+    return 2.0f / (1.0f + sqrtf(1.0f + alpha * alpha * ((1.0f - c2) / c2)));
+}
+CG_D float ggx_G(float alpha, float3 V, float3 L, float3 N, float3 H) {
+    const float VdotH = dot(V, H), VdotN = dot(V, N), LdotH = dot(L, H), LdotN = dot(L, N);
+    if (!((VdotH * VdotN > 0.0f) && (LdotH * LdotN > 0.0f))) return 0.0f;
+    return ggx_G1(alpha, VdotN) * ggx_G1(alpha, LdotN);
+}
+// D(h) cos(theta_h) sampling: tan(theta) = alpha sqrt(u / (1 - u)), u clamped to
+// [0, 0.9999]; cos(theta) = sqrt((1 - u) / (1 - u + alpha^2 u)).
+CG_D float3 ggx_sample_h(float alpha, float u0, float u1) {
+    const float s0 = fminf(fmaxf(u0, 0.0f), 0.9999f);
+    const float s1 = fminf(fmaxf(u1, 0.0f), 0.9999f);
+    float sp, cp;
+    sincospif(2.0f * s0, &sp, &cp);
+    const float a2 = alpha * alpha;
+    const float c = sqrtf((1.0f - s1) / (1.0f - s1 + a2 * s1));
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    return mk(sp * s, c, cp * s);
+}
+// SchlickConductorFresnel::evaluateReflectance (schlickConductorFresnel.cpp:28-41)
+CG_D float3 schlick(float3 f0, float cosI) {
+    const float c = 1.0f - fabsf(cosI);
+    return f0 + (splat3(1.0f) - f0) * (c * (c * c) * (c * c));
+}
+// VanillaDielectricFresnel::evaluateReflectance (vanillaDielectricFresnel.cpp:17-48)
+CG_D float fresnel_dielectric(float etaI, float etaT, float cosI) {
+    if (cosI < 0.0f) { const float t = etaI; etaI = etaT; etaT = t; cosI = -cosI; }
+    const float ratio = etaI / etaT;
+    const float sinT2 = ratio * ratio * (1.0f - cosI * cosI);
+    if (sinT2 >= 1.0f) return 1.0f;
+    const float cosT = sqrtf(1.0f - sinT2);
+    const float rPar = (etaT * cosI - etaI * cosT) / (etaT * cosI + etaI * cosT);
+    const float rPer = (etaI * cosI - etaT * cosT) / (etaI * cosI + etaT * cosT);
+    return 0.5f * (rPar * rPar + rPer * rPer);
+}
+// TVector::canRefract (tVector.ipp:468-503)
+CG_D bool refract_dir(float3 v, float3 n, float etaI, float etaT, float3* out) {
+    float sgn = 1.0f;
+    const float cosI = dot(v, n);
+    if (cosI < 0.0f) { const float t = etaI; etaI = etaT; etaT = t; sgn = -1.0f; }
+    const float ratio = etaI / etaT;
+    const float sinT2 = ratio * ratio * (1.0f - cosI * cosI);
+    if (sinT2 >= 1.0f) return false;
+    const float cosT = sqrtf(1.0f - sinT2);
+    *out = normalize(v * (-ratio) + n * ((ratio * sgn * cosI - cosT) * sgn));
+    return true;
+}
+
+// -------------------------------------------------------------------- BSDF --
+CG_HD bool bsdf_is_specular(int type) { return type == BSDF_GLASS; }
+
+// Rough dielectric (no reference counterpart): GGX BRDF + BTDF of Walter,
+// Marschner, Li & Torrance, "Microfacet Models for Refraction through Rough
+// Surfaces" (EGSR 2007), radiance form, Fresnel-weighted lobe choice.
+// Everything is expressed with the normal turned to V's side.
+CG_D void rough_dielectric_eval(const MaterialD& m, float3 albedo, float3 V, float3 L, float3 N, float3* f, float* pdf) {
+    *f = splat3(0.0f);
+    *pdf = 0.0f;
+    const float cv = dot(V, N), cl = dot(L, N);
+    if (cv == 0.0f || cl == 0.0f) return;
+    const float3 Nv = cv > 0.0f ? N : -N;
+    const float etaV = cv > 0.0f ? m.ior_outer : m.ior_inner;
+    const float etaL = cv > 0.0f ? m.ior_inner : m.ior_outer;
+    const float acv = fabsf(cv), acl = fabsf(cl);
+    const float alpha = m.alpha;
+    if (cv * cl > 0.0f) {
+        float3 H = V + L;
+        if (is_zero(H)) return;
+        H = normalize(H);
+        const float VH = dot(V, H);
+        if (VH <= 0.0f) return;
+        const float F = fresnel_dielectric(etaV, etaL, VH);
+        const float NH = dot(Nv, H);
+        const float D = ggx_D(alpha, NH);
+        const float G = ggx_G(alpha, V, L, Nv, H);
+        *f = albedo * (F * D * G / (4.0f * acv * acl));
+        *pdf = F * D * NH / (4.0f * VH);
+    } else {
+        const float eta = etaL / etaV;
+        float3 H = V + L * eta;
+        if (is_zero(H)) return;
+        H = normalize(H);
+        if (dot(H, Nv) < 0.0f) H = -H;
+        const float VH = dot(V, H), LH = dot(L, H);
+        if (!(VH > 0.0f && LH < 0.0f)) return;
+        const float F = fresnel_dielectric(etaV, etaL, VH);
+        const float NH = dot(Nv, H);
+        const float D = ggx_D(alpha, NH);
+        const float G = ggx_G(alpha, V, L, Nv, H);
+        const float den = VH + eta * LH;
+        const float den2 = den * den;
+        *f = albedo * ((1.0f - F) * D * G * fabsf(VH * LH) / (acv * acl * den2));
+        *pdf = (1.0f - F) * D * NH * eta * eta * fabsf(LH) / den2;
+    }
+    if (!isfinite(*pdf)) { *pdf = 0.0f; *f = splat3(0.0f); }
+}
+
+// Bsdf::evaluate (lambertianDiffuse.cpp:27-44, conductorMicrofacet.cpp:32-66)
+CG_D float3 bsdf_eval(const SceneD& S, const MaterialD& m, const SurfaceD& si, float3 L) {
+    const float3 N = si.Ns, V = si.wi;
+    if (m.type == BSDF_LAMBERTIAN) {
+        if (dot(V, N) * dot(L, N) <= 0.0f) return splat3(0.0f);
+        return albedo_of(S, m, si.uvw) * kInvPi;
+    }
+    if (m.type == BSDF_CONDUCTOR) {
+        const float VdotN = dot(V, N), LdotN = dot(L, N);
+        if (VdotN * LdotN <= 0.0f) return splat3(0.0f);
+        float3 H = (V + L) * (VdotN > 0.0f ? 1.0f : -1.0f);
+        if (is_zero(H)) return splat3(0.0f);
+        H = normalize(H);
+        const float3 F = schlick(m.f0, dot(L, H));
+        const float D = ggx_D(m.alpha, dot(N, H));
+        const float G = ggx_G(m.alpha, V, L, N, H);
+        return F * G * D * (1.0f / (4.0f * fabsf(VdotN * LdotN)));
+    }
+    if (m.type == BSDF_DIELECTRIC_GGX) {
+        float3 f;
+        float pdf;
+        rough_dielectric_eval(m, albedo_of(S, m, si.uvw), V, L, N, &f, &pdf);
+        return f;
+    }
+    return splat3(0.0f);
+}
+
+// Bsdf::evaluatePdfW (lambertianDiffuse.cpp:83-96, conductorMicrofacet.cpp:126-163)
+CG_D float bsdf_pdf(const SceneD& S, const MaterialD& m, const SurfaceD& si, float3 L) {
+    const float3 N = si.Ns, V = si.wi;
+    if (m.type == BSDF_LAMBERTIAN) {
+        if (dot(V, N) * dot(L, N) <= 0.0f) return 0.0f;
+        return absdot(L, N) * kInvPi;
+    }
+    if (m.type == BSDF_CONDUCTOR) {
+        const float VdotN = dot(V, N), LdotN = dot(L, N);
+        if (VdotN * LdotN <= 0.0f) return 0.0f;
+        float3 H = (V + L) * (VdotN > 0.0f ? 1.0f : -1.0f);
+        if (is_zero(H)) return 0.0f;
+        H = normalize(H);
+        const float D = ggx_D(m.alpha, dot(N, H));
+        const float pdfL = fabsf(fabsf(D * dot(N, H)) / (4.0f * dot(L, H)));
+        return isfinite(pdfL) ? pdfL : 0.0f;
+    }
+    if (m.type == BSDF_DIELECTRIC_GGX) {
+        float3 f;
+        float pdf;
+        rough_dielectric_eval(m, splat3(1.0f), V, L, N, &f, &pdf);
+        return pdf;
+    }
+    return 0.0f;
+}
+
+struct BsdfS {
+    float3 f, L;
+    float pdf;
+    CG_D bool valid() const { return !is_zero(f) && pdf > 0.0f; }  // bsdfSample.cpp:39-41
+};
+
+// Bsdf::evaluateSample (lambertianDiffuse.cpp:46-81, conductorMicrofacet.cpp:68-124,
+// specularDielectric.cpp:35-127)
+CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, Rng& rng) {
+    BsdfS out;
+    out.f = splat3(0.0f);
+    out.L = mk(0.0f, 1.0f, 0.0f);
+    out.pdf = 0.0f;
+    const float3 N = si.Ns, V = si.wi;
+    if (m.type == BSDF_LAMBERTIAN) {
+        float3 z, x;
+        frame_from_y(N, &z, &x);
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        // Hemisphere::cosineWeightedSampling (hemisphere.cpp:30-48):
+        // theta = acos(1 - 2 u1) / 2, i.e. cos(theta) = sqrt(1 - u1)
+        float sp, cp;
+        sincospif(2.0f * u0, &sp, &cp);
+        const float c = sqrtf(1.0f - u1);
+        const float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+        float3 L = x * (sp * s) + N * c + z * (cp * s);
+        L = normalize(L);
+        if (dot(V, N) <= 0.0f) L = -L;
+        out.f = albedo_of(S, m, si.uvw) * kInvPi;
+        out.L = L;
+        out.pdf = c * kInvPi;
+        return out;
+    }
+    if (m.type == BSDF_CONDUCTOR) {
+        const float nf = dot(V, N) > 0.0f ? 1.0f : -1.0f;
+        float3 z, x;
+        frame_from_y(N, &z, &x);
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        const float3 hl = ggx_sample_h(m.alpha, u0, u1);
+        const float3 H = normalize(x * hl.x + N * hl.y + z * hl.z);
+        const float3 L = reflect(V, H * nf);
+        const float VdotN = dot(V, N), LdotN = dot(L, N), LdotH = dot(L, H), NdotH = dot(N, H);
+        if (VdotN * LdotN <= 0.0f) return out;
+        const float3 F = schlick(m.f0, LdotH);
+        const float D = ggx_D(m.alpha, NdotH);
+        const float G = ggx_G(m.alpha, V, L, N, H);
+        const float pdfL = fabsf(fabsf(D * NdotH) / (4.0f * LdotH));
+        if (!isfinite(pdfL)) return out;
+        out.f = F * G * D * (1.0f / (4.0f * fabsf(VdotN * LdotN)));
+        out.L = L;
+        out.pdf = pdfL;
+        return out;
+    }
+    if (m.type == BSDF_GLASS) {
+        const float VdotN = dot(V, N);
+        const float R = fresnel_dielectric(m.ior_outer, m.ior_inner, VdotN);
+        const float pr = (R + R + R) / 3.0f;  // Spectrum::average of a grey reflectance
+        const float u = rng.next();
+        const float3 alb = albedo_of(S, m, si.uvw);
+        if (u < pr) {
+            const float3 L = reflect(V, N * (VdotN > 0.0f ? 1.0f : -1.0f));
+            out.f = alb * R * (1.0f / absdot(L, N));
+            out.L = L;
+            out.pdf = pr;
+        } else {
+            float3 L;
+            if (!refract_dir(V, N, m.ior_outer, m.ior_inner, &L)) return out;
+            const float cosI = dot(L, N);
+            const float Rt = fresnel_dielectric(m.ior_outer, m.ior_inner, cosI);
+            float etaI = m.ior_outer, etaT = m.ior_inner;
+            if (cosI < 0.0f) { const float t = etaI; etaI = etaT; etaT = t; }
+            const float btdf = (etaT * etaT) / (etaI * etaI);
+            out.f = alb * (1.0f - Rt) * btdf * (1.0f / fabsf(cosI));
+            out.L = L;
+            out.pdf = 1.0f - pr;
+        }
+        return out;
+    }
+    if (m.type == BSDF_DIELECTRIC_GGX) {
+        const float cv = dot(V, N);
+        if (cv == 0.0f) return out;
+        const float3 Nv = cv > 0.0f ? N : -N;
+        const float etaV = cv > 0.0f ? m.ior_outer : m.ior_inner;
+        const float etaL = cv > 0.0f ? m.ior_inner : m.ior_outer;
+        float3 z, x;
+        frame_from_y(Nv, &z, &x);
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        const float3 hl = ggx_sample_h(m.alpha, u0, u1);
+        const float3 H = normalize(x * hl.x + Nv * hl.y + z * hl.z);
+        const float VH = dot(V, H);
+        const float u = rng.next();
+        if (VH <= 0.0f) return out;
+        const float F = fresnel_dielectric(etaV, etaL, VH);
+        float3 L;
+        if (u < F) {
+            L = H * (2.0f * VH) - V;
+        } else {
+            const float ratio = etaV / etaL;
+            const float sinT2 = ratio * ratio * (1.0f - VH * VH);
+            if (sinT2 >= 1.0f) return out;
+            const float cosT = sqrtf(1.0f - sinT2);
+            L = normalize(V * (-ratio) + H * (ratio * VH - cosT));
+        }
+        float3 f;
+        float pdf;
+        rough_dielectric_eval(m, albedo_of(S, m, si.uvw), V, L, N, &f, &pdf);
+        out.f = f;
+        out.L = L;
+        out.pdf = pdf;
+        return out;
+    }
+    return out;  // absorber: never valid (absorberBsdf.cpp)
+}
+
+// ------------------------------------------------------------------ lights --
+CG_D bool can_emit(const LightD& l, float3 dir, float3 N) { return (dot(dir, N) >= 0.0f) != (l.back_face != 0); }
+
+struct LightS {
+    float3 pos, radiance;
+    float pdfW;
+    CG_D bool valid() const { return !is_zero(radiance) && pdfW > 0.0f; }  // directLightSample.cpp:53-55
+};
+
+// SingleAreaLight::evaluateDirectSample (singleAreaLight.cpp:54-85) with
+// Triangle / Rectangle::evaluatePositionSample (triangle.cpp:162-193,
+// sampleWarp.cpp:10-19; rectangle.cpp:134-169 rejection sampler).
+CG_D LightS light_sample(const LightD& l, float3 target, Rng& rng) {
+    LightS out;
+    out.radiance = splat3(0.0f);
+    out.pdfW = 0.0f;
+    out.pos = splat3(0.0f);
+    float3 P, Ns;
+    if (l.kind == 0) {
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        const float sa = sqrtf(u0);
+        const float s = 1.0f - sa, t = sa * u1;
+        P = l.p0 + l.e0 * s + l.e1 * t;
+        if (l.has_normals) {
+            const float3 n = l.nA * (1.0f - s - t) + l.nB * s + l.nC * t;
+            Ns = is_zero(n) ? l.n : n;
+        } else {
+            Ns = l.n;
+        }
+    } else {
+        const float ratio = l.short_len / l.long_len;
+        float a = 0.0f, b = 2.0f;
+        for (int it = 0; it < 4096 && b > ratio; ++it) {
+            a = rng.next();
+            b = rng.next();
+        }
+        if (b > ratio) return out;  // bounded rejection loop gave up
+        P = l.p0 + l.long_e * a + l.short_dir * (b * l.long_len);
+        Ns = l.n;
+    }
+    const float3 ev = target - P;
+    if (!can_emit(l, ev, Ns)) return out;
+    const float d2 = len2(ev);
+    const float cosE = absdot(ev * (1.0f / sqrtf(d2)), Ns);
+    if (cosE <= 0.0f) return out;
+    out.pos = P;
+    out.pdfW = l.pdf_area * d2 / cosE;
+    out.radiance = l.radiance;
+    return out;
+}
+
+// SingleAreaLight::emittance (singleAreaLight.cpp:39-52)
+CG_D float3 light_emittance(const LightD& l, const SurfaceD& si) {
+    return can_emit(l, si.wi, si.Ns) ? l.radiance : splat3(0.0f);
+}
+// SingleAreaLight::evaluateDirectPdfW (singleAreaLight.cpp:87-109)
+CG_D float light_pdfW(const LightD& l, const SurfaceD& si, float3 target) {
+    if (!can_emit(l, si.wi, si.Ns)) return 0.0f;
+    const float c = absdot(si.wi, si.Ns);
+    if (c <= 0.0f) return 0.0f;
+    return l.pdf_area * len2(target - si.P) / c;
+}
+
+CG_D float mis_power(float a, float b) {  // TMis<POWER>::weight (tMis.h:21-47)
+    const float a2 = a * a, b2 = b * b;
+    return a2 / (a2 + b2);
+}
+
+// ------------------------------------------------------------ vertex plan --
+struct VertexPlan {
+    float3 emit;          // T * Le, added to L now
+    int shadow;           // shadow ray (P, sdir, stmax) unoccluded => Ls += scontrib
+    float3 sdir, scontrib;
+    float stmax;
+    int mis;              // MIS ray (P, mdir): hitting light `mlight` => L += mis_resolve(...)
+    float3 mdir, mfactor;
+    float mpdf;
+    int mlight;
+    int cont;             // continuation (P, cdir) with throughput T
+    float3 cdir, T;
+    int count_emission;
+};
+
+// One vertex of PtEstimator::estimate (ptEstimator.cpp:43-119) and the
+// light-sampling half of DirectLightEvaluator::evaluate
+// (directLightEvaluator.cpp:36-76); random numbers in the reference's order:
+// light pick, light position, MIS BSDF sample, continuation sample, roulette.
+CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool count_emission, int bounce, Rng& rng) {
+    VertexPlan p;
+    p.emit = splat3(0.0f);
+    p.shadow = 0;
+    p.mis = 0;
+    p.cont = 0;
+    p.mlight = -1;
+    const MaterialD m = S.materials[si.material];
+    if (si.light >= 0 && count_emission) p.emit = T * light_emittance(S.lights[si.light], si);
+    if (!bsdf_is_specular(m.type)) {
+        p.count_emission = 0;
+        const int li = rng.index(S.num_lights);
+        const float pick = 1.0f / float(S.num_lights);
+        if (m.type != BSDF_ABSORBER) {
+            const LightD& l = S.lights[li];
+            const LightS ls = light_sample(l, si.P, rng);
+            if (ls.valid()) {
+                const float3 Lv = ls.pos - si.P;
+                const float dist = len(Lv);
+                const float3 L = divs(Lv, dist);
+                const float3 f = bsdf_eval(S, m, si, L);
+                const float3 factor = f * absdot(L, si.Ns);
+                const float bp = bsdf_pdf(S, m, si, L);
+                const float w = mis_power(ls.pdfW, bp);
+                const float3 part = divs(divs(ls.radiance * w * factor, ls.pdfW), pick);
+                p.shadow = 1;
+                p.sdir = normalize(L);
+                p.stmax = dist - kRayEps;
+                p.scontrib = T * part;
+            }
+            const BsdfS bs = bsdf_sample(S, m, si, rng);
+            if (bs.valid()) {
+                p.mis = 1;
+                p.mdir = normalize(bs.L);
+                p.mfactor = bs.f * absdot(bs.L, si.Ns);
+                p.mpdf = bs.pdf;
+                p.mlight = li;
+            }
+        }
+    } else {
+        p.count_emission = 1;
+    }
+    const BsdfS bs = bsdf_sample(S, m, si, rng);
+    if (!bs.valid()) return p;
+    T *= divs(bs.f * absdot(bs.L, si.Ns), bs.pdf);
+    if (bounce > 2) {  // RussianRoulette::isSurvivedOnNextRound (russianRoulette.cpp:9-28)
+        const float q = fminf(fmaxf(1.0f - max_comp(T), 0.05f), 1.0f);
+        const float u = rng.next();
+        if (!(u > q)) return p;
+        T = T * (1.0f / (1.0f - q));
+    }
+    if (is_zero(T)) return p;
+    p.cont = 1;
+    p.cdir = normalize(bs.L);
+    p.T = T;
+    return p;
+}
+
+// The BSDF-sampling half of DirectLightEvaluator::evaluate
+// (directLightEvaluator.cpp:79-106), divided by the pick pdf and weighted by
+// the throughput at the vertex (ptEstimator.cpp:80-83).
+CG_D float3 mis_resolve(const SceneD& S, const SurfaceD& hit, float3 origin, float3 T, float3 factor, float pdf) {
+    const LightD& l = S.lights[hit.light];
+    const float3 rad = light_emittance(l, hit);
+    const float lp = light_pdfW(l, hit, origin);
+    const float w = mis_power(pdf, lp);
+    const float pick = 1.0f / float(S.num_lights);
+    return T * divs(divs(rad * w * factor, pdf), pick);
+}
+
+}  // namespace cg

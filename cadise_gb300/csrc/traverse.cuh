@@ -1,0 +1,218 @@
+// Closest-hit and any-hit traversal of the 4-wide BVH with a watertight
+// FP32 ray/triangle test.
+//
+// Replaces BvhAccelerator::isIntersecting / isOccluded
+// (source/core/intersector/accelerator/bvh/bvhAccelerator.cpp:40-156) and
+// Triangle::isIntersecting (source/core/intersector/primitive/triangle.cpp:54-123):
+// same contract - closest hit with t in [t_min, t_max] (inclusive), or any
+// hit in that range - but every ray/triangle decision is watertight
+// (Woop, Benthin & Wald, "Watertight Ray/Triangle Intersection", JCGT 2013):
+// the three edge functions are evaluated in a ray-aligned sheared space with
+// exactly rounded products (no contraction), falling back to FP64 when one of
+// them is exactly zero, so a ray through a shared edge or vertex hits exactly
+// one of the adjoining triangles.  Box tests widen t_max by 1 + 2 gamma(3) to
+// stay conservative.
+#pragma once
+
+#include "scene_device.cuh"
+
+namespace cg {
+
+struct RayPre {
+    float3 o, d, inv;
+    float tmin, tmax;
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+
+CG_D RayPre ray_prep(float3 o, float3 d, float tmin, float tmax) {
+    RayPre r;
+    r.o = o;
+    r.d = d;
+    r.tmin = tmin;
+    r.tmax = tmax;
+    // zero components would make (lo - o) * inf = NaN on a box face plane
+    const float e = 1e-30f;
+    const float dx = fabsf(d.x) < e ? copysignf(e, d.x) : d.x;
+    const float dy = fabsf(d.y) < e ? copysignf(e, d.y) : d.y;
+    const float dz = fabsf(d.z) < e ? copysignf(e, d.z) : d.z;
+    r.inv = mk(1.0f / dx, 1.0f / dy, 1.0f / dz);
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int kz = 0;
+    if (ay > ax) kz = 1;
+    if (az > fmaxf(ax, ay)) kz = 2;
+    int kx = kz + 1 == 3 ? 0 : kz + 1;
+    int ky = kx + 1 == 3 ? 0 : kx + 1;
+    if (comp(d, kz) < 0.0f) { const int t = kx; kx = ky; ky = t; }
+    r.kx = kx; r.ky = ky; r.kz = kz;
+    const float dkz = comp(d, kz);
+    r.Sx = comp(d, kx) / dkz;
+    r.Sy = comp(d, ky) / dkz;
+    r.Sz = 1.0f / dkz;
+    return r;
+}
+
+// Watertight test.  On a hit inside [tmin, tcur] writes t and the
+// barycentrics of vertices B (u) and C (v).
+CG_D bool tri_test(const RayPre& r, float3 A3, float3 B3, float3 C3, float tcur, float* tout, float* uout, float* vout) {
+    const float3 A = A3 - r.o, B = B3 - r.o, C = C3 - r.o;
+    const float Akz = comp(A, r.kz), Bkz = comp(B, r.kz), Ckz = comp(C, r.kz);
+    const float Ax = comp(A, r.kx) - r.Sx * Akz;
+    const float Ay = comp(A, r.ky) - r.Sy * Akz;
+    const float Bx = comp(B, r.kx) - r.Sx * Bkz;
+    const float By = comp(B, r.ky) - r.Sy * Bkz;
+    const float Cx = comp(C, r.kx) - r.Sx * Ckz;
+    const float Cy = comp(C, r.ky) - r.Sy * Ckz;
+    float U = __fsub_rn(__fmul_rn(Cx, By), __fmul_rn(Cy, Bx));
+    float V = __fsub_rn(__fmul_rn(Ax, Cy), __fmul_rn(Ay, Cx));
+    float W = __fsub_rn(__fmul_rn(Bx, Ay), __fmul_rn(By, Ax));
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {
+        U = float(double(Cx) * double(By) - double(Cy) * double(Bx));
+        V = float(double(Ax) * double(Cy) - double(Ay) * double(Cx));
+        W = float(double(Bx) * double(Ay) - double(By) * double(Ax));
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    const float Az = r.Sz * Akz, Bz = r.Sz * Bkz, Cz = r.Sz * Ckz;
+    float T = U * Az + V * Bz + W * Cz;
+    if (det < 0.0f) { T = -T; det = -det; U = -U; V = -V; W = -W; }
+    if (T < r.tmin * det || T > tcur * det) return false;
+    const float inv = 1.0f / det;
+    *tout = T * inv;
+    *uout = V * inv;
+    *vout = W * inv;
+    return true;
+}
+
+struct HitD {
+    float t;
+    int slot;  // triangle slot in leaf order, -1 on a miss
+    float u, v;
+};
+
+struct TraceCounters {
+    uint32_t nodes;
+    uint32_t tris;
+};
+
+CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, float4 (&q)[7]) {
+    const float4* p = reinterpret_cast<const float4*>(nodes + idx);
+#pragma unroll
+    for (int i = 0; i < 7; ++i) q[i] = __ldg(p + i);
+}
+
+CG_D float4 ldg4(const float4* p) { return __ldg(p); }
+
+// Child box distances; tnear = +inf marks a miss.
+CG_D void child_hits(const RayPre& r, const float4 (&q)[7], float tcur, float (&tn)[4]) {
+    const float lox[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
+    const float hix[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
+    const float loy[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
+    const float hiy[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
+    const float loz[4] = {q[4].x, q[4].y, q[4].z, q[4].w};
+    const float hiz[4] = {q[5].x, q[5].y, q[5].z, q[5].w};
+    const float tlim = tcur * 1.00000036f;  // 1 + 2 gamma(3)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const float t0x = (lox[i] - r.o.x) * r.inv.x, t1x = (hix[i] - r.o.x) * r.inv.x;
+        const float t0y = (loy[i] - r.o.y) * r.inv.y, t1y = (hiy[i] - r.o.y) * r.inv.y;
+        const float t0z = (loz[i] - r.o.z) * r.inv.z, t1z = (hiz[i] - r.o.z) * r.inv.z;
+        const float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), r.tmin));
+        const float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tlim));
+        tn[i] = (tnear <= tfar * 1.00000036f) ? tnear : __int_as_float(0x7f800000);
+    }
+}
+
+template <bool ANY, bool COUNT>
+CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    uint32_t cur = 0;  // root is always an inner node
+    float tcur = r.tmax;
+    int hslot = -1;
+    float hu = 0.0f, hv = 0.0f;
+    const float kInf = __int_as_float(0x7f800000);
+    for (;;) {
+        if (entry_is_leaf(cur)) {
+            const uint32_t first = leaf_first(cur), n = leaf_count(cur);
+            for (uint32_t k = 0; k < n; ++k) {
+                const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
+                const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+                if (COUNT) cnt->tris++;
+                float t, u, v;
+                if (tri_test(r, f3(a), f3(b), f3(c), tcur, &t, &u, &v)) {
+                    hslot = int(first + k);
+                    if (ANY) {
+                        hit->slot = hslot;
+                        hit->t = t;
+                        return true;
+                    }
+                    tcur = t;
+                    hu = u;
+                    hv = v;
+                }
+            }
+        } else {
+            float4 q[7];
+            load_node(S.nodes, cur, q);
+            if (COUNT) cnt->nodes++;
+            float tn[4];
+            child_hits(r, q, tcur, tn);
+            uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
+                              __float_as_uint(q[6].w)};
+            if (!ANY) {
+                // ascending by distance (misses sort last)
+#define CG_CSWAP(i, j)                                                      \
+    if (tn[j] < tn[i]) {                                                    \
+        const float tt = tn[i]; tn[i] = tn[j]; tn[j] = tt;                  \
+        const uint32_t ee = ce[i]; ce[i] = ce[j]; ce[j] = ee;               \
+    }
+                CG_CSWAP(0, 1) CG_CSWAP(2, 3) CG_CSWAP(0, 2) CG_CSWAP(1, 3) CG_CSWAP(1, 2)
+#undef CG_CSWAP
+            }
+            int nhit = 0;
+            uint32_t nearest = 0;
+            float nearest_t = kInf;
+            // push farther hits first so the nearest is visited next
+#pragma unroll
+            for (int i = 3; i >= 0; --i) {
+                if (tn[i] < kInf) {
+                    if (nhit > 0) {
+                        if (sp < kStackSize) {
+                            stack_e[sp] = nearest;
+                            stack_t[sp] = nearest_t;
+                            ++sp;
+                        }
+                    }
+                    nearest = ce[i];
+                    nearest_t = tn[i];
+                    ++nhit;
+                }
+            }
+            if (nhit > 0) {
+                cur = nearest;
+                continue;
+            }
+        }
+        // pop the next entry that can still hold a closer hit
+        bool found = false;
+        while (sp > 0) {
+            --sp;
+            if (ANY || stack_t[sp] <= tcur * 1.00000036f) {
+                cur = stack_e[sp];
+                found = true;
+                break;
+            }
+        }
+        if (!found) break;
+    }
+    hit->slot = hslot;
+    hit->t = tcur;
+    hit->u = hu;
+    hit->v = hv;
+    return hslot >= 0;
+}
+
+}  // namespace cg

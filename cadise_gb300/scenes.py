@@ -63,6 +63,16 @@ class Rectangle:
 
 
 @dataclass
+class Triangle:
+    """A single ``triangle`` primitive (can carry an area light)."""
+    name: str
+    material: str
+    v1: tuple
+    v2: tuple
+    v3: tuple
+
+
+@dataclass
 class TriangleMesh:
     name: str
     material: str
@@ -109,14 +119,19 @@ class SceneSpec:
         mesh triangle), i.e. the length of its intersector list."""
         n = 0
         for p in self.primitives:
-            n += 1 if isinstance(p, Rectangle) else int(p.positions.shape[0])
+            n += 1 if isinstance(p, (Rectangle, Triangle)) else int(p.positions.shape[0])
         return n
 
     def num_triangles(self) -> int:
         """Triangles after splitting every rectangle in two."""
         n = 0
         for p in self.primitives:
-            n += 2 if isinstance(p, Rectangle) else int(p.positions.shape[0])
+            if isinstance(p, Rectangle):
+                n += 2
+            elif isinstance(p, Triangle):
+                n += 1
+            else:
+                n += int(p.positions.shape[0])
         return n
 
     # ------------------------------------------------------------------- CRSD
@@ -157,7 +172,11 @@ class SceneSpec:
                     w("    [roughness real \"%.9g\"]\n" % m.roughness)
             w("}\n")
         for p in self.primitives:
-            if isinstance(p, Rectangle):
+            if isinstance(p, Triangle):
+                w("primitive {\n    [type string \"triangle\"]\n    [name string \"%s\"]\n"
+                  "    [bsdf material \"%s\"]\n    [v1 vector3r \"%s\"]\n    [v2 vector3r \"%s\"]\n"
+                  "    [v3 vector3r \"%s\"]\n}\n" % (p.name, p.material, v3(p.v1), v3(p.v2), v3(p.v3)))
+            elif isinstance(p, Rectangle):
                 w("primitive {\n    [type string \"rectangle\"]\n    [name string \"%s\"]\n"
                   "    [bsdf material \"%s\"]\n    [v1 vector3r \"%s\"]\n    [v2 vector3r \"%s\"]\n"
                   "    [v3 vector3r \"%s\"]\n}\n" % (p.name, p.material, v3(p.v1), v3(p.v2), v3(p.v3)))
@@ -332,4 +351,44 @@ def icosphere_field(n_spheres: int = 200, subdivision: int = 4, n_lights: int = 
         s.primitives.append(Rectangle(name, "lightBase", (cx + side / 2, y, cz - side / 2),
                                       (cx - side / 2, y, cz - side / 2), (cx - side / 2, y, cz + side / 2)))
         s.lights.append(AreaLight(name, (e, e, e), _quad_light_watt((e, e, e), side * side)))
+    return s
+
+
+def feature_scene(width: int = 48, height: int = 40, spp: int = 16, max_depth: int = 8, seed: int = 11,
+                  dielectric: str = GLASS) -> SceneSpec:
+    """Small scene touching every primitive / light / BSDF path of the
+    estimator: rectangle walls, single-triangle area lights (one two-sided),
+    a smooth-normal icosphere mesh with per-vertex uvws, flat icospheres in
+    Lambert, GGX conductor and dielectric, a rectangle light."""
+    rng = np.random.default_rng(seed)
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(0.0, 6.0, -22.0), cam_direction=(0.0, -0.2, 1.0),
+                  cam_up=(0.0, 1.0, 0.0), fov=50.0)
+    s.materials = [Material("floor", LAMBERT, albedo=(0.6, 0.6, 0.55)),
+                   Material("wall", LAMBERT, albedo=(0.3, 0.5, 0.7)),
+                   Material("gold", CONDUCTOR, roughness=0.25, f0=(1.0, 0.78, 0.34)),
+                   Material("steel", CONDUCTOR, roughness=0.05, f0=(0.56, 0.57, 0.58)),
+                   Material("glass", dielectric, albedo=(1.0, 1.0, 1.0), roughness=0.15, ior_inner=1.5),
+                   Material("clay", LAMBERT, albedo=(0.8, 0.35, 0.2)),
+                   Material("emitterBase", LAMBERT, albedo=(0.2, 0.2, 0.2))]
+    s.primitives.append(Rectangle("floor", "floor", (15, 0, -15), (-15, 0, -15), (-15, 0, 15)))
+    s.primitives.append(Rectangle("back", "wall", (-15, 0, 12), (15, 0, 12), (15, 20, 12)))
+    unit = icosphere(2)
+    smooth = (unit / np.linalg.norm(unit, axis=2, keepdims=True)).astype(np.float32)
+    uv = np.zeros_like(smooth)
+    uv[..., 0] = 0.5 + np.arctan2(smooth[..., 0], smooth[..., 2]) / (2 * math.pi)
+    uv[..., 1] = 0.5 + np.arcsin(np.clip(smooth[..., 1], -1, 1)) / math.pi
+    s.primitives.append(TriangleMesh("smooth", "clay", (unit * 3.0 + [-6.0, 3.0, 2.0]).astype(np.float32),
+                                     normals=smooth, uvws=uv.astype(np.float32)))
+    for j, (mname, c, r) in enumerate([("gold", (0.0, 2.5, 0.0), 2.5), ("steel", (6.0, 2.0, -2.0), 2.0),
+                                       ("glass", (1.5, 1.5, -6.0), 1.5)]):
+        s.primitives.append(TriangleMesh("ball%d" % j, mname, (unit * r + c).astype(np.float32)))
+    s.primitives.append(Triangle("triLight", "emitterBase", (-4, 12, -2), (4, 12, -2), (0, 12, 4)))
+    s.primitives.append(Triangle("sideLight", "emitterBase", (12, 2, -4), (12, 8, 0), (12, 2, 4)))
+    s.primitives.append(Rectangle("quadLight", "emitterBase", (3, 10, 6), (-3, 10, 6), (-3, 10, 9)))
+    s.lights = [AreaLight("triLight", (10.0, 9.0, 8.0), 10.0 * 1.0),
+                AreaLight("sideLight", (2.0, 4.0, 8.0), 600.0, back_face_emit=True),
+                AreaLight("quadLight", (6.0, 6.0, 5.0), _quad_light_watt((6.0, 6.0, 5.0), 18.0))]
+    # watt of the triangle light chosen so its radiance is ~(17, 15, 13)
+    s.lights[0].watt = float(sum((10.0, 9.0, 8.0))) * 24.0 * math.pi * 1.7
     return s

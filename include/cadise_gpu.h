@@ -225,16 +225,38 @@ cgpu_status cgpu_render_paths(cgpu_ctx* ctx, int32_t scene, int32_t mode, uint32
 /* Device-side counters of the last render (for throughput and roofline). */
 typedef struct cgpu_render_stats {
     uint64_t paths;
-    uint64_t closest_rays;
+    uint64_t closest_rays;        /* counting renders only (cgpu_set_counting), else 0 */
     uint64_t any_rays;
-    uint64_t node_visits;      /* 4-wide nodes fetched (counting builds only, else 0) */
-    uint64_t triangle_tests;
-    uint32_t kernel_launches;  /* kernels this library launched in the last cgpu_render */
-    uint32_t timeouts;
+    uint64_t node_visits;         /* 4-wide nodes fetched by closest-hit rays */
+    uint64_t triangle_tests;      /* triangles tested by closest-hit rays */
+    uint64_t any_node_visits;     /* ... by any-hit rays */
+    uint64_t any_triangle_tests;
+    uint64_t h2d_bytes;           /* host->device bytes the last cgpu_render copied (batch tables) */
+    uint32_t kernel_launches;     /* kernels this library launched in the last cgpu_render */
+    uint32_t batches;             /* path batches the last cgpu_render ran */
 } cgpu_render_stats;
 cgpu_status cgpu_render_stats_get(cgpu_ctx* ctx, cgpu_render_stats* out_stats);
 /* Count rays, node fetches and triangle tests in every following render (slower). */
 cgpu_status cgpu_set_counting(cgpu_ctx* ctx, int32_t enabled);
+
+/* Per-kernel CUDA-event timing of the following renders (launches are made
+ * one by one instead of through the captured graph while it is on). */
+enum {
+    CGPU_KERNEL_GENERATE = 0,
+    CGPU_KERNEL_EXTEND = 1,     /* closest-hit traversal (continuation + MIS rays) */
+    CGPU_KERNEL_SHADOW = 2,     /* any-hit traversal */
+    CGPU_KERNEL_SHADE = 3,      /* all shade-by-BSDF kernels */
+    CGPU_KERNEL_SPLAT = 4,
+    CGPU_KERNEL_MEGAKERNEL = 5,
+    CGPU_KERNEL_CLASSES = 8
+};
+typedef struct cgpu_kernel_times {
+    double ms[CGPU_KERNEL_CLASSES];
+    uint32_t launches[CGPU_KERNEL_CLASSES];
+} cgpu_kernel_times;
+cgpu_status cgpu_set_profiling(cgpu_ctx* ctx, int32_t enabled);
+/* Totals over the last cgpu_render call. */
+cgpu_status cgpu_kernel_times_get(cgpu_ctx* ctx, cgpu_kernel_times* out_times);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,227 @@
+"""GPU parity: the CUDA path (through the C ABI) against the reference's own
+outputs (tests/golden/) and against the oracle restatement.
+
+Tolerances (FP32 path tracer):
+  * camera rays: 2e-6 absolute per component;
+  * closest hits: identical hit/miss and primitive id except rays whose hit
+    point lies within 1e-5 (relative barycentric / edge coordinate) of a
+    primitive edge, where the reference's non-watertight test and the
+    watertight one may legitimately disagree; |dt| / t <= 1e-5;
+  * per-path radiance: the GPU evaluates transcendental functions and
+    contracted products differently from the host, so a path may branch
+    differently after a near-tie; >= 97 % of paths within 1e-3 relative
+    (+1e-5 absolute) and the mean over all paths within 1 %;
+  * images: relMSE <= 1e-3 against the converged reference render and a
+    per-pixel Welch z-test failure fraction <= 1 % + 3 sigma (p = 0.01);
+  * wavefront vs megakernel: bit-identical per path.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from cadise_gb300 import CGPU_MODE_MEGAKERNEL, CGPU_MODE_WAVEFRONT, CgpuError, abi, scenes
+from golden_scenes import image, specs, vectors
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["cornell", "field", "features"]
+
+
+@pytest.fixture(scope="module")
+def uploaded(gpu_ctx):
+    out = {}
+    for name, spec in specs().items():
+        flat = abi.flatten(spec)
+        out[name] = (spec, flat, gpu_ctx.upload(flat))
+    return out
+
+
+def edge_margin(flat, prim, P):
+    """Smallest relative distance of points P (n, 3) to the edges of their
+    primitives (barycentric for triangles, edge coordinates for rectangles)."""
+    m = np.full(len(prim), np.inf)
+    for i, (p, x) in enumerate(zip(prim, P)):
+        if p < 0:
+            continue
+        v = flat.vertices[p].reshape(3, 3).astype(np.float64)
+        if flat.kind[p] == abi.CGPU_PRIM_TRIANGLE:
+            e0, e1, w = v[1] - v[0], v[2] - v[0], x - v[0]
+            d00, d01, d11 = e0 @ e0, e0 @ e1, e1 @ e1
+            d20, d21 = w @ e0, w @ e1
+            den = d00 * d11 - d01 * d01
+            if den == 0:
+                m[i] = 0
+                continue
+            b1 = (d11 * d20 - d01 * d21) / den
+            b2 = (d00 * d21 - d01 * d20) / den
+            m[i] = min(abs(b1), abs(b2), abs(1 - b1 - b2))
+        else:
+            eA, eB = v[0] - v[1], v[2] - v[1]
+            w = x - v[1]
+            a = w @ eA / (eA @ eA)
+            b = w @ eB / (eB @ eB)
+            m[i] = min(abs(a), abs(1 - a), abs(b), abs(1 - b))
+    return m
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_camera_rays_match_reference(name, gpu_ctx, uploaded):
+    v = vectors(name)
+    spec, flat, sid = uploaded[name]
+    rays = gpu_ctx.camera_rays(sid, v["camera_xy"])
+    assert np.max(np.abs(rays - v["camera_rays"])) <= 2e-6 * max(1.0, np.abs(v["camera_rays"]).max())
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_closest_hits_match_reference(name, gpu_ctx, uploaded):
+    v = vectors(name)
+    spec, flat, sid = uploaded[name]
+    rays = v["trace_rays"]
+    prim, t, u, w = gpu_ctx.trace_closest(sid, rays)
+    ref_p, ref_t = v["trace_bvh_prim"], v["trace_bvh_t"]
+    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
+    near = np.zeros(len(prim), bool)
+    diff = np.where(prim != ref_p)[0]
+    if len(diff):
+        m_ref = edge_margin(flat, ref_p[diff], o[diff] + d[diff] * ref_t[diff, None])
+        m_gpu = edge_margin(flat, prim[diff], o[diff] + d[diff] * t[diff, None])
+        near[diff] = (m_ref < 1e-5) | (m_gpu < 1e-5)
+    tie = ref_p != v["trace_bf_prim"]  # the reference's own BVH / brute-force tie
+    keep = ~(near | tie)
+    assert np.mean(keep) > 0.98
+    assert np.array_equal(prim[keep], ref_p[keep]), np.where(prim[keep] != ref_p[keep])
+    both = keep & (prim >= 0)
+    rel = np.abs(t[both] - ref_t[both]) / np.maximum(np.abs(ref_t[both]), 1e-6)
+    assert rel.max() <= 1e-5
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_any_hit_matches_reference(name, gpu_ctx, uploaded):
+    v = vectors(name)
+    spec, flat, sid = uploaded[name]
+    rays = v["trace_rays"]
+    occ = gpu_ctx.trace_any(sid, rays).astype(np.int32)
+    prim, t, _, _ = gpu_ctx.trace_closest(sid, rays)
+    # exclude grazing edge hits and occluders sitting on the t_max boundary
+    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
+    m = edge_margin(flat, prim, o + d * t[:, None])
+    boundary = (prim >= 0) & (np.abs(t - rays[:, 7]) <= 1e-5 * np.abs(rays[:, 7]))
+    keep = (m >= 1e-5) & ~boundary
+    assert np.array_equal(occ[keep], v["trace_occluded"][keep])
+    # occlusion is consistent with the closest hit on the same rays
+    assert np.array_equal(occ[keep], (prim[keep] >= 0).astype(np.int32))
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_path_radiance_matches_reference(name, gpu_ctx, uploaded):
+    v = vectors(name)
+    spec, flat, sid = uploaded[name]
+    rgb = gpu_ctx.path_radiance(sid, v["paths_xy"], v["paths_keys"])
+    ref = v["paths_rgb"]
+    close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
+    assert close.mean() >= 0.97, close.mean()
+    assert abs(rgb.mean() - ref.mean()) <= 0.01 * abs(ref.mean()) + 1e-6
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_wavefront_equals_megakernel_per_path(name, gpu_ctx, uploaded):
+    spec, flat, sid = uploaded[name]
+    wf = gpu_ctx.render_paths(sid, 0, 4, seed=5, mode=CGPU_MODE_WAVEFRONT)
+    mk = gpu_ctx.render_paths(sid, 0, 4, seed=5, mode=CGPU_MODE_MEGAKERNEL)
+    assert np.array_equal(wf, mk)
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_render_paths_match_oracle(name, gpu_ctx, uploaded):
+    spec, flat, sid = uploaded[name]
+    gpu = gpu_ctx.render_paths(sid, 3, 2, seed=11, mode=CGPU_MODE_WAVEFRONT)
+    ps = oracle.PortScene(flat)
+    _, port = ps.render(seed=11, first=3, count=2, threads=8, want_paths=True)
+    close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
+    assert close.mean() >= 0.97, close.mean()
+
+
+def test_film_equals_sum_of_paths(gpu_ctx, uploaded):
+    spec, flat, sid = uploaded["features"]
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, 8, seed=21, mode=CGPU_MODE_WAVEFRONT, graph=True)
+    s, q, n = gpu_ctx.film_read(sid)
+    paths = gpu_ctx.render_paths(sid, 0, 8, seed=21, mode=CGPU_MODE_WAVEFRONT).astype(np.float64)
+    finite = np.all(np.isfinite(paths), axis=-1)
+    p = np.where(finite[..., None], paths, 0.0)
+    np.testing.assert_allclose(s, p.sum(0), rtol=1e-9, atol=1e-12)
+    np.testing.assert_allclose(q, (p * p).sum(0), rtol=1e-9, atol=1e-12)
+    assert np.array_equal(n, finite.sum(0).astype(np.float64))
+
+
+def test_graph_replay_equals_direct_launches(gpu_ctx, uploaded):
+    spec, flat, sid = uploaded["field"]
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, 4, seed=8, mode=CGPU_MODE_WAVEFRONT, graph=True)
+    a = gpu_ctx.film_read(sid)
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, 4, seed=8, mode=CGPU_MODE_WAVEFRONT, graph=False)
+    b = gpu_ctx.film_read(sid)
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, 4, seed=8, mode=CGPU_MODE_MEGAKERNEL)
+    c = gpu_ctx.film_read(sid)
+    for x, y, z in zip(a, b, c):
+        assert np.array_equal(x, y)
+        assert np.array_equal(x, z)
+
+
+def rel_mse(x, ref):
+    return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
+
+
+@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("field", 8192), ("features", 8192)])
+def test_image_converges_to_reference(name, spp, gpu_ctx, uploaded):
+    spec, flat, sid = uploaded[name]
+    ref = image(name)
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, spp, seed=1234, mode=CGPU_MODE_WAVEFRONT)
+    s, q, n = gpu_ctx.film_read(sid)
+    mean_g = s / n[..., None]
+    var_g = (q / n[..., None] - mean_g ** 2) / n[..., None]
+    mean_r = ref["sum"] / ref["count"][..., None]
+    var_r = (ref["sum_sq"] / ref["count"][..., None] - mean_r ** 2) / ref["count"][..., None]
+    assert rel_mse(mean_g, mean_r) <= 1e-3
+    z = (mean_g - mean_r) / np.sqrt(var_g + var_r + 1e-30)
+    frac = float(np.mean(np.abs(z) > 2.576))
+    assert frac <= 0.01 + 3 * np.sqrt(0.01 * 0.99 / z.size) + 0.005, frac
+
+
+def test_invalid_arguments_are_reported(gpu_ctx, uploaded):
+    with pytest.raises(CgpuError) as e:
+        gpu_ctx.render([12345], 0, 1, seed=0)
+    assert e.value.status == 6  # CGPU_ERR_NOT_FOUND
+    bad = scenes.cornell_box(8, 8, 1, 2)
+    bad.lights = []
+    with pytest.raises(CgpuError) as e:
+        gpu_ctx.upload(bad)
+    assert e.value.status == 1  # CGPU_ERR_INVALID_ARGUMENT
+    empty_film = scenes.cornell_box(8, 8, 1, 2)
+    empty_film.width = 0
+    with pytest.raises(CgpuError):
+        gpu_ctx.upload(empty_film)
+
+
+def test_full_size_field_properties(gpu_ctx):
+    """The 1,024,000-triangle field at 1920x1080: one pass in both modes
+    agrees path for path on a sample of pixels, every pixel receives its
+    sample, and the film holds no NaN."""
+    spec = scenes.icosphere_field()
+    flat = abi.flatten(spec)
+    sid = gpu_ctx.upload(flat)
+    info = gpu_ctx.info(sid)
+    assert info.num_triangles == 1024000 + 2 + 2 * 8
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, 1, seed=3, mode=CGPU_MODE_WAVEFRONT)
+    s, q, n = gpu_ctx.film_read(sid)
+    assert np.all(n == 1.0)
+    assert np.all(np.isfinite(s))
+    gpu_ctx.film_clear(sid)
+    gpu_ctx.render([sid], 0, 1, seed=3, mode=CGPU_MODE_MEGAKERNEL)
+    s2, q2, n2 = gpu_ctx.film_read(sid)
+    assert np.array_equal(s, s2)
+    gpu_ctx.release(sid)
