@@ -30,6 +30,9 @@ EXPORTED = [
     "cgpu_camera_rays", "cgpu_render", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
     "cgpu_kernel_times_get",
+    # include/cadise_crsd.h
+    "cgpu_crsd_load_file", "cgpu_crsd_load_text", "cgpu_crsd_desc", "cgpu_crsd_settings_get",
+    "cgpu_crsd_primitive_index", "cgpu_crsd_free",
 ]
 
 KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel"]
@@ -44,7 +47,7 @@ class CgpuError(RuntimeError):
 
 
 def build(verbose: bool = False) -> str:
-    from .build import build as _build
+    from .native_build import build as _build
     return _build(verbose=verbose)
 
 
@@ -85,6 +88,15 @@ def load(path: Optional[str] = None):
     L.cgpu_set_counting.argtypes = [vp, C.c_int32]
     L.cgpu_set_profiling.argtypes = [vp, C.c_int32]
     L.cgpu_kernel_times_get.argtypes = [vp, C.POINTER(abi.cgpu_kernel_times)]
+    L.cgpu_crsd_load_file.argtypes = [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]
+    L.cgpu_crsd_load_text.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(vp), C.c_char_p, C.c_size_t]
+    L.cgpu_crsd_desc.argtypes = [vp]
+    L.cgpu_crsd_desc.restype = C.POINTER(abi.cgpu_scene_desc)
+    L.cgpu_crsd_settings_get.argtypes = [vp, C.POINTER(abi.cgpu_crsd_settings)]
+    L.cgpu_crsd_primitive_index.argtypes = [vp, C.c_char_p]
+    L.cgpu_crsd_primitive_index.restype = C.c_int32
+    L.cgpu_crsd_free.argtypes = [vp]
+    L.cgpu_crsd_free.restype = None
     _lib = L
     return L
 
@@ -129,7 +141,11 @@ class Context:
 
     # ---------------------------------------------------------------- scenes
     def upload(self, scene) -> int:
-        flat = scene if isinstance(scene, FlatScene) else flatten(scene)
+        """Upload a SceneSpec, a FlatScene or a CrsdScene."""
+        if isinstance(scene, CrsdScene):
+            flat = scene
+        else:
+            flat = scene if isinstance(scene, FlatScene) else flatten(scene)
         sid = C.c_int32(-1)
         self._check(self.L.cgpu_scene_upload(self.h, C.addressof(flat.desc), C.byref(sid)))
         self._scenes[sid.value] = flat
@@ -229,6 +245,57 @@ class Context:
         out = abi.cgpu_kernel_times()
         self._check(self.L.cgpu_kernel_times_get(self.h, C.byref(out)))
         return {name: (out.ms[i], out.launches[i]) for i, name in enumerate(KERNEL_CLASSES)}
+
+
+class CrsdScene:
+    """A CRSD scene parsed by the library's C++ loader (include/cadise_crsd.h).
+
+    ``desc`` points into memory owned by the loader; it can be handed to
+    :meth:`Context.upload` directly."""
+
+    def __init__(self, path: Optional[str] = None, text: Optional[str] = None):
+        self.L = load()
+        h = C.c_void_p()
+        err = C.create_string_buffer(512)
+        if path is not None:
+            st = self.L.cgpu_crsd_load_file(path.encode(), C.byref(h), err, 512)
+        else:
+            b = text.encode()
+            st = self.L.cgpu_crsd_load_text(b, len(b), C.byref(h), err, 512)
+        if st != 0:
+            raise CgpuError(st, err.value.decode())
+        self.h = h
+        self.desc = self.L.cgpu_crsd_desc(h).contents
+
+    def settings(self) -> "abi.cgpu_crsd_settings":
+        out = abi.cgpu_crsd_settings()
+        st = self.L.cgpu_crsd_settings_get(self.h, C.byref(out))
+        if st != 0:
+            raise CgpuError(st, "settings")
+        return out
+
+    def primitive_index(self, name: str) -> int:
+        return self.L.cgpu_crsd_primitive_index(self.h, name.encode())
+
+    def arrays(self):
+        """numpy views of the flat primitive arrays (kind, vertices, material)."""
+        d = self.desc
+        n = d.num_primitives
+        kind = np.ctypeslib.as_array(d.prim_kind, shape=(n,)).copy()
+        verts = np.ctypeslib.as_array(d.prim_vertices, shape=(n, 9)).copy()
+        mat = np.ctypeslib.as_array(d.prim_material, shape=(n,)).copy()
+        return kind, verts, mat
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.cgpu_crsd_free(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def gpu_available() -> bool:

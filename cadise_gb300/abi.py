@@ -102,6 +102,12 @@ class cgpu_render_stats(C.Structure):
                 ("h2d_bytes", C.c_uint64), ("kernel_launches", C.c_uint32), ("batches", C.c_uint32)]
 
 
+class cgpu_crsd_settings(C.Structure):
+    _fields_ = [("renderer_type", C.c_char * 32), ("estimator", C.c_char * 16), ("sampler", C.c_char * 16),
+                ("output_filename", C.c_char * 256), ("spp", C.c_int32), ("max_depth", C.c_int32),
+                ("mode", C.c_int32), ("use_graph", C.c_int32), ("seed", C.c_uint64)]
+
+
 class cgpu_kernel_times(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint32 * 8)]
 

@@ -15,9 +15,11 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
+HOST = os.path.join(HERE, "host")
 BUILD = os.path.join(HERE, "_build")
 INCLUDE = os.path.abspath(os.path.join(HERE, "..", "include"))
 LIB = os.path.join(BUILD, "libcadise_gpu.so")
+CLI = os.path.join(BUILD, "cadise-gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -37,12 +39,16 @@ def _cuda_include() -> str:
 
 
 def sources():
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
+    out = []
+    for d in (CSRC, HOST):
+        out += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".cu", ".cpp")) and f != "cli.cpp"]
+    return sorted(out)
 
 
 def headers():
-    hs = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
-    hs.append(os.path.join(INCLUDE, "cadise_gpu.h"))
+    hs = []
+    for d in (CSRC, HOST, INCLUDE):
+        hs += [os.path.join(d, f) for f in os.listdir(d) if f.endswith((".cuh", ".h"))]
     return hs
 
 
@@ -86,6 +92,13 @@ def build(verbose: bool = False, jobs: int = 0) -> str:
         if r.returncode != 0:
             raise RuntimeError("link failed: %s\n%s" % (r.stdout, r.stderr))
         os.replace(tmp, LIB)
+    cli_src = os.path.join(HOST, "cli.cpp")
+    if _stale(CLI, [cli_src, LIB] + headers()):
+        cmd = ["g++"] + CXX_FLAGS + ["-I", INCLUDE, "-I", _cuda_include(), cli_src, "-o", CLI, "-L", BUILD,
+                                     "-lcadise_gpu", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("cli build failed: %s\n%s" % (r.stdout, r.stderr))
     return LIB
 
 

@@ -9,12 +9,15 @@ import pytest
 import cadise_gb300 as cg
 from cadise_gb300 import abi
 
-HEADER = os.path.join(os.path.dirname(__file__), "..", "include", "cadise_gpu.h")
+INCLUDE = os.path.join(os.path.dirname(__file__), "..", "include")
 
 
 def declared_functions():
-    text = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(cgpu_[a-z_0-9]+)\s*\(", text)))
+    names = set()
+    for f in os.listdir(INCLUDE):
+        if f.endswith(".h"):
+            names |= set(re.findall(r"\b(cgpu_[a-z_0-9]+)\s*\(", open(os.path.join(INCLUDE, f)).read()))
+    return sorted(names)
 
 
 @pytest.fixture(scope="module")
