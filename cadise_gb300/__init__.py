@@ -29,7 +29,8 @@ EXPORTED = [
     "cgpu_trace_closest", "cgpu_trace_any", "cgpu_trace_closest_device", "cgpu_trace_any_device",
     "cgpu_camera_rays", "cgpu_render", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
-    "cgpu_kernel_times_get",
+    "cgpu_kernel_times_get", "cgpu_param_counts_get", "cgpu_params_get", "cgpu_params_set",
+    "cgpu_adjoint_forward", "cgpu_adjoint_backward",
     # include/cadise_crsd.h
     "cgpu_crsd_load_file", "cgpu_crsd_load_text", "cgpu_crsd_desc", "cgpu_crsd_settings_get",
     "cgpu_crsd_primitive_index", "cgpu_crsd_free",
@@ -88,6 +89,11 @@ def load(path: Optional[str] = None):
     L.cgpu_set_counting.argtypes = [vp, C.c_int32]
     L.cgpu_set_profiling.argtypes = [vp, C.c_int32]
     L.cgpu_kernel_times_get.argtypes = [vp, C.POINTER(abi.cgpu_kernel_times)]
+    L.cgpu_param_counts_get.argtypes = [vp, C.c_int32, C.POINTER(abi.cgpu_param_counts)]
+    L.cgpu_params_get.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.cgpu_params_set.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.cgpu_adjoint_forward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp]
+    L.cgpu_adjoint_backward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp, vp, vp, vp]
     L.cgpu_crsd_load_file.argtypes = [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]
     L.cgpu_crsd_load_text.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(vp), C.c_char_p, C.c_size_t]
     L.cgpu_crsd_desc.argtypes = [vp]
@@ -236,6 +242,47 @@ class Context:
 
     def set_counting(self, on: bool):
         self._check(self.L.cgpu_set_counting(self.h, 1 if on else 0))
+
+    # --------------------------------------------------------------- adjoint
+    def param_counts(self, sid: int):
+        out = abi.cgpu_param_counts()
+        self._check(self.L.cgpu_param_counts_get(self.h, sid, C.byref(out)))
+        return int(out.texel_floats), int(out.materials), int(out.lights)
+
+    def get_params(self, sid: int):
+        nt, nm, nl = self.param_counts(sid)
+        tex = np.zeros(nt, np.float32)
+        rough = np.zeros(nm, np.float32)
+        rad = np.zeros((nl, 3), np.float32)
+        self._check(self.L.cgpu_params_get(self.h, sid, _p(tex) if nt else None, _p(rough), _p(rad)))
+        return tex, rough, rad
+
+    def set_params(self, sid: int, texels=None, roughness=None, radiance=None):
+        args = []
+        keep = []
+        for a in (texels, roughness, radiance):
+            if a is None:
+                args.append(None)
+            else:
+                a = np.ascontiguousarray(a, dtype=np.float32)
+                keep.append(a)
+                args.append(_p(a))
+        self._check(self.L.cgpu_params_set(self.h, sid, *args))
+
+    def adjoint_forward(self, sid: int, spp: int, seed: int) -> np.ndarray:
+        flat = self._scenes[sid]
+        img = np.zeros((flat.desc.height, flat.desc.width, 3), np.float32)
+        self._check(self.L.cgpu_adjoint_forward(self.h, sid, spp, seed, _p(img)))
+        return img
+
+    def adjoint_backward(self, sid: int, spp: int, seed: int, d_loss_d_image: np.ndarray):
+        nt, nm, nl = self.param_counts(sid)
+        dl = np.ascontiguousarray(d_loss_d_image, dtype=np.float32)
+        gt = np.zeros(max(nt, 1), np.float64)
+        gr = np.zeros(max(nm, 1), np.float64)
+        gl = np.zeros((max(nl, 1), 3), np.float64)
+        self._check(self.L.cgpu_adjoint_backward(self.h, sid, spp, seed, _p(dl), _p(gt), _p(gr), _p(gl)))
+        return gt[:nt], gr[:nm], gl[:nl]
 
     def set_profiling(self, on: bool):
         self._check(self.L.cgpu_set_profiling(self.h, 1 if on else 0))

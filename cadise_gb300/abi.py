@@ -108,6 +108,10 @@ class cgpu_crsd_settings(C.Structure):
                 ("mode", C.c_int32), ("use_graph", C.c_int32), ("seed", C.c_uint64)]
 
 
+class cgpu_param_counts(C.Structure):
+    _fields_ = [("texel_floats", C.c_uint64), ("materials", C.c_uint32), ("lights", C.c_uint32)]
+
+
 class cgpu_kernel_times(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint32 * 8)]
 

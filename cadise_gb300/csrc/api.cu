@@ -404,6 +404,11 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
         return st;
     }
     sl.film = FilmD{film, film + 3 * npix, film + 6 * npix};
+    sl.h_mats = mats;
+    sl.h_lights = lights;
+    sl.h_texs = texs;
+    sl.d_mats = dm;
+    sl.d_lights = dl;
     SceneD& S = sl.d;
     S.nodes = dn;
     S.tris = dt;

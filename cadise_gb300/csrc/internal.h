@@ -70,6 +70,12 @@ struct RenderArgs {
 struct SceneSlot {
     bool live = false;
     cg::SceneD d{};
+    // host copies of the differentiable tables (cgpu_params_get / _set)
+    std::vector<cg::MaterialD> h_mats;
+    std::vector<cg::LightD> h_lights;
+    std::vector<cg::TextureD> h_texs;  // device texel pointers
+    cg::MaterialD* d_mats = nullptr;
+    cg::LightD* d_lights = nullptr;
     std::vector<void*> allocations;
     cgpu_scene_info info{};
     cg::FilmD film{};

@@ -14,109 +14,12 @@
 // Queues hold path ids; per-path state lives in SoA arrays indexed by path.
 // Queue appends are warp-aggregated (ballot / match + one atomic per group).
 #include "internal.h"
-#include "shading.cuh"
+#include "pathtrace.cuh"
 
 #include <algorithm>
 #include <cstring>
 
 namespace cg {
-
-struct PathId {
-    int scene;
-    uint32_t pixel, sample, width;
-};
-
-CG_D int find_chunk(const Chunk* ch, int n, uint32_t p) {
-    int lo = 0, hi = n - 1;
-    while (lo < hi) {
-        const int mid = (lo + hi + 1) >> 1;
-        if (ch[mid].path_begin <= p) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-CG_D PathId path_id(const Chunk* chunks, int nchunks, uint32_t p) {
-    const Chunk& c = chunks[find_chunk(chunks, nchunks, p)];
-    const uint32_t local = p - c.path_begin;
-    PathId id;
-    id.scene = c.scene;
-    id.sample = c.sample0 + local / c.npix;
-    id.pixel = local % c.npix;
-    id.width = c.width;
-    return id;
-}
-
-CG_D void primary_ray(const SceneD& S, const PathId& id, uint64_t seed, Rng& rng, float3* o, float3* d) {
-    rng.key = path_key(seed, uint32_t(id.scene), id.pixel, id.sample);
-    rng.ctr = 0;
-    float jx, jy;
-    stratum_jitter(S.spp, id.sample, rng, &jx, &jy);
-    const float fx = float(id.pixel % id.width) + jx;
-    const float fy = float(id.pixel / id.width) + jy;
-    camera_ray(S.cam, fx, fy, o, d);
-}
-
-CG_D int light_of_slot(const SceneD& S, int slot) {
-    const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
-    return int(__float_as_uint(ldg4(tp + 1).w) >> 16) - 1;
-}
-CG_D int material_of_slot(const SceneD& S, int slot) {
-    const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
-    return int(__float_as_uint(ldg4(tp + 1).w) & 0xFFFFu);
-}
-
-// Counting replay: [0] closest rays, [1] any-hit rays, [2] / [3] 4-wide
-// nodes / triangles fetched by closest-hit rays, [4] / [5] by any-hit rays.
-template <bool COUNT>
-CG_D void count_flush(unsigned long long* counters, const TraceCounters& cc, const TraceCounters& ca, uint32_t closest,
-                      uint32_t any) {
-    if (!COUNT) return;
-    if (closest) atomicAdd(counters + 0, (unsigned long long)closest);
-    if (any) atomicAdd(counters + 1, (unsigned long long)any);
-    if (cc.nodes) atomicAdd(counters + 2, (unsigned long long)cc.nodes);
-    if (cc.tris) atomicAdd(counters + 3, (unsigned long long)cc.tris);
-    if (ca.nodes) atomicAdd(counters + 4, (unsigned long long)ca.nodes);
-    if (ca.tris) atomicAdd(counters + 5, (unsigned long long)ca.tris);
-}
-
-// One whole path sample (PtEstimator::estimate): the megakernel body.
-template <bool COUNT>
-CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, float3* Lsout, TraceCounters* tc,
-                  TraceCounters* ta, uint32_t* nclosest, uint32_t* nany) {
-    float3 L = splat3(0.0f), Ls = splat3(0.0f), T = splat3(1.0f);
-    bool ce = true;
-    for (int b = 0; b < S.max_depth; ++b) {
-        const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
-        HitD hit;
-        if (COUNT) ++*nclosest;
-        if (!traverse<false, COUNT>(S, r, &hit, tc)) break;
-        const SurfaceD si = surface_at(S, o, d, hit);
-        const VertexPlan pl = plan_vertex(S, si, T, ce, b, rng);
-        L += pl.emit;
-        if (pl.shadow) {
-            const RayPre sr = ray_prep(si.P, pl.sdir, kRayEps, pl.stmax);
-            HitD sh;
-            if (COUNT) ++*nany;
-            if (!traverse<true, COUNT>(S, sr, &sh, ta)) Ls += pl.scontrib;
-        }
-        if (pl.mis) {
-            const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
-            HitD mh;
-            if (COUNT) ++*nclosest;
-            if (traverse<false, COUNT>(S, mr, &mh, tc) && light_of_slot(S, mh.slot) == pl.mlight) {
-                const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
-                L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);
-            }
-        }
-        if (!pl.cont) break;
-        T = pl.T;
-        ce = pl.count_emission != 0;
-        o = si.P;
-        d = pl.cdir;
-    }
-    *Lout = L;
-    *Lsout = Ls;
-}
 
 template <bool COUNT>
 __global__ void k_megakernel(RenderArgs a) {

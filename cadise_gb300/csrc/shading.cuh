@@ -468,6 +468,8 @@ struct VertexPlan {
     float3 emit;          // T * Le, added to L now
     int shadow;           // shadow ray (P, sdir, stmax) unoccluded => Ls += scontrib
     float3 sdir, scontrib;
+    float3 sx;            // scontrib without the light's radiance factor (adjoint)
+    int slight;
     float stmax;
     int mis;              // MIS ray (P, mdir): hitting light `mlight` => L += mis_resolve(...)
     float3 mdir, mfactor;
@@ -511,6 +513,8 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
                 p.sdir = normalize(L);
                 p.stmax = dist - kRayEps;
                 p.scontrib = T * part;
+                p.sx = T * divs(divs(factor * w, ls.pdfW), pick);
+                p.slight = li;
             }
             const BsdfS bs = bsdf_sample(S, m, si, rng);
             if (bs.valid()) {
@@ -543,13 +547,62 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
 // The BSDF-sampling half of DirectLightEvaluator::evaluate
 // (directLightEvaluator.cpp:79-106), divided by the pick pdf and weighted by
 // the throughput at the vertex (ptEstimator.cpp:80-83).
-CG_D float3 mis_resolve(const SceneD& S, const SurfaceD& hit, float3 origin, float3 T, float3 factor, float pdf) {
+CG_D float3 mis_resolve(const SceneD& S, const SurfaceD& hit, float3 origin, float3 T, float3 factor, float pdf,
+                        float3* x_out = nullptr) {
     const LightD& l = S.lights[hit.light];
     const float3 rad = light_emittance(l, hit);
     const float lp = light_pdfW(l, hit, origin);
     const float w = mis_power(pdf, lp);
     const float pick = 1.0f / float(S.num_lights);
+    if (x_out) *x_out = can_emit(l, hit.wi, hit.Ns) ? T * divs(divs(factor * w, pdf), pick) : splat3(0.0f);
     return T * divs(divs(rad * w * factor, pdf), pick);
+}
+
+// d ln(D G) / d alpha of the isotropic GGX terms above (D of isotropicGgx.cpp:11-34,
+// separable Smith G of :36-69) at microfacet normal cosine NH and the two
+// direction cosines: ln D = 2 ln a - 4 ln c - 2 ln(a^2 + tan^2) + const,
+// ln G1 = ln 2 - ln(1 + s), s = sqrt(1 + a^2 tan^2(theta_v)).
+CG_D float ggx_dlogDG_dalpha(float a, float NH, float cv, float cl) {
+    const float c2 = NH * NH;
+    const float t2 = (1.0f - c2) / c2;
+    float g = 2.0f / a - 4.0f * a / (a * a + t2);
+    const float tv = (1.0f - cv * cv) / (cv * cv), tl = (1.0f - cl * cl) / (cl * cl);
+    const float sv = sqrtf(1.0f + a * a * tv), sl = sqrtf(1.0f + a * a * tl);
+    g -= a * tv / (sv * (1.0f + sv));
+    g -= a * tl / (sl * (1.0f + sl));
+    return g;
+}
+
+// d ln f / d roughness of a GGX BSDF for the pair (V, L) (0 where f does not
+// depend on roughness or the roughness floor clamps it), with
+// alpha = max(max(r, 1e-3)^2, 1e-3) (tRoughnessMapper.h:18-40).
+CG_D float dlogf_droughness(const MaterialD& m, float3 V, float3 L, float3 N) {
+    if (m.type != BSDF_CONDUCTOR && m.type != BSDF_DIELECTRIC_GGX) return 0.0f;
+    const float r = m.roughness;
+    if (!(r > 1e-3f) || !(r * r > 1e-3f)) return 0.0f;
+    const float cv = dot(V, N), cl = dot(L, N);
+    if (cv == 0.0f || cl == 0.0f) return 0.0f;
+    float3 H;
+    if (cv * cl > 0.0f) {
+        H = V + L;
+    } else {
+        const float etaV = cv > 0.0f ? m.ior_outer : m.ior_inner;
+        const float etaL = cv > 0.0f ? m.ior_inner : m.ior_outer;
+        H = V + L * (etaL / etaV);
+    }
+    if (is_zero(H)) return 0.0f;
+    H = normalize(H);
+    const float NH = fabsf(dot(N, H));
+    const float g = ggx_dlogDG_dalpha(m.alpha, NH, fabsf(cv), fabsf(cl)) * (2.0f * r);
+    return isfinite(g) ? g : 0.0f;
+}
+
+CG_D int texel_index(const TextureD& t, float3 uvw) {
+    const float u = uvw.x - floorf(uvw.x), v = uvw.y - floorf(uvw.y);
+    int x = int(u * float(t.width)), y = int(v * float(t.height));
+    x = x < t.width ? x : x - 1;
+    y = y < t.height ? y : y - 1;
+    return y * t.width + x;
 }
 
 }  // namespace cg

@@ -392,3 +392,71 @@ def feature_scene(width: int = 48, height: int = 40, spp: int = 16, max_depth: i
     # watt of the triangle light chosen so its radiance is ~(17, 15, 13)
     s.lights[0].watt = float(sum((10.0, 9.0, 8.0))) * 24.0 * math.pi * 1.7
     return s
+
+
+def _smooth_texture(rng, size: int, lo: float = 0.2, hi: float = 0.8) -> np.ndarray:
+    """Seeded smooth RGB pattern in [lo, hi] (sum of a few random sinusoids)."""
+    y, x = np.mgrid[0:size, 0:size].astype(np.float64) / size
+    img = np.zeros((size, size, 3))
+    for c in range(3):
+        acc = np.zeros((size, size))
+        for _ in range(4):
+            fx, fy = rng.integers(1, 6, 2)
+            ph = rng.uniform(0, 2 * math.pi, 2)
+            acc += np.sin(2 * math.pi * fx * x + ph[0]) * np.cos(2 * math.pi * fy * y + ph[1])
+        acc = (acc - acc.min()) / max(acc.max() - acc.min(), 1e-9)
+        img[..., c] = lo + (hi - lo) * acc
+    return img.astype(np.float32)
+
+
+def diff_scene(width: int = 512, height: int = 512, spp: int = 32, max_depth: int = 6, seed: int = 4,
+               n_spheres: int = 20, subdivision: int = 4, tex_size: int = 256, n_conductors: int = 8,
+               n_lights: int = 4) -> SceneSpec:
+    """Differentiable-rendering scene: `n_spheres` displaced icospheres (20 x
+    subdivision 4 = 102,400 triangles) over a ground plane; the Lambert
+    spheres and the ground share one RGB float albedo texture with uniform
+    (spherical / planar) uvs, `n_conductors` spheres each have their own GGX
+    conductor material (one roughness parameter each), and `n_lights` quad
+    lights carry the emitter-radiance parameters."""
+    rng = np.random.default_rng(seed)
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(0.0, 9.0, -26.0), cam_direction=(0.0, -0.35, 1.0), cam_up=(0.0, 1.0, 0.0),
+                  fov=50.0)
+    s.textures.append(ImageTexture("albedoTex", _smooth_texture(rng, tex_size)))
+    s.materials.append(Material("texLambert", LAMBERT, albedo_texture="albedoTex"))
+    for k in range(n_conductors):
+        s.materials.append(Material("metal%d" % k, CONDUCTOR, roughness=float(rng.uniform(0.2, 0.5)),
+                                    f0=tuple(rng.uniform(0.6, 0.95, 3))))
+    s.materials.append(Material("lightBase", LAMBERT, albedo=(0.3, 0.3, 0.3)))
+    g = 20.0
+    ground = np.array([[[-g, 0, -g], [g, 0, g], [g, 0, -g]], [[-g, 0, -g], [-g, 0, g], [g, 0, g]]], np.float32)
+    guv = np.zeros_like(ground)
+    guv[..., 0] = (ground[..., 0] + g) / (2 * g)
+    guv[..., 1] = (ground[..., 2] + g) / (2 * g)
+    s.primitives.append(TriangleMesh("ground", "texLambert", ground, uvws=guv))
+    unit = icosphere(subdivision)
+    flat = unit.reshape(-1, 3)
+    for i in range(n_spheres):
+        r = float(rng.uniform(1.0, 2.2))
+        c = np.array([rng.uniform(-9, 9), r, rng.uniform(-6, 9)])
+        lattice = rng.uniform(-1.0, 1.0, (8, 8, 8))
+        disp = 1.0 + 0.1 * _value_noise(flat + 1.0, lattice, 1.7)
+        pos = (flat * (r * disp)[:, None] + c).astype(np.float32).reshape(-1, 3, 3)
+        if i < n_conductors:
+            s.primitives.append(TriangleMesh("ball%d" % i, "metal%d" % i, pos))
+        else:
+            n = unit / np.linalg.norm(unit, axis=2, keepdims=True)
+            uv = np.zeros_like(unit)
+            uv[..., 0] = 0.5 + np.arctan2(n[..., 0], n[..., 2]) / (2 * math.pi)
+            uv[..., 1] = 0.5 + np.arcsin(np.clip(n[..., 1], -1, 1)) / math.pi
+            s.primitives.append(TriangleMesh("ball%d" % i, "texLambert", pos, uvws=uv.astype(np.float32)))
+    for j in range(n_lights):
+        cx, cz = rng.uniform(-8, 8, 2)
+        e = float(rng.uniform(4.0, 12.0))
+        col = tuple(float(x) for x in e * rng.uniform(0.6, 1.0, 3))
+        name = "lamp%d" % j
+        h = 3.0
+        s.primitives.append(Rectangle(name, "lightBase", (cx + h, 14.0, cz - h), (cx - h, 14.0, cz - h),
+                                      (cx - h, 14.0, cz + h)))
+        s.lights.append(AreaLight(name, col, _quad_light_watt(col, (2 * h) ** 2)))
+    return s

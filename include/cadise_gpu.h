@@ -239,6 +239,30 @@ cgpu_status cgpu_render_stats_get(cgpu_ctx* ctx, cgpu_render_stats* out_stats);
 /* Count rays, node fetches and triangle tests in every following render (slower). */
 cgpu_status cgpu_set_counting(cgpu_ctx* ctx, int32_t enabled);
 
+/* -------------------------------------------------------------- adjoint -- */
+/* Differentiable parameters of an uploaded scene: the texels of every albedo
+ * texture (concatenated in texture order, RGB floats), one GGX roughness per
+ * material (CRSD "roughness"), one emitted radiance RGB per area light. */
+typedef struct cgpu_param_counts {
+    uint64_t texel_floats;
+    uint32_t materials;
+    uint32_t lights;
+} cgpu_param_counts;
+cgpu_status cgpu_param_counts_get(cgpu_ctx* ctx, int32_t scene, cgpu_param_counts* out_counts);
+/* Any pointer may be NULL to skip that group. */
+cgpu_status cgpu_params_get(cgpu_ctx* ctx, int32_t scene, float* texels, float* roughness, float* radiance);
+cgpu_status cgpu_params_set(cgpu_ctx* ctx, int32_t scene, const float* texels, const float* roughness,
+                            const float* radiance);
+/* Forward pass: clears the film, renders samples [0, spp) with `seed` and
+ * returns the mean image (width * height * 3 floats; may be NULL). */
+cgpu_status cgpu_adjoint_forward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uint64_t seed, float* image_out);
+/* Backward pass: replays the same path samples from their seeds and writes
+ * d loss / d parameter (FP64) for d loss / d image (width * height * 3
+ * floats, host).  Output arrays are overwritten; any may be NULL. */
+cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uint64_t seed,
+                                  const float* d_loss_d_image, double* grad_texels, double* grad_roughness,
+                                  double* grad_radiance);
+
 /* Per-kernel CUDA-event timing of the following renders (launches are made
  * one by one instead of through the captured graph while it is on). */
 enum {

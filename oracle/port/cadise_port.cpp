@@ -118,10 +118,15 @@ struct Triangle {  // triangle.cpp:14-42
 struct Rectangle {  // rectangle.cpp:14-35
     V3 vA, vB, vC, vD, eA, eB;
 };
+struct Texture {
+    int w = 0, h = 0;
+    std::vector<float> texels;
+};
 struct Material {
     int type;
     V3 albedo, f0;
     float roughness, iorOuter, iorInner;
+    int tex;
 };
 struct Light {
     int prim;
@@ -137,6 +142,7 @@ struct Scene {
     std::vector<Triangle> tris;
     std::vector<Rectangle> rects;
     std::vector<Material> mats;
+    std::vector<Texture> textures;
     std::vector<Light> lights;
     // reference BVH (bvhBuilder.cpp / bvhLinearNode.h): binary, 1-primitive leaves
     struct Node { V3 lo, hi; int second; int prim; int count; int axis; };
@@ -482,13 +488,27 @@ bool canRefract(const V3& v, const V3& n, float etaI, float etaT, V3* out) {
     return true;
 }
 
+// RgbImageTexture::evaluate with the nearest sampler and repeat wrap
+// (rgbImageTexture.cpp:8-15, tNearestPixelSampler.ipp:14-31, repeatUvwWrapper.cpp:9-15)
+const Scene* g_scene = nullptr;
+V3 albedoAt(const Material& m, const V3& uvw) {
+    if (m.tex < 0) return m.albedo;
+    const Texture& t = g_scene->textures[size_t(m.tex)];
+    const float u = uvw.x - std::floor(uvw.x), v = uvw.y - std::floor(uvw.y);
+    int x = static_cast<int>(u * t.w), y = static_cast<int>(v * t.h);
+    x = x < t.w ? x : x - 1;
+    y = y < t.h ? y : y - 1;
+    const float* p = &t.texels[3 * (size_t(y) * t.w + x)];
+    return V3(p[0], p[1], p[2]);
+}
+
 // lambertianDiffuse.cpp:27-44 / conductorMicrofacet.cpp:32-66
 V3 bsdfEval(const Material& m, const Surface& si, const V3& L) {
     const V3& Ns = si.Ns;
     const V3& V = si.wi;
     if (m.type == CGPU_BSDF_LAMBERTIAN) {
         if (V.dot(Ns) * L.dot(Ns) <= 0.0f) return V3(0.0f);
-        return m.albedo * kInvPi;
+        return albedoAt(m, si.uvw) * kInvPi;
     }
     if (m.type == CGPU_BSDF_CONDUCTOR_GGX) {
         const float VdotN = V.dot(Ns), LdotN = L.dot(Ns);
@@ -549,7 +569,7 @@ BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng) {
         L = x * L.x + Ns * L.y + z * L.z;
         L = L.normalize();
         if (V.dot(Ns) <= 0.0f) L = -L;
-        out.f = m.albedo * kInvPi;
+        out.f = albedoAt(m, si.uvw) * kInvPi;
         out.L = L;
         out.pdf = pdf;
         return out;
@@ -584,11 +604,12 @@ BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng) {
         const V3 reflectance(R);
         const float pr = reflectance.average();
         const float u = rng.next();
+        const V3 alb = albedoAt(m, si.uvw);
         if (u < pr) {
             const float nf = VdotN > 0.0f ? 1.0f : -1.0f;
             const V3 L = V.reflect(Ns * nf);
             const float LdotN = L.absDot(Ns);
-            out.f = m.albedo * reflectance / LdotN;
+            out.f = alb * reflectance / LdotN;
             out.L = L;
             out.pdf = pr;
         } else {
@@ -601,7 +622,7 @@ BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng) {
             const float btdf = (etaT * etaT) / (etaI * etaI);
             const float LdotN = std::abs(cosI);
             const V3 trans = Rt.complement();
-            out.f = m.albedo * trans * btdf / LdotN;
+            out.f = alb * trans * btdf / LdotN;
             out.L = L;
             out.pdf = 1.0f - pr;
         }
@@ -812,7 +833,14 @@ Scene* create(const cgpu_scene_desc* d) {
     s->W = d->width; s->H = d->height; s->maxDepth = d->max_depth; s->spp = d->spp > 0 ? d->spp : 1;
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const cgpu_material& m = d->materials[i];
-        s->mats.push_back({m.type, vload(m.albedo), vload(m.f0), m.roughness, m.ior_outer, m.ior_inner});
+        s->mats.push_back({m.type, vload(m.albedo), vload(m.f0), m.roughness, m.ior_outer, m.ior_inner, m.albedo_texture});
+    }
+    for (uint32_t i = 0; i < d->num_textures; ++i) {
+        Texture t;
+        t.w = d->textures[i].width;
+        t.h = d->textures[i].height;
+        t.texels.assign(d->textures[i].texels, d->textures[i].texels + size_t(t.w) * t.h * 3);
+        s->textures.push_back(std::move(t));
     }
     for (uint32_t i = 0; i < d->num_primitives; ++i) {
         const int kind = d->prim_kind ? d->prim_kind[i] : CGPU_PRIM_TRIANGLE;
@@ -923,6 +951,7 @@ void port_trace(void* sp, const float* rays, uint32_t n, int32_t* prim, float* t
 
 void port_paths(void* sp, const double* xy, const uint64_t* keys, uint32_t n, float* rgb, uint32_t* draws) {
     const port::Scene& s = *static_cast<port::Scene*>(sp);
+    port::g_scene = &s;
     for (uint32_t i = 0; i < n; ++i) {
         port::Rng rng;
         rng.s.key = keys[i];
@@ -940,6 +969,7 @@ void port_paths(void* sp, const double* xy, const uint64_t* keys, uint32_t n, fl
 void port_render(void* sp, uint64_t seed, uint32_t scene_index, uint32_t first, uint32_t count,
                  int32_t row0, int32_t row1, int32_t threads, double* film, float* path_rgb) {
     const port::Scene& s = *static_cast<port::Scene*>(sp);
+    port::g_scene = &s;
     std::atomic<int> next{row0};
     auto worker = [&]() {
         for (;;) {

@@ -1,0 +1,127 @@
+"""The path-replay adjoint (cgpu_adjoint_backward) against central finite
+differences of the forward renderer (cgpu_adjoint_forward) with common random
+numbers (same seed, same samples), FP64 film accumulation.
+
+Loss: linear, loss = sum(W * image) with a fixed random weight image W, so
+d loss / d image = W.  With roulette off (max depth 3) the same-seed
+estimator is polynomial in the albedo texels and linear in the emitter
+radiances, so adjoint and finite differences agree to FP32 noise; the GGX
+roughness moves the sampled directions (finite differences see that, the
+detached adjoint does not), so there the two agree in expectation and the
+check is statistical at 4096 spp: 2 % relative.
+"""
+import numpy as np
+import pytest
+
+from cadise_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+H = 1e-3
+
+
+@pytest.fixture(scope="module")
+def diff(gpu_ctx):
+    spec = scenes.diff_scene(width=48, height=48, spp=64, max_depth=3, n_spheres=10, subdivision=2,
+                             tex_size=16, n_conductors=3, n_lights=2, seed=5)
+    sid = gpu_ctx.upload(spec)
+    yield spec, sid
+    gpu_ctx.release(sid)
+
+
+def weights(spec, seed=3):
+    return np.random.default_rng(seed).normal(size=(spec.height, spec.width, 3)).astype(np.float32)
+
+
+def loss(ctx, sid, W, spp, seed):
+    img = ctx.adjoint_forward(sid, spp, seed).astype(np.float64)
+    return float((W.astype(np.float64) * img).sum())
+
+
+def test_params_round_trip(gpu_ctx, diff):
+    spec, sid = diff
+    tex, rough, rad = gpu_ctx.get_params(sid)
+    assert tex.size == 16 * 16 * 3
+    np.testing.assert_array_equal(tex, spec.textures[0].texels.reshape(-1))
+    assert rough.size == len(spec.materials) and rad.shape == (2, 3)
+    gpu_ctx.set_params(sid, texels=tex * 0.5, roughness=rough, radiance=rad)
+    t2, _, _ = gpu_ctx.get_params(sid)
+    np.testing.assert_array_equal(t2, tex * 0.5)
+    gpu_ctx.set_params(sid, texels=tex)
+
+
+def test_zero_and_linear_in_loss_gradient(gpu_ctx, diff):
+    spec, sid = diff
+    z = np.zeros((spec.height, spec.width, 3), np.float32)
+    gt, gr, gl = gpu_ctx.adjoint_backward(sid, 16, 7, z)
+    assert not gt.any() and not gr.any() and not gl.any()
+    W1, W2 = weights(spec, 1), weights(spec, 2)
+    a = gpu_ctx.adjoint_backward(sid, 16, 7, W1)
+    b = gpu_ctx.adjoint_backward(sid, 16, 7, W2)
+    c = gpu_ctx.adjoint_backward(sid, 16, 7, W1 + W2)
+    for x, y, s in zip(a, b, c):
+        np.testing.assert_allclose(x + y, s, rtol=1e-4, atol=1e-9 * (np.abs(s).max() + 1))
+
+
+def test_radiance_gradient_matches_finite_differences(gpu_ctx, diff):
+    spec, sid = diff
+    W = weights(spec)
+    spp, seed = 256, 11
+    _, _, gl = gpu_ctx.adjoint_backward(sid, spp, seed, W)
+    tex, rough, rad = gpu_ctx.get_params(sid)
+    for l in range(rad.shape[0]):
+        for c in range(3):
+            h = H * rad[l, c]
+            r = rad.copy()
+            r[l, c] += h
+            gpu_ctx.set_params(sid, radiance=r)
+            lp = loss(gpu_ctx, sid, W, spp, seed)
+            r[l, c] -= 2 * h
+            gpu_ctx.set_params(sid, radiance=r)
+            lm = loss(gpu_ctx, sid, W, spp, seed)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - gl[l, c]) <= 2e-3 * abs(fd) + 1e-6, (l, c, fd, gl[l, c])
+    gpu_ctx.set_params(sid, radiance=rad)
+
+
+def test_texel_gradient_matches_finite_differences(gpu_ctx, diff):
+    spec, sid = diff
+    W = weights(spec)
+    spp, seed = 256, 13
+    gt, _, _ = gpu_ctx.adjoint_backward(sid, spp, seed, W)
+    tex, _, _ = gpu_ctx.get_params(sid)
+    top = np.argsort(-np.abs(gt))[:6]
+    assert np.abs(gt[top[0]]) > 0
+    for i in top:
+        h = H * tex[i]
+        t = tex.copy()
+        t[i] += h
+        gpu_ctx.set_params(sid, texels=t)
+        lp = loss(gpu_ctx, sid, W, spp, seed)
+        t[i] -= 2 * h
+        gpu_ctx.set_params(sid, texels=t)
+        lm = loss(gpu_ctx, sid, W, spp, seed)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - gt[i]) <= 5e-3 * abs(fd) + 1e-6, (i, fd, gt[i])
+    gpu_ctx.set_params(sid, texels=tex)
+
+
+def test_roughness_gradient_matches_finite_differences(gpu_ctx, diff):
+    spec, sid = diff
+    W = np.ones((spec.height, spec.width, 3), np.float32)  # d mean-brightness / d roughness
+    spp, seed = 4096, 17
+    _, gr, _ = gpu_ctx.adjoint_backward(sid, spp, seed, W)
+    tex, rough, rad = gpu_ctx.get_params(sid)
+    metals = [i for i, m in enumerate(spec.materials) if m.type == scenes.CONDUCTOR]
+    for i in metals:
+        h = H
+        r = rough.copy()
+        r[i] += h
+        gpu_ctx.set_params(sid, roughness=r)
+        lp = loss(gpu_ctx, sid, W, spp, seed)
+        r[i] -= 2 * h
+        gpu_ctx.set_params(sid, roughness=r)
+        lm = loss(gpu_ctx, sid, W, spp, seed)
+        fd = (lp - lm) / (2 * h)
+        assert abs(fd - gr[i]) <= 0.02 * abs(fd) + 1e-3 * np.abs(gr).max(), (i, fd, gr[i])
+    gpu_ctx.set_params(sid, roughness=rough)
