@@ -68,6 +68,8 @@ def lib():
         L.port_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
         L.port_render.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                   C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
+        L.port_adjoint_fp64.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
+                                        C.c_int32, C.c_int32, C.c_void_p]
     return _lib
 
 
@@ -123,6 +125,19 @@ class PortScene:
         paths = np.zeros((count, self.height, self.width, 3), dtype=np.float32) if want_paths else None
         lib().port_render(self.handle, seed, scene_index, first, count, r0, r1, threads, _p(film), _p(paths))
         return film, paths
+
+
+    def adjoint_fp64(self, seed: int, spp: int, d_loss_d_image: np.ndarray, params, threads: int = 8,
+                     scene_index: int = 0) -> np.ndarray:
+        """FP64 forward-mode reference gradient for up to 16 parameters
+        [(kind, index, channel)], kind 0 texel float, 1 roughness, 2 radiance."""
+        dl = np.ascontiguousarray(d_loss_d_image, dtype=np.float32)
+        pr = np.ascontiguousarray(np.asarray(params, dtype=np.int32).reshape(-1, 3))
+        if pr.shape[0] > 16:
+            raise ValueError("at most 16 parameters per call")
+        g = np.zeros(pr.shape[0], np.float64)
+        lib().port_adjoint_fp64(self.handle, seed, scene_index, spp, _p(dl), _p(pr), pr.shape[0], threads, _p(g))
+        return g
 
 
 # ---------------------------------------------------------------------------

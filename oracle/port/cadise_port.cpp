@@ -502,6 +502,53 @@ V3 albedoAt(const Material& m, const V3& uvw) {
     return V3(p[0], p[1], p[2]);
 }
 
+// Rough GGX dielectric: no reference counterpart (the reference only has the
+// smooth SpecularDielectric).  Walter, Marschner, Li & Torrance 2007 BRDF +
+// BTDF in radiance form with a Fresnel-weighted lobe choice, normal turned to
+// V's side; the same definition as the CUDA library's.  Parity for this
+// material is unpinned against the reference.
+void roughDielectric(const Material& m, const V3& alb, const V3& V, const V3& L, const V3& N, V3* f, float* pdf) {
+    *f = V3(0.0f);
+    *pdf = 0.0f;
+    const float cv = V.dot(N), cl = L.dot(N);
+    if (cv == 0.0f || cl == 0.0f) return;
+    const V3 Nv = cv > 0.0f ? N : -N;
+    const float etaV = cv > 0.0f ? m.iorOuter : m.iorInner;
+    const float etaL = cv > 0.0f ? m.iorInner : m.iorOuter;
+    const float acv = std::abs(cv), acl = std::abs(cl);
+    const float alpha = roughnessToAlpha(m.roughness);
+    if (cv * cl > 0.0f) {
+        V3 H = V + L;
+        if (H.isZero()) return;
+        H = H.normalize();
+        const float VH = V.dot(H);
+        if (VH <= 0.0f) return;
+        const float F = dielectricFresnel(etaV, etaL, VH);
+        const float NH = Nv.dot(H);
+        const float D = ggxD(alpha, Nv, H);
+        const float G = ggxG(alpha, V, L, Nv, H);
+        *f = alb * (F * D * G / (4.0f * acv * acl));
+        *pdf = F * D * NH / (4.0f * VH);
+    } else {
+        const float eta = etaL / etaV;
+        V3 H = V + L * eta;
+        if (H.isZero()) return;
+        H = H.normalize();
+        if (H.dot(Nv) < 0.0f) H = -H;
+        const float VH = V.dot(H), LH = L.dot(H);
+        if (!(VH > 0.0f && LH < 0.0f)) return;
+        const float F = dielectricFresnel(etaV, etaL, VH);
+        const float NH = Nv.dot(H);
+        const float D = ggxD(alpha, Nv, H);
+        const float G = ggxG(alpha, V, L, Nv, H);
+        const float den = VH + eta * LH;
+        const float den2 = den * den;
+        *f = alb * ((1.0f - F) * D * G * std::abs(VH * LH) / (acv * acl * den2));
+        *pdf = (1.0f - F) * D * NH * eta * eta * std::abs(LH) / den2;
+    }
+    if (!std::isfinite(*pdf)) { *pdf = 0.0f; *f = V3(0.0f); }
+}
+
 // lambertianDiffuse.cpp:27-44 / conductorMicrofacet.cpp:32-66
 V3 bsdfEval(const Material& m, const Surface& si, const V3& L) {
     const V3& Ns = si.Ns;
@@ -522,6 +569,12 @@ V3 bsdfEval(const Material& m, const Surface& si, const V3& L) {
         const float D = ggxD(alpha, Ns, H);
         const float G = ggxG(alpha, V, L, Ns, H);
         return F * G * D / (4.0f * std::abs(VdotN * LdotN));
+    }
+    if (m.type == CGPU_BSDF_DIELECTRIC_GGX) {
+        V3 f;
+        float pdf;
+        roughDielectric(m, albedoAt(m, si.uvw), si.wi, L, si.Ns, &f, &pdf);
+        return f;
     }
     return V3(0.0f);
 }
@@ -546,6 +599,12 @@ float bsdfPdf(const Material& m, const Surface& si, const V3& L) {
         const float pdfH = std::abs(D * Ns.dot(H));
         const float pdfL = std::abs(pdfH / (4.0f * L.dot(H)));
         return std::isfinite(pdfL) ? pdfL : 0.0f;
+    }
+    if (m.type == CGPU_BSDF_DIELECTRIC_GGX) {
+        V3 f;
+        float pdf;
+        roughDielectric(m, V3(1.0f), si.wi, L, si.Ns, &f, &pdf);
+        return pdf;
     }
     return 0.0f;
 }
@@ -626,6 +685,36 @@ BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng) {
             out.L = L;
             out.pdf = 1.0f - pr;
         }
+        return out;
+    }
+    if (m.type == CGPU_BSDF_DIELECTRIC_GGX) {
+        const float cv = V.dot(Ns);
+        if (cv == 0.0f) return out;
+        const V3 Nv = cv > 0.0f ? Ns : -Ns;
+        const float etaV = cv > 0.0f ? m.iorOuter : m.iorInner;
+        const float etaL = cv > 0.0f ? m.iorInner : m.iorOuter;
+        V3 z, x;
+        buildCoordinateSystem(Nv, &z, &x);
+        float u0, u1;
+        rng.next2(&u0, &u1);
+        V3 H = ggxSampleH(roughnessToAlpha(m.roughness), u0, u1);
+        H = (x * H.x + Nv * H.y + z * H.z).normalize();
+        const float VH = V.dot(H);
+        const float u = rng.next();
+        if (VH <= 0.0f) return out;
+        const float F = dielectricFresnel(etaV, etaL, VH);
+        V3 L;
+        if (u < F) {
+            L = H * (2.0f * VH) - V;
+        } else {
+            const float ratio = etaV / etaL;
+            const float sinT2 = ratio * ratio * (1.0f - VH * VH);
+            if (sinT2 >= 1.0f) return out;
+            const float cosT = std::sqrt(1.0f - sinT2);
+            L = (V * (-ratio) + H * (ratio * VH - cosT)).normalize();
+        }
+        roughDielectric(m, albedoAt(m, si.uvw), V, L, Ns, &out.f, &out.pdf);
+        out.L = L;
         return out;
     }
     return out;  // absorber: invalid (absorberBsdf.cpp)
@@ -914,6 +1003,187 @@ Scene* create(const cgpu_scene_desc* d) {
     return s.release();
 }
 
+
+// ------------------------------------------------------ FP64 gradient ----
+// Reference gradient for the adjoint (which has no counterpart in the
+// reference renderer): forward-mode dual numbers over an FP64 evaluation of
+// the same estimator with detached sampling - every random decision, sampled
+// direction, pdf, MIS weight and roulette probability is taken from the FP32
+// path above (so paths are identical), while the BSDF values, albedo texels,
+// GGX roughness and emitted radiance carry tangents.  d/dtheta of the path's
+// FP64 radiance is then exactly the detached path derivative.
+constexpr int kMaxTangents = 16;
+struct Dual {
+    double v = 0.0;
+    double t[kMaxTangents] = {0};
+};
+struct DualParam { int kind; int index; int channel; };  // kind 0 texel float, 1 roughness, 2 radiance
+int g_ntan = 0;
+const DualParam* g_params = nullptr;
+
+Dual dconst(double v) { Dual d; d.v = v; return d; }
+Dual operator+(const Dual& a, const Dual& b) { Dual r; r.v = a.v + b.v; for (int i = 0; i < g_ntan; ++i) r.t[i] = a.t[i] + b.t[i]; return r; }
+Dual operator-(const Dual& a, const Dual& b) { Dual r; r.v = a.v - b.v; for (int i = 0; i < g_ntan; ++i) r.t[i] = a.t[i] - b.t[i]; return r; }
+Dual operator*(const Dual& a, const Dual& b) { Dual r; r.v = a.v * b.v; for (int i = 0; i < g_ntan; ++i) r.t[i] = a.t[i] * b.v + a.v * b.t[i]; return r; }
+Dual operator*(const Dual& a, double s) { Dual r; r.v = a.v * s; for (int i = 0; i < g_ntan; ++i) r.t[i] = a.t[i] * s; return r; }
+Dual operator/(const Dual& a, const Dual& b) { Dual r; r.v = a.v / b.v; for (int i = 0; i < g_ntan; ++i) r.t[i] = (a.t[i] * b.v - a.v * b.t[i]) / (b.v * b.v); return r; }
+Dual dsqrt(const Dual& a) { Dual r; r.v = std::sqrt(a.v); for (int i = 0; i < g_ntan; ++i) r.t[i] = a.t[i] / (2.0 * r.v); return r; }
+struct D3 { Dual c[3]; };
+D3 d3(const V3& v) { D3 r; r.c[0] = dconst(v.x); r.c[1] = dconst(v.y); r.c[2] = dconst(v.z); return r; }
+D3 operator*(const D3& a, const D3& b) { D3 r; for (int k = 0; k < 3; ++k) r.c[k] = a.c[k] * b.c[k]; return r; }
+D3 operator*(const D3& a, const Dual& s) { D3 r; for (int k = 0; k < 3; ++k) r.c[k] = a.c[k] * s; return r; }
+D3 operator*(const D3& a, double s) { D3 r; for (int k = 0; k < 3; ++k) r.c[k] = a.c[k] * s; return r; }
+D3 operator+(const D3& a, const D3& b) { D3 r; for (int k = 0; k < 3; ++k) r.c[k] = a.c[k] + b.c[k]; return r; }
+
+Dual param_value(int kind, int index, int channel, double v) {
+    Dual d = dconst(v);
+    for (int i = 0; i < g_ntan; ++i)
+        if (g_params[i].kind == kind && g_params[i].index == index && g_params[i].channel == channel) d.t[i] = 1.0;
+    return d;
+}
+
+D3 albedoDual(const Scene& s, const Material& m, const V3& uvw) {
+    if (m.tex < 0) return d3(m.albedo);
+    const Texture& t = s.textures[size_t(m.tex)];
+    const float u = uvw.x - std::floor(uvw.x), v = uvw.y - std::floor(uvw.y);
+    int x = static_cast<int>(u * t.w), y = static_cast<int>(v * t.h);
+    x = x < t.w ? x : x - 1;
+    y = y < t.h ? y : y - 1;
+    int base = 0;
+    for (int i = 0; i < m.tex; ++i) base += s.textures[size_t(i)].w * s.textures[size_t(i)].h * 3;
+    const int off = base + 3 * (y * t.w + x);
+    D3 r;
+    for (int k = 0; k < 3; ++k) r.c[k] = param_value(0, off + k, 0, t.texels[size_t(3 * (y * t.w + x) + k)]);
+    return r;
+}
+
+D3 radianceDual(const Scene& s, int li) {
+    const V3& L = s.lights[size_t(li)].radiance;
+    D3 r;
+    for (int k = 0; k < 3; ++k) r.c[k] = param_value(2, li, k, L[k]);
+    return r;
+}
+
+// GGX D * G with alpha(roughness) carrying tangents (isotropicGgx.cpp:11-69)
+Dual ggxDG(const Scene& s, int mi, const Material& m, const V3& V, const V3& L, const V3& N, const V3& H) {
+    const float NdotH = N.dot(H);
+    if (NdotH <= 0.0f) return dconst(0.0);
+    const float VdotH = V.dot(H), VdotN = V.dot(N), LdotH = L.dot(H), LdotN = L.dot(N);
+    if (!((VdotH * VdotN > 0.0f) && (LdotH * LdotN > 0.0f))) return dconst(0.0);
+    Dual r = param_value(1, mi, 0, m.roughness);
+    Dual a;
+    if (m.roughness > 0.001f && double(m.roughness) * m.roughness > 0.001) a = r * r;
+    else a = dconst(roughnessToAlpha(m.roughness));
+    const Dual a2 = a * a;
+    const double c2 = double(NdotH) * NdotH, c4 = c2 * c2, tan2 = (1.0 - c2) / c2;
+    const Dual q = a2 + dconst(tan2);
+    const Dual D = a2 / (q * q * (kPi * c4));
+    auto G1 = [&](double c) {
+        const double cc = c * c;
+        const double tv = (1.0 - cc) / cc;
+        return dconst(2.0) / (dconst(1.0) + dsqrt(dconst(1.0) + a2 * tv));
+    };
+    return D * G1(VdotN) * G1(LdotN);
+}
+
+// BSDF value with tangents, at the same directions the FP32 path used
+D3 bsdfDual(const Scene& s, int mi, const Surface& si, const V3& L) {
+    const Material& m = s.mats[size_t(mi)];
+    const V3& N = si.Ns;
+    const V3& V = si.wi;
+    if (m.type == CGPU_BSDF_LAMBERTIAN) {
+        if (V.dot(N) * L.dot(N) <= 0.0f) return d3(V3(0.0f));
+        return albedoDual(s, m, si.uvw) * (1.0 / kPi);
+    }
+    if (m.type == CGPU_BSDF_CONDUCTOR_GGX) {
+        const float VdotN = V.dot(N), LdotN = L.dot(N);
+        if (VdotN * LdotN <= 0.0f) return d3(V3(0.0f));
+        const float sgn = static_cast<float>((0.0f < VdotN) - (VdotN < 0.0f));
+        V3 H = (V + L) * sgn;
+        if (H.isZero()) return d3(V3(0.0f));
+        H = H.normalize();
+        const V3 F = schlick(m.f0, L.dot(H));
+        return d3(F) * (ggxDG(s, mi, m, V, L, N, H) * (1.0 / (4.0 * std::abs(double(VdotN) * LdotN))));
+    }
+    return d3(V3(0.0f));  // glass: no differentiable parameter here
+}
+
+D3 estimateDual(const Scene& s, Ray ray, Rng& rng) {
+    D3 L = d3(V3(0.0f)), T = d3(V3(1.0f));
+    V3 Tf(1.0f);
+    bool countEmission = true;
+    for (int bounce = 0; bounce < s.maxDepth; ++bounce) {
+        Surface si;
+        if (!intersect(s, ray, &si)) break;
+        const Prim& pr = s.prims[si.prim];
+        const Material& m = s.mats[pr.material];
+        if (pr.light >= 0 && countEmission && canEmit(s.lights[pr.light], si.wi, si.Ns))
+            L = L + T * radianceDual(s, pr.light);
+        if (!isSpecular(m.type)) {
+            countEmission = false;
+            const std::size_t li = rng.index(0, s.lights.size());
+            const double pick = 1.0 / double(s.lights.size());
+            if (m.type != CGPU_BSDF_ABSORBER) {
+                const Light& l = s.lights[li];
+                const LightSample ls = lightSample(s, l, si.P, rng);
+                if (ls.valid()) {
+                    const V3 Lv = ls.pos - si.P;
+                    const float dist = Lv.length();
+                    const V3 Ld = Lv / dist;
+                    Ray shadow;
+                    shadow.o = si.P;
+                    shadow.d = Ld.normalize();
+                    shadow.maxT = dist - kRayEps;
+                    if (!occluded(s, shadow)) {
+                        const float w = misPower(ls.pdfW, bsdfPdf(m, si, Ld));
+                        const D3 f = bsdfDual(s, pr.material, si, Ld);
+                        L = L + T * (radianceDual(s, int(li)) * f * (double(w) * Ld.absDot(si.Ns) / ls.pdfW / pick));
+                    }
+                }
+                const BsdfSample bs = bsdfSample(m, si, rng);
+                if (bs.valid()) {
+                    Ray r;
+                    r.o = si.P;
+                    r.d = bs.L.normalize();
+                    Surface hit;
+                    if (intersect(s, r, &hit) && s.prims[hit.prim].light == int(li)) {
+                        const Light& hl = s.lights[li];
+                        if (canEmit(hl, hit.wi, hit.Ns)) {
+                            const float lp = lightPdfW(s, hl, hit, si.P);
+                            const float w = misPower(bs.pdf, lp);
+                            const D3 f = bsdfDual(s, pr.material, si, bs.L);
+                            L = L + T * (radianceDual(s, int(li)) * f * (double(w) * bs.L.absDot(si.Ns) / bs.pdf / pick));
+                        }
+                    }
+                }
+            }
+        } else {
+            countEmission = true;
+        }
+        const BsdfSample bs = bsdfSample(m, si, rng);
+        if (!bs.valid()) break;
+        const float LdotN = bs.L.absDot(si.Ns);
+        Tf *= bs.f * LdotN / bs.pdf;
+        if (m.type == CGPU_BSDF_GLASS) T = T * d3(bs.f * LdotN / bs.pdf);
+        else T = T * (bsdfDual(s, pr.material, si, bs.L) * (double(LdotN) / bs.pdf));
+        if (bounce > 2) {
+            const float q = std::min(std::max(1.0f - Tf.maxComponent(), 0.05f), 1.0f);
+            const float u = rng.next();
+            if (u > q) {
+                Tf = Tf * (1.0f / (1.0f - q));
+                T = T * (1.0 / (1.0 - double(q)));
+            } else {
+                break;
+            }
+        }
+        if (Tf.isZero()) break;
+        ray = Ray();
+        ray.o = si.P;
+        ray.d = bs.L.normalize();
+    }
+    return L;
+}
+
 }  // namespace port
 
 extern "C" {
@@ -1009,6 +1279,54 @@ void port_render(void* sp, uint64_t seed, uint32_t scene_index, uint32_t first, 
         std::vector<std::thread> pool;
         for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
         for (auto& t : pool) t.join();
+    }
+}
+
+
+// FP64 reference gradient of loss = sum_pixels dLdI . image over samples
+// [0, spp) (paths keyed like the CUDA renderer): params = K (kind, index,
+// channel) triples, kind 0 = texel float (index into the concatenated
+// textures), 1 = roughness of material `index`, 2 = radiance of light
+// `index` channel `channel`; grad: K doubles.
+void port_adjoint_fp64(void* sp, uint64_t seed, uint32_t scene_index, uint32_t spp, const float* dLdI,
+                       const int32_t* params, int32_t K, int32_t threads, double* grad) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    port::g_scene = &s;
+    std::vector<port::DualParam> ps(static_cast<size_t>(K));
+    for (int i = 0; i < K; ++i) ps[size_t(i)] = port::DualParam{params[3 * i], params[3 * i + 1], params[3 * i + 2]};
+    port::g_params = ps.data();
+    port::g_ntan = K;
+    std::vector<std::vector<double>> acc(static_cast<size_t>(std::max(threads, 1)), std::vector<double>(size_t(K), 0.0));
+    std::atomic<int> next{0};
+    auto worker = [&](int tid) {
+        for (;;) {
+            const int iy = next.fetch_add(1);
+            if (iy >= s.H) break;
+            for (int ix = 0; ix < s.W; ++ix) {
+                const uint32_t pixel = static_cast<uint32_t>(iy * s.W + ix);
+                const float* d = dLdI + 3 * size_t(pixel);
+                if (d[0] == 0.0f && d[1] == 0.0f && d[2] == 0.0f) continue;
+                for (uint32_t si = 0; si < spp; ++si) {
+                    port::Rng rng;
+                    rng.s.key = oracle_rng::path_key(seed, scene_index, pixel, si);
+                    rng.s.counter = 0;
+                    float jx, jy;
+                    port::jitter(s.spp, si, rng, &jx, &jy);
+                    const port::Ray r = port::cameraRay(s, static_cast<float>(ix) + jx, static_cast<float>(iy) + jy);
+                    const port::D3 L = port::estimateDual(s, r, rng);
+                    if (!(std::isfinite(L.c[0].v) && std::isfinite(L.c[1].v) && std::isfinite(L.c[2].v))) continue;
+                    for (int k = 0; k < 3; ++k)
+                        for (int i = 0; i < K; ++i) acc[size_t(tid)][size_t(i)] += double(d[k]) / spp * L.c[k].t[i];
+                }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < std::max(threads, 1); ++t) pool.emplace_back(worker, t);
+    for (auto& t : pool) t.join();
+    for (int i = 0; i < K; ++i) {
+        grad[i] = 0.0;
+        for (auto& a : acc) grad[i] += a[size_t(i)];
     }
 }
 

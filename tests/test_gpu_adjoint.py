@@ -125,3 +125,24 @@ def test_roughness_gradient_matches_finite_differences(gpu_ctx, diff):
         fd = (lp - lm) / (2 * h)
         assert abs(fd - gr[i]) <= 0.02 * abs(fd) + 1e-3 * np.abs(gr).max(), (i, fd, gr[i])
     gpu_ctx.set_params(sid, roughness=rough)
+
+
+def test_adjoint_matches_fp64_reference_gradient(gpu_ctx, diff):
+    """Seed for seed: the GPU's FP32 path replay with FP64 reductions against
+    the oracle's FP64 forward-mode gradient of the same detached estimator.
+    The paths are the same, so all parameter kinds agree to FP32 rounding
+    (1 % allows for the rare path that branches differently on the GPU)."""
+    import oracle
+    from cadise_gb300 import abi
+    spec, sid = diff
+    W = weights(spec, 5)
+    spp, seed = 64, 23
+    gt, gr, gl = gpu_ctx.adjoint_backward(sid, spp, seed, W)
+    ps = oracle.PortScene(abi.flatten(spec))
+    metals = [i for i, m in enumerate(spec.materials) if m.type == scenes.CONDUCTOR]
+    top = list(np.argsort(-np.abs(gt))[:6])
+    params = [(0, int(i), 0) for i in top] + [(1, i, 0) for i in metals] + [(2, 0, c) for c in range(3)]
+    ref = ps.adjoint_fp64(seed, spp, W, params, scene_index=sid)
+    gpu = np.concatenate([gt[top], gr[metals], gl[0]])
+    scale = np.abs(ref).max()
+    assert np.all(np.abs(gpu - ref) <= 0.01 * np.abs(ref) + 1e-4 * scale), np.stack([gpu, ref])

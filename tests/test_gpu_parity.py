@@ -136,7 +136,7 @@ def test_render_paths_match_oracle(name, gpu_ctx, uploaded):
     spec, flat, sid = uploaded[name]
     gpu = gpu_ctx.render_paths(sid, 3, 2, seed=11, mode=CGPU_MODE_WAVEFRONT)
     ps = oracle.PortScene(flat)
-    _, port = ps.render(seed=11, first=3, count=2, threads=8, want_paths=True)
+    _, port = ps.render(seed=11, first=3, count=2, threads=8, want_paths=True, scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
     assert close.mean() >= 0.97, close.mean()
 
@@ -224,4 +224,20 @@ def test_full_size_field_properties(gpu_ctx):
     gpu_ctx.render([sid], 0, 1, seed=3, mode=CGPU_MODE_MEGAKERNEL)
     s2, q2, n2 = gpu_ctx.film_read(sid)
     assert np.array_equal(s, s2)
+    gpu_ctx.release(sid)
+
+
+def test_rough_dielectric_paths_match_oracle(gpu_ctx):
+    """The GGX dielectric (no reference counterpart, parity unpinned against
+    the reference) against the oracle's restatement of the same definition."""
+    spec = scenes.icosphere_field(n_spheres=12, subdivision=2, n_lights=3, seed=9, width=40, height=30,
+                                  spp=4, max_depth=8, dielectric=scenes.ROUGH_DIELECTRIC, box=30.0,
+                                  radius_range=(2.0, 6.0))
+    flat = abi.flatten(spec)
+    sid = gpu_ctx.upload(flat)
+    gpu = gpu_ctx.render_paths(sid, 0, 4, seed=3, mode=CGPU_MODE_WAVEFRONT)
+    _, port = oracle.PortScene(flat).render(seed=3, first=0, count=4, threads=8, want_paths=True,
+                                            scene_index=sid)
+    close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
+    assert close.mean() >= 0.97, close.mean()
     gpu_ctx.release(sid)
