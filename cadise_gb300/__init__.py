@@ -30,7 +30,7 @@ EXPORTED = [
     "cgpu_camera_rays", "cgpu_render", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
     "cgpu_kernel_times_get", "cgpu_param_counts_get", "cgpu_params_get", "cgpu_params_set",
-    "cgpu_adjoint_forward", "cgpu_adjoint_backward",
+    "cgpu_adjoint_forward", "cgpu_adjoint_backward", "cgpu_tuning_get", "cgpu_tuning_set", "cgpu_autotune",
     # include/cadise_crsd.h
     "cgpu_crsd_load_file", "cgpu_crsd_load_text", "cgpu_crsd_desc", "cgpu_crsd_settings_get",
     "cgpu_crsd_primitive_index", "cgpu_crsd_free",
@@ -94,6 +94,9 @@ def load(path: Optional[str] = None):
     L.cgpu_params_set.argtypes = [vp, C.c_int32, vp, vp, vp]
     L.cgpu_adjoint_forward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp]
     L.cgpu_adjoint_backward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp, vp, vp, vp]
+    L.cgpu_tuning_get.argtypes = [vp, C.POINTER(abi.cgpu_tuning)]
+    L.cgpu_tuning_set.argtypes = [vp, C.POINTER(abi.cgpu_tuning)]
+    L.cgpu_autotune.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_char_p, C.POINTER(abi.cgpu_tuning)]
     L.cgpu_crsd_load_file.argtypes = [C.c_char_p, C.POINTER(vp), C.c_char_p, C.c_size_t]
     L.cgpu_crsd_load_text.argtypes = [C.c_char_p, C.c_size_t, C.POINTER(vp), C.c_char_p, C.c_size_t]
     L.cgpu_crsd_desc.argtypes = [vp]
@@ -283,6 +286,23 @@ class Context:
         gl = np.zeros((max(nl, 1), 3), np.float64)
         self._check(self.L.cgpu_adjoint_backward(self.h, sid, spp, seed, _p(dl), _p(gt), _p(gr), _p(gl)))
         return gt[:nt], gr[:nm], gl[:nl]
+
+    # -------------------------------------------------------------- autotune
+    def tuning(self) -> dict:
+        t = abi.cgpu_tuning()
+        self._check(self.L.cgpu_tuning_get(self.h, C.byref(t)))
+        return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths}
+
+    def set_tuning(self, block_trace: int, block_shade: int, max_paths: int = 0):
+        t = abi.cgpu_tuning(block_trace=block_trace, block_shade=block_shade, max_paths=max_paths, reserved=0)
+        self._check(self.L.cgpu_tuning_set(self.h, C.byref(t)))
+
+    def autotune(self, sids, samples: int = 1, cache_path: Optional[str] = None) -> dict:
+        arr = (C.c_int32 * len(sids))(*sids)
+        t = abi.cgpu_tuning()
+        self._check(self.L.cgpu_autotune(self.h, arr, len(sids), samples,
+                                         cache_path.encode() if cache_path else None, C.byref(t)))
+        return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths}
 
     def set_profiling(self, on: bool):
         self._check(self.L.cgpu_set_profiling(self.h, 1 if on else 0))

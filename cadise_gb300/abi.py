@@ -108,6 +108,11 @@ class cgpu_crsd_settings(C.Structure):
                 ("mode", C.c_int32), ("use_graph", C.c_int32), ("seed", C.c_uint64)]
 
 
+class cgpu_tuning(C.Structure):
+    _fields_ = [("block_trace", C.c_int32), ("block_shade", C.c_int32), ("max_paths", C.c_uint32),
+                ("reserved", C.c_int32)]
+
+
 class cgpu_param_counts(C.Structure):
     _fields_ = [("texel_floats", C.c_uint64), ("materials", C.c_uint32), ("lights", C.c_uint32)]
 

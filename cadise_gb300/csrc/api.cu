@@ -156,7 +156,7 @@ cgpu_status cgpu_create(cgpu_ctx** out_ctx, const cgpu_options* options) {
         delete ctx;
         return CGPU_ERR_CUDA;
     }
-    ctx->max_paths_opt = options ? options->max_paths : 0;
+    ctx->tuning.max_paths = options ? options->max_paths : 0;
     *out_ctx = ctx;
     return CGPU_OK;
 }

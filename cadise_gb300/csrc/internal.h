@@ -90,8 +90,8 @@ struct cgpu_ctx {
     std::string last_error;
     std::vector<SceneSlot> scenes;
     int num_sms = 0;
-    uint32_t max_paths_opt = 0;
     bool counting = false;
+    cgpu_tuning tuning{128, 128, 0, 0};
 
     // device tables (rebuilt when the scene set changes)
     cg::SceneD* d_scenes = nullptr;

@@ -319,7 +319,7 @@ using namespace cg;
 
 namespace {
 
-constexpr int kBlock = 128;
+constexpr int kBlock = 128;  // fixed-size utility kernels
 
 template <typename K>
 int grid_for(cgpu_ctx* ctx, K kernel, int block, uint64_t work) {
@@ -332,7 +332,7 @@ int grid_for(cgpu_ctx* ctx, K kernel, int block, uint64_t work) {
 }
 
 uint32_t paths_capacity(cgpu_ctx* ctx, uint32_t max_npix) {
-    uint32_t cap = ctx->max_paths_opt ? ctx->max_paths_opt : (1u << 21);
+    uint32_t cap = ctx->tuning.max_paths ? ctx->tuning.max_paths : (1u << 21);
     if (cap < max_npix) cap = max_npix;
     return cap;
 }
@@ -428,33 +428,34 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
     cudaMemsetAsync(ctx->wf.cnt, 0, size_t(depth + 2) * kCntStride * sizeof(int), s);
     uint32_t launches = 1;
+    const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
     const int ggen = grid_for(ctx, k_wf_generate, kBlock, paths);
     timed(ctx, CGPU_KERNEL_GENERATE, s, [&] { k_wf_generate<<<ggen, kBlock, 0, s>>>(a); });
-    auto gext = counting ? grid_for(ctx, k_wf_extend<true>, kBlock, paths) : grid_for(ctx, k_wf_extend<false>, kBlock, paths);
-    auto gsh = counting ? grid_for(ctx, k_wf_shadow<true>, kBlock, paths) : grid_for(ctx, k_wf_shadow<false>, kBlock, paths);
-    const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, kBlock, paths), grid_for(ctx, k_wf_shade<1>, kBlock, paths),
-                                    grid_for(ctx, k_wf_shade<2>, kBlock, paths), grid_for(ctx, k_wf_shade<3>, kBlock, paths),
-                                    grid_for(ctx, k_wf_shade<4>, kBlock, paths)};
+    auto gext = counting ? grid_for(ctx, k_wf_extend<true>, bt, paths) : grid_for(ctx, k_wf_extend<false>, bt, paths);
+    auto gsh = counting ? grid_for(ctx, k_wf_shadow<true>, bt, paths) : grid_for(ctx, k_wf_shadow<false>, bt, paths);
+    const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
+                                    grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
+                                    grid_for(ctx, k_wf_shade<4>, bs, paths)};
     for (int b = 0; b <= depth; ++b) {
         cudaEventRecord(fork, s);
         cudaStreamWaitEvent(side, fork, 0);
         if (counting) {
-            k_wf_extend<true><<<gext, kBlock, 0, s>>>(a, b);
-            k_wf_shadow<true><<<gsh, kBlock, 0, side>>>(a, b);
+            k_wf_extend<true><<<gext, bt, 0, s>>>(a, b);
+            k_wf_shadow<true><<<gsh, bt, 0, side>>>(a, b);
         } else {
-            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { k_wf_extend<false><<<gext, kBlock, 0, s>>>(a, b); });
-            timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { k_wf_shadow<false><<<gsh, kBlock, 0, side>>>(a, b); });
+            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { k_wf_extend<false><<<gext, bt, 0, s>>>(a, b); });
+            timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { k_wf_shadow<false><<<gsh, bt, 0, side>>>(a, b); });
         }
         cudaEventRecord(join, side);
         cudaStreamWaitEvent(s, join, 0);
         launches += 2;
         if (b == depth) break;
         timed(ctx, CGPU_KERNEL_SHADE, s, [&] {
-            k_wf_shade<0><<<gsd[0], kBlock, 0, s>>>(a, b);
-            k_wf_shade<1><<<gsd[1], kBlock, 0, s>>>(a, b);
-            k_wf_shade<2><<<gsd[2], kBlock, 0, s>>>(a, b);
-            k_wf_shade<3><<<gsd[3], kBlock, 0, s>>>(a, b);
-            k_wf_shade<4><<<gsd[4], kBlock, 0, s>>>(a, b);
+            k_wf_shade<0><<<gsd[0], bs, 0, s>>>(a, b);
+            k_wf_shade<1><<<gsd[1], bs, 0, s>>>(a, b);
+            k_wf_shade<2><<<gsd[2], bs, 0, s>>>(a, b);
+            k_wf_shade<3><<<gsd[3], bs, 0, s>>>(a, b);
+            k_wf_shade<4><<<gsd[4], bs, 0, s>>>(a, b);
         });
         launches += kNumBsdfKinds;
     }
@@ -474,10 +475,12 @@ cgpu_status run_batch(cgpu_ctx* ctx, int mode, int depth, uint32_t paths, bool s
     if (mode == CGPU_MODE_MEGAKERNEL) {
         RenderArgs a = make_args(ctx);
         if (counting) {
-            k_megakernel<true><<<grid_for(ctx, k_megakernel<true>, kBlock, paths), kBlock, 0, ctx->stream>>>(a);
+            const int bt = ctx->tuning.block_trace;
+            k_megakernel<true><<<grid_for(ctx, k_megakernel<true>, bt, paths), bt, 0, ctx->stream>>>(a);
         } else {
-            const int g = grid_for(ctx, k_megakernel<false>, kBlock, paths);
-            timed(ctx, CGPU_KERNEL_MEGAKERNEL, ctx->stream, [&] { k_megakernel<false><<<g, kBlock, 0, ctx->stream>>>(a); });
+            const int bt = ctx->tuning.block_trace;
+            const int g = grid_for(ctx, k_megakernel<false>, bt, paths);
+            timed(ctx, CGPU_KERNEL_MEGAKERNEL, ctx->stream, [&] { k_megakernel<false><<<g, bt, 0, ctx->stream>>>(a); });
         }
         ctx->stats.kernel_launches += 1;
         if (splat) {

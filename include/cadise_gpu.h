@@ -239,6 +239,22 @@ cgpu_status cgpu_render_stats_get(cgpu_ctx* ctx, cgpu_render_stats* out_stats);
 /* Count rays, node fetches and triangle tests in every following render (slower). */
 cgpu_status cgpu_set_counting(cgpu_ctx* ctx, int32_t enabled);
 
+/* ------------------------------------------------------------ autotune -- */
+typedef struct cgpu_tuning {
+    int32_t block_trace;   /* threads per block: extend, shadow and megakernel (32..1024, multiple of 32) */
+    int32_t block_shade;   /* threads per block: shade-by-BSDF kernels */
+    uint32_t max_paths;    /* paths in flight per wavefront batch; 0 = automatic (2^21, at least one frame) */
+    int32_t reserved;
+} cgpu_tuning;
+cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out_tuning);
+cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* tuning);
+/* Times wavefront passes of `scenes` (`samples` samples each) over a small
+ * search of cgpu_tuning values and applies the fastest.  With a cache path,
+ * a result stored for the same GPU and scene sizes is reused without timing
+ * and new results are appended (one JSON object per line). */
+cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t num_scenes, uint32_t samples,
+                          const char* cache_path, cgpu_tuning* out_tuning);
+
 /* -------------------------------------------------------------- adjoint -- */
 /* Differentiable parameters of an uploaded scene: the texels of every albedo
  * texture (concatenated in texture order, RGB floats), one GGX roughness per
