@@ -66,7 +66,8 @@ class cgpu_scene_desc(C.Structure):
                 ("prim_uvws", C.POINTER(C.c_float)), ("prim_material", C.POINTER(C.c_int32)),
                 ("num_materials", C.c_uint32), ("materials", C.POINTER(cgpu_material)),
                 ("num_textures", C.c_uint32), ("textures", C.POINTER(cgpu_texture)),
-                ("num_lights", C.c_uint32), ("lights", C.POINTER(cgpu_area_light))]
+                ("num_lights", C.c_uint32), ("lights", C.POINTER(cgpu_area_light)),
+                ("environment_texture", C.c_int32)]
 
 
 class cgpu_scene_info(C.Structure):
@@ -225,4 +226,5 @@ def flatten(spec: "S.SceneSpec") -> FlatScene:
     d.textures = texs
     d.num_lights = len(spec.lights)
     d.lights = lights
+    d.environment_texture = tex_index[spec.environment] + 1 if spec.environment else 0
     return FlatScene(d, kind, verts, mat, normals, uvws, mats, lights, texs, tex_arrays, names, mat_index)

@@ -81,7 +81,7 @@ __global__ void k_adjoint(AdjArgs a) {
         for (int b = 0; b < S.max_depth; ++b) {
             const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
             HitD hit;
-            if (!traverse<false, false>(S, r, &hit, &tc)) break;
+            if (!traverse<false, false>(S, r, &hit, &tc)) break;  // the sky has no parameters here
             const SurfaceD si = surface_at(S, o, d, hit);
             const VertexPlan pl = plan_vertex(S, si, T, ce, b, rng);
             const MaterialD& m = S.materials[si.material];
@@ -99,16 +99,19 @@ __global__ void k_adjoint(AdjArgs a) {
                 HitD sh2;
                 if (!traverse<true, false>(S, sr, &sh2, &ta)) {
                     A = pl.scontrib;
-                    const float3 gx = delta * pl.sx;
-                    shared_add(shl, 3 * pl.slight + 0, gx.x);
-                    shared_add(shl, 3 * pl.slight + 1, gx.y);
-                    shared_add(shl, 3 * pl.slight + 2, gx.z);
+                    if (pl.slight < a.nlight) {
+                        const float3 gx = delta * pl.sx;
+                        shared_add(shl, 3 * pl.slight + 0, gx.x);
+                        shared_add(shl, 3 * pl.slight + 1, gx.y);
+                        shared_add(shl, 3 * pl.slight + 2, gx.z);
+                    }
                 }
             }
             if (pl.mis) {
                 const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
                 HitD mh;
-                if (traverse<false, false>(S, mr, &mh, &tc) && light_of_slot(S, mh.slot) == pl.mlight) {
+                const bool hitp = traverse<false, false>(S, mr, &mh, &tc);
+                if (hitp && light_of_slot(S, mh.slot) == pl.mlight) {
                     const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
                     float3 X;
                     B = mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf, &X);
@@ -116,6 +119,8 @@ __global__ void k_adjoint(AdjArgs a) {
                     shared_add(shl, 3 * pl.mlight + 0, gx.x);
                     shared_add(shl, 3 * pl.mlight + 1, gx.y);
                     shared_add(shl, 3 * pl.mlight + 2, gx.z);
+                } else if (!hitp && pl.mlight == S.env_light) {
+                    B = mis_resolve_env(S, pl.mdir, T, pl.mfactor, pl.mpdf);
                 }
             }
             const float3 after = Ltot - acc - A - B;  // radiance of the vertices after this one
@@ -174,7 +179,7 @@ cgpu_status cgpu_param_counts_get(cgpu_ctx* ctx, int32_t scene, cgpu_param_count
     const SceneSlot& sl = ctx->scenes[size_t(scene)];
     out->texel_floats = texel_floats(sl);
     out->materials = uint32_t(sl.h_mats.size());
-    out->lights = uint32_t(sl.h_lights.size());
+    out->lights = uint32_t(sl.num_area_lights);
     return CGPU_OK;
 }
 
@@ -195,7 +200,7 @@ cgpu_status cgpu_params_get(cgpu_ctx* ctx, int32_t scene, float* texels, float* 
     if (roughness)
         for (size_t i = 0; i < sl.h_mats.size(); ++i) roughness[i] = sl.h_mats[i].roughness;
     if (radiance)
-        for (size_t i = 0; i < sl.h_lights.size(); ++i) {
+        for (size_t i = 0; i < size_t(sl.num_area_lights); ++i) {
             radiance[3 * i + 0] = sl.h_lights[i].radiance.x;
             radiance[3 * i + 1] = sl.h_lights[i].radiance.y;
             radiance[3 * i + 2] = sl.h_lights[i].radiance.z;
@@ -231,7 +236,7 @@ cgpu_status cgpu_params_set(cgpu_ctx* ctx, int32_t scene, const float* texels, c
         if (e != cudaSuccess) return cg_cuda(ctx, e, "params_set roughness");
     }
     if (radiance) {
-        for (size_t i = 0; i < sl.h_lights.size(); ++i)
+        for (size_t i = 0; i < size_t(sl.num_area_lights); ++i)
             sl.h_lights[i].radiance = make_float3(radiance[3 * i], radiance[3 * i + 1], radiance[3 * i + 2]);
         cudaError_t e = cudaMemcpy(sl.d_lights, sl.h_lights.data(), sl.h_lights.size() * sizeof(LightD), cudaMemcpyHostToDevice);
         if (e != cudaSuccess) return cg_cuda(ctx, e, "params_set radiance");
@@ -279,7 +284,7 @@ cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, ui
     const SceneSlot& sl = ctx->scenes[size_t(scene)];
     const size_t npix = size_t(sl.width) * sl.height;
     const uint64_t ntex = texel_floats(sl);
-    const int nmat = int(sl.h_mats.size()), nlight = int(sl.h_lights.size());
+    const int nmat = int(sl.h_mats.size()), nlight = sl.num_area_lights;
     const size_t shared_bytes = size_t(nmat + 3 * nlight) * sizeof(double);
     if (shared_bytes > 96 * 1024) return cg_fail(ctx, CGPU_ERR_UNSUPPORTED, "adjoint_backward: too many materials and lights");
     std::vector<int> offs(sl.h_texs.size());

@@ -191,7 +191,7 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: no primitives");
     if (d->width <= 0 || d->height <= 0 || d->max_depth < 0)
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: bad film size or depth");
-    if (d->num_lights == 0 || !d->lights)
+    if ((d->num_lights == 0 || !d->lights) && d->environment_texture == 0)
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: the estimator needs at least one light");
     if (d->num_materials == 0 || !d->materials || d->num_materials > 0xFFFFu)
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: bad material table");
@@ -359,6 +359,48 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
         const HostV3 total = scale(unit, l.watt);
         L.radiance = f3h(scale(scale(total, 1.0f / area), 0.3183098861837906f));
     }
+    // ---- environment light (environmentLight.cpp:16-57): sampling weights
+    // luminance x sin(theta) per texel, Rec. 709 luminance
+    const int env_tex = d->environment_texture - 1;
+    std::vector<float> env_marg, env_cond;
+    if (d->environment_texture != 0) {
+        if (env_tex < 0 || env_tex >= int(d->num_textures) || !d->textures[env_tex].texels)
+            return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: environment texture index out of range");
+        const cgpu_texture& et = d->textures[env_tex];
+        const int W = et.width, H = et.height;
+        if (W <= 0 || H <= 0) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: empty environment texture");
+        env_marg.assign(size_t(H) + 1, 0.0f);
+        env_cond.assign(size_t(H) * (W + 1), 0.0f);
+        std::vector<double> rows(static_cast<size_t>(H), 0.0);
+        double total = 0.0;
+        for (int y = 0; y < H; ++y) {
+            const double st = std::sin((1.0 - (y + 0.5) / H) * 3.14159265358979323846);
+            double acc = 0.0;
+            std::vector<double> wrow(static_cast<size_t>(W));
+            for (int x = 0; x < W; ++x) {
+                const float* t = et.texels + 3 * (size_t(y) * W + x);
+                const double lum = 0.2126 * t[0] + 0.7152 * t[1] + 0.0722 * t[2];
+                wrow[size_t(x)] = std::max(lum, 0.0) * st;
+                acc += wrow[size_t(x)];
+            }
+            float* c = &env_cond[size_t(y) * (W + 1)];
+            double run = 0.0;
+            for (int x = 0; x < W; ++x) {
+                run += acc > 0.0 ? wrow[size_t(x)] / acc : 1.0 / W;
+                c[x + 1] = float(run);
+            }
+            c[W] = 1.0f;
+            rows[size_t(y)] = acc;
+            total += acc;
+        }
+        if (!(total > 0.0)) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: environment map is black");
+        double run = 0.0;
+        for (int y = 0; y < H; ++y) {
+            run += rows[size_t(y)] / total;
+            env_marg[size_t(y) + 1] = float(run);
+        }
+        env_marg[size_t(H)] = 1.0f;
+    }
     // ---- textures
     SceneSlot sl;
     std::vector<TextureD> texs(d->num_textures);
@@ -388,6 +430,26 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     if (st == CGPU_OK && d->prim_normals) st = upload(ctx, sl, d->prim_normals, size_t(np) * 9, &dnorm);
     if (st == CGPU_OK && d->prim_uvws) st = upload(ctx, sl, d->prim_uvws, size_t(np) * 9, &duvw);
     if (st == CGPU_OK) st = upload(ctx, sl, rect_frames.data(), rect_frames.size(), &drect);
+    sl.num_area_lights = int(lights.size());
+    if (st == CGPU_OK && env_tex >= 0) {
+        float *dm_cdf = nullptr, *dc_cdf = nullptr;
+        st = upload(ctx, sl, env_marg.data(), env_marg.size(), &dm_cdf);
+        if (st == CGPU_OK) st = upload(ctx, sl, env_cond.data(), env_cond.size(), &dc_cdf);
+        if (st == CGPU_OK) {
+            LightD E;
+            std::memset(&E, 0, sizeof(E));
+            E.prim = -1;
+            E.kind = 2;
+            E.tex = env_tex;
+            E.ew = d->textures[env_tex].width;
+            E.eh = d->textures[env_tex].height;
+            E.marg_cdf = dm_cdf;
+            E.cond_cdf = dc_cdf;
+            lights.push_back(E);
+            // re-upload the light table with the environment appended
+            st = upload(ctx, sl, lights.data(), lights.size(), &dl);
+        }
+    }
     const size_t npix = size_t(d->width) * size_t(d->height);
     double* film = nullptr;
     if (st == CGPU_OK) {
@@ -418,7 +480,8 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.prim_normals = dnorm;
     S.prim_uvws = duvw;
     S.rect_frames = drect;
-    S.num_lights = int(d->num_lights);
+    S.num_lights = int(lights.size());
+    S.env_light = env_tex >= 0 ? int(lights.size()) - 1 : -1;
     S.num_tris = int(ntris);
     S.width = d->width;
     S.height = d->height;
@@ -454,7 +517,7 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     I.num_primitives = np;
     I.num_triangles = ntris;
     I.num_bvh_nodes = uint32_t(bvh.nodes.size());
-    I.num_lights = d->num_lights;
+    I.num_lights = uint32_t(lights.size());
     I.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     {
         float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};

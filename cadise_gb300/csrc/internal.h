@@ -76,6 +76,7 @@ struct SceneSlot {
     std::vector<cg::TextureD> h_texs;  // device texel pointers
     cg::MaterialD* d_mats = nullptr;
     cg::LightD* d_lights = nullptr;
+    int num_area_lights = 0;  // h_lights[0, num_area_lights) are area lights
     std::vector<void*> allocations;
     cgpu_scene_info info{};
     cg::FilmD film{};

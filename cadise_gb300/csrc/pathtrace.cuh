@@ -75,7 +75,10 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
         const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
         HitD hit;
         if (COUNT) ++*nclosest;
-        if (!traverse<false, COUNT>(S, r, &hit, tc)) break;
+        if (!traverse<false, COUNT>(S, r, &hit, tc)) {
+            if (S.env_light >= 0 && ce) L += T * env_radiance(S, d);
+            break;
+        }
         const SurfaceD si = surface_at(S, o, d, hit);
         const VertexPlan pl = plan_vertex(S, si, T, ce, b, rng);
         L += pl.emit;
@@ -89,9 +92,13 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
             const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
             HitD mh;
             if (COUNT) ++*nclosest;
-            if (traverse<false, COUNT>(S, mr, &mh, tc) && light_of_slot(S, mh.slot) == pl.mlight) {
-                const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
-                L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);
+            if (traverse<false, COUNT>(S, mr, &mh, tc)) {
+                if (light_of_slot(S, mh.slot) == pl.mlight) {
+                    const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
+                    L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);
+                }
+            } else if (pl.mlight == S.env_light) {
+                L += mis_resolve_env(S, pl.mdir, T, pl.mfactor, pl.mpdf);
             }
         }
         if (!pl.cont) break;

@@ -118,6 +118,16 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
             if (traverse<false, COUNT>(S, r, &hit, &tc)) {
                 w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
                 key = S.materials[material_of_slot(S, hit.slot)].type;
+            } else if (S.env_light >= 0) {
+                const float4 tw = w.thr[p];
+                if (__float_as_int(tw.w) & 1) {
+                    const float3 add = f3(tw) * env_radiance(S, d);
+                    float4 L = w.L[p];
+                    L.x += add.x;
+                    L.y += add.y;
+                    L.z += add.z;
+                    w.L[p] = L;
+                }
             }
         } else {
             p = qm[i - ncont];
@@ -127,18 +137,29 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
             const RayPre r = ray_prep(o, md, kRayEps, kFloatMax);
             HitD hit;
             if (COUNT) ++nclosest;
-            if (traverse<false, COUNT>(S, r, &hit, &tc)) {
-                const float4 mb = w.mis_b[p];
-                if (light_of_slot(S, hit.slot) == __float_as_int(mb.w)) {
+            const bool hitp = traverse<false, COUNT>(S, r, &hit, &tc);
+            const float4 mb = w.mis_b[p];
+            const int mlight = __float_as_int(mb.w);
+            float3 add = splat3(0.0f);
+            bool has = false;
+            if (hitp) {
+                if (light_of_slot(S, hit.slot) == mlight) {
                     const SurfaceD hs = surface_at(S, o, md, hit);
                     const float4 ma = w.mis_a[p];
-                    const float3 add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w);
-                    float4 L = w.L[p];
-                    L.x += add.x;
-                    L.y += add.y;
-                    L.z += add.z;
-                    w.L[p] = L;
+                    add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w);
+                    has = true;
                 }
+            } else if (mlight == S.env_light) {
+                const float4 ma = w.mis_a[p];
+                add = mis_resolve_env(S, md, f3(mb), f3(ma), ma.w);
+                has = true;
+            }
+            if (has) {
+                float4 L = w.L[p];
+                L.x += add.x;
+                L.y += add.y;
+                L.z += add.z;
+                w.L[p] = L;
             }
         }
         grouped_push(qmat, cnt + 3, key, p);

@@ -58,7 +58,7 @@ struct __align__(16) MaterialD {
 
 struct __align__(16) LightD {
     int prim;
-    int kind;        // 0 triangle, 1 rectangle
+    int kind;        // 0 triangle, 1 rectangle, 2 environment
     int back_face;
     float pdf_area;  // 1 / area
     float3 radiance; // color / sum(color) * watt / (area * pi)
@@ -70,6 +70,12 @@ struct __align__(16) LightD {
     int has_normals;
     float long_len, short_len;  // rectangle rejection sampler
     float3 long_e, short_dir;    // rectangle: longer edge, unit shorter edge
+    // environment: radiance texture and its piecewise-constant 2-D sampling
+    // distribution (luminance x sin(theta) per texel): row CDF (eh + 1) and
+    // per-row column CDFs (eh x (ew + 1))
+    int tex, ew, eh;
+    const float* marg_cdf;
+    const float* cond_cdf;
 };
 
 struct TextureD {
@@ -92,7 +98,8 @@ struct SceneD {
     const float* prim_normals;  // 9 per primitive or null
     const float* prim_uvws;     // 9 per primitive or null
     const float* rect_frames;   // 9 per rectangle (vB, eA, eB), indexed by the rectangle index
-    int num_lights;
+    int num_lights;  // area lights + environment
+    int env_light;   // index of the environment light, -1 if none
     int num_tris;
     int width, height;
     int max_depth;

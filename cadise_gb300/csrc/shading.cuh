@@ -403,10 +403,86 @@ struct LightS {
     CG_D bool valid() const { return !is_zero(radiance) && pdfW > 0.0f; }  // directLightSample.cpp:53-55
 };
 
+// ------------------------------------------------------------- environment --
+// One direction <-> (u, v) mapping for both lookup and sampling: the one of
+// SphericalMapper::mappingToUvw (sphericalMapper.cpp:14-28), y up,
+// phi = atan2(x, z), v = (pi - theta) / pi.  (The reference samples with a
+// z-up inverse, infiniteSphere.cpp:62-78, which does not invert its lookup;
+// this library keeps one mapping so NEE and BSDF sampling see the same sky.)
+CG_D float3 env_dir(float u, float v) {
+    const float theta = (1.0f - v) * kPi;
+    float sp, cp, st, ct;
+    sincospif(2.0f * u, &sp, &cp);
+    sincospif(1.0f - v, &st, &ct);
+    (void)theta;
+    return mk(st * sp, ct, st * cp);
+}
+CG_D float3 env_uvw(float3 d) {
+    const float3 n = normalize(d);
+    const float theta = acosf(fminf(fmaxf(n.y, -1.0f), 1.0f));
+    float phi = atan2f(n.x, n.z);
+    if (phi < 0.0f) phi += 2.0f * kPi;
+    return mk(phi * (0.5f / kPi), (kPi - theta) * kInvPi, 0.0f);
+}
+CG_D int cdf_find(const float* cdf, int n, float u) {
+    int lo = 0, hi = n - 1;  // largest i with cdf[i] <= u, in [0, n-1]
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(cdf + mid) <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+// pdf over (u, v) in [0, 1]^2 (Distribution2D::pdfContinuous, distribution2D.cpp:42-50)
+CG_D float env_pdf_uv(const LightD& l, float u, float v) {
+    int iy = min(int(v * float(l.eh)), l.eh - 1);
+    int ix = min(int(u * float(l.ew)), l.ew - 1);
+    iy = max(iy, 0);
+    ix = max(ix, 0);
+    const float* c = l.cond_cdf + size_t(iy) * (l.ew + 1);
+    return (__ldg(l.marg_cdf + iy + 1) - __ldg(l.marg_cdf + iy)) * float(l.eh) * (__ldg(c + ix + 1) - __ldg(c + ix)) * float(l.ew);
+}
+CG_D float env_pdfW(const LightD& l, float3 dir) {
+    const float3 uvw = env_uvw(dir);
+    const float s = sinf((1.0f - uvw.y) * kPi);
+    if (s <= 0.0f) return 0.0f;
+    return env_pdf_uv(l, uvw.x, uvw.y) / (2.0f * kPi * kPi * s);
+}
+
 // SingleAreaLight::evaluateDirectSample (singleAreaLight.cpp:54-85) with
 // Triangle / Rectangle::evaluatePositionSample (triangle.cpp:162-193,
 // sampleWarp.cpp:10-19; rectangle.cpp:134-169 rejection sampler).
-CG_D LightS light_sample(const LightD& l, float3 target, Rng& rng) {
+// EnvironmentLight::evaluateDirectSample (environmentLight.cpp:67-92) with
+// Distribution2D::sampleContinuous (distribution2D.cpp:27-40): the row from
+// the .y draw, the column from the .x draw.
+CG_D LightS env_sample(const SceneD& S, const LightD& l, float3 target, Rng& rng) {
+    LightS out;
+    out.radiance = splat3(0.0f);
+    out.pdfW = 0.0f;
+    out.pos = splat3(0.0f);
+    float sx, sy;
+    rng.next2(&sx, &sy);
+    const int iy = cdf_find(l.marg_cdf, l.eh, sy);
+    const float* c = l.cond_cdf + size_t(iy) * (l.ew + 1);
+    const int ix = cdf_find(c, l.ew, sx);
+    const float m0 = __ldg(l.marg_cdf + iy), m1 = __ldg(l.marg_cdf + iy + 1);
+    const float c0 = __ldg(c + ix), c1 = __ldg(c + ix + 1);
+    float dy = sy - m0, dx = sx - c0;
+    if (m1 > m0) dy /= m1 - m0;
+    if (c1 > c0) dx /= c1 - c0;
+    const float v = fminf(fmaxf((float(iy) + dy) / float(l.eh), 0.0f), 1.0f);
+    const float u = fminf(fmaxf((float(ix) + dx) / float(l.ew), 0.0f), 1.0f);
+    const float pdf_uv = (m1 - m0) * float(l.eh) * (c1 - c0) * float(l.ew);
+    const float s = sinf((1.0f - v) * kPi);
+    if (s <= 0.0f || !(pdf_uv > 0.0f)) return out;
+    const float3 dir = env_dir(u, v);
+    out.pos = target + dir * 1.0e6f;  // the reference's sky sphere radius (infiniteSphere.cpp:17-20)
+    out.pdfW = pdf_uv / (2.0f * kPi * kPi * s);
+    out.radiance = texture_rgb(S.textures[l.tex], mk(u, v, 0.0f));
+    return out;
+}
+
+CG_D LightS light_sample(const SceneD& S, const LightD& l, float3 target, Rng& rng) {
+    if (l.kind == 2) return env_sample(S, l, target, rng);
     LightS out;
     out.radiance = splat3(0.0f);
     out.pdfW = 0.0f;
@@ -499,7 +575,7 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
         const float pick = 1.0f / float(S.num_lights);
         if (m.type != BSDF_ABSORBER) {
             const LightD& l = S.lights[li];
-            const LightS ls = light_sample(l, si.P, rng);
+            const LightS ls = light_sample(S, l, si.P, rng);
             if (ls.valid()) {
                 const float3 Lv = ls.pos - si.P;
                 const float dist = len(Lv);
@@ -555,6 +631,23 @@ CG_D float3 mis_resolve(const SceneD& S, const SurfaceD& hit, float3 origin, flo
     const float w = mis_power(pdf, lp);
     const float pick = 1.0f / float(S.num_lights);
     if (x_out) *x_out = can_emit(l, hit.wi, hit.Ns) ? T * divs(divs(factor * w, pdf), pick) : splat3(0.0f);
+    return T * divs(divs(rad * w * factor, pdf), pick);
+}
+
+// A ray that leaves the scene sees the environment: the emission counted at
+// a background "hit" (scene.cpp:47-62, environmentLight.cpp:59-65).
+CG_D float3 env_radiance(const SceneD& S, float3 dir) {
+    const LightD& l = S.lights[S.env_light];
+    return texture_rgb(S.textures[l.tex], env_uvw(dir));
+}
+// The BSDF-sampling half of DirectLightEvaluator for a sampled direction
+// that escapes while the environment is the picked light.
+CG_D float3 mis_resolve_env(const SceneD& S, float3 dir, float3 T, float3 factor, float pdf, float3* x_out = nullptr) {
+    const LightD& l = S.lights[S.env_light];
+    const float3 rad = env_radiance(S, dir);
+    const float w = mis_power(pdf, env_pdfW(l, dir));
+    const float pick = 1.0f / float(S.num_lights);
+    if (x_out) *x_out = T * divs(divs(factor * w, pdf), pick);
     return T * divs(divs(rad * w * factor, pdf), pick);
 }
 

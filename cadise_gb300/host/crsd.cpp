@@ -352,8 +352,22 @@ struct cgpu_crsd_scene {
         if (int(kind.size()) > first) prim_names.emplace(name, first);  // std::map::insert keeps the first
     }
 
+    int env_texture = 0;
+
     void light_block(const Block& b) {
         const std::string type = find_str(b, "type", "");
+        if (type == "environment") {  // lightInstantiator.cpp:60-82 (PFM images here)
+            std::string fn = find_str(b, "hdr-filename", "");
+            if (!fn.empty() && fn[0] != '/') fn = base_dir + fn;
+            cgpu_texture t{};
+            std::vector<float> px;
+            if (!read_pfm(fn, &t.width, &t.height, &px))
+                fail(CGPU_ERR_UNSUPPORTED, "environment map '" + fn + "' (PFM RGB float images only)");
+            texels.push_back(std::move(px));
+            textures.push_back(t);
+            env_texture = int(textures.size());
+            return;
+        }
         if (type != "area") fail(CGPU_ERR_UNSUPPORTED, "light type '" + type + "'");
         const std::string pn = find_str(b, "primitive", "");
         auto it = prim_names.find(pn);
@@ -433,6 +447,7 @@ struct cgpu_crsd_scene {
         desc.textures = textures.data();
         desc.num_lights = uint32_t(lights.size());
         desc.lights = lights.data();
+        desc.environment_texture = env_texture;
     }
 };
 

@@ -112,6 +112,8 @@ class SceneSpec:
     primitives: List[object] = field(default_factory=list)
     lights: List[AreaLight] = field(default_factory=list)
     textures: List[ImageTexture] = field(default_factory=list)
+    # name of an ImageTexture used as a latitude-longitude environment light
+    environment: Optional[str] = None
 
     # ------------------------------------------------------------------ sizes
     def num_primitives(self) -> int:
@@ -459,4 +461,48 @@ def diff_scene(width: int = 512, height: int = 512, spp: int = 32, max_depth: in
         s.primitives.append(Rectangle(name, "lightBase", (cx + h, 14.0, cz - h), (cx - h, 14.0, cz - h),
                                       (cx - h, 14.0, cz + h)))
         s.lights.append(AreaLight(name, col, _quad_light_watt(col, (2 * h) ** 2)))
+    return s
+
+
+def lognormal_sky(width: int = 2048, height: int = 1024, sigma: float = 1.5, seed: int = 5) -> np.ndarray:
+    """Procedural HDR environment map: smooth log-normal luminance field
+    (log-luminance ~ N(0, sigma^2), spatially correlated) with a warm/cool tint."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:height, 0:width].astype(np.float64)
+    u, v = x / width, y / height
+    field = np.zeros((height, width))
+    for k in range(12):
+        fu, fv = rng.integers(1, 8), rng.integers(1, 5)
+        ph = rng.uniform(0, 2 * math.pi, 2)
+        field += np.sin(2 * math.pi * fu * u + ph[0]) * np.sin(math.pi * fv * v + ph[1])
+    field = (field - field.mean()) / max(field.std(), 1e-9) * sigma
+    lum = np.exp(field)
+    tint = np.stack([1.0 + 0.2 * v, np.ones_like(v), 1.2 - 0.3 * v], -1)
+    return (lum[..., None] * tint).astype(np.float32)
+
+
+def env_field(n_spheres: int = 4000, subdivision: int = 4, n_lights: int = 64, width: int = 3840, height: int = 2160,
+              spp: int = 1024, max_depth: int = 32, seed: int = 7, sky: tuple = (2048, 1024)) -> SceneSpec:
+    """The stress configuration: displaced icospheres (4000 x subdivision 4
+    = 20,480,000 triangles) over a ground plane, mixed Lambert / GGX
+    conductor / GGX dielectric, a log-normal HDR sky and quad lights."""
+    s = icosphere_field(n_spheres=n_spheres, subdivision=subdivision, n_lights=n_lights, seed=seed, width=width,
+                        height=height, spp=spp, max_depth=max_depth, box=100.0 * (n_spheres / 200.0) ** (1 / 3))
+    s.textures.append(ImageTexture("sky", lognormal_sky(sky[0], sky[1], 1.5, seed)))
+    s.environment = "sky"
+    return s
+
+
+def furnace_scene(width: int = 32, height: int = 32, spp: int = 64, albedo: float = 0.5, sky: float = 1.0,
+                  max_depth: int = 4) -> SceneSpec:
+    """White-furnace check: a convex Lambert icosphere under a constant sky of
+    radiance `sky`.  Light leaving the sphere never returns to it, so every
+    pixel's expected radiance is exactly `albedo * sky` on the sphere and
+    `sky` elsewhere."""
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth, cam_position=(0.0, 0.0, -6.0),
+                  cam_direction=(0.0, 0.0, 1.0), cam_up=(0.0, 1.0, 0.0), fov=40.0)
+    s.materials = [Material("grey", LAMBERT, albedo=(albedo, albedo, albedo))]
+    s.primitives = [TriangleMesh("ball", "grey", icosphere(3).astype(np.float32))]
+    s.textures = [ImageTexture("sky", np.full((8, 16, 3), sky, np.float32))]
+    s.environment = "sky"
     return s

@@ -132,6 +132,12 @@ typedef struct cgpu_scene_desc {
     const cgpu_texture* textures;
     uint32_t num_lights;
     const cgpu_area_light* lights;
+
+    /* Environment light (environmentLight.cpp:16-105): 1 + index into
+     * `textures` of an RGB latitude-longitude radiance map lighting the scene
+     * from infinity, 0 for none.  It joins the uniform light pick after the
+     * area lights. */
+    int32_t environment_texture;
 } cgpu_scene_desc;
 
 typedef struct cgpu_scene_info {

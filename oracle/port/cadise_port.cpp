@@ -150,6 +150,9 @@ struct Scene {
     std::vector<int> order;
     // camera (perspectivePinholeCamera.cpp:32-50)
     int W = 0, H = 0, maxDepth = 0, spp = 1;
+    // environment light (no reference parity: see env* below)
+    int envLight = -1, envTex = -1;
+    std::vector<float> envMarg, envCond;
     V3 camPos, camX, camY, camZ;
     float sx = 0, sy = 0, tx = 0, ty = 0, offset = 0;
 };
@@ -725,10 +728,76 @@ struct LightSample { V3 pos, N, radiance; float pdfW = 0.0f; bool valid() const 
 
 bool canEmit(const Light& l, const V3& dir, const V3& N) { return (dir.dot(N) >= 0.0f) != l.backFace; }  // areaLight.cpp:24-28
 
+// Environment light.  The reference samples its sky with a z-up inverse
+// (infiniteSphere.cpp:62-78) of a y-up lookup (sphericalMapper.cpp:14-28), so
+// its NEE and BSDF sampling see differently rotated skies; this restatement
+// (and the CUDA library) use the y-up mapping for both.  Unpinned against the
+// reference.
+V3 envDir(float u, float v) {
+    const float st = std::sin((1.0f - v) * kPi), ct = std::cos((1.0f - v) * kPi);
+    return V3(st * std::sin(kTwoPi * u), ct, st * std::cos(kTwoPi * u));
+}
+V3 envUvw(const V3& d) {
+    const V3 n = d.normalize();
+    const float theta = std::acos(std::min(std::max(n.y, -1.0f), 1.0f));
+    float phi = std::atan2(n.x, n.z);
+    if (phi < 0.0f) phi += kTwoPi;
+    return V3(phi * (0.5f / kPi), (kPi - theta) * kInvPi, 0.0f);
+}
+V3 texel(const Scene& s, int tex, const V3& uvw) {
+    const Texture& t = s.textures[size_t(tex)];
+    const float u = uvw.x - std::floor(uvw.x), v = uvw.y - std::floor(uvw.y);
+    int x = static_cast<int>(u * t.w), y = static_cast<int>(v * t.h);
+    x = x < t.w ? x : x - 1;
+    y = y < t.h ? y : y - 1;
+    const float* p = &t.texels[3 * (size_t(y) * t.w + x)];
+    return V3(p[0], p[1], p[2]);
+}
+int cdfFind(const float* cdf, int n, float u) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cdf[mid] <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+float envPdfW(const Scene& s, const V3& dir) {
+    const V3 uvw = envUvw(dir);
+    const float st = std::sin((1.0f - uvw.y) * kPi);
+    if (st <= 0.0f) return 0.0f;
+    const Texture& t = s.textures[size_t(s.envTex)];
+    const int iy = std::max(std::min(int(uvw.y * t.h), t.h - 1), 0);
+    const int ix = std::max(std::min(int(uvw.x * t.w), t.w - 1), 0);
+    const float* c = &s.envCond[size_t(iy) * (t.w + 1)];
+    const float pdf = (s.envMarg[iy + 1] - s.envMarg[iy]) * float(t.h) * (c[ix + 1] - c[ix]) * float(t.w);
+    return pdf / (2.0f * kPi * kPi * st);
+}
+
 // singleAreaLight.cpp:54-85 with the position samplers of
 // triangle.cpp:162-193 (sampleWarp.cpp:10-19) and rectangle.cpp:134-169.
 LightSample lightSample(const Scene& s, const Light& l, const V3& target, Rng& rng) {
     LightSample out;
+    if (l.prim < 0) {  // environment: Distribution2D row from .y, column from .x
+        const Texture& t = s.textures[size_t(s.envTex)];
+        float sx, sy;
+        rng.next2(&sx, &sy);
+        const int iy = cdfFind(s.envMarg.data(), t.h, sy);
+        const float* c = &s.envCond[size_t(iy) * (t.w + 1)];
+        const int ix = cdfFind(c, t.w, sx);
+        const float m0 = s.envMarg[iy], m1 = s.envMarg[iy + 1], c0 = c[ix], c1 = c[ix + 1];
+        float dy = sy - m0, dx = sx - c0;
+        if (m1 > m0) dy /= m1 - m0;
+        if (c1 > c0) dx /= c1 - c0;
+        const float v = std::min(std::max((float(iy) + dy) / float(t.h), 0.0f), 1.0f);
+        const float u = std::min(std::max((float(ix) + dx) / float(t.w), 0.0f), 1.0f);
+        const float pdfUv = (m1 - m0) * float(t.h) * (c1 - c0) * float(t.w);
+        const float st = std::sin((1.0f - v) * kPi);
+        if (st <= 0.0f || !(pdfUv > 0.0f)) return out;
+        out.pos = target + envDir(u, v) * 1.0e6f;
+        out.pdfW = pdfUv / (2.0f * kPi * kPi * st);
+        out.radiance = texel(s, s.envTex, V3(u, v, 0.0f));
+        return out;
+    }
     const Prim& pr = s.prims[l.prim];
     V3 P, Ns;
     float pdfA;
@@ -836,6 +905,11 @@ V3 directLight(const Scene& s, const Surface& si, const Material& m, int lightIn
                     const float w = misPower(bs.pdf, lp);
                     result += w * rad * factor / bs.pdf;
                 }
+            } else if (lightIndex == s.envLight) {
+                const V3 factor = bs.f * bs.L.absDot(Ns);
+                const V3 rad = texel(s, s.envTex, envUvw(r.d));
+                const float w = misPower(bs.pdf, envPdfW(s, r.d));
+                result += w * rad * factor / bs.pdf;
             }
         }
     }
@@ -848,7 +922,10 @@ V3 estimate(const Scene& s, Ray ray, Rng& rng) {
     bool countEmission = true;
     for (int bounce = 0; bounce < s.maxDepth; ++bounce) {
         Surface si;
-        if (!intersect(s, ray, &si)) break;
+        if (!intersect(s, ray, &si)) {
+            if (s.envLight >= 0 && countEmission) L += T * texel(s, s.envTex, envUvw(ray.d));
+            break;
+        }
         const Prim& pr = s.prims[si.prim];
         const Material& m = s.mats[pr.material];
         if (pr.light >= 0 && countEmission) {
@@ -977,6 +1054,47 @@ Scene* create(const cgpu_scene_desc* d) {
         const float area = lightArea(*s, s->lights.back());
         s->lights.back().radiance = total / area * kInvPi;  // singleAreaLight.cpp:32-36
         s->prims[l.primitive].light = static_cast<int>(i);
+    }
+    if (d->environment_texture > 0) {  // same weights and CDFs as the CUDA library's upload
+        const int tex = d->environment_texture - 1;
+        const Texture& t = s->textures[size_t(tex)];
+        const int W = t.w, H = t.h;
+        s->envTex = tex;
+        s->envMarg.assign(size_t(H) + 1, 0.0f);
+        s->envCond.assign(size_t(H) * (W + 1), 0.0f);
+        std::vector<double> rows(static_cast<size_t>(H), 0.0);
+        double total = 0.0;
+        for (int y = 0; y < H; ++y) {
+            const double st = std::sin((1.0 - (y + 0.5) / H) * 3.14159265358979323846);
+            double acc = 0.0;
+            std::vector<double> wrow(static_cast<size_t>(W));
+            for (int x = 0; x < W; ++x) {
+                const float* p = &t.texels[3 * (size_t(y) * W + x)];
+                const double lum = 0.2126 * p[0] + 0.7152 * p[1] + 0.0722 * p[2];
+                wrow[size_t(x)] = std::max(lum, 0.0) * st;
+                acc += wrow[size_t(x)];
+            }
+            float* c = &s->envCond[size_t(y) * (W + 1)];
+            double run = 0.0;
+            for (int x = 0; x < W; ++x) {
+                run += acc > 0.0 ? wrow[size_t(x)] / acc : 1.0 / W;
+                c[x + 1] = float(run);
+            }
+            c[W] = 1.0f;
+            rows[size_t(y)] = acc;
+            total += acc;
+        }
+        double run = 0.0;
+        for (int y = 0; y < H; ++y) {
+            run += rows[size_t(y)] / total;
+            s->envMarg[size_t(y) + 1] = float(run);
+        }
+        s->envMarg[size_t(H)] = 1.0f;
+        Light env;
+        env.prim = -1;
+        env.backFace = false;
+        s->envLight = static_cast<int>(s->lights.size());
+        s->lights.push_back(env);
     }
     std::vector<BuildItem> items(s->prims.size());
     for (std::size_t i = 0; i < s->prims.size(); ++i) {

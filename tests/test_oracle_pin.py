@@ -101,3 +101,26 @@ def test_port_render_converges_to_reference_image(ports):
     frac = np.mean(np.abs(z) > 2.576)  # two-sided p < 0.01
     n = z.size
     assert frac <= 0.01 + 3 * np.sqrt(0.01 * 0.99 / n) + 0.005
+
+
+def test_oracle_environment_furnace():
+    """The oracle's sky light passes the same white-furnace known answer."""
+    from cadise_gb300 import scenes
+    spec = scenes.furnace_scene(width=16, height=16, spp=64)
+    film, _ = oracle.PortScene(abi.flatten(spec)).render(seed=2, first=0, count=64, threads=8)
+    mean = film[..., :3] / film[..., 6:7]
+    var = film[..., 3:6] / film[..., 6:7] - mean ** 2
+    sphere = furnace_mask(spec)
+    m = mean[sphere].mean()
+    se = np.sqrt(var[sphere].sum() / film[..., 6][sphere].sum()) / np.sqrt(sphere.sum())
+    assert abs(m - 0.5) <= 4 * se + 1e-4, (m, se)
+
+
+def furnace_mask(spec):
+    """Pixels whose whole footprint lies on the sphere (icosphere of radius 1
+    at distance 6; faceting shrinks it to > 0.95, plus a 1.5-pixel margin)."""
+    import math
+    f = (spec.width / 2) / math.tan(math.radians(spec.fov / 2))
+    r = f * math.tan(math.asin(0.95 / 6.0)) - 1.5
+    y, x = np.mgrid[0:spec.height, 0:spec.width] + 0.5
+    return (x - spec.width / 2) ** 2 + (y - spec.height / 2) ** 2 <= r * r
