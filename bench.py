@@ -37,6 +37,8 @@ def parse():
     ap.add_argument("--spp", type=int, default=64)
     ap.add_argument("--quick", action="store_true", help="small frame for a fast check (not a bench number)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     return ap.parse_args()
 
 
@@ -154,6 +156,11 @@ def run_gpu(args, rank, world, local):
     def render(mode, graph=True):
         ctx.render([sid], first, spp, seed=2024, mode=mode, graph=graph, sync=False)
 
+    tuning = ctx.tuning()
+    if not args.no_autotune:
+        cache = os.path.join(tempfile.gettempdir(), "cadise_gb300_tune.jsonl")
+        tuning = ctx.autotune([sid], samples=1, cache_path=cache)
+
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):
             flush.fill_(1)
@@ -245,6 +252,10 @@ def run_gpu(args, rank, world, local):
         pass
     rays_per_sample = (st.closest_rays + st.any_rays) / float(npix)
 
+    adjoint = None
+    if not args.no_adjoint:
+        adjoint = adjoint_rate(ctx, args)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         rate, cores, sample = cpu_rate(flat)
@@ -258,7 +269,7 @@ def run_gpu(args, rank, world, local):
                    "height": spec.height, "spp": spp, "max_depth": spec.max_depth,
                    "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
                    "schedule": "wavefront, CUDA graph per batch", "l2": "256 MB buffer written between steps",
-                   "parallelism": "replicas" if world > 1 else "single"},
+                   "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
         "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value},
         "rays": {"closest_per_sample": st.closest_rays / float(npix), "any_per_sample": st.any_rays / float(npix),
                  "mrays_per_s": value * rays_per_sample / 1e6},
@@ -270,6 +281,7 @@ def run_gpu(args, rank, world, local):
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": npix * 7 * 8,
                 "path": "cgpu_film_clear + cgpu_render + cgpu_film_read into pinned host buffers"},
+        "adjoint": adjoint,
         "gpu_launches": launches,
         "clocks": clk,
         "cpu_baseline": cpu,
@@ -280,6 +292,48 @@ def run_gpu(args, rank, world, local):
     ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def adjoint_rate(ctx, args):
+    """Differentiable-rendering iteration on the 102,400-triangle scene:
+    512x512, 32 spp forward pass + path-replay adjoint of the L2 loss against
+    a target rendered from perturbed parameters."""
+    import numpy as np
+    import torch
+
+    from cadise_gb300 import scenes
+    if args.quick:
+        spec = scenes.diff_scene(width=128, height=128, spp=8, n_spheres=8, subdivision=3)
+    else:
+        spec = scenes.diff_scene()
+    sid = ctx.upload(spec)
+    tex, rough, rad = ctx.get_params(sid)
+    rng = np.random.default_rng(0)
+    # target from perturbed parameters (albedo +-0.2, roughness +-0.15)
+    ctx.set_params(sid, texels=np.clip(tex + rng.uniform(-0.2, 0.2, tex.shape), 0.02, 0.98).astype(np.float32),
+                   roughness=np.clip(rough + rng.uniform(-0.15, 0.15, rough.shape), 0.05, 1.0).astype(np.float32))
+    target = ctx.adjoint_forward(sid, 256 if args.quick else 1024, 77)
+    ctx.set_params(sid, texels=tex, roughness=rough)
+    npix = spec.width * spec.height
+    times_f, times_b = [], []
+    for it in range(3):
+        t0 = time.perf_counter()
+        img = ctx.adjoint_forward(sid, spec.spp, 1000 + it)
+        t1 = time.perf_counter()
+        grad_img = (2.0 * (img - target) / img.size).astype(np.float32)
+        gt, gr, gl = ctx.adjoint_backward(sid, spec.spp, 1000 + it, grad_img)
+        t2 = time.perf_counter()
+        if it > 0:
+            times_f.append(t1 - t0)
+            times_b.append(t2 - t1)
+    nparams = gt.size + gr.size + gl.size
+    ctx.release(sid)
+    fwd, bwd = statistics.mean(times_f), statistics.mean(times_b)
+    return {"workload": "diff-scene-102k-tris-%dx%d-%dspp" % (spec.width, spec.height, spec.spp),
+            "iterations_per_s": 1.0 / (fwd + bwd), "grads_per_s": nparams / (fwd + bwd),
+            "unit": "gradient evaluations/s (forward + adjoint)", "parameters": int(nparams),
+            "forward_ms": fwd * 1e3, "backward_ms": bwd * 1e3,
+            "backward_path_samples_per_s": npix * spec.spp / bwd}
 
 
 # ---------------------------------------------------------- reference arm --

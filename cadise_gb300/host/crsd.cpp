@@ -312,6 +312,18 @@ struct cgpu_crsd_scene {
         spectrum_tex.emplace(name, int(textures.size()) - 1);
     }
 
+    void read_f32_file(const std::string& name, std::vector<float>* out) {
+        const std::string fn = (!name.empty() && name[0] != '/') ? base_dir + name : name;
+        std::ifstream f(fn, std::ios::binary | std::ios::ate);
+        if (!f) fail(CGPU_ERR_NOT_FOUND, "cannot open mesh sidecar " + fn);
+        const std::streamsize n = f.tellg();
+        if (n % 36 != 0) fail(CGPU_ERR_PARSE, "mesh sidecar " + fn + " is not whole float32 triangles");
+        out->resize(size_t(n) / 4);
+        f.seekg(0);
+        f.read(reinterpret_cast<char*>(out->data()), n);
+        if (!f) fail(CGPU_ERR_PARSE, "short read of mesh sidecar " + fn);
+    }
+
     int material_for(const Block& b, bool required) {
         const std::string n = find_str(b, "bsdf", "");
         auto it = mat_names.find(n);
@@ -334,6 +346,10 @@ struct cgpu_crsd_scene {
             if (const Unit* u = b.find("positions")) to_vec3_array(u->value, &pos);
             if (const Unit* u = b.find("normals")) to_vec3_array(u->value, &nrm);
             if (const Unit* u = b.find("uvws")) to_vec3_array(u->value, &uvw);
+            // binary sidecars: raw little-endian float32, 3 per vertex, 3 vertices per triangle
+            if (const Unit* u = b.find("positions-file")) read_f32_file(u->value, &pos);
+            if (const Unit* u = b.find("normals-file")) read_f32_file(u->value, &nrm);
+            if (const Unit* u = b.find("uvws-file")) read_f32_file(u->value, &uvw);
             if (pos.size() % 9 != 0) fail(CGPU_ERR_PARSE, "triangle-mesh positions are not whole triangles");
             const size_t nt = pos.size() / 9;
             if (!nrm.empty() && nrm.size() != pos.size()) fail(CGPU_ERR_PARSE, "triangle-mesh normals size");

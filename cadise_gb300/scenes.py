@@ -137,7 +137,17 @@ class SceneSpec:
         return n
 
     # ------------------------------------------------------------------- CRSD
-    def to_crsd(self, with_header: bool = True) -> str:
+    def write_crsd(self, path: str, sidecar_min_triangles: int = 4096) -> None:
+        """Write the scene as a CRSD file; meshes with at least
+        `sidecar_min_triangles` triangles go to binary float32 sidecar files
+        next to it (`[positions-file string ...]`) instead of text arrays."""
+        import os
+        base = os.path.dirname(os.path.abspath(path))
+        stem = os.path.splitext(os.path.basename(path))[0]
+        with open(path, "w") as f:
+            f.write(self.to_crsd(sidecar=(base, stem, sidecar_min_triangles)))
+
+    def to_crsd(self, with_header: bool = True, sidecar=None) -> str:
         out: List[str] = []
         w = out.append
 
@@ -182,6 +192,18 @@ class SceneSpec:
                 w("primitive {\n    [type string \"rectangle\"]\n    [name string \"%s\"]\n"
                   "    [bsdf material \"%s\"]\n    [v1 vector3r \"%s\"]\n    [v2 vector3r \"%s\"]\n"
                   "    [v3 vector3r \"%s\"]\n}\n" % (p.name, p.material, v3(p.v1), v3(p.v2), v3(p.v3)))
+            elif sidecar is not None and p.positions.shape[0] >= sidecar[2]:
+                import os
+                base, stem, _ = sidecar
+                w("primitive {\n    [type string \"triangle-mesh\"]\n    [name string \"%s\"]\n"
+                  "    [bsdf material \"%s\"]\n" % (p.name, p.material))
+                for key, arr in (("positions", p.positions), ("normals", p.normals), ("uvws", p.uvws)):
+                    if arr is None:
+                        continue
+                    fn = "%s.%s.%s.f32" % (stem, p.name, key)
+                    np.ascontiguousarray(arr, dtype="<f4").tofile(os.path.join(base, fn))
+                    w("    [%s-file string \"%s\"]\n" % (key, fn))
+                w("}\n")
             else:
                 pos = p.positions.reshape(-1, 3)
                 w("primitive {\n    [type string \"triangle-mesh\"]\n    [name string \"%s\"]\n"

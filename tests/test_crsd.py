@@ -92,3 +92,22 @@ def test_missing_file_is_not_found():
     with pytest.raises(CgpuError) as e:
         cg.CrsdScene(path="/nonexistent/scene.crsd")
     assert e.value.status == 6
+
+
+def test_binary_mesh_sidecars_load_like_text(tmp_path):
+    """Large meshes written as float32 sidecars load to the same arrays as
+    the text vector3r-array form (and much faster)."""
+    import time
+    spec = scenes.icosphere_field(n_spheres=20, subdivision=3, width=32, height=32, spp=1)
+    path = str(tmp_path / "field.crsd")
+    spec.write_crsd(path, sidecar_min_triangles=100)
+    t0 = time.perf_counter()
+    sc = cg.CrsdScene(path=path)
+    t_bin = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    txt = cg.CrsdScene(text=spec.to_crsd())
+    t_txt = time.perf_counter() - t0
+    a, b = sc.arrays(), txt.arrays()
+    for x, y in zip(a, b):
+        assert np.array_equal(x, y)
+    assert t_bin < t_txt
