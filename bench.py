@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--profile-case", action="store_true",
+                    help="for ncu: upload the frame and run --steps wavefront passes of 1 spp, nothing else")
     return ap.parse_args()
 
 
@@ -373,9 +375,25 @@ def run_reference(args, rank, world, local):
     print(json.dumps(out), flush=True)
 
 
+def run_profile_case(args):
+    import cadise_gb300 as cg
+    from cadise_gb300 import abi
+    ctx = cg.Context()
+    spec = make_scene(args)
+    sid = ctx.upload(abi.flatten(spec))
+    for i in range(args.steps):
+        ctx.render([sid], i, 1, seed=2024, mode=cg.CGPU_MODE_WAVEFRONT, graph=False)
+    print(json.dumps({"profile_case": WORKLOAD if not args.quick else "quick", "passes": args.steps,
+                      "kernel_launches_last_pass": ctx.stats().kernel_launches}))
+    ctx.close()
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.profile_case:
+        run_profile_case(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world, local)
     else:
