@@ -15,7 +15,7 @@ namespace {
 
 bool valid_tuning(const cgpu_tuning& t) {
     auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
-    return ok_block(t.block_trace) && ok_block(t.block_shade);
+    return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal == 0 || t.traversal == 1);
 }
 
 void apply(cgpu_ctx* ctx, const cgpu_tuning& t) {
@@ -60,13 +60,17 @@ bool cache_lookup(const char* path, const std::string& key, cgpu_tuning* out) {
         const char* p = std::strstr(line.c_str(), "\"block_trace\":");
         const char* q = std::strstr(line.c_str(), "\"block_shade\":");
         const char* r = std::strstr(line.c_str(), "\"max_paths\":");
+        const char* tv = std::strstr(line.c_str(), "\"traversal\":");
         if (!p || !q || !r) continue;
+        int trav = 0;
+        if (tv) std::sscanf(tv, "\"traversal\": %d", &trav);
         if (std::sscanf(p, "\"block_trace\": %d", &a) != 1 || std::sscanf(q, "\"block_shade\": %d", &b) != 1 ||
             std::sscanf(r, "\"max_paths\": %u", &c) != 1)
             continue;
         t.block_trace = a;
         t.block_shade = b;
         t.max_paths = c;
+        t.traversal = trav;
         if (valid_tuning(t)) {
             *out = t;
             found = true;  // the last matching line wins
@@ -144,12 +148,13 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     cgpu_status st = time_one(best, &best_ms);
     const int blocks[] = {64, 128, 256};
     const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
-    for (int pass = 0; pass < 3 && st == CGPU_OK; ++pass) {
+    for (int pass = 0; pass < 4 && st == CGPU_OK; ++pass) {
         for (int k = 0; k < 3 && st == CGPU_OK; ++k) {
             cgpu_tuning t = best;
-            if (pass == 0) t.block_trace = blocks[k];
-            if (pass == 1) t.block_shade = blocks[k];
-            if (pass == 2) t.max_paths = caps[k];
+            if (pass == 0) t.traversal = k < 2 ? k : best.traversal;
+            if (pass == 1) t.block_trace = blocks[k];
+            if (pass == 2) t.block_shade = blocks[k];
+            if (pass == 3) t.max_paths = caps[k];
             if (std::memcmp(&t, &best, sizeof(t)) == 0) continue;
             float ms = 0.0f;
             st = time_one(t, &ms);
@@ -170,7 +175,8 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     if (cache_path) {
         std::ofstream f(cache_path, std::ios::app);
         f << "{\"key\": \"" << key << "\", \"block_trace\": " << best.block_trace << ", \"block_shade\": "
-          << best.block_shade << ", \"max_paths\": " << best.max_paths << ", \"ms\": " << best_ms << "}\n";
+          << best.block_shade << ", \"max_paths\": " << best.max_paths << ", \"traversal\": " << best.traversal
+          << ", \"ms\": " << best_ms << "}\n";
     }
     if (out) *out = best;
     return CGPU_OK;

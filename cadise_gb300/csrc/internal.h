@@ -42,8 +42,9 @@ struct FilmD {
 
 // Counters per bounce b at cnt[b * kCntStride + k]:
 //   k = 0 continuation rays to extend, 1 MIS rays to extend, 2 shadow rays,
-//   3 + kind: hits waiting for the shade kernel of that BSDF kind.
-constexpr int kCntStride = 8;
+//   3 + kind: hits waiting for the shade kernel of that BSDF kind,
+//   8 / 9: rays handed out so far by the persistent extend / shadow kernels.
+constexpr int kCntStride = 16;
 
 struct WfBuffers {
     float4 *ray_o, *ray_d, *hit, *thr, *L, *Ls, *mis_a, *mis_b, *mis_d, *sh_d, *sh_c;

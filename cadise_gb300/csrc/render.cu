@@ -94,6 +94,67 @@ CG_D void grouped_push(int* const* queues, int* counters, int key, int p) {
     if (key >= 0) queues[key][base + __popc(grp & ((1u << lane) - 1u))] = p;
 }
 
+// After a closest-hit trace of queue entry p: a continuation hit is stored
+// and its BSDF kind returned (the shade queue to join); an escaped
+// continuation ray picks up the sky; a MIS ray that reaches its light adds
+// the BSDF-sampling half of the NEE estimate.  Returns -1 when nothing is
+// queued.
+CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, float3 o, float3 d, bool hitp,
+                       const HitD& hit) {
+    if (cont) {
+        if (hitp) {
+            w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
+            return S.materials[material_of_slot(S, hit.slot)].type;
+        }
+        if (S.env_light >= 0) {
+            const float4 tw = w.thr[p];
+            if (__float_as_int(tw.w) & 1) {
+                const float3 add = f3(tw) * env_radiance(S, d);
+                float4 L = w.L[p];
+                L.x += add.x;
+                L.y += add.y;
+                L.z += add.z;
+                w.L[p] = L;
+            }
+        }
+        return -1;
+    }
+    const float4 mb = w.mis_b[p];
+    const int mlight = __float_as_int(mb.w);
+    float3 add = splat3(0.0f);
+    bool has = false;
+    if (hitp) {
+        if (light_of_slot(S, hit.slot) == mlight) {
+            const SurfaceD hs = surface_at(S, o, d, hit);
+            const float4 ma = w.mis_a[p];
+            add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w);
+            has = true;
+        }
+    } else if (mlight == S.env_light) {
+        const float4 ma = w.mis_a[p];
+        add = mis_resolve_env(S, d, f3(mb), f3(ma), ma.w);
+        has = true;
+    }
+    if (has) {
+        float4 L = w.L[p];
+        L.x += add.x;
+        L.y += add.y;
+        L.z += add.z;
+        w.L[p] = L;
+    }
+    return -1;
+}
+
+CG_D void shadow_finish(const WfBuffers& w, int p, bool occluded) {
+    if (occluded) return;
+    const float4 c = w.sh_c[p];
+    float4 Ls = w.Ls[p];
+    Ls.x += c.x;
+    Ls.y += c.y;
+    Ls.z += c.z;
+    w.Ls[p] = Ls;
+}
+
 template <bool COUNT>
 __global__ void k_wf_extend(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
@@ -106,62 +167,16 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
     uint32_t nclosest = 0;
     int* const* qmat = w.q_mat;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        int key = -1;
-        int p;
-        if (i < ncont) {
-            p = qc[i];
-            const SceneD& S = a.scenes[w.meta[p].x];
-            const float3 o = f3(w.ray_o[p]), d = f3(w.ray_d[p]);
-            const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
-            HitD hit;
-            if (COUNT) ++nclosest;
-            if (traverse<false, COUNT>(S, r, &hit, &tc)) {
-                w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
-                key = S.materials[material_of_slot(S, hit.slot)].type;
-            } else if (S.env_light >= 0) {
-                const float4 tw = w.thr[p];
-                if (__float_as_int(tw.w) & 1) {
-                    const float3 add = f3(tw) * env_radiance(S, d);
-                    float4 L = w.L[p];
-                    L.x += add.x;
-                    L.y += add.y;
-                    L.z += add.z;
-                    w.L[p] = L;
-                }
-            }
-        } else {
-            p = qm[i - ncont];
-            const SceneD& S = a.scenes[w.meta[p].x];
-            const float3 o = f3(w.ray_o[p]);
-            const float3 md = f3(w.mis_d[p]);
-            const RayPre r = ray_prep(o, md, kRayEps, kFloatMax);
-            HitD hit;
-            if (COUNT) ++nclosest;
-            const bool hitp = traverse<false, COUNT>(S, r, &hit, &tc);
-            const float4 mb = w.mis_b[p];
-            const int mlight = __float_as_int(mb.w);
-            float3 add = splat3(0.0f);
-            bool has = false;
-            if (hitp) {
-                if (light_of_slot(S, hit.slot) == mlight) {
-                    const SurfaceD hs = surface_at(S, o, md, hit);
-                    const float4 ma = w.mis_a[p];
-                    add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w);
-                    has = true;
-                }
-            } else if (mlight == S.env_light) {
-                const float4 ma = w.mis_a[p];
-                add = mis_resolve_env(S, md, f3(mb), f3(ma), ma.w);
-                has = true;
-            }
-            if (has) {
-                float4 L = w.L[p];
-                L.x += add.x;
-                L.y += add.y;
-                L.z += add.z;
-                w.L[p] = L;
-            }
-        }
+        const bool cont = i < ncont;
+        const int p = cont ? qc[i] : qm[i - ncont];
+        const SceneD& S = a.scenes[w.meta[p].x];
+        const float3 o = f3(w.ray_o[p]);
+        const float3 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+        const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
+        HitD hit;
+        if (COUNT) ++nclosest;
+        const bool hitp = traverse<false, COUNT>(S, r, &hit, &tc);
+        const int key = extend_finish(w, S, p, cont, o, d, hitp, hit);
         grouped_push(qmat, cnt + 3, key, p);
     }
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
@@ -181,13 +196,119 @@ __global__ void k_wf_shadow(RenderArgs a, int b) {
         const RayPre r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
         HitD hit;
         if (COUNT) ++nany;
-        if (!traverse<true, COUNT>(S, r, &hit, &tc)) {
-            const float4 c = w.sh_c[p];
-            float4 Ls = w.Ls[p];
-            Ls.x += c.x;
-            Ls.y += c.y;
-            Ls.z += c.z;
-            w.Ls[p] = Ls;
+        shadow_finish(w, p, traverse<true, COUNT>(S, r, &hit, &tc));
+    }
+    count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
+}
+
+// Persistent variants: each lane takes rays from the queue through a
+// warp-aggregated counter and, whenever its ray finishes, the next one, so no
+// lane idles while the warp's longest ray is still traversing.
+constexpr int kStepsPerFetch = 4;
+
+// Hands the lanes in `need` consecutive entries of [0, n); returns this lane's
+// entry or -1 when the queue is drained.
+CG_D int warp_take(int* work, bool need, int n) {
+    const unsigned mask = __activemask();
+    const unsigned nb = __ballot_sync(mask, need);
+    if (nb == 0) return -1;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(nb) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(work, __popc(nb));
+    base = __shfl_sync(mask, base, leader);
+    if (!need) return -1;
+    const int k = base + __popc(nb & ((1u << lane) - 1u));
+    return k < n ? k : -1;
+}
+
+template <bool COUNT>
+__global__ void k_wf_extend_dyn(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    int* cnt = w.cnt + b * kCntStride;
+    const int ncont = cnt[0], nmis = cnt[1];
+    const int n = ncont + nmis;
+    const int* qc = w.q_cont[b & 1];
+    const int* qm = w.q_mis[b & 1];
+    TraceCounters tc{0, 0};
+    uint32_t nclosest = 0;
+    int* const* qmat = w.q_mat;
+    TravState st;
+    RayPre r;
+    int i = -1, p = -1;
+    bool drained = false;
+    float3 o = splat3(0.0f), d = splat3(0.0f);
+    for (;;) {
+        const bool need = i < 0 && !drained;
+        const int k = warp_take(cnt + 8, need, n);
+        if (need) {
+            if (k < 0) {
+                drained = true;
+            } else {
+                i = k;
+                const bool cont = i < ncont;
+                p = cont ? qc[i] : qm[i - ncont];
+                o = f3(w.ray_o[p]);
+                d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+                r = ray_prep(o, d, kRayEps, kFloatMax);
+                trav_begin(st, r);
+                if (COUNT) ++nclosest;
+            }
+        }
+        if (__all_sync(__activemask(), i < 0)) break;
+        if (i >= 0) {
+            const SceneD& S = a.scenes[w.meta[p].x];
+            for (int s = 0; s < kStepsPerFetch && !st.done; ++s) trav_step<false, COUNT>(S, r, st, &tc);
+            if (st.done) {
+                HitD hit;
+                hit.slot = st.hslot;
+                hit.t = st.tcur;
+                hit.u = st.hu;
+                hit.v = st.hv;
+                const int key = extend_finish(w, S, p, i < ncont, o, d, st.hslot >= 0, hit);
+                grouped_push(qmat, cnt + 3, key, p);
+                i = -1;
+            }
+        }
+    }
+    count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
+}
+
+template <bool COUNT>
+__global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    int* cnt = w.cnt + b * kCntStride;
+    const int n = cnt[2];
+    const int* q = w.q_shadow[b & 1];
+    TraceCounters tc{0, 0};
+    uint32_t nany = 0;
+    TravState st;
+    RayPre r;
+    int i = -1, p = -1;
+    bool drained = false;
+    for (;;) {
+        const bool need = i < 0 && !drained;
+        const int k = warp_take(cnt + 9, need, n);
+        if (need) {
+            if (k < 0) {
+                drained = true;
+            } else {
+                i = k;
+                p = q[i];
+                const float4 sd = w.sh_d[p];
+                r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
+                trav_begin(st, r);
+                if (COUNT) ++nany;
+            }
+        }
+        if (__all_sync(__activemask(), i < 0)) break;
+        if (i >= 0) {
+            const SceneD& S = a.scenes[w.meta[p].x];
+            for (int s = 0; s < kStepsPerFetch && !st.done; ++s) trav_step<true, COUNT>(S, r, st, &tc);
+            if (st.done) {
+                shadow_finish(w, p, st.hslot >= 0);
+                i = -1;
+            }
         }
     }
     count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
@@ -452,21 +573,21 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
     const int ggen = grid_for(ctx, k_wf_generate, kBlock, paths);
     timed(ctx, CGPU_KERNEL_GENERATE, s, [&] { k_wf_generate<<<ggen, kBlock, 0, s>>>(a); });
-    auto gext = counting ? grid_for(ctx, k_wf_extend<true>, bt, paths) : grid_for(ctx, k_wf_extend<false>, bt, paths);
-    auto gsh = counting ? grid_for(ctx, k_wf_shadow<true>, bt, paths) : grid_for(ctx, k_wf_shadow<false>, bt, paths);
+    const bool dyn = ctx->tuning.traversal == 1;
+    auto ext_kernel = dyn ? (counting ? k_wf_extend_dyn<true> : k_wf_extend_dyn<false>)
+                          : (counting ? k_wf_extend<true> : k_wf_extend<false>);
+    auto sh_kernel = dyn ? (counting ? k_wf_shadow_dyn<true> : k_wf_shadow_dyn<false>)
+                         : (counting ? k_wf_shadow<true> : k_wf_shadow<false>);
+    const int gext = grid_for(ctx, ext_kernel, bt, paths);
+    const int gsh = grid_for(ctx, sh_kernel, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
                                     grid_for(ctx, k_wf_shade<4>, bs, paths)};
     for (int b = 0; b <= depth; ++b) {
         cudaEventRecord(fork, s);
         cudaStreamWaitEvent(side, fork, 0);
-        if (counting) {
-            k_wf_extend<true><<<gext, bt, 0, s>>>(a, b);
-            k_wf_shadow<true><<<gsh, bt, 0, side>>>(a, b);
-        } else {
-            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { k_wf_extend<false><<<gext, bt, 0, s>>>(a, b); });
-            timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { k_wf_shadow<false><<<gsh, bt, 0, side>>>(a, b); });
-        }
+        timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, 0, s>>>(a, b); });
+        timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, 0, side>>>(a, b); });
         cudaEventRecord(join, side);
         cudaStreamWaitEvent(s, join, 0);
         launches += 2;

@@ -215,4 +215,99 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
     return hslot >= 0;
 }
 
+// Resumable form of the same traversal for persistent kernels that replace
+// finished rays (a warp keeps all lanes busy by giving a lane whose ray is
+// done the next ray from a global counter; Aila & Laine, "Understanding the
+// efficiency of ray traversal on GPUs", HPG 2009).  trav_step performs one
+// node visit or one leaf test; the same decisions as traverse().
+struct TravState {
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp;
+    uint32_t cur;
+    float tcur;
+    int hslot;
+    float hu, hv;
+    bool done;
+};
+
+CG_D void trav_begin(TravState& st, const RayPre& r) {
+    st.sp = 0;
+    st.cur = 0;
+    st.tcur = r.tmax;
+    st.hslot = -1;
+    st.hu = st.hv = 0.0f;
+    st.done = false;
+}
+
+template <bool ANY, bool COUNT>
+CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounters* cnt) {
+    const float kInf = __int_as_float(0x7f800000);
+    if (entry_is_leaf(st.cur)) {
+        const uint32_t first = leaf_first(st.cur), n = leaf_count(st.cur);
+        for (uint32_t k = 0; k < n; ++k) {
+            const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
+            const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+            if (COUNT) cnt->tris++;
+            float t, u, v;
+            if (tri_test(r, f3(a), f3(b), f3(c), st.tcur, &t, &u, &v)) {
+                st.hslot = int(first + k);
+                if (ANY) {
+                    st.tcur = t;
+                    st.done = true;
+                    return;
+                }
+                st.tcur = t;
+                st.hu = u;
+                st.hv = v;
+            }
+        }
+    } else {
+        float4 q[7];
+        load_node(S.nodes, st.cur, q);
+        if (COUNT) cnt->nodes++;
+        float tn[4];
+        child_hits(r, q, st.tcur, tn);
+        uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
+                          __float_as_uint(q[6].w)};
+        if (!ANY) {
+#define CG_CSWAP(i, j)                                                      \
+    if (tn[j] < tn[i]) {                                                    \
+        const float tt = tn[i]; tn[i] = tn[j]; tn[j] = tt;                  \
+        const uint32_t ee = ce[i]; ce[i] = ce[j]; ce[j] = ee;               \
+    }
+            CG_CSWAP(0, 1) CG_CSWAP(2, 3) CG_CSWAP(0, 2) CG_CSWAP(1, 3) CG_CSWAP(1, 2)
+#undef CG_CSWAP
+        }
+        int nhit = 0;
+        uint32_t nearest = 0;
+        float nearest_t = kInf;
+#pragma unroll
+        for (int i = 3; i >= 0; --i) {
+            if (tn[i] < kInf) {
+                if (nhit > 0 && st.sp < kStackSize) {
+                    st.stack_e[st.sp] = nearest;
+                    st.stack_t[st.sp] = nearest_t;
+                    ++st.sp;
+                }
+                nearest = ce[i];
+                nearest_t = tn[i];
+                ++nhit;
+            }
+        }
+        if (nhit > 0) {
+            st.cur = nearest;
+            return;
+        }
+    }
+    while (st.sp > 0) {
+        --st.sp;
+        if (ANY || st.stack_t[st.sp] <= st.tcur * 1.00000036f) {
+            st.cur = st.stack_e[st.sp];
+            return;
+        }
+    }
+    st.done = true;
+}
+
 }  // namespace cg
