@@ -8,11 +8,33 @@
 #include <cuda_runtime.h>
 
 #ifndef __CUDACC__
+// Host compilation of the device headers (the CPU check of the kernel logic
+// in tests/native/ and the host-side scene build): plain C++ stand-ins for
+// the CUDA intrinsics these headers use, with the same arithmetic meaning.
+#include <algorithm>
+#include <cstring>
 using std::fabs;
 using std::isfinite;
 using std::sqrt;
 inline float fabsf(float x) { return std::fabs(x); }
 inline float sqrtf(float x) { return std::sqrt(x); }
+template <typename T>
+inline T __ldg(const T* p) { return *p; }
+inline float __fmul_rn(float a, float b) { volatile float r = a * b; return r; }
+inline float __fsub_rn(float a, float b) { volatile float r = a - b; return r; }
+inline unsigned __float_as_uint(float f) { unsigned u; std::memcpy(&u, &f, 4); return u; }
+inline int __float_as_int(float f) { int u; std::memcpy(&u, &f, 4); return u; }
+inline float __uint_as_float(unsigned u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline float __int_as_float(int u) { float f; std::memcpy(&f, &u, 4); return f; }
+inline void sincospif(float x, float* s, float* c) {
+    const double a = 3.14159265358979323846 * double(x);
+    *s = float(std::sin(a));
+    *c = float(std::cos(a));
+}
+using std::max;
+using std::min;
+inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v) { unsigned long long o = *p; *p += v; return o; }
+inline double atomicAdd(double* p, double v) { double o = *p; *p += v; return o; }
 #endif
 
 #define CG_HD __host__ __device__ __forceinline__

@@ -1,0 +1,38 @@
+// Host-side construction of a scene's device tables from a cgpu_scene_desc:
+// validation, rectangle expansion, BVH build, triangle records, materials,
+// lights (area + environment distribution), camera.  cgpu_scene_upload copies
+// the result to the device; the CPU check of the kernel logic uses it in
+// place (host_view).
+#pragma once
+
+#include "../../include/cadise_gpu.h"
+#include "scene_device.cuh"
+
+#include <string>
+#include <vector>
+
+namespace cg {
+
+struct HostScene {
+    std::vector<Bvh4Node> nodes;
+    std::vector<TriRecord> tris;
+    std::vector<MaterialD> mats;
+    std::vector<LightD> lights;      // area lights, then the environment light if any
+    int num_area_lights = 0;
+    int env_light = -1;
+    int env_tex = -1;
+    std::vector<float> env_marg, env_cond;
+    std::vector<TextureD> textures;  // texel pointers into the caller's desc
+    std::vector<float> rect_frames;  // vB, eA, eB per rectangle
+    CameraD cam{};
+    cgpu_scene_info info{};
+    int wide_depth = 0;
+};
+
+// Returns CGPU_OK or an error status with a message in *err.
+cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err);
+
+// A SceneD whose pointers are the host arrays (for running the kernel logic on the CPU).
+SceneD host_view(HostScene& hs, const cgpu_scene_desc* d);
+
+}  // namespace cg

@@ -3,8 +3,9 @@
 //  * Bvh4Node, 128 B, one L2 line: four child boxes stored SoA
 //    (lo/hi x, y, z) + four 32-bit child entries.  A child entry is either an
 //    inner node index (bit 31 clear) or a leaf: bit 31 set, (count - 1) in
-//    bits 28..30, first triangle slot in bits 0..27.  Empty slots carry an
-//    inverted box (lo = +inf, hi = -inf) and never hit.
+//    bits 28..30, first triangle slot in bits 0..27.  Empty slots hold entry
+//    0 (the root can be no node's child) with an inverted box; the traversal
+//    tests the entry, not the box.
 //  * TriRecord, 48 B per triangle in leaf order: the three vertices in the
 //    primitive's own vertex order (so the geometric normal is the reference's
 //    eAB x eAC) with the primitive index, the packed material / light id and

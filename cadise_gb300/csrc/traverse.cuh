@@ -104,8 +104,12 @@ CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, float4 (&q)[7]) {
 
 CG_D float4 ldg4(const float4* p) { return __ldg(p); }
 
-// Child box distances; tnear = +inf marks a miss.
+// Child box distances; tnear = +inf marks a miss.  Empty child slots hold
+// entry 0 (the root, never anyone's child) and are always a miss: their
+// inverted box would not stay inverted under the min/max slab form below.
 CG_D void child_hits(const RayPre& r, const float4 (&q)[7], float tcur, float (&tn)[4]) {
+    const uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
+                            __float_as_uint(q[6].w)};
     const float lox[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
     const float hix[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
     const float loy[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
@@ -120,7 +124,7 @@ CG_D void child_hits(const RayPre& r, const float4 (&q)[7], float tcur, float (&
         const float t0z = (loz[i] - r.o.z) * r.inv.z, t1z = (hiz[i] - r.o.z) * r.inv.z;
         const float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), r.tmin));
         const float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tlim));
-        tn[i] = (tnear <= tfar * 1.00000036f) ? tnear : __int_as_float(0x7f800000);
+        tn[i] = (ce[i] != 0u && tnear <= tfar * 1.00000036f) ? tnear : __int_as_float(0x7f800000);
     }
 }
 

@@ -6,7 +6,9 @@ Tolerances (FP32 path tracer):
   * closest hits: identical hit/miss and primitive id except rays whose hit
     point lies within 1e-5 (relative barycentric / edge coordinate) of a
     primitive edge, where the reference's non-watertight test and the
-    watertight one may legitimately disagree; |dt| / t <= 1e-5;
+    watertight one may legitimately disagree, and equal-t ties (another
+    primitive at the same distance, e.g. coplanar faces);
+    |dt| <= 1e-5 t + 1e-6 (1 + |origin|_inf);
   * per-path radiance: the GPU evaluates transcendental functions and
     contracted products differently from the host, so a path may branch
     differently after a near-tie; >= 97 % of paths within 1e-3 relative
@@ -87,12 +89,15 @@ def test_closest_hits_match_reference(name, gpu_ctx, uploaded):
         m_gpu = edge_margin(flat, prim[diff], o[diff] + d[diff] * t[diff, None])
         near[diff] = (m_ref < 1e-5) | (m_gpu < 1e-5)
     tie = ref_p != v["trace_bf_prim"]  # the reference's own BVH / brute-force tie
+    # equal-t ties: a different primitive hit at the same distance (coplanar faces)
+    tie |= (prim != ref_p) & (prim >= 0) & (ref_p >= 0) & (np.abs(t - ref_t) <= 1e-5 * np.abs(ref_t))
     keep = ~(near | tie)
     assert np.mean(keep) > 0.98
     assert np.array_equal(prim[keep], ref_p[keep]), np.where(prim[keep] != ref_p[keep])
     both = keep & (prim >= 0)
-    rel = np.abs(t[both] - ref_t[both]) / np.maximum(np.abs(ref_t[both]), 1e-6)
-    assert rel.max() <= 1e-5
+    # 1e-5 relative, plus the FP32 resolution of the ray origin for hits at tiny t
+    tol = 1e-5 * np.abs(ref_t) + 1e-6 * (1.0 + np.abs(rays[:, :3]).max(1))
+    assert np.all(np.abs(t - ref_t)[both] <= tol[both])
 
 
 @pytest.mark.parametrize("name", NAMES)

@@ -1,0 +1,153 @@
+"""The CUDA library's device code, compiled as host C++ (tests/native/), run on
+the CPU against the reference's golden vectors and the oracle: traversal
+(both the per-ray loop and the resumable stepper of the persistent kernels),
+the per-path estimator, scene construction.  Catches logic errors - wrong
+hits, endless loops, wrong random-number order - before GPU time is spent.
+Same tolerances as the GPU parity tests."""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+from cadise_gb300 import abi, scenes
+from golden_scenes import specs, vectors
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+BUILD = os.path.join(ROOT, "tests", "native", "_build")
+LIB = os.path.join(BUILD, "libkhc.so")
+SRCS = [os.path.join(ROOT, "tests", "native", "kernel_host_check.cpp"),
+        os.path.join(ROOT, "cadise_gb300", "csrc", "scene_build.cpp"),
+        os.path.join(ROOT, "cadise_gb300", "csrc", "bvh_build.cpp")]
+
+
+def _cuda_include():
+    import shutil
+    nvcc = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nvcc))), "include")
+
+
+@pytest.fixture(scope="module")
+def khc():
+    deps = SRCS + [os.path.join(ROOT, "cadise_gb300", "csrc", f) for f in os.listdir(os.path.join(ROOT, "cadise_gb300", "csrc"))
+                   if f.endswith((".cuh", ".h"))]
+    if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
+        os.makedirs(BUILD, exist_ok=True)
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread",
+                               "-I", os.path.join(ROOT, "include"), "-I", _cuda_include()] + SRCS + ["-o", LIB])
+    L = C.CDLL(LIB)
+    L.khc_create.restype = C.c_void_p
+    L.khc_create.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
+    L.khc_destroy.argtypes = [C.c_void_p]
+    L.khc_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int] + [C.c_void_p] * 5
+    L.khc_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
+    L.khc_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
+    return L
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Host:
+    def __init__(self, L, flat):
+        self.L, self.flat = L, flat
+        err = C.create_string_buffer(256)
+        self.h = L.khc_create(C.addressof(flat.desc), err, 256)
+        assert self.h, err.value
+
+    def trace(self, rays, dyn=0):
+        r = np.ascontiguousarray(rays, np.float32)
+        n = r.shape[0]
+        prim, occ = np.zeros(n, np.int32), np.zeros(n, np.int32)
+        t, u, v = np.zeros(n, np.float32), np.zeros(n, np.float32), np.zeros(n, np.float32)
+        self.L.khc_trace(self.h, _p(r), n, dyn, _p(prim), _p(t), _p(u), _p(v), _p(occ))
+        return prim, t, occ
+
+    def paths(self, xy, keys):
+        xy = np.ascontiguousarray(xy, np.float64)
+        k = np.ascontiguousarray(keys, np.uint64)
+        out = np.zeros((xy.shape[0], 3), np.float32)
+        self.L.khc_paths(self.h, _p(xy), _p(k), xy.shape[0], _p(out))
+        return out
+
+    def render_paths(self, seed, first, count, scene_index=0):
+        d = self.flat.desc
+        out = np.zeros((count, d.height, d.width, 3), np.float32)
+        self.L.khc_render_paths(self.h, seed, scene_index, first, count, _p(out))
+        return out
+
+    def close(self):
+        self.L.khc_destroy(self.h)
+
+
+NAMES = ["cornell", "field", "features"]
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_kernel_traversal_matches_reference_hits(khc, name):
+    from test_gpu_parity import edge_margin
+    v = vectors(name)
+    flat = abi.flatten(specs()[name])
+    h = Host(khc, flat)
+    rays = v["trace_rays"]
+    prim, t, occ = h.trace(rays)
+    ref_p, ref_t = v["trace_bvh_prim"], v["trace_bvh_t"]
+    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
+    near = np.zeros(len(prim), bool)
+    diff = np.where(prim != ref_p)[0]
+    if len(diff):
+        near[diff] = (edge_margin(flat, ref_p[diff], o[diff] + d[diff] * ref_t[diff, None]) < 1e-5) | \
+                     (edge_margin(flat, prim[diff], o[diff] + d[diff] * t[diff, None]) < 1e-5)
+    # equal-t ties: a different primitive hit at the same distance (coplanar faces)
+    tie = (prim != ref_p) & (prim >= 0) & (ref_p >= 0) & (np.abs(t - ref_t) <= 1e-5 * np.abs(ref_t))
+    keep = ~(near | tie | (ref_p != v["trace_bf_prim"]))
+    assert keep.mean() > 0.98
+    assert np.array_equal(prim[keep], ref_p[keep])
+    both = keep & (prim >= 0)
+    # 1e-5 relative, plus the FP32 resolution of the ray origin for hits at tiny t
+    tol = 1e-5 * np.abs(ref_t) + 1e-6 * (1.0 + np.abs(rays[:, :3]).max(1))
+    assert np.all(np.abs(t - ref_t)[both] <= tol[both])
+    # the resumable stepper of the persistent kernels takes the same decisions
+    p2, t2, occ2 = h.trace(rays, dyn=1)
+    assert np.array_equal(p2, prim) and np.array_equal(t2, t) and np.array_equal(occ2, occ)
+    h.close()
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_kernel_paths_match_reference(khc, name):
+    v = vectors(name)
+    h = Host(khc, abi.flatten(specs()[name]))
+    rgb = h.paths(v["paths_xy"], v["paths_keys"])
+    ref = v["paths_rgb"]
+    close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
+    assert close.mean() >= 0.97, close.mean()
+    h.close()
+
+
+@pytest.mark.parametrize("name", ["field", "features"])
+def test_kernel_render_paths_match_oracle(khc, name):
+    flat = abi.flatten(specs()[name])
+    h = Host(khc, flat)
+    got = h.render_paths(11, 3, 2)
+    _, port = oracle.PortScene(flat).render(seed=11, first=3, count=2, threads=8, want_paths=True)
+    close = np.all(np.abs(got - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
+    assert close.mean() >= 0.97, close.mean()
+    h.close()
+
+
+def test_kernel_rough_dielectric_and_sky_match_oracle(khc):
+    for spec in (scenes.icosphere_field(n_spheres=12, subdivision=2, n_lights=3, seed=9, width=40, height=30,
+                                        spp=4, max_depth=8, dielectric=scenes.ROUGH_DIELECTRIC, box=30.0,
+                                        radius_range=(2.0, 6.0)),
+                 scenes.env_field(n_spheres=10, subdivision=2, n_lights=2, width=32, height=24, spp=4,
+                                  max_depth=6, sky=(64, 32))):
+        flat = abi.flatten(spec)
+        h = Host(khc, flat)
+        got = h.render_paths(3, 0, 4)
+        _, port = oracle.PortScene(flat).render(seed=3, first=0, count=4, threads=8, want_paths=True)
+        close = np.all(np.abs(got - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
+        assert close.mean() >= 0.97, close.mean()
+        h.close()
