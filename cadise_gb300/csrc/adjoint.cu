@@ -20,7 +20,7 @@
 // (shared-memory block sums for roughness and radiance, global atomics for
 // texels).
 #include "internal.h"
-#include "pathtrace.cuh"
+#include "adjoint.cuh"
 
 #include <algorithm>
 #include <vector>
@@ -45,13 +45,23 @@ CG_D void shared_add(double* sh, int i, double v) {
     if (v != 0.0) atomicAdd(sh + i, v);
 }
 
+// Roughness and radiance reduce in shared memory, texels in global memory.
+struct BlockSink {
+    double* shr;
+    double* shl;
+    double* g_tex;
+    const int* tex_offset;
+    CG_D void rough(int m, double v) { shared_add(shr, m, v); }
+    CG_D void rad(int i, double v) { shared_add(shl, i, v); }
+    CG_D void tex(int t, int k, double v) { atomicAdd(g_tex + tex_offset[t] + k, v); }
+};
+
 __global__ void k_adjoint(AdjArgs a) {
     extern __shared__ double sh[];  // [0, nmat) roughness, [nmat, nmat + 3 nlight) radiance
     const int nsh = a.nmat + 3 * a.nlight;
     for (int i = threadIdx.x; i < nsh; i += blockDim.x) sh[i] = 0.0;
     __syncthreads();
-    double* shr = sh;
-    double* shl = sh + a.nmat;
+    BlockSink sink{sh, sh + a.nmat, a.g_tex, a.tex_offset};
     const SceneD& S = a.scenes[a.scene];
     for (uint64_t p = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; p < a.npaths; p += uint64_t(gridDim.x) * blockDim.x) {
         const uint32_t pixel = uint32_t(p % a.npix);
@@ -64,94 +74,13 @@ __global__ void k_adjoint(AdjArgs a) {
         id.pixel = pixel;
         id.sample = sample;
         id.width = a.width;
-        // ---- replay 1: the path's radiance
-        Rng rng;
-        float3 o, d;
-        primary_ray(S, id, a.seed, rng, &o, &d);
-        float3 L1, Ls1;
-        TraceCounters tc{0, 0}, ta{0, 0};
-        uint32_t nc = 0, na = 0;
-        mk_path<false>(S, o, d, rng, &L1, &Ls1, &tc, &ta, &nc, &na);
-        const float3 Ltot = L1 + Ls1;
-        if (!finite3(Ltot)) continue;  // the film drops this sample too
-        // ---- replay 2: the same path with gradient bookkeeping
-        primary_ray(S, id, a.seed, rng, &o, &d);
-        float3 T = splat3(1.0f), acc = splat3(0.0f);
-        bool ce = true;
-        for (int b = 0; b < S.max_depth; ++b) {
-            const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
-            HitD hit;
-            if (!traverse<false, false>(S, r, &hit, &tc)) break;  // the sky has no parameters here
-            const SurfaceD si = surface_at(S, o, d, hit);
-            const VertexPlan pl = plan_vertex(S, si, T, ce, b, rng);
-            const MaterialD& m = S.materials[si.material];
-            // emission term E_j = T * Le
-            if (si.light >= 0 && ce && can_emit(S.lights[si.light], si.wi, si.Ns)) {
-                const float3 gx = delta * T;
-                shared_add(shl, 3 * si.light + 0, gx.x);
-                shared_add(shl, 3 * si.light + 1, gx.y);
-                shared_add(shl, 3 * si.light + 2, gx.z);
-            }
-            acc += pl.emit;
-            float3 A = splat3(0.0f), B = splat3(0.0f);
-            if (pl.shadow) {
-                const RayPre sr = ray_prep(si.P, pl.sdir, kRayEps, pl.stmax);
-                HitD sh2;
-                if (!traverse<true, false>(S, sr, &sh2, &ta)) {
-                    A = pl.scontrib;
-                    if (pl.slight < a.nlight) {
-                        const float3 gx = delta * pl.sx;
-                        shared_add(shl, 3 * pl.slight + 0, gx.x);
-                        shared_add(shl, 3 * pl.slight + 1, gx.y);
-                        shared_add(shl, 3 * pl.slight + 2, gx.z);
-                    }
-                }
-            }
-            if (pl.mis) {
-                const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
-                HitD mh;
-                const bool hitp = traverse<false, false>(S, mr, &mh, &tc);
-                if (hitp && light_of_slot(S, mh.slot) == pl.mlight) {
-                    const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
-                    float3 X;
-                    B = mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf, &X);
-                    const float3 gx = delta * X;
-                    shared_add(shl, 3 * pl.mlight + 0, gx.x);
-                    shared_add(shl, 3 * pl.mlight + 1, gx.y);
-                    shared_add(shl, 3 * pl.mlight + 2, gx.z);
-                } else if (!hitp && pl.mlight == S.env_light) {
-                    B = mis_resolve_env(S, pl.mdir, T, pl.mfactor, pl.mpdf);
-                }
-            }
-            const float3 after = Ltot - acc - A - B;  // radiance of the vertices after this one
-            if (m.type == BSDF_LAMBERTIAN && m.albedo_tex >= 0) {
-                const TextureD& tex = S.textures[m.albedo_tex];
-                const float3 alb = texture_rgb(tex, si.uvw);
-                const float3 num = delta * (A + B + after);
-                double* g = a.g_tex + a.tex_offset[m.albedo_tex] + 3 * size_t(texel_index(tex, si.uvw));
-                if (alb.x > 0.0f && num.x != 0.0f) atomicAdd(g + 0, double(num.x / alb.x));
-                if (alb.y > 0.0f && num.y != 0.0f) atomicAdd(g + 1, double(num.y / alb.y));
-                if (alb.z > 0.0f && num.z != 0.0f) atomicAdd(g + 2, double(num.z / alb.z));
-            } else if (m.type == BSDF_CONDUCTOR || m.type == BSDF_DIELECTRIC_GGX) {
-                float gr = 0.0f;
-                if (!is_zero(A)) gr += dot(delta, A) * dlogf_droughness(m, si.wi, pl.sdir, si.Ns);
-                if (!is_zero(B)) gr += dot(delta, B) * dlogf_droughness(m, si.wi, pl.mdir, si.Ns);
-                if (pl.cont) gr += dot(delta, after) * dlogf_droughness(m, si.wi, pl.cdir, si.Ns);
-                shared_add(shr, si.material, double(gr));
-            }
-            acc += A + B;
-            if (!pl.cont) break;
-            T = pl.T;
-            ce = pl.count_emission != 0;
-            o = si.P;
-            d = pl.cdir;
-        }
+        adjoint_path(S, id, a.seed, delta, a.nlight, sink);
     }
     __syncthreads();
     for (int i = threadIdx.x; i < a.nmat; i += blockDim.x)
-        if (shr[i] != 0.0) atomicAdd(a.g_rough + i, shr[i]);
+        if (sink.shr[i] != 0.0) atomicAdd(a.g_rough + i, sink.shr[i]);
     for (int i = threadIdx.x; i < 3 * a.nlight; i += blockDim.x)
-        if (shl[i] != 0.0) atomicAdd(a.g_rad + i, shl[i]);
+        if (sink.shl[i] != 0.0) atomicAdd(a.g_rad + i, sink.shl[i]);
 }
 
 }  // namespace cg

@@ -48,6 +48,10 @@ constexpr int kCntStride = 16;
 
 struct WfBuffers {
     float4 *ray_o, *ray_d, *hit, *thr, *L, *Ls, *mis_a, *mis_b, *mis_d, *sh_d, *sh_c;
+    // Sky radiance picked up by an escaped continuation ray.  Kept apart from
+    // L: the MIS ray of the same path's last vertex adds to L in the same
+    // extend pass.  A path sample is (L + Le) + Ls.
+    float4* Le;
     uint4* meta;      // scene, pixel, sample, rng counter
     int* q_cont[2];
     int* q_mis[2];

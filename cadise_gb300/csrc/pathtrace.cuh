@@ -66,17 +66,20 @@ CG_D void count_flush(unsigned long long* counters, const TraceCounters& cc, con
 }
 
 // One whole path sample (PtEstimator::estimate): the megakernel body.
+// Three accumulators, as the wavefront keeps them: L (emission and the
+// BSDF-sampled half of NEE), Le (the sky seen by an escaping continuation
+// ray) and Ls (the light-sampled half of NEE); the sample is (L + Le) + Ls.
 template <bool COUNT>
-CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, float3* Lsout, TraceCounters* tc,
-                  TraceCounters* ta, uint32_t* nclosest, uint32_t* nany) {
-    float3 L = splat3(0.0f), Ls = splat3(0.0f), T = splat3(1.0f);
+CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, float3* Leout, float3* Lsout,
+                  TraceCounters* tc, TraceCounters* ta, uint32_t* nclosest, uint32_t* nany) {
+    float3 L = splat3(0.0f), Le = splat3(0.0f), Ls = splat3(0.0f), T = splat3(1.0f);
     bool ce = true;
     for (int b = 0; b < S.max_depth; ++b) {
         const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
         HitD hit;
         if (COUNT) ++*nclosest;
         if (!traverse<false, COUNT>(S, r, &hit, tc)) {
-            if (S.env_light >= 0 && ce) L += T * env_radiance(S, d);
+            if (S.env_light >= 0 && ce) Le = T * env_radiance(S, d);
             break;
         }
         const SurfaceD si = surface_at(S, o, d, hit);
@@ -108,7 +111,10 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
         d = pl.cdir;
     }
     *Lout = L;
+    *Leout = Le;
     *Lsout = Ls;
 }
+
+CG_HD float3 path_sample(float3 L, float3 Le, float3 Ls) { return (L + Le) + Ls; }
 
 }  // namespace cg

@@ -32,9 +32,10 @@ __global__ void k_megakernel(RenderArgs a) {
         Rng rng;
         float3 o, d;
         primary_ray(S, id, h.seed, rng, &o, &d);
-        float3 L, Ls;
-        mk_path<COUNT>(S, o, d, rng, &L, &Ls, &tc, &ta, &nc, &na);
+        float3 L, Le, Ls;
+        mk_path<COUNT>(S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
         a.wf.L[p] = make_float4(L.x, L.y, L.z, 0.0f);
+        a.wf.Le[p] = make_float4(Le.x, Le.y, Le.z, 0.0f);
         a.wf.Ls[p] = make_float4(Ls.x, Ls.y, Ls.z, 0.0f);
     }
     count_flush<COUNT>(a.counters, tc, ta, nc, na);
@@ -50,13 +51,14 @@ __global__ void k_paths_explicit(const SceneD* scenes, int scene, const double* 
         rng.ctr = 0;
         float3 o, d;
         camera_ray(S.cam, float(xy[2 * i]), float(xy[2 * i + 1]), &o, &d);
-        float3 L, Ls;
+        float3 L, Le, Ls;
         TraceCounters tc{0, 0}, ta{0, 0};
         uint32_t nc = 0, na = 0;
-        mk_path<false>(S, o, d, rng, &L, &Ls, &tc, &ta, &nc, &na);
-        out[3 * i + 0] = L.x + Ls.x;
-        out[3 * i + 1] = L.y + Ls.y;
-        out[3 * i + 2] = L.z + Ls.z;
+        mk_path<false>(S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
+        const float3 v = path_sample(L, Le, Ls);
+        out[3 * i + 0] = v.x;
+        out[3 * i + 1] = v.y;
+        out[3 * i + 2] = v.z;
     }
 }
 
@@ -74,6 +76,7 @@ __global__ void k_wf_generate(RenderArgs a) {
         w.ray_d[p] = make_float4(d.x, d.y, d.z, 0.0f);
         w.thr[p] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(1));
         w.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.Le[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.Ls[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         w.meta[p] = make_uint4(uint32_t(id.scene), id.pixel, id.sample, rng.ctr);
         w.q_cont[0][p] = int(p);
@@ -109,12 +112,8 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
         if (S.env_light >= 0) {
             const float4 tw = w.thr[p];
             if (__float_as_int(tw.w) & 1) {
-                const float3 add = f3(tw) * env_radiance(S, d);
-                float4 L = w.L[p];
-                L.x += add.x;
-                L.y += add.y;
-                L.z += add.z;
-                w.L[p] = L;
+                const float3 e = f3(tw) * env_radiance(S, d);
+                w.Le[p] = make_float4(e.x, e.y, e.z, 0.0f);
             }
         }
         return -1;
@@ -389,8 +388,8 @@ __global__ void k_splat(RenderArgs a) {
         double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0, n = 0;
         for (uint32_t k = 0; k < c.nsamples; ++k) {
             const uint32_t p = c.path_begin + k * c.npix + pixel;
-            const float4 L = a.wf.L[p], Ls = a.wf.Ls[p];
-            const float x = L.x + Ls.x, y = L.y + Ls.y, z = L.z + Ls.z;
+            const float3 v = path_sample(f3(a.wf.L[p]), f3(a.wf.Le[p]), f3(a.wf.Ls[p]));
+            const float x = v.x, y = v.y, z = v.z;
             if (!(isfinite(x) && isfinite(y) && isfinite(z))) continue;
             s0 += x; s1 += y; s2 += z;
             q0 += double(x) * x; q1 += double(y) * y; q2 += double(z) * z;
@@ -407,12 +406,12 @@ __global__ void k_splat(RenderArgs a) {
     }
 }
 
-__global__ void k_gather_paths(const float4* L, const float4* Ls, uint32_t n, float* out) {
+__global__ void k_gather_paths(const float4* L, const float4* Le, const float4* Ls, uint32_t n, float* out) {
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-        const float4 a = L[p], b = Ls[p];
-        out[3 * p + 0] = a.x + b.x;
-        out[3 * p + 1] = a.y + b.y;
-        out[3 * p + 2] = a.z + b.z;
+        const float3 v = path_sample(f3(L[p]), f3(Le[p]), f3(Ls[p]));
+        out[3 * p + 0] = v.x;
+        out[3 * p + 1] = v.y;
+        out[3 * p + 2] = v.z;
     }
 }
 
@@ -422,7 +421,9 @@ __global__ void k_trace(const SceneD* scenes, int scene, const cgpu_ray* rays, u
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const SceneD& S = scenes[scene];
         const cgpu_ray r = rays[i];
-        const RayPre pr = ray_prep(mk(r.org[0], r.org[1], r.org[2]), mk(r.dir[0], r.dir[1], r.dir[2]), r.t_min, r.t_max);
+        // the direction is normalised again, as the reference's Ray constructor does (ray.cpp:19-30)
+        const RayPre pr = ray_prep(mk(r.org[0], r.org[1], r.org[2]), normalize(mk(r.dir[0], r.dir[1], r.dir[2])),
+                                   r.t_min, r.t_max);
         HitD h;
         TraceCounters tc{0, 0};
         if (occ) {
@@ -430,10 +431,11 @@ __global__ void k_trace(const SceneD* scenes, int scene, const cgpu_ray* rays, u
         } else {
             cgpu_hit out;
             if (traverse<false, false>(S, pr, &h, &tc)) {
-                out.t = h.t;
+                const HitPoint hp = hit_point(S, pr.o, pr.d, h);
+                out.t = hp.t;
                 out.primitive = __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + h.slot)).w);
-                out.u = h.u;
-                out.v = h.v;
+                out.u = hp.rect >= 0 ? hp.p1 : hp.b1;
+                out.v = hp.rect >= 0 ? hp.p2 : hp.b2;
             } else {
                 out.t = 0.0f;
                 out.primitive = -1;
@@ -493,7 +495,7 @@ cgpu_status ensure_path_buffers(cgpu_ctx* ctx, uint32_t cap, int depth) {
     char* c = static_cast<char*>(block);
     auto take = [&](size_t b) { char* r = c; c += (b + 255) & ~size_t(255); return r; };
     WfBuffers& w = ctx->wf;
-    float4** f4s[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.L, &w.Ls, &w.mis_a, &w.mis_b, &w.mis_d, &w.sh_d, &w.sh_c};
+    float4** f4s[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.L, &w.Le, &w.Ls, &w.mis_a, &w.mis_b, &w.mis_d, &w.sh_d, &w.sh_c};
     for (float4** f : f4s) *f = reinterpret_cast<float4*>(take(P * 16));
     w.meta = reinterpret_cast<uint4*>(take(P * 16));
     for (int k = 0; k < 2; ++k) {
@@ -787,7 +789,7 @@ cgpu_status cg_render_paths_raw(cgpu_ctx* ctx, int scene, int mode, uint32_t fir
         cudaMemcpyAsync(ctx->d_header, ctx->h_header, sizeof(BatchHeader), cudaMemcpyHostToDevice, ctx->stream);
         st = run_batch(ctx, mode, sl.max_depth, k * npix, false, false);
         if (st != CGPU_OK) break;
-        k_gather_paths<<<grid_for(ctx, k_gather_paths, 256, k * npix), 256, 0, ctx->stream>>>(ctx->wf.L, ctx->wf.Ls, k * npix, d_out);
+        k_gather_paths<<<grid_for(ctx, k_gather_paths, 256, k * npix), 256, 0, ctx->stream>>>(ctx->wf.L, ctx->wf.Le, ctx->wf.Ls, k * npix, d_out);
         cudaMemcpyAsync(host_rgb + size_t(done) * npix * 3, d_out, size_t(k) * npix * 3 * sizeof(float),
                         cudaMemcpyDeviceToHost, ctx->stream);
         done += k;

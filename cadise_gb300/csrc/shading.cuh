@@ -52,6 +52,97 @@ struct SurfaceD {
     int prim, material, light;
 };
 
+// The distance the reference reports for the primitive a ray hit: the
+// Moller-Trumbore distance of a triangle (triangle.cpp:54-89, edges swapped
+// to face the ray) or the plane distance of a rectangle (rectangle.cpp:49-75).
+// The traversal's watertight distance `t_wt` decides which primitive is hit;
+// this one places the hit point, so that o + d t is the reference's point to
+// the bit (the next ray starts there: one ulp decides self-shadowing at
+// grazing angles).  Falls back to t_wt where the formula degenerates.
+CG_D float ref_tri_t(float3 o, float3 d, float3 A, float3 B, float3 C, float t_wt) {
+    float3 eAB = B - A, eAC = C - A;
+    if (dot(d, cross(eAB, eAC)) > 0.0f) {
+        const float3 t = eAB;
+        eAB = eAC;
+        eAC = t;
+    }
+    const float3 T = o - A;
+    const float3 Q = cross(T, eAB);
+    const float3 P = cross(d, eAC);
+    const float den = dot(P, eAB);
+    if (den == 0.0f) return t_wt;
+    const float inv = 1.0f / den;
+    const float t = dot(Q, eAC) * inv;
+    return isfinite(t) ? t : t_wt;
+}
+CG_D float ref_rect_t(float3 o, float3 d, float3 vB, float3 eA, float3 eB, float t_wt) {
+    if (dot(d, cross(eA, eB)) > 0.0f) {
+        const float3 t = eA;
+        eA = eB;
+        eB = t;
+    }
+    const float3 n = normalize(cross(eA, eB));
+    const float t = dot(n, vB - o) / dot(n, d);
+    return isfinite(t) ? t : t_wt;
+}
+
+// Hit point, reference distance and surface coordinates of a closest hit:
+// for a triangle the barycentrics of its vertices recomputed from the hit
+// point (Triangle::barycentric, triangle.cpp:233-262); for a rectangle the
+// edge coordinates (p1, p2), both divided by |eA| as rectangle.cpp:122-129
+// does.
+struct HitPoint {
+    float t;
+    float3 P;
+    float b0, b1, b2;  // triangle barycentrics (b1 of B, b2 of C)
+    float p1, p2;      // rectangle coordinates
+    int rect;          // rectangle index, -1 for a triangle
+};
+
+CG_D void rect_frame(const SceneD& S, int rect, float3* vB, float3* eA, float3* eB) {
+    const float* fr = S.rect_frames + 9 * size_t(rect);
+    *vB = mk(fr[0], fr[1], fr[2]);
+    *eA = mk(fr[3], fr[4], fr[5]);
+    *eB = mk(fr[6], fr[7], fr[8]);
+}
+
+CG_D HitPoint hit_point(const SceneD& S, float3 o, float3 d, const HitD& h) {
+    HitPoint hp;
+    const float4* tp = reinterpret_cast<const float4*>(S.tris + h.slot);
+    const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+    const uint32_t flags = __float_as_uint(c.w);
+    if (flags & 1u) {
+        hp.rect = int(flags >> 1);
+        float3 vB, eA, eB;
+        rect_frame(S, hp.rect, &vB, &eA, &eB);
+        hp.t = ref_rect_t(o, d, vB, eA, eB, h.t);
+        hp.P = o + d * hp.t;
+        const float3 onp = hp.P - vB;
+        const float la = len(eA);
+        hp.p1 = dot(onp, normalize(eA)) / la;
+        hp.p2 = dot(onp, normalize(eB)) / la;
+        hp.b0 = hp.b1 = hp.b2 = 0.0f;
+        return hp;
+    }
+    hp.rect = -1;
+    const float3 A = f3(a), B = f3(b), C = f3(c);
+    hp.t = ref_tri_t(o, d, A, B, C, h.t);
+    hp.P = o + d * hp.t;
+    const float3 v0 = B - A, v1 = C - A, v2 = hp.P - A;
+    const float d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1), d20 = dot(v2, v0), d21 = dot(v2, v1);
+    const float den = d00 * d11 - d01 * d01;
+    if (den == 0.0f) {
+        hp.b0 = hp.b1 = hp.b2 = 0.0f;
+    } else {
+        const float inv = 1.0f / den;
+        hp.b1 = (d11 * d20 - d01 * d21) * inv;
+        hp.b2 = (d00 * d21 - d01 * d20) * inv;
+        hp.b0 = 1.0f - hp.b1 - hp.b2;
+    }
+    hp.p1 = hp.p2 = 0.0f;
+    return hp;
+}
+
 // Scene::isIntersecting surface detail (scene.cpp:30-65, triangle.cpp:125-160,
 // rectangle.cpp:102-132).
 CG_D SurfaceD surface_at(const SceneD& S, float3 o, float3 d, const HitD& h) {
@@ -62,25 +153,24 @@ CG_D SurfaceD surface_at(const SceneD& S, float3 o, float3 d, const HitD& h) {
     const uint32_t packed = __float_as_uint(b.w);
     si.material = int(packed & 0xFFFFu);
     si.light = int(packed >> 16) - 1;
-    const uint32_t flags = __float_as_uint(c.w);
-    si.P = o + d * h.t;
+    const HitPoint hp = hit_point(S, o, d, h);
+    si.P = hp.P;
     si.wi = -d;
-    const float b1 = h.u, b2 = h.v, b0 = 1.0f - h.u - h.v;
-    if (flags & 1u) {
-        // half of a rectangle: normal and uvw from the rectangle's own frame
-        const float* fr = S.rect_frames + 9 * size_t(flags >> 1);
-        const float3 vB = mk(fr[0], fr[1], fr[2]), eA = mk(fr[3], fr[4], fr[5]), eB = mk(fr[6], fr[7], fr[8]);
+    if (hp.rect >= 0) {
+        // normal and uvw from the rectangle's own frame; the uvw is the
+        // bilinear blend of the corner uvws (1,0) (0,0) (0,1) (1,1) as the
+        // reference evaluates it, which rounds like this
+        float3 vB, eA, eB;
+        rect_frame(S, hp.rect, &vB, &eA, &eB);
         float3 N = cross(eA, eB);
         N = is_zero(N) ? mk(0.0f, 1.0f, 0.0f) : normalize(N);
         si.Ng = N;
         si.Ns = N;
-        const float3 onp = si.P - vB;
-        const float la = len(eA);
-        const float p1 = dot(onp, normalize(eA)) / la;
-        const float p2 = dot(onp, normalize(eB)) / la;  // rectangle.cpp:125 divides by |eA| too
-        si.uvw = mk(p1, p2, 0.0f);
+        const float p1 = hp.p1, p2 = hp.p2;
+        si.uvw = mk(p1 * ((1.0f - p2) + p2), (1.0f - p1) * p2 + p1 * p2, 0.0f);
         return si;
     }
+    const float b0 = hp.b0, b1 = hp.b1, b2 = hp.b2;
     const float3 A = f3(a), B = f3(b), C = f3(c);
     float3 Ng = cross(B - A, C - A);
     Ng = is_zero(Ng) ? mk(0.0f, 1.0f, 0.0f) : normalize(Ng);

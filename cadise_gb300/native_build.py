@@ -22,9 +22,13 @@ LIB = os.path.join(BUILD, "libcadise_gpu.so")
 CLI = os.path.join(BUILD, "cadise-gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
-              "-Xptxas", "-warn-spills"] + ARCH
-CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-pthread"]
+# No contraction of a * b + c into one fused multiply-add: every kernel then
+# rounds each product and sum the way the reference's FP32 code does, and the
+# same inlined function rounds identically in every kernel it lands in (the
+# wavefront and the megakernel agree path for path).
+NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "-Xcompiler",
+              "-ffp-contract=off", "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"] + ARCH
+CXX_FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-pthread"]
 
 
 def _nvcc() -> str:

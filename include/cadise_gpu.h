@@ -173,7 +173,8 @@ cgpu_status cgpu_scene_info_get(cgpu_ctx* ctx, int32_t scene, cgpu_scene_info* o
 
 /* ------------------------------------------------------------ ray queries -- */
 
-/* 32-byte ray: origin, t_min, direction (normalised), t_max. */
+/* 32-byte ray: origin, t_min, direction, t_max.  The direction is
+ * normalised by the call, as the reference's Ray constructor does. */
 typedef struct cgpu_ray {
     float org[3];
     float t_min;
@@ -181,7 +182,11 @@ typedef struct cgpu_ray {
     float t_max;
 } cgpu_ray;
 
-/* Closest hit: primitive = -1 on a miss; u, v barycentrics of vB and vC. */
+/* Closest hit: primitive = -1 on a miss.  t is the distance the reference
+ * reports for that primitive (Moller-Trumbore for a triangle, the plane
+ * distance for a rectangle); u, v are the barycentrics of vB and vC of a
+ * triangle, recomputed from the hit point, or a rectangle's edge
+ * coordinates (both divided by |eA|). */
 typedef struct cgpu_hit {
     float t;
     int32_t primitive;

@@ -36,7 +36,7 @@ def build_port(force: bool = False) -> str:
         return PORT_SO
     os.makedirs(BUILD, exist_ok=True)
     tmp = PORT_SO + ".tmp%d" % os.getpid()
-    subprocess.check_call(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-pthread",
+    subprocess.check_call(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
                            src, "-o", tmp])
     os.replace(tmp, PORT_SO)
     return PORT_SO

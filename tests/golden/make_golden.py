@@ -49,7 +49,7 @@ def golden_scenes():
         "field": (scenes.icosphere_field(n_spheres=10, subdivision=2, n_lights=3, seed=3, width=48,
                                          height=36, spp=16, max_depth=8, dielectric=scenes.GLASS,
                                          box=30.0, radius_range=(2.0, 6.0)), 2048),
-        "features": (scenes.feature_scene(), 2048),
+        "features": (scenes.feature_scene(), 32768),
     }
 
 

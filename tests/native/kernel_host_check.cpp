@@ -1,20 +1,32 @@
 // CPU execution of the CUDA library's device code for testing (test
 // infrastructure, never part of the library): the traversal
 // (traverse.cuh), the per-path estimator (pathtrace.cuh / shading.cuh) and
+// the per-path adjoint (adjoint.cuh) and
 // the scene construction (scene_build.cpp, bvh_build.cpp) compiled as plain
 // host C++, so their logic is checked against the golden vectors before any
 // GPU time is spent.
-#include "../../cadise_gb300/csrc/pathtrace.cuh"
+#include "../../cadise_gb300/csrc/adjoint.cuh"
 #include "../../cadise_gb300/csrc/scene_build.h"
 
 #include <cstdio>
 #include <memory>
 #include <string>
+#include <vector>
 
 namespace {
 struct Check {
     cg::HostScene hs;
     cg::SceneD S;
+};
+
+struct HostSink {
+    double* g_rough;
+    double* g_rad;
+    double* g_tex;
+    const std::vector<int>& tex_offset;
+    void rough(int m, double v) { g_rough[m] += v; }
+    void rad(int i, double v) { g_rad[i] += v; }
+    void tex(int t, int k, double v) { g_tex[tex_offset[size_t(t)] + k] += v; }
 };
 }  // namespace
 
@@ -39,7 +51,7 @@ void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, f
     const Check& c = *static_cast<Check*>(p);
     for (uint32_t i = 0; i < n; ++i) {
         const float* r = rays + 8 * size_t(i);
-        const cg::RayPre pr = cg::ray_prep(cg::mk(r[0], r[1], r[2]), cg::mk(r[4], r[5], r[6]), r[3], r[7]);
+        const cg::RayPre pr = cg::ray_prep(cg::mk(r[0], r[1], r[2]), cg::normalize(cg::mk(r[4], r[5], r[6])), r[3], r[7]);
         cg::TraceCounters tc{0, 0};
         cg::HitD h;
         bool hit, any;
@@ -61,9 +73,11 @@ void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, f
             any = cg::traverse<true, false>(c.S, pr, &h2, &tc);
         }
         prim[i] = hit ? __float_as_int(c.S.tris[h.slot].v0.w) : -1;
-        t[i] = hit ? h.t : 0.0f;
-        u[i] = hit ? h.u : 0.0f;
-        v[i] = hit ? h.v : 0.0f;
+        cg::HitPoint hp{};
+        if (hit) hp = cg::hit_point(c.S, pr.o, pr.d, h);
+        t[i] = hit ? hp.t : 0.0f;
+        u[i] = hit ? (hp.rect >= 0 ? hp.p1 : hp.b1) : 0.0f;
+        v[i] = hit ? (hp.rect >= 0 ? hp.p2 : hp.b2) : 0.0f;
         occ[i] = any ? 1 : 0;
     }
 }
@@ -76,13 +90,14 @@ void khc_paths(void* p, const double* xy, const uint64_t* keys, uint32_t n, floa
         rng.ctr = 0;
         float3 o, d;
         cg::camera_ray(c.S.cam, float(xy[2 * i]), float(xy[2 * i + 1]), &o, &d);
-        float3 L, Ls;
+        float3 L, Le, Ls;
         cg::TraceCounters tc{0, 0}, ta{0, 0};
         uint32_t nc = 0, na = 0;
-        cg::mk_path<false>(c.S, o, d, rng, &L, &Ls, &tc, &ta, &nc, &na);
-        rgb[3 * i + 0] = L.x + Ls.x;
-        rgb[3 * i + 1] = L.y + Ls.y;
-        rgb[3 * i + 2] = L.z + Ls.z;
+        cg::mk_path<false>(c.S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
+        const float3 v = cg::path_sample(L, Le, Ls);
+        rgb[3 * i + 0] = v.x;
+        rgb[3 * i + 1] = v.y;
+        rgb[3 * i + 2] = v.z;
     }
 }
 
@@ -100,14 +115,43 @@ void khc_render_paths(void* p, uint64_t seed, uint32_t scene_index, uint32_t fir
             cg::Rng rng;
             float3 o, d;
             cg::primary_ray(c.S, id, seed, rng, &o, &d);
-            float3 L, Ls;
+            float3 L, Le, Ls;
             cg::TraceCounters tc{0, 0}, ta{0, 0};
             uint32_t nc = 0, na = 0;
-            cg::mk_path<false>(c.S, o, d, rng, &L, &Ls, &tc, &ta, &nc, &na);
+            cg::mk_path<false>(c.S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
+            const float3 v = cg::path_sample(L, Le, Ls);
             float* q = out + 3 * (size_t(k) * npix + px);
-            q[0] = L.x + Ls.x;
-            q[1] = L.y + Ls.y;
-            q[2] = L.z + Ls.z;
+            q[0] = v.x;
+            q[1] = v.y;
+            q[2] = v.z;
+        }
+}
+
+// Gradients of sum(dLdI * image) over samples [0, spp) of every pixel, as
+// cgpu_adjoint_backward: texel floats (all textures back to back),
+// roughness per material, radiance per area light and channel.
+void khc_adjoint(void* p, uint64_t seed, uint32_t scene_index, uint32_t spp, const float* dLdI, double* g_tex,
+                 double* g_rough, double* g_rad) {
+    const Check& c = *static_cast<Check*>(p);
+    std::vector<int> off;
+    int acc = 0;
+    for (const cg::TextureD& t : c.hs.textures) {
+        off.push_back(acc);
+        acc += t.width * t.height * 3;
+    }
+    HostSink sink{g_rough, g_rad, g_tex, off};
+    const uint32_t npix = uint32_t(c.S.width) * uint32_t(c.S.height);
+    const float inv_spp = 1.0f / float(spp);
+    for (uint32_t k = 0; k < spp; ++k)
+        for (uint32_t px = 0; px < npix; ++px) {
+            const float3 delta = cg::mk(dLdI[3 * px] * inv_spp, dLdI[3 * px + 1] * inv_spp, dLdI[3 * px + 2] * inv_spp);
+            if (cg::is_zero(delta)) continue;
+            cg::PathId id;
+            id.scene = int(scene_index);
+            id.pixel = px;
+            id.sample = k;
+            id.width = uint32_t(c.S.width);
+            cg::adjoint_path(c.S, id, seed, delta, c.hs.num_area_lights, sink);
         }
 }
 

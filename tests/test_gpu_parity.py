@@ -7,12 +7,13 @@ Tolerances (FP32 path tracer):
     point lies within 1e-5 (relative barycentric / edge coordinate) of a
     primitive edge, where the reference's non-watertight test and the
     watertight one may legitimately disagree, and equal-t ties (another
-    primitive at the same distance, e.g. coplanar faces);
-    |dt| <= 1e-5 t + 1e-6 (1 + |origin|_inf);
-  * per-path radiance: the GPU evaluates transcendental functions and
-    contracted products differently from the host, so a path may branch
-    differently after a near-tie; >= 97 % of paths within 1e-3 relative
-    (+1e-5 absolute) and the mean over all paths within 1 %;
+    primitive at the same distance, e.g. coplanar faces); where the
+    primitive agrees, t is the reference's to the bit (the kernels compute
+    it with the reference's own formula and no contracted multiply-adds);
+  * per-path radiance: the GPU evaluates transcendental functions
+    differently from the host, so a path may branch differently after a
+    near-tie; >= 99 % of paths within 1e-3 relative (+1e-5 absolute) and the
+    mean over all paths within 1 %;
   * images: relMSE <= 1e-3 against the converged reference render and a
     per-pixel Welch z-test failure fraction <= 1 % + 3 sigma (p = 0.01);
   * wavefront vs megakernel: bit-identical per path.
@@ -94,10 +95,8 @@ def test_closest_hits_match_reference(name, gpu_ctx, uploaded):
     keep = ~(near | tie)
     assert np.mean(keep) > 0.98
     assert np.array_equal(prim[keep], ref_p[keep]), np.where(prim[keep] != ref_p[keep])
-    both = keep & (prim >= 0)
-    # 1e-5 relative, plus the FP32 resolution of the ray origin for hits at tiny t
-    tol = 1e-5 * np.abs(ref_t) + 1e-6 * (1.0 + np.abs(rays[:, :3]).max(1))
-    assert np.all(np.abs(t - ref_t)[both] <= tol[both])
+    both = (prim == ref_p) & (prim >= 0)
+    assert np.array_equal(t[both], ref_t[both]), np.abs(t - ref_t)[both].max()
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -124,7 +123,7 @@ def test_path_radiance_matches_reference(name, gpu_ctx, uploaded):
     rgb = gpu_ctx.path_radiance(sid, v["paths_xy"], v["paths_keys"])
     ref = v["paths_rgb"]
     close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
-    assert close.mean() >= 0.97, close.mean()
+    assert close.mean() >= 0.99, close.mean()
     assert abs(rgb.mean() - ref.mean()) <= 0.01 * abs(ref.mean()) + 1e-6
 
 
@@ -143,7 +142,7 @@ def test_render_paths_match_oracle(name, gpu_ctx, uploaded):
     ps = oracle.PortScene(flat)
     _, port = ps.render(seed=11, first=3, count=2, threads=8, want_paths=True, scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.97, close.mean()
+    assert close.mean() >= 0.99, close.mean()
 
 
 def test_film_equals_sum_of_paths(gpu_ctx, uploaded):
@@ -179,7 +178,7 @@ def rel_mse(x, ref):
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("field", 8192), ("features", 8192)])
+@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("field", 8192), ("features", 32768)])
 def test_image_converges_to_reference(name, spp, gpu_ctx, uploaded):
     spec, flat, sid = uploaded[name]
     ref = image(name)
@@ -244,7 +243,7 @@ def test_rough_dielectric_paths_match_oracle(gpu_ctx):
     _, port = oracle.PortScene(flat).render(seed=3, first=0, count=4, threads=8, want_paths=True,
                                             scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.97, close.mean()
+    assert close.mean() >= 0.99, close.mean()
     gpu_ctx.release(sid)
 
 
@@ -283,7 +282,7 @@ def test_environment_paths_match_oracle(gpu_ctx):
     assert np.array_equal(gpu, mk)
     _, port = oracle.PortScene(flat).render(seed=9, first=0, count=4, threads=8, want_paths=True, scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.97, close.mean()
+    assert close.mean() >= 0.99, close.mean()
     gpu_ctx.release(sid)
 
 

@@ -1,9 +1,10 @@
 """The CUDA library's device code, compiled as host C++ (tests/native/), run on
 the CPU against the reference's golden vectors and the oracle: traversal
 (both the per-ray loop and the resumable stepper of the persistent kernels),
-the per-path estimator, scene construction.  Catches logic errors - wrong
+the per-path estimator, the per-path adjoint, scene construction.  Catches logic errors - wrong
 hits, endless loops, wrong random-number order - before GPU time is spent.
-Same tolerances as the GPU parity tests."""
+Same tolerances as the GPU parity tests.  The host build does not contract
+multiply-adds either (-ffp-contract=off), like the kernels (-fmad=false)."""
 import ctypes as C
 import os
 import subprocess
@@ -35,7 +36,7 @@ def khc():
                    if f.endswith((".cuh", ".h"))]
     if not os.path.exists(LIB) or any(os.path.getmtime(d) > os.path.getmtime(LIB) for d in deps):
         os.makedirs(BUILD, exist_ok=True)
-        subprocess.check_call(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread",
+        subprocess.check_call(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-pthread",
                                "-I", os.path.join(ROOT, "include"), "-I", _cuda_include()] + SRCS + ["-o", LIB])
     L = C.CDLL(LIB)
     L.khc_create.restype = C.c_void_p
@@ -44,6 +45,7 @@ def khc():
     L.khc_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int] + [C.c_void_p] * 5
     L.khc_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
     L.khc_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
+    L.khc_adjoint.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
     return L
 
 
@@ -106,10 +108,8 @@ def test_kernel_traversal_matches_reference_hits(khc, name):
     keep = ~(near | tie | (ref_p != v["trace_bf_prim"]))
     assert keep.mean() > 0.98
     assert np.array_equal(prim[keep], ref_p[keep])
-    both = keep & (prim >= 0)
-    # 1e-5 relative, plus the FP32 resolution of the ray origin for hits at tiny t
-    tol = 1e-5 * np.abs(ref_t) + 1e-6 * (1.0 + np.abs(rays[:, :3]).max(1))
-    assert np.all(np.abs(t - ref_t)[both] <= tol[both])
+    both = (prim == ref_p) & (prim >= 0)
+    assert np.array_equal(t[both], ref_t[both])  # the reference's own distance formula
     # the resumable stepper of the persistent kernels takes the same decisions
     p2, t2, occ2 = h.trace(rays, dyn=1)
     assert np.array_equal(p2, prim) and np.array_equal(t2, t) and np.array_equal(occ2, occ)
@@ -123,7 +123,7 @@ def test_kernel_paths_match_reference(khc, name):
     rgb = h.paths(v["paths_xy"], v["paths_keys"])
     ref = v["paths_rgb"]
     close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
-    assert close.mean() >= 0.97, close.mean()
+    assert close.mean() >= 0.99, close.mean()
     h.close()
 
 
@@ -134,7 +134,7 @@ def test_kernel_render_paths_match_oracle(khc, name):
     got = h.render_paths(11, 3, 2)
     _, port = oracle.PortScene(flat).render(seed=11, first=3, count=2, threads=8, want_paths=True)
     close = np.all(np.abs(got - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.97, close.mean()
+    assert close.mean() >= 0.99, close.mean()
     h.close()
 
 
@@ -149,5 +149,28 @@ def test_kernel_rough_dielectric_and_sky_match_oracle(khc):
         got = h.render_paths(3, 0, 4)
         _, port = oracle.PortScene(flat).render(seed=3, first=0, count=4, threads=8, want_paths=True)
         close = np.all(np.abs(got - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-        assert close.mean() >= 0.97, close.mean()
+        assert close.mean() >= 0.99, close.mean()
         h.close()
+
+
+def test_kernel_adjoint_matches_fp64_reference(khc):
+    """The adjoint's per-path replay (the kernel's own code, run on the CPU)
+    against the oracle's FP64 forward-mode gradient of the same detached
+    estimator: texels, GGX roughness and emitter radiance."""
+    spec = scenes.diff_scene(width=32, height=32, spp=16, max_depth=3, n_spheres=10, subdivision=2,
+                             tex_size=16, n_conductors=3, n_lights=2, seed=5)
+    flat = abi.flatten(spec)
+    h = Host(khc, flat)
+    W = np.random.default_rng(5).normal(size=(spec.height, spec.width, 3)).astype(np.float32)
+    spp, seed, scene_index = 16, 23, 1
+    gt, gr, gl = np.zeros(16 * 16 * 3), np.zeros(len(spec.materials)), np.zeros((2, 3))
+    khc.khc_adjoint(h.h, seed, scene_index, spp, _p(W), _p(gt), _p(gr), _p(gl))
+    h.close()
+    metals = [i for i, m in enumerate(spec.materials) if m.type == scenes.CONDUCTOR]
+    top = list(np.argsort(-np.abs(gt))[:6])
+    params = [(0, int(i), 0) for i in top] + [(1, i, 0) for i in metals] + [(2, 0, c) for c in range(3)] + \
+             [(2, 1, c) for c in range(3)]
+    ref = oracle.PortScene(flat).adjoint_fp64(seed, spp, W, params, scene_index=scene_index)
+    got = np.concatenate([gt[top], gr[metals], gl[0], gl[1]])
+    assert np.all(ref[:6] != 0) and np.all(ref[6:9] != 0)
+    assert np.all(np.abs(got - ref) <= 1e-3 * np.abs(ref) + 1e-4 * np.abs(ref).max()), np.stack([got, ref])
