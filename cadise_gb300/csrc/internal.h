@@ -61,6 +61,32 @@ struct WfBuffers {
     int cnt_depth;    // bounces the counter array covers
 };
 
+// Lays the path state of `cap` paths and the counters of `cnt_rows` bounces
+// out from `base` (256-byte aligned arrays) and returns the bytes used.  With
+// base == nullptr it only measures: the allocation is sized by the same walk
+// that carves it.
+inline size_t wf_layout(char* base, size_t cap, int cnt_rows, WfBuffers* w) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* r = base ? base + off : nullptr;
+        off += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    float4** f4s[] = {&w->ray_o, &w->ray_d, &w->hit, &w->thr, &w->L, &w->Le, &w->Ls,
+                      &w->mis_a, &w->mis_b, &w->mis_d, &w->sh_d, &w->sh_c};
+    for (float4** f : f4s) *f = reinterpret_cast<float4*>(take(cap * sizeof(float4)));
+    w->meta = reinterpret_cast<uint4*>(take(cap * sizeof(uint4)));
+    for (int k = 0; k < 2; ++k) {
+        w->q_cont[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+        w->q_mis[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+        w->q_shadow[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+    }
+    for (int k = 0; k < kNumBsdfKinds; ++k) w->q_mat[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+    w->cnt = reinterpret_cast<int*>(take(size_t(cnt_rows) * kCntStride * sizeof(int)));
+    w->cnt_depth = cnt_rows;
+    return off;
+}
+
 struct RenderArgs {
     const SceneD* scenes;
     const Chunk* chunks;

@@ -484,28 +484,13 @@ uint32_t paths_capacity(cgpu_ctx* ctx, uint32_t max_npix) {
 cgpu_status ensure_path_buffers(cgpu_ctx* ctx, uint32_t cap, int depth) {
     if (ctx->path_cap >= cap && ctx->wf.cnt_depth >= depth + 2) return CGPU_OK;
     cg_free_render_state(ctx);
-    const size_t P = cap;
-    const size_t n_f4 = 11, n_u4 = 1;
-    const size_t q_ints = 2 * 3 + kNumBsdfKinds;
     const int cdepth = std::max(depth + 2, 34);
-    size_t bytes = P * 16 * (n_f4 + n_u4) + P * 4 * q_ints + size_t(cdepth) * kCntStride * 4 + 1024;
+    WfBuffers w{};
+    const size_t bytes = wf_layout(nullptr, cap, cdepth, &w);
     void* block = nullptr;
     cudaError_t e = cudaMalloc(&block, bytes);
     if (e != cudaSuccess) return cg_fail(ctx, CGPU_ERR_OUT_OF_MEMORY, "path buffers: " + std::string(cudaGetErrorString(e)));
-    char* c = static_cast<char*>(block);
-    auto take = [&](size_t b) { char* r = c; c += (b + 255) & ~size_t(255); return r; };
-    WfBuffers& w = ctx->wf;
-    float4** f4s[] = {&w.ray_o, &w.ray_d, &w.hit, &w.thr, &w.L, &w.Le, &w.Ls, &w.mis_a, &w.mis_b, &w.mis_d, &w.sh_d, &w.sh_c};
-    for (float4** f : f4s) *f = reinterpret_cast<float4*>(take(P * 16));
-    w.meta = reinterpret_cast<uint4*>(take(P * 16));
-    for (int k = 0; k < 2; ++k) {
-        w.q_cont[k] = reinterpret_cast<int*>(take(P * 4));
-        w.q_mis[k] = reinterpret_cast<int*>(take(P * 4));
-        w.q_shadow[k] = reinterpret_cast<int*>(take(P * 4));
-    }
-    for (int k = 0; k < kNumBsdfKinds; ++k) w.q_mat[k] = reinterpret_cast<int*>(take(P * 4));
-    w.cnt = reinterpret_cast<int*>(take(size_t(cdepth) * kCntStride * 4));
-    w.cnt_depth = cdepth;
+    wf_layout(static_cast<char*>(block), cap, cdepth, &ctx->wf);
     ctx->wf_block = block;
     ctx->path_cap = cap;
     if (!ctx->d_counters) {

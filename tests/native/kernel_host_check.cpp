@@ -155,4 +155,35 @@ void khc_adjoint(void* p, uint64_t seed, uint32_t scene_index, uint32_t spp, con
         }
 }
 
+// The path-state layout of the wavefront (wf_layout) for `cap` paths and
+// `rows` counter rows: 0 when every array lies inside the measured size,
+// 256-byte aligned and disjoint from the others, else the failing array + 1.
+int khc_wf_layout_check(uint64_t cap, int rows) {
+    cg::WfBuffers w{};
+    const size_t total = cg::wf_layout(nullptr, size_t(cap), rows, &w);
+    char* base = reinterpret_cast<char*>(size_t(1) << 40);  // carve from a fake, aligned base; nothing is touched
+    cg::wf_layout(base, size_t(cap), rows, &w);
+    struct Span { const void* p; size_t bytes; };
+    std::vector<Span> v;
+    const float4* f4s[] = {w.ray_o, w.ray_d, w.hit, w.thr, w.L, w.Le, w.Ls, w.mis_a, w.mis_b, w.mis_d, w.sh_d, w.sh_c};
+    for (const float4* f : f4s) v.push_back({f, size_t(cap) * 16});
+    v.push_back({w.meta, size_t(cap) * 16});
+    for (int k = 0; k < 2; ++k) {
+        v.push_back({w.q_cont[k], size_t(cap) * 4});
+        v.push_back({w.q_mis[k], size_t(cap) * 4});
+        v.push_back({w.q_shadow[k], size_t(cap) * 4});
+    }
+    for (int k = 0; k < cg::kNumBsdfKinds; ++k) v.push_back({w.q_mat[k], size_t(cap) * 4});
+    v.push_back({w.cnt, size_t(rows) * cg::kCntStride * 4});
+    for (size_t i = 0; i < v.size(); ++i) {
+        const size_t a = size_t(static_cast<const char*>(v[i].p) - base);
+        if (a % 256 != 0 || a + v[i].bytes > total) return int(i) + 1;
+        for (size_t j = 0; j < i; ++j) {
+            const size_t b = size_t(static_cast<const char*>(v[j].p) - base);
+            if (a < b + v[j].bytes && b < a + v[i].bytes) return int(i) + 1;
+        }
+    }
+    return w.cnt_depth == rows ? 0 : -1;
+}
+
 }  // extern "C"

@@ -46,6 +46,7 @@ def khc():
     L.khc_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
     L.khc_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
     L.khc_adjoint.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
+    L.khc_wf_layout_check.argtypes = [C.c_uint64, C.c_int]
     return L
 
 
@@ -174,3 +175,11 @@ def test_kernel_adjoint_matches_fp64_reference(khc):
     got = np.concatenate([gt[top], gr[metals], gl[0], gl[1]])
     assert np.all(ref[:6] != 0) and np.all(ref[6:9] != 0)
     assert np.all(np.abs(got - ref) <= 1e-3 * np.abs(ref) + 1e-4 * np.abs(ref).max()), np.stack([got, ref])
+
+
+@pytest.mark.parametrize("cap", [1, 63, 20000, 1 << 14, 2073600, (1 << 21) + 5])
+def test_wavefront_buffer_layout_fits(khc, cap):
+    """The path-state arrays of the wavefront stay inside the block they are
+    carved from, for capacities that are not multiples of the alignment."""
+    for rows in (3, 34, 66):
+        assert khc.khc_wf_layout_check(cap, rows) == 0
