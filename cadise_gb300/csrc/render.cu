@@ -551,7 +551,9 @@ void collect_profile(cgpu_ctx* ctx) {
 // Enqueue the wavefront schedule for one batch on ctx->stream.
 cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool splat, bool counting) {
     RenderArgs a = make_args(ctx);
-    cudaStream_t s = ctx->stream, side = ctx->side;
+    // With per-kernel timing on, the shadow pass runs after the extend pass on
+    // the same stream, so that each event pair brackets one kernel alone.
+    cudaStream_t s = ctx->stream, side = ctx->profiling ? ctx->stream : ctx->side;
     cudaEvent_t fork = nullptr, join = nullptr;
     cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
     cudaEventCreateWithFlags(&join, cudaEventDisableTiming);

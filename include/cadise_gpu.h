@@ -292,7 +292,9 @@ cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, ui
                                   double* grad_radiance);
 
 /* Per-kernel CUDA-event timing of the following renders (launches are made
- * one by one instead of through the captured graph while it is on). */
+ * one by one instead of through the captured graph while it is on, and the
+ * shadow pass runs after the extend pass instead of beside it, so that each
+ * kernel is timed alone). */
 enum {
     CGPU_KERNEL_GENERATE = 0,
     CGPU_KERNEL_EXTEND = 1,     /* closest-hit traversal (continuation + MIS rays) */
