@@ -27,7 +27,7 @@ EXPORTED = [
     "cgpu_create", "cgpu_destroy", "cgpu_last_error", "cgpu_status_string", "cgpu_abi_version",
     "cgpu_synchronize", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
     "cgpu_trace_closest", "cgpu_trace_any", "cgpu_trace_closest_device", "cgpu_trace_any_device",
-    "cgpu_camera_rays", "cgpu_render", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
+    "cgpu_camera_rays", "cgpu_render", "cgpu_render_noalloc", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
     "cgpu_kernel_times_get", "cgpu_param_counts_get", "cgpu_params_get", "cgpu_params_set",
     "cgpu_adjoint_forward", "cgpu_adjoint_backward", "cgpu_tuning_get", "cgpu_tuning_set", "cgpu_autotune",
@@ -81,6 +81,7 @@ def load(path: Optional[str] = None):
     L.cgpu_trace_any_device.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
     L.cgpu_camera_rays.argtypes = [vp, C.c_int32, vp, C.c_uint32, vp]
     L.cgpu_render.argtypes = [vp, C.POINTER(cgpu_render_params)]
+    L.cgpu_render_noalloc.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint32, C.c_uint64]
     L.cgpu_film_clear.argtypes = [vp, C.c_int32]
     L.cgpu_film_read.argtypes = [vp, C.c_int32, vp, vp, vp]
     L.cgpu_path_radiance.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, C.c_uint32, vp]
@@ -211,6 +212,14 @@ class Context:
         p = cgpu_render_params(scenes=arr, num_scenes=len(sids), first_sample=first, num_samples=count,
                                seed=seed, mode=mode, use_graph=1 if graph else 0)
         self._check(self.L.cgpu_render(self.h, C.byref(p)))
+        if sync:
+            self.synchronize()
+
+    def render_noalloc(self, sid: int, first: int, count: int, seed: int, sync: bool = True):
+        """cgpu_render_noalloc: the wavefront render with every device buffer
+        of the call in the library's static scratch (frames up to 262144
+        pixels, max depth 62, scene ids below 64)."""
+        self._check(self.L.cgpu_render_noalloc(self.h, sid, first, count, seed))
         if sync:
             self.synchronize()
 

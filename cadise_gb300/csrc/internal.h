@@ -87,6 +87,40 @@ inline size_t wf_layout(char* base, size_t cap, int cnt_rows, WfBuffers* w) {
     return off;
 }
 
+// Static scratch of cgpu_render_noalloc: every device buffer of that call
+// lives in one file-scope array of kNoAllocScratchBytes, laid out by
+// noalloc_layout.  Limits: a frame of at most kNoAllocMaxPaths pixels (one
+// path per pixel per batch), max_depth <= kNoAllocMaxDepth, scene ids below
+// kNoAllocMaxScenes (the scene and film tables are indexed by scene id).
+constexpr uint32_t kNoAllocMaxPaths = 1u << 18;
+constexpr int kNoAllocMaxDepth = 62;
+constexpr int kNoAllocMaxScenes = 64;
+constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+
+struct NoAllocView {
+    BatchHeader* header;
+    Chunk* chunk;
+    SceneD* scenes;               // kNoAllocMaxScenes entries
+    FilmD* films;                 // kNoAllocMaxScenes entries
+    unsigned long long* counters; // 8
+    WfBuffers wf;                 // kNoAllocMaxPaths paths, kNoAllocMaxDepth + 2 counter rows
+};
+
+inline size_t noalloc_layout(char* base, NoAllocView* v) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* r = base ? base + off : nullptr;
+        off += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    v->header = reinterpret_cast<BatchHeader*>(take(sizeof(BatchHeader)));
+    v->chunk = reinterpret_cast<Chunk*>(take(sizeof(Chunk)));
+    v->scenes = reinterpret_cast<SceneD*>(take(sizeof(SceneD) * kNoAllocMaxScenes));
+    v->films = reinterpret_cast<FilmD*>(take(sizeof(FilmD) * kNoAllocMaxScenes));
+    v->counters = reinterpret_cast<unsigned long long*>(take(8 * sizeof(unsigned long long)));
+    return off + wf_layout(base ? base + off : nullptr, kNoAllocMaxPaths, kNoAllocMaxDepth + 2, &v->wf);
+}
+
 struct RenderArgs {
     const SceneD* scenes;
     const Chunk* chunks;

@@ -18,6 +18,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 
 namespace cg {
 
@@ -838,4 +840,138 @@ cgpu_status cg_film_clear(cgpu_ctx* ctx, int scene) {
     cudaMemsetAsync(sl.film.sumsq, 0, npix * 3 * sizeof(double), ctx->stream);
     cudaMemsetAsync(sl.film.count, 0, npix * sizeof(double), ctx->stream);
     return cg_cuda(ctx, cudaGetLastError(), "film clear");
+}
+
+// =========================================================== no-alloc render ==
+// cgpu_render_noalloc: the wavefront render of one scene with every device
+// buffer the call needs in a static array of this library, so that the call
+// itself allocates nothing.  Same kernels as cgpu_render; the batch tables are
+// written by a one-block setup kernel (arguments by value, no copies), the
+// traversal passes run one after the other on the context stream (no side
+// stream, no events, no graph).
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+namespace cg {
+
+// Writes the batch tables and zeroes the queue counters of one batch.
+__global__ void k_noalloc_setup(NoAllocView v, BatchHeader h, Chunk c, SceneD sd, FilmD fd, int scene, int cnt_ints) {
+    for (int i = threadIdx.x; i < cnt_ints; i += blockDim.x) v.wf.cnt[i] = 0;
+    if (threadIdx.x == 0) {
+        *v.header = h;
+        *v.chunk = c;
+        v.scenes[scene] = sd;
+        v.films[scene] = fd;
+    }
+}
+
+}  // namespace cg
+
+namespace {
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+char* g_noalloc_base[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch, looked up once per device (the caller has
+// made ctx->device current).
+cgpu_status noalloc_base(cgpu_ctx* ctx, char** out) {
+    if (ctx->device < 0 || ctx->device >= kNoAllocMaxDevices)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render_noalloc: device index out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    char*& p = g_noalloc_base[ctx->device];
+    if (!p) {
+        void* a = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&a, g_noalloc_scratch);
+        if (e != cudaSuccess) return cg_cuda(ctx, e, "render_noalloc: scratch address");
+        p = static_cast<char*>(a);
+    }
+    *out = p;
+    return CGPU_OK;
+}
+
+void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_t paths, uint32_t npix) {
+    cudaStream_t s = ctx->stream;
+    const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
+    const bool dyn = ctx->tuning.traversal == 1;
+    auto ext = dyn ? k_wf_extend_dyn<false> : k_wf_extend<false>;
+    auto sh = dyn ? k_wf_shadow_dyn<false> : k_wf_shadow<false>;
+    k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
+    const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, sh, bt, paths);
+    const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
+                                    grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
+                                    grid_for(ctx, k_wf_shade<4>, bs, paths)};
+    for (int b = 0; b <= depth; ++b) {
+        ext<<<gext, bt, 0, s>>>(a, b);
+        sh<<<gsh, bt, 0, s>>>(a, b);
+        if (b == depth) break;
+        k_wf_shade<0><<<gsd[0], bs, 0, s>>>(a, b);
+        k_wf_shade<1><<<gsd[1], bs, 0, s>>>(a, b);
+        k_wf_shade<2><<<gsd[2], bs, 0, s>>>(a, b);
+        k_wf_shade<3><<<gsd[3], bs, 0, s>>>(a, b);
+        k_wf_shade<4><<<gsd[4], bs, 0, s>>>(a, b);
+    }
+    k_splat<<<grid_for(ctx, k_splat, 256, npix), 256, 0, s>>>(a);
+    ctx->stats.kernel_launches += uint32_t(3 + 2 * (depth + 1) + kNumBsdfKinds * depth);
+}
+
+}  // namespace
+
+extern "C" cgpu_status cgpu_render_noalloc(cgpu_ctx* ctx, int32_t scene, uint32_t first_sample, uint32_t num_samples,
+                                           uint64_t seed) {
+    if (!ctx) return CGPU_ERR_INVALID_ARGUMENT;
+    if (scene < 0 || scene >= int32_t(ctx->scenes.size()) || !ctx->scenes[size_t(scene)].live)
+        return cg_fail(ctx, CGPU_ERR_NOT_FOUND, "render_noalloc: unknown scene id");
+    const SceneSlot& sl = ctx->scenes[size_t(scene)];
+    const uint64_t npix = uint64_t(sl.width) * uint64_t(sl.height);
+    if (scene >= kNoAllocMaxScenes)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render_noalloc: scene id " + std::to_string(scene) +
+                                                           " is not below the static scratch's " +
+                                                           std::to_string(kNoAllocMaxScenes) + " scene slots");
+    if (npix > kNoAllocMaxPaths)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render_noalloc: " + std::to_string(sl.width) + " x " +
+                                                           std::to_string(sl.height) + " pixels exceed the " +
+                                                           std::to_string(kNoAllocMaxPaths) +
+                                                           " paths of the static scratch");
+    if (sl.max_depth > kNoAllocMaxDepth)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render_noalloc: max depth " + std::to_string(sl.max_depth) +
+                                                           " exceeds " + std::to_string(kNoAllocMaxDepth));
+    if (uint64_t(first_sample) + num_samples > 0xFFFFFFFFull)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render_noalloc: sample range overflows 32 bits");
+    if (num_samples == 0) return CGPU_OK;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return cg_cuda(ctx, e, "render_noalloc: set device");
+    char* base = nullptr;
+    cgpu_status st = noalloc_base(ctx, &base);
+    if (st != CGPU_OK) return st;
+    NoAllocView v;
+    if (noalloc_layout(base, &v) > kNoAllocScratchBytes)
+        return cg_fail(ctx, CGPU_ERR_UNSUPPORTED, "render_noalloc: scratch layout exceeds the static array");
+    RenderArgs a;
+    a.scenes = v.scenes;
+    a.chunks = v.chunk;
+    a.header = v.header;
+    a.films = v.films;
+    a.wf = v.wf;
+    a.counters = v.counters;
+    const uint32_t n = uint32_t(npix);
+    const uint32_t per = kNoAllocMaxPaths / n;  // samples per batch
+    const int depth = sl.max_depth;
+    ctx->stats = cgpu_render_stats{};
+    for (uint32_t done = 0; done < num_samples;) {
+        const uint32_t k = std::min(per, num_samples - done);
+        BatchHeader h;
+        h.num_chunks = 1;
+        h.total_paths = k * n;
+        h.total_pixels = n;
+        h.max_depth = depth;
+        h.seed = seed;
+        const Chunk c{scene, 0, n, uint32_t(sl.width), first_sample + done, k, 0, 0};
+        k_noalloc_setup<<<1, 256, 0, ctx->stream>>>(v, h, c, sl.d, sl.film, scene, (depth + 2) * kCntStride);
+        enqueue_wavefront_serial(ctx, a, depth, k * n, n);
+        ctx->stats.batches += 1;
+        ctx->stats.paths += uint64_t(k) * n;
+        done += k;
+    }
+    return cg_cuda(ctx, cudaGetLastError(), "render_noalloc launch");
 }

@@ -224,6 +224,29 @@ cgpu_status cgpu_film_clear(cgpu_ctx* ctx, int32_t scene);
 /* Film read-back: each pointer may be NULL; sizes width*height*3 / *3 / *1 doubles. */
 cgpu_status cgpu_film_read(cgpu_ctx* ctx, int32_t scene, double* sum_rgb, double* sum_sq_rgb, double* count);
 
+/* Allocation-free variant of cgpu_render (no counterpart in the reference):
+ * the wavefront render of samples [first_sample, first_sample + num_samples)
+ * of one scene into its film, with every device buffer of the call in one
+ * static 64 MiB array of this library instead of memory from cudaMalloc.
+ * For callers that must not allocate or free device memory at render time
+ * (cudaMalloc / cudaFree synchronise the device and may fail under memory
+ * pressure): a caller with its own memory budget, or one that keeps a render
+ * inside a latency-bound loop.  Same kernels, paths and results as
+ * cgpu_render (the film may differ in the last FP64 bits: batches split
+ * differently).  Limits, else CGPU_ERR_INVALID_ARGUMENT with the reason in
+ * cgpu_last_error: width * height <= 262144 pixels, max_depth <= 62, scene
+ * id < 64.  Nothing in the scratch needs to start at zero: each batch's
+ * setup kernel zeroes the queue counters and writes the batch tables, and
+ * generate writes every path's state before it is read.  The first call on
+ * a device looks the scratch up (cudaGetSymbolAddress) and, with lazy module
+ * loading, loads the library's device code, which reserves the array: make
+ * one call before relying on the no-allocation property.  One scratch per
+ * device and process: calls that overlap in time (any contexts, streams or
+ * threads on one device) race on it and must be serialised by the caller.
+ * Asynchronous on the context stream, like cgpu_render. */
+cgpu_status cgpu_render_noalloc(cgpu_ctx* ctx, int32_t scene, uint32_t first_sample, uint32_t num_samples,
+                                uint64_t seed);
+
 /* Per-path estimate for given film positions and path keys (path stream starts
  * at draw 0 with the estimator).  out_rgb: 3 floats per path. */
 cgpu_status cgpu_path_radiance(cgpu_ctx* ctx, int32_t scene, int32_t mode, const double* film_xy,

@@ -186,4 +186,11 @@ int khc_wf_layout_check(uint64_t cap, int rows) {
     return w.cnt_depth == rows ? 0 : -1;
 }
 
+// Bytes the static scratch of cgpu_render_noalloc needs, and its size.
+uint64_t khc_noalloc_layout_bytes() {
+    cg::NoAllocView v;
+    return cg::noalloc_layout(nullptr, &v);
+}
+uint64_t khc_noalloc_scratch_bytes() { return cg::kNoAllocScratchBytes; }
+
 }  // extern "C"

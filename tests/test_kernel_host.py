@@ -47,6 +47,8 @@ def khc():
     L.khc_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
     L.khc_adjoint.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
     L.khc_wf_layout_check.argtypes = [C.c_uint64, C.c_int]
+    L.khc_noalloc_layout_bytes.restype = C.c_uint64
+    L.khc_noalloc_scratch_bytes.restype = C.c_uint64
     return L
 
 
@@ -183,3 +185,11 @@ def test_wavefront_buffer_layout_fits(khc, cap):
     carved from, for capacities that are not multiples of the alignment."""
     for rows in (3, 34, 66):
         assert khc.khc_wf_layout_check(cap, rows) == 0
+
+
+def test_noalloc_scratch_holds_its_layout(khc):
+    """Header, batch tables and the path state of 262144 paths fit the 64 MiB
+    static array of cgpu_render_noalloc."""
+    need, have = khc.khc_noalloc_layout_bytes(), khc.khc_noalloc_scratch_bytes()
+    assert have == 64 << 20
+    assert 0 < need <= have, (need, have)
