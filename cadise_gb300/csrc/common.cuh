@@ -35,6 +35,9 @@ using std::max;
 using std::min;
 inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v) { unsigned long long o = *p; *p += v; return o; }
 inline double atomicAdd(double* p, double v) { double o = *p; *p += v; return o; }
+// one thread is a whole warp on the host
+inline unsigned __activemask() { return 1u; }
+inline int __any_sync(unsigned, int pred) { return pred; }
 #endif
 
 #define CG_HD __host__ __device__ __forceinline__

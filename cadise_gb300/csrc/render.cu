@@ -176,7 +176,7 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
         const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
         HitD hit;
         if (COUNT) ++nclosest;
-        const bool hitp = traverse<false, COUNT>(S, r, &hit, &tc);
+        const bool hitp = traverse_warp<COUNT>(S, r, &hit, &tc);
         const int key = extend_finish(w, S, p, cont, o, d, hitp, hit);
         grouped_push(qmat, cnt + 3, key, p);
     }
@@ -432,7 +432,7 @@ __global__ void k_trace(const SceneD* scenes, int scene, const cgpu_ray* rays, u
             occ[i] = traverse<true, false>(S, pr, &h, &tc) ? 1 : 0;
         } else {
             cgpu_hit out;
-            if (traverse<false, false>(S, pr, &h, &tc)) {
+            if (traverse_warp<false>(S, pr, &h, &tc)) {
                 const HitPoint hp = hit_point(S, pr.o, pr.d, h);
                 out.t = hp.t;
                 out.primitive = __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + h.slot)).w);

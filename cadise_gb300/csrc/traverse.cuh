@@ -9,9 +9,10 @@
 // (Woop, Benthin & Wald, "Watertight Ray/Triangle Intersection", JCGT 2013):
 // the three edge functions are evaluated in a ray-aligned sheared space with
 // exactly rounded products (no contraction), falling back to FP64 when one of
-// them is exactly zero, so a ray through a shared edge or vertex hits exactly
-// one of the adjoining triangles.  Box tests widen t_max by 1 + 2 gamma(3) to
-// stay conservative.
+// them is exactly zero, so no ray slips between adjoining triangles (a ray
+// through a shared edge or vertex may hit both at the same t: the lower
+// triangle slot is kept).  Box tests widen t_max by 1 + 2 gamma(3) to stay
+// conservative.
 #pragma once
 
 #include "scene_device.cuh"
@@ -128,89 +129,175 @@ CG_D void child_hits(const RayPre& r, const float4 (&q)[7], float tcur, float (&
     }
 }
 
+constexpr uint32_t kNoEntry = 0xFFFFFFFFu;  // never a node or leaf entry (28-bit triangle range)
+
+// Which of two hits a closest-hit query keeps: the smaller distance, and on
+// an exact tie (a ray through an edge shared by two triangles hits both at
+// the same t) the lower triangle slot, so that the answer does not depend on
+// the order in which the traversal met them.
+CG_D bool closer_hit(float t, int slot, float tcur, int hslot) {
+    return hslot < 0 ? t <= tcur : (t < tcur || (t == tcur && slot < hslot));
+}
+
+// Visits inner node `e`: pushes the children the ray enters, farthest first,
+// except the nearest, which it returns (kNoEntry when the ray misses all four).
 template <bool ANY, bool COUNT>
-CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
-    int sp = 0;
-    uint32_t cur = 0;  // root is always an inner node
-    float tcur = r.tmax;
-    int hslot = -1;
-    float hu = 0.0f, hv = 0.0f;
+CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcur, uint32_t (&stack_e)[kStackSize],
+                         float (&stack_t)[kStackSize], int& sp, TraceCounters* cnt) {
     const float kInf = __int_as_float(0x7f800000);
-    for (;;) {
-        if (entry_is_leaf(cur)) {
-            const uint32_t first = leaf_first(cur), n = leaf_count(cur);
-            for (uint32_t k = 0; k < n; ++k) {
-                const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
-                const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
-                if (COUNT) cnt->tris++;
-                float t, u, v;
-                if (tri_test(r, f3(a), f3(b), f3(c), tcur, &t, &u, &v)) {
-                    hslot = int(first + k);
-                    if (ANY) {
-                        hit->slot = hslot;
-                        hit->t = t;
-                        return true;
-                    }
-                    tcur = t;
-                    hu = u;
-                    hv = v;
-                }
-            }
-        } else {
-            float4 q[7];
-            load_node(S.nodes, cur, q);
-            if (COUNT) cnt->nodes++;
-            float tn[4];
-            child_hits(r, q, tcur, tn);
-            uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
-                              __float_as_uint(q[6].w)};
-            if (!ANY) {
-                // ascending by distance (misses sort last)
+    float4 q[7];
+    load_node(S.nodes, e, q);
+    if (COUNT) cnt->nodes++;
+    float tn[4];
+    child_hits(r, q, tcur, tn);
+    uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
+                      __float_as_uint(q[6].w)};
+    if (!ANY) {
+        // ascending by distance (misses sort last)
 #define CG_CSWAP(i, j)                                                      \
     if (tn[j] < tn[i]) {                                                    \
         const float tt = tn[i]; tn[i] = tn[j]; tn[j] = tt;                  \
         const uint32_t ee = ce[i]; ce[i] = ce[j]; ce[j] = ee;               \
     }
-                CG_CSWAP(0, 1) CG_CSWAP(2, 3) CG_CSWAP(0, 2) CG_CSWAP(1, 3) CG_CSWAP(1, 2)
+        CG_CSWAP(0, 1) CG_CSWAP(2, 3) CG_CSWAP(0, 2) CG_CSWAP(1, 3) CG_CSWAP(1, 2)
 #undef CG_CSWAP
-            }
-            int nhit = 0;
-            uint32_t nearest = 0;
-            float nearest_t = kInf;
-            // push farther hits first so the nearest is visited next
+    }
+    uint32_t nearest = kNoEntry;
+    float nearest_t = kInf;
 #pragma unroll
-            for (int i = 3; i >= 0; --i) {
-                if (tn[i] < kInf) {
-                    if (nhit > 0) {
-                        if (sp < kStackSize) {
-                            stack_e[sp] = nearest;
-                            stack_t[sp] = nearest_t;
-                            ++sp;
-                        }
-                    }
-                    nearest = ce[i];
-                    nearest_t = tn[i];
-                    ++nhit;
-                }
+    for (int i = 3; i >= 0; --i) {
+        if (tn[i] < kInf) {
+            if (nearest != kNoEntry && sp < kStackSize) {
+                stack_e[sp] = nearest;
+                stack_t[sp] = nearest_t;
+                ++sp;
             }
-            if (nhit > 0) {
-                cur = nearest;
-                continue;
+            nearest = ce[i];
+            nearest_t = tn[i];
+        }
+    }
+    return nearest;
+}
+
+// Tests the triangles of leaf `e`; returns true when an any-hit query is
+// answered (the hit is in slot / tcur).
+template <bool ANY, bool COUNT>
+CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, int& hslot, float& hu, float& hv,
+                     TraceCounters* cnt) {
+    const uint32_t first = leaf_first(e), n = leaf_count(e);
+    for (uint32_t k = 0; k < n; ++k) {
+        const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
+        const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+        if (COUNT) cnt->tris++;
+        float t, u, v;
+        // closest hit: a bound one rounding wider than tcur, so that every
+        // triangle whose t rounds to <= tcur reaches closer_hit
+        if (tri_test(r, f3(a), f3(b), f3(c), ANY ? tcur : tcur * 1.00000036f, &t, &u, &v)) {
+            const int slot = int(first + k);
+            if (ANY) {
+                hslot = slot;
+                tcur = t;
+                return true;
+            }
+            if (closer_hit(t, slot, tcur, hslot)) {
+                hslot = slot;
+                tcur = t;
+                hu = u;
+                hv = v;
             }
         }
-        // pop the next entry that can still hold a closer hit
-        bool found = false;
+    }
+    return false;
+}
+
+// One ray per thread, one node or one leaf per loop iteration: the
+// megakernel's traversal (its threads are at different bounces anyway) and
+// every any-hit query (the first hit ends the walk, so there is nothing to
+// gain from holding leaves back).
+template <bool ANY, bool COUNT>
+CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    float tcur = r.tmax;
+    int hslot = -1;
+    float hu = 0.0f, hv = 0.0f;
+    uint32_t cur = 0;  // root first (always an inner node)
+    for (;;) {
+        uint32_t next = kNoEntry;
+        if (entry_is_leaf(cur)) {
+            if (visit_leaf<ANY, COUNT>(S, r, cur, tcur, hslot, hu, hv, cnt)) {
+                hit->slot = hslot;
+                hit->t = tcur;
+                return true;
+            }
+        } else {
+            next = visit_node<ANY, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, cnt);
+        }
+        // else the next stack entry that can still hold a closer hit
+        while (next == kNoEntry && sp > 0) {
+            --sp;
+            if (ANY || stack_t[sp] <= tcur * 1.00000036f) next = stack_e[sp];
+        }
+        if (next == kNoEntry) break;
+        cur = next;
+    }
+    hit->slot = hslot;
+    hit->t = tcur;
+    hit->u = hu;
+    hit->v = hv;
+    return hslot >= 0;
+}
+
+// Closest hit for a warp of independent rays (the wavefront's extend pass and
+// the ray queries): while-while traversal with postponed leaves (Aila &
+// Laine, "Understanding the efficiency of ray traversal on GPUs", HPG 2009).
+// A lane that reaches a leaf keeps it and walks on through inner nodes until
+// every active lane of the warp holds a leaf; then the warp tests its leaves
+// together, so inner-node and triangle work run with more lanes in step.
+// Finds the same hit as traverse<false> (closer_hit does not depend on the
+// visiting order).
+template <bool COUNT>
+CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    float tcur = r.tmax;
+    int hslot = -1;
+    float hu = 0.0f, hv = 0.0f;
+    uint32_t cur = 0;          // root first (always an inner node)
+    uint32_t leaf = kNoEntry;  // postponed leaf
+    // next stack entry that can still hold a closer hit
+    auto pop = [&]() -> uint32_t {
         while (sp > 0) {
             --sp;
-            if (ANY || stack_t[sp] <= tcur * 1.00000036f) {
-                cur = stack_e[sp];
-                found = true;
-                break;
+            if (stack_t[sp] <= tcur * 1.00000036f) return stack_e[sp];
+        }
+        return kNoEntry;
+    };
+    while (cur != kNoEntry || leaf != kNoEntry) {
+        while (cur != kNoEntry && !entry_is_leaf(cur)) {
+            cur = visit_node<false, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, cnt);
+            if (cur == kNoEntry) cur = pop();
+            if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
+                leaf = cur;
+                cur = pop();
+            }
+            if (!__any_sync(__activemask(), leaf == kNoEntry)) break;
+        }
+        if (leaf == kNoEntry) {
+            if (cur == kNoEntry) break;
+            leaf = cur;  // the walk stopped on a leaf
+            cur = pop();
+        }
+        while (leaf != kNoEntry) {
+            visit_leaf<false, COUNT>(S, r, leaf, tcur, hslot, hu, hv, cnt);
+            leaf = kNoEntry;
+            if (cur != kNoEntry && entry_is_leaf(cur)) {
+                leaf = cur;
+                cur = pop();
             }
         }
-        if (!found) break;
     }
     hit->slot = hslot;
     hit->t = tcur;
@@ -223,7 +310,8 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
 // finished rays (a warp keeps all lanes busy by giving a lane whose ray is
 // done the next ray from a global counter; Aila & Laine, "Understanding the
 // efficiency of ray traversal on GPUs", HPG 2009).  trav_step performs one
-// node visit or one leaf test; the same decisions as traverse().
+// node visit or one leaf test and finds the same hit as traverse() (the
+// closest-hit rule does not depend on the visiting order).
 struct TravState {
     uint32_t stack_e[kStackSize];
     float stack_t[kStackSize];
@@ -246,61 +334,15 @@ CG_D void trav_begin(TravState& st, const RayPre& r) {
 
 template <bool ANY, bool COUNT>
 CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounters* cnt) {
-    const float kInf = __int_as_float(0x7f800000);
     if (entry_is_leaf(st.cur)) {
-        const uint32_t first = leaf_first(st.cur), n = leaf_count(st.cur);
-        for (uint32_t k = 0; k < n; ++k) {
-            const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
-            const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
-            if (COUNT) cnt->tris++;
-            float t, u, v;
-            if (tri_test(r, f3(a), f3(b), f3(c), st.tcur, &t, &u, &v)) {
-                st.hslot = int(first + k);
-                if (ANY) {
-                    st.tcur = t;
-                    st.done = true;
-                    return;
-                }
-                st.tcur = t;
-                st.hu = u;
-                st.hv = v;
-            }
+        if (visit_leaf<ANY, COUNT>(S, r, st.cur, st.tcur, st.hslot, st.hu, st.hv, cnt)) {
+            st.done = true;
+            return;
         }
     } else {
-        float4 q[7];
-        load_node(S.nodes, st.cur, q);
-        if (COUNT) cnt->nodes++;
-        float tn[4];
-        child_hits(r, q, st.tcur, tn);
-        uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
-                          __float_as_uint(q[6].w)};
-        if (!ANY) {
-#define CG_CSWAP(i, j)                                                      \
-    if (tn[j] < tn[i]) {                                                    \
-        const float tt = tn[i]; tn[i] = tn[j]; tn[j] = tt;                  \
-        const uint32_t ee = ce[i]; ce[i] = ce[j]; ce[j] = ee;               \
-    }
-            CG_CSWAP(0, 1) CG_CSWAP(2, 3) CG_CSWAP(0, 2) CG_CSWAP(1, 3) CG_CSWAP(1, 2)
-#undef CG_CSWAP
-        }
-        int nhit = 0;
-        uint32_t nearest = 0;
-        float nearest_t = kInf;
-#pragma unroll
-        for (int i = 3; i >= 0; --i) {
-            if (tn[i] < kInf) {
-                if (nhit > 0 && st.sp < kStackSize) {
-                    st.stack_e[st.sp] = nearest;
-                    st.stack_t[st.sp] = nearest_t;
-                    ++st.sp;
-                }
-                nearest = ce[i];
-                nearest_t = tn[i];
-                ++nhit;
-            }
-        }
-        if (nhit > 0) {
-            st.cur = nearest;
+        const uint32_t next = visit_node<ANY, COUNT>(S, r, st.cur, st.tcur, st.stack_e, st.stack_t, st.sp, cnt);
+        if (next != kNoEntry) {
+            st.cur = next;
             return;
         }
     }

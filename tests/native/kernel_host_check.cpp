@@ -45,7 +45,7 @@ void* khc_create(const cgpu_scene_desc* d, char* err, int errlen) {
 
 void khc_destroy(void* p) { delete static_cast<Check*>(p); }
 
-// rays: 8 floats (org, t_min, dir, t_max); dyn != 0 uses the resumable stepper
+// rays: 8 floats (org, t_min, dir, t_max); dyn 1 uses the resumable stepper, 2 the warp traversal
 void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, float* t, float* u, float* v,
                int32_t* occ) {
     const Check& c = *static_cast<Check*>(p);
@@ -55,7 +55,7 @@ void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, f
         cg::TraceCounters tc{0, 0};
         cg::HitD h;
         bool hit, any;
-        if (dyn) {
+        if (dyn == 1) {
             std::unique_ptr<cg::TravState> st(new cg::TravState());
             cg::trav_begin(*st, pr);
             while (!st->done) cg::trav_step<false, false>(c.S, pr, *st, &tc);
@@ -67,6 +67,10 @@ void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, f
             cg::trav_begin(*st, pr);
             while (!st->done) cg::trav_step<true, false>(c.S, pr, *st, &tc);
             any = st->hslot >= 0;
+        } else if (dyn == 2) {
+            hit = cg::traverse_warp<false>(c.S, pr, &h, &tc);
+            cg::HitD h2;
+            any = cg::traverse<true, false>(c.S, pr, &h2, &tc);
         } else {
             hit = cg::traverse<false, false>(c.S, pr, &h, &tc);
             cg::HitD h2;

@@ -113,9 +113,11 @@ def test_kernel_traversal_matches_reference_hits(khc, name):
     assert np.array_equal(prim[keep], ref_p[keep])
     both = (prim == ref_p) & (prim >= 0)
     assert np.array_equal(t[both], ref_t[both])  # the reference's own distance formula
-    # the resumable stepper of the persistent kernels takes the same decisions
-    p2, t2, occ2 = h.trace(rays, dyn=1)
-    assert np.array_equal(p2, prim) and np.array_equal(t2, t) and np.array_equal(occ2, occ)
+    # the resumable stepper of the persistent kernels and the warp traversal
+    # of the extend pass find the same hits
+    for variant in (1, 2):
+        p2, t2, occ2 = h.trace(rays, dyn=variant)
+        assert np.array_equal(p2, prim) and np.array_equal(t2, t) and np.array_equal(occ2, occ)
     h.close()
 
 
