@@ -161,7 +161,7 @@ def run_gpu(args, rank, world, local):
     tuning = ctx.tuning()
     if not args.no_autotune:
         cache = os.path.join(tempfile.gettempdir(), "cadise_gb300_tune.jsonl")
-        tuning = ctx.autotune([sid], samples=1, cache_path=cache)
+        tuning = ctx.autotune([sid], samples=8, cache_path=cache)
 
     with torch.cuda.stream(stream):
         for _ in range(args.warmup):

@@ -29,7 +29,7 @@ void apply(cgpu_ctx* ctx, const cgpu_tuning& t) {
     if (realloc) cg_free_render_state(ctx);
 }
 
-std::string cache_key(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n) {
+std::string cache_key(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint32_t samples) {
     cudaDeviceProp prop;
     cudaGetDeviceProperties(&prop, ctx->device);
     uint64_t tris = 0, pix = 0;
@@ -42,7 +42,7 @@ std::string cache_key(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n) {
     }
     std::ostringstream os;
     os << prop.name << "|sm" << prop.multiProcessorCount << "|tris" << tris << "|pix" << pix << "|depth" << depth
-       << "|scenes" << n;
+       << "|scenes" << n << "|samples" << samples;
     return os.str();
 }
 
@@ -104,7 +104,8 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
         if (scenes[i] < 0 || scenes[i] >= int32_t(ctx->scenes.size()) || !ctx->scenes[size_t(scenes[i])].live)
             return cg_fail(ctx, CGPU_ERR_NOT_FOUND, "autotune: unknown scene id");
     cudaSetDevice(ctx->device);
-    const std::string key = cache_key(ctx, scenes, n);
+    if (samples == 0) samples = 1;
+    const std::string key = cache_key(ctx, scenes, n, samples);
     cgpu_tuning best = ctx->tuning;
     if (cache_path && cache_lookup(cache_path, key, &best)) {
         cudaStreamSynchronize(ctx->stream);
@@ -112,7 +113,6 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
         if (out) *out = best;
         return CGPU_OK;
     }
-    if (samples == 0) samples = 1;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -147,11 +147,14 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     float best_ms = 0.0f;
     cgpu_status st = time_one(best, &best_ms);
     const int blocks[] = {64, 128, 256};
-    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22};
+    // paths in flight: larger batches hold several samples per pixel and
+    // share one tail of short late-bounce queues among them
+    const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
+    const int options[] = {2, 3, 3, 5};
     for (int pass = 0; pass < 4 && st == CGPU_OK; ++pass) {
-        for (int k = 0; k < 3 && st == CGPU_OK; ++k) {
+        for (int k = 0; k < options[pass] && st == CGPU_OK; ++k) {
             cgpu_tuning t = best;
-            if (pass == 0) t.traversal = k < 2 ? k : best.traversal;
+            if (pass == 0) t.traversal = k;
             if (pass == 1) t.block_trace = blocks[k];
             if (pass == 2) t.block_shade = blocks[k];
             if (pass == 3) t.max_paths = caps[k];

@@ -284,9 +284,10 @@ typedef struct cgpu_tuning {
 cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out_tuning);
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* tuning);
 /* Times wavefront passes of `scenes` (`samples` samples each) over a small
- * search of cgpu_tuning values and applies the fastest.  With a cache path,
- * a result stored for the same GPU and scene sizes is reused without timing
- * and new results are appended (one JSON object per line). */
+ * search of cgpu_tuning values (traversal variant, block sizes, 2^20..2^24
+ * paths in flight) and applies the fastest.  With a cache path, a result
+ * stored for the same GPU, scene sizes and sample count is reused without
+ * timing and new results are appended (one JSON object per line). */
 cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t num_scenes, uint32_t samples,
                           const char* cache_path, cgpu_tuning* out_tuning);
 
