@@ -97,34 +97,45 @@ struct TraceCounters {
     uint32_t tris;
 };
 
-CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, float4 (&q)[7]) {
-    const float4* p = reinterpret_cast<const float4*>(nodes + idx);
-#pragma unroll
-    for (int i = 0; i < 7; ++i) q[i] = __ldg(p + i);
-}
-
 CG_D float4 ldg4(const float4* p) { return __ldg(p); }
 
+// Loads node `idx` as the ray sees it: q[0..2] the near slab planes of x, y,
+// z (lo, or hi for a ray running towards -axis), q[3..5] the far planes,
+// q[6] the four child entries.  Picking the planes by address leaves the
+// slab test without the per-child min / max that orders each plane pair.
+CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, const RayPre& r, float4 (&q)[7]) {
+    const float4* p = reinterpret_cast<const float4*>(nodes + idx);
+    // 1 where the ray runs towards -axis (the sign bit of 1 / d)
+    const int sx = int(__float_as_uint(r.inv.x) >> 31), sy = int(__float_as_uint(r.inv.y) >> 31),
+              sz = int(__float_as_uint(r.inv.z) >> 31);
+    q[0] = __ldg(p + 0 + sx);
+    q[3] = __ldg(p + 1 - sx);
+    q[1] = __ldg(p + 2 + sy);
+    q[4] = __ldg(p + 3 - sy);
+    q[2] = __ldg(p + 4 + sz);
+    q[5] = __ldg(p + 5 - sz);
+    q[6] = __ldg(p + 6);
+}
+
 // Child box distances; tnear = +inf marks a miss.  Empty child slots hold
-// entry 0 (the root, never anyone's child) and are always a miss: their
-// inverted box would not stay inverted under the min/max slab form below.
+// entry 0 (the root, never anyone's child) and are always a miss.
 CG_D void child_hits(const RayPre& r, const float4 (&q)[7], float tcur, float (&tn)[4]) {
     const uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
                             __float_as_uint(q[6].w)};
-    const float lox[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
-    const float hix[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
-    const float loy[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
-    const float hiy[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
-    const float loz[4] = {q[4].x, q[4].y, q[4].z, q[4].w};
-    const float hiz[4] = {q[5].x, q[5].y, q[5].z, q[5].w};
+    const float nx[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
+    const float ny[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
+    const float nz[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
+    const float fx[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
+    const float fy[4] = {q[4].x, q[4].y, q[4].z, q[4].w};
+    const float fz[4] = {q[5].x, q[5].y, q[5].z, q[5].w};
     const float tlim = tcur * 1.00000036f;  // 1 + 2 gamma(3)
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const float t0x = (lox[i] - r.o.x) * r.inv.x, t1x = (hix[i] - r.o.x) * r.inv.x;
-        const float t0y = (loy[i] - r.o.y) * r.inv.y, t1y = (hiy[i] - r.o.y) * r.inv.y;
-        const float t0z = (loz[i] - r.o.z) * r.inv.z, t1z = (hiz[i] - r.o.z) * r.inv.z;
-        const float tnear = fmaxf(fmaxf(fminf(t0x, t1x), fminf(t0y, t1y)), fmaxf(fminf(t0z, t1z), r.tmin));
-        const float tfar = fminf(fminf(fmaxf(t0x, t1x), fmaxf(t0y, t1y)), fminf(fmaxf(t0z, t1z), tlim));
+        const float tnx = (nx[i] - r.o.x) * r.inv.x, tfx = (fx[i] - r.o.x) * r.inv.x;
+        const float tny = (ny[i] - r.o.y) * r.inv.y, tfy = (fy[i] - r.o.y) * r.inv.y;
+        const float tnz = (nz[i] - r.o.z) * r.inv.z, tfz = (fz[i] - r.o.z) * r.inv.z;
+        const float tnear = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
+        const float tfar = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
         tn[i] = (ce[i] != 0u && tnear <= tfar * 1.00000036f) ? tnear : __int_as_float(0x7f800000);
     }
 }
@@ -146,7 +157,7 @@ CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcu
                          float (&stack_t)[kStackSize], int& sp, TraceCounters* cnt) {
     const float kInf = __int_as_float(0x7f800000);
     float4 q[7];
-    load_node(S.nodes, e, q);
+    load_node(S.nodes, e, r, q);
     if (COUNT) cnt->nodes++;
     float tn[4];
     child_hits(r, q, tcur, tn);
