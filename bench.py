@@ -41,6 +41,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--profile-case", action="store_true",
                     help="for ncu: upload the frame and run --steps wavefront passes of 1 spp, nothing else")
+    ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2: the headline line (default); c1 Cornell box, c3 64 batched scenes, "
+                         "c4 differentiable scene forward, c5 20.48 M-triangle stress frame: one JSON line each")
     return ap.parse_args()
 
 
@@ -375,6 +378,100 @@ def run_reference(args, rank, world, local):
     print(json.dumps(out), flush=True)
 
 
+# ------------------------------------------------------ other configurations --
+CONFIGS = {
+    "c1": "cornell-box-256x256-16spp-depth6",
+    "c3": "64-batched-icosphere-fields-10k-2M-tris-128..1024px-4..256spp-depth4..16",
+    "c4": "diff-scene-102k-tris-512x512-32spp-depth6-forward",
+    "c5": "env-field-20.48M-tris-3840x2160-depth32-64-lights-hdr-sky (4 spp per step of the 1024)",
+}
+
+
+def run_config(args):
+    """The other configurations, one JSON line each: wavefront and
+    megakernel path samples/s on the GPU, the oracle's CPU rate on a bounded
+    slice, and the set-up times (scene generation, upload with BVH build)."""
+    import torch
+
+    import cadise_gb300 as cg
+    from cadise_gb300 import abi, scenes
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    ctx = cg.Context(device=0, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    if args.config == "c1":
+        specs = [scenes.cornell_box()]
+    elif args.config == "c3":
+        specs = scenes.batch_scenes()
+    elif args.config == "c4":
+        specs = [scenes.diff_scene()]
+    else:
+        specs = [scenes.env_field()]
+    gen_s = time.perf_counter() - t0
+    flats = [abi.flatten(s) for s in specs]
+    t0 = time.perf_counter()
+    sids = [ctx.upload(f) for f in flats]
+    upload_s = time.perf_counter() - t0
+    infos = [ctx.info(s) for s in sids]
+    npix = [s.width * s.height for s in specs]
+    # samples per step: the whole job (c1, c3, c4) or 4 of the 1024 spp (c5)
+    counts = [4 if args.config == "c5" else s.spp for s in specs]
+    mk_counts = [max(1, c // 8) for c in counts] if args.config in ("c3", "c5") else counts
+    steps, warmup = (1, 1) if args.config == "c3" else (args.steps, args.warmup)
+    tuning = ctx.autotune(sids, samples=1 if args.config in ("c3", "c5") else 8)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def timed(mode, cnt, k):
+        ms = 0.0
+        with torch.cuda.stream(stream):
+            for i in range(k):
+                flush.fill_(1)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                ctx.render(sids, 0, cnt, seed=11 + i, mode=mode, sync=False)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                ms += e0.elapsed_time(e1)
+        return sum(n * c for n, c in zip(npix, cnt)) * k / (ms / 1e3), ms / k
+
+    timed(cg.CGPU_MODE_WAVEFRONT, counts, warmup)
+    clocks = ClockSampler(0)
+    clocks.start()
+    wf, wf_ms = timed(cg.CGPU_MODE_WAVEFRONT, counts, steps)
+    clk = clocks.stop()
+    timed(cg.CGPU_MODE_MEGAKERNEL, mk_counts, 1)
+    mk, _ = timed(cg.CGPU_MODE_MEGAKERNEL, mk_counts, 1)
+    # CPU: the oracle on a bounded slice of (a spread of) the scenes
+    cpu = None
+    if not args.no_cpu_baseline:
+        order = sorted(range(len(specs)), key=lambda i: infos[i].num_triangles)
+        pick = order if len(order) <= 1 else [order[int(round(j * (len(order) - 1) / 7))] for j in range(8)]
+        rates = []
+        for i in sorted(set(pick)):
+            rate, cores, _ = cpu_rate(flats[i], seconds=12.0 / len(set(pick)))
+            rates.append(rate)
+        cpu = {"value": statistics.mean(rates), "unit": UNIT, "cores": cores, "kind": "port",
+               "sample": "%d scene(s), 1-spp row slices of ~%.1f s each" % (len(rates), 12.0 / len(rates))}
+    out = {
+        "metric": METRIC, "value": wf, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": warmup,
+        "ms_per_step": wf_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": CONFIGS[args.config], "scenes": len(specs),
+                   "triangles": int(sum(i.num_triangles for i in infos)),
+                   "samples_per_step": int(sum(n * c for n, c in zip(npix, counts))), "tuning": tuning,
+                   "l2": "256 MB buffer written between steps"},
+        "megakernel": {"value": mk, "unit": UNIT, "speedup_wavefront": wf / mk,
+                       "samples_per_step": int(sum(n * c for n, c in zip(npix, mk_counts)))},
+        "setup_s": {"scene_generation": gen_s, "upload_with_bvh_build": upload_s,
+                    "bvh_build": sum(i.build_ms for i in infos) / 1e3},
+        "clocks": clk,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+    ctx.close()
+
+
 def run_profile_case(args):
     import cadise_gb300 as cg
     from cadise_gb300 import abi
@@ -393,6 +490,10 @@ def main():
     rank, world, local = dist_env()
     if args.profile_case:
         run_profile_case(args)
+        return
+    if args.config != "c2":
+        if rank == 0:
+            run_config(args)
         return
     if args.impl == "reference":
         run_reference(args, rank, world, local)

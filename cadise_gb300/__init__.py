@@ -206,11 +206,17 @@ class Context:
         self._check(self.L.cgpu_render_paths(self.h, sid, mode, first, count, seed, _p(out)))
         return out
 
-    def render(self, sids: Sequence[int], first: int, count: int, seed: int,
+    def render(self, sids: Sequence[int], first: int, count, seed: int,
                mode: int = CGPU_MODE_WAVEFRONT, graph: bool = True, sync: bool = True):
+        """Samples [first, first + count) of every scene; `count` may be a
+        sequence with one sample count per scene."""
         arr = (C.c_int32 * len(sids))(*sids)
+        per = None
+        if not isinstance(count, int):
+            per = (C.c_uint32 * len(sids))(*[int(c) for c in count])
+            count = 0
         p = cgpu_render_params(scenes=arr, num_scenes=len(sids), first_sample=first, num_samples=count,
-                               seed=seed, mode=mode, use_graph=1 if graph else 0)
+                               seed=seed, mode=mode, use_graph=1 if graph else 0, scene_samples=per)
         self._check(self.L.cgpu_render(self.h, C.byref(p)))
         if sync:
             self.synchronize()

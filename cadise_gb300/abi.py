@@ -93,7 +93,7 @@ class cgpu_hit(C.Structure):
 class cgpu_render_params(C.Structure):
     _fields_ = [("scenes", C.POINTER(C.c_int32)), ("num_scenes", C.c_uint32),
                 ("first_sample", C.c_uint32), ("num_samples", C.c_uint32), ("seed", C.c_uint64),
-                ("mode", C.c_int32), ("use_graph", C.c_int32)]
+                ("mode", C.c_int32), ("use_graph", C.c_int32), ("scene_samples", C.POINTER(C.c_uint32))]
 
 
 class cgpu_render_stats(C.Structure):

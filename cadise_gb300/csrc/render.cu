@@ -691,18 +691,23 @@ cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p) {
     ctx->times = cgpu_kernel_times{};
     if (ctx->counting) cudaMemsetAsync(ctx->d_counters, 0, 8 * sizeof(unsigned long long), ctx->stream);
     // remaining samples per scene
-    std::vector<uint32_t> next(p->num_scenes, p->first_sample);
-    const uint32_t end = p->first_sample + p->num_samples;
+    std::vector<uint32_t> next(p->num_scenes, p->first_sample), end(p->num_scenes);
+    for (uint32_t i = 0; i < p->num_scenes; ++i) {
+        const uint64_t n = p->scene_samples ? p->scene_samples[i] : p->num_samples;
+        if (uint64_t(p->first_sample) + n > 0xFFFFFFFFull)
+            return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render: sample range overflows 32 bits");
+        end[i] = p->first_sample + uint32_t(n);
+    }
     uint64_t total_paths = 0;
     for (;;) {
         uint32_t used = 0, pix = 0, nch = 0;
         for (uint32_t i = 0; i < p->num_scenes && nch < uint32_t(kMaxChunks); ++i) {
-            if (next[i] >= end) continue;
+            if (next[i] >= end[i]) continue;
             const SceneSlot& sl = ctx->scenes[p->scenes[i]];
             const uint32_t npix = uint32_t(sl.width) * uint32_t(sl.height);
             const uint32_t room = (ctx->path_cap - used) / npix;
             if (room == 0) continue;
-            const uint32_t k = std::min(room, end - next[i]);
+            const uint32_t k = std::min(room, end[i] - next[i]);
             Chunk& c = ctx->h_chunks[nch++];
             c.scene = p->scenes[i];
             c.path_begin = used;

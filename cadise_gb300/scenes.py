@@ -486,6 +486,26 @@ def diff_scene(width: int = 512, height: int = 512, spp: int = 32, max_depth: in
     return s
 
 
+def batch_scenes(count: int = 64, seed: int = 3, tri_range=(10_000, 2_000_000)) -> list:
+    """The batched configuration: `count` icosphere fields with triangle
+    counts log-uniform in `tri_range` (subdivision 4 spheres of 5,120
+    triangles, or subdivision 3 of 1,280 below 51,200), each with its own
+    resolution from {128, 256, 512, 1024}^2, spp from {4, 16, 64, 256} and
+    max depth from {4, 8, 16}."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        tris = math.exp(rng.uniform(math.log(tri_range[0]), math.log(tri_range[1])))
+        sub = 4 if tris >= 51_200 else 3
+        n = max(1, int(round(tris / (20 * 4 ** sub))))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = int(rng.choice([4, 16, 64, 256]))
+        depth = int(rng.choice([4, 8, 16]))
+        out.append(icosphere_field(n_spheres=n, subdivision=sub, n_lights=8, seed=1000 + i, width=res, height=res,
+                                   spp=spp, max_depth=depth, box=100.0 * (n / 200.0) ** (1 / 3)))
+    return out
+
+
 def lognormal_sky(width: int = 2048, height: int = 1024, sigma: float = 1.5, seed: int = 5) -> np.ndarray:
     """Procedural HDR environment map: smooth log-normal luminance field
     (log-luminance ~ N(0, sigma^2), spatially correlated) with a warm/cool tint."""

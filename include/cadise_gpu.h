@@ -48,7 +48,7 @@
 extern "C" {
 #endif
 
-#define CGPU_ABI_VERSION 1
+#define CGPU_ABI_VERSION 2
 
 typedef enum cgpu_status {
     CGPU_OK = 0,
@@ -216,6 +216,9 @@ typedef struct cgpu_render_params {
     uint64_t seed;
     int32_t mode;              /* CGPU_MODE_* */
     int32_t use_graph;         /* wavefront: replay a captured CUDA graph per pass */
+    /* optional, one per scene: scene i renders samples
+     * [first_sample, first_sample + scene_samples[i]); NULL: num_samples for all */
+    const uint32_t* scene_samples;
 } cgpu_render_params;
 
 /* Accumulates into each scene's FP64 film on the device (asynchronous). */

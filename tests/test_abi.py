@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.cgpu_abi_version() == 1
+    assert lib.cgpu_abi_version() == 2
     for code, name in abi.STATUS_NAMES.items():
         assert lib.cgpu_status_string(code).decode() == name
 
@@ -61,3 +61,4 @@ def test_struct_layouts_match_header():
     assert C.sizeof(abi.cgpu_hit) == 16
     assert C.sizeof(abi.cgpu_material) == 48
     assert C.sizeof(abi.cgpu_area_light) == 24
+    assert C.sizeof(abi.cgpu_render_params) == 48

@@ -54,6 +54,24 @@ def test_batch_equals_individual_renders(gpu_ctx, uneven):
             assert np.array_equal(x, y)
 
 
+def test_per_scene_sample_counts(gpu_ctx, uneven):
+    """One call, a different sample range per scene (cgpu_render_params.scene_samples)."""
+    specs, sids = uneven
+    counts = [3, 8, 5]
+    for s in sids:
+        gpu_ctx.film_clear(s)
+    gpu_ctx.render(sids, 2, counts, seed=19, mode=CGPU_MODE_WAVEFRONT)
+    together = films(gpu_ctx, sids)
+    for s, c in zip(sids, counts):
+        gpu_ctx.film_clear(s)
+        gpu_ctx.render([s], 2, c, seed=19, mode=CGPU_MODE_WAVEFRONT)
+    alone = films(gpu_ctx, sids)
+    for a, b, c in zip(together, alone, counts):
+        assert a[2].max() == c
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+
+
 def test_tuning_does_not_change_results(gpu_ctx, uneven):
     specs, sids = uneven
     base = gpu_ctx.tuning()
