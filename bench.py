@@ -277,7 +277,11 @@ def run_gpu(args, rank, world, local):
                    "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
         "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value},
         "rays": {"closest_per_sample": st.closest_rays / float(npix), "any_per_sample": st.any_rays / float(npix),
-                 "mrays_per_s": value * rays_per_sample / 1e6},
+                 "mrays_per_s": value * rays_per_sample / 1e6,
+                 "nodes_per_closest_ray": st.node_visits / max(1, st.closest_rays),
+                 "triangles_per_closest_ray": st.triangle_tests / max(1, st.closest_rays),
+                 "nodes_per_any_ray": st.any_node_visits / max(1, st.any_rays),
+                 "triangles_per_any_ray": st.any_triangle_tests / max(1, st.any_rays)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "k_wf_extend (closest-hit traversal)",
