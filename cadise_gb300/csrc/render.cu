@@ -275,6 +275,106 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
 }
 
+// Persistent closest-hit pass: the while-while traversal of traverse_warp
+// with dynamic ray fetch (Aila & Laine 2009).  A lane keeps its ray across
+// rounds; after each round of leaves, once fewer than kRefillLanes lanes of
+// the warp still hold an unfinished ray, the finished lanes store their hits
+// and take the next rays of the queue, so lanes do not idle until the warp's
+// longest ray is done.  Same hits as the other extend kernels (closer_hit).
+constexpr int kRefillLanes = 16;
+
+template <bool COUNT>
+__global__ void k_wf_extend_pww(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    int* cnt = w.cnt + b * kCntStride;
+    const int ncont = cnt[0], nmis = cnt[1];
+    const int n = ncont + nmis;
+    const int* qc = w.q_cont[b & 1];
+    const int* qm = w.q_mis[b & 1];
+    int* const* qmat = w.q_mat;
+    TraceCounters tc{0, 0};
+    uint32_t nclosest = 0;
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    RayPre r{};
+    float tcur = 0.0f, hu = 0.0f, hv = 0.0f;
+    int hslot = -1;
+    uint32_t cur = kNoEntry, leaf = kNoEntry;
+    int i = -1, p = -1;  // queue entry and path of this lane's ray (i < 0: none)
+    bool drained = false;
+    auto pop = [&]() -> uint32_t {
+        while (sp > 0) {
+            --sp;
+            if (stack_t[sp] <= tcur * 1.00000036f) return stack_e[sp];
+        }
+        return kNoEntry;
+    };
+    for (;;) {
+        const bool need = i < 0 && !drained;
+        const int k = warp_take(cnt + 8, need, n);
+        if (need) {
+            if (k < 0) {
+                drained = true;
+            } else {
+                i = k;
+                p = i < ncont ? qc[i] : qm[i - ncont];
+                const float3 o = f3(w.ray_o[p]);
+                const float3 d = i < ncont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+                r = ray_prep(o, d, kRayEps, kFloatMax);
+                tcur = r.tmax;
+                hslot = -1;
+                hu = hv = 0.0f;
+                cur = 0;
+                leaf = kNoEntry;
+                sp = 0;
+                if (COUNT) ++nclosest;
+            }
+        }
+        if (__all_sync(__activemask(), i < 0)) break;
+        if (i < 0) continue;
+        const SceneD& S = a.scenes[w.meta[p].x];
+        for (;;) {
+            while (cur != kNoEntry && !entry_is_leaf(cur)) {
+                cur = visit_node<false, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, &tc);
+                if (cur == kNoEntry) cur = pop();
+                if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
+                    leaf = cur;
+                    cur = pop();
+                }
+                if (!__any_sync(__activemask(), leaf == kNoEntry)) break;
+            }
+            if (leaf == kNoEntry) {
+                if (cur == kNoEntry) break;  // the ray is done
+                leaf = cur;
+                cur = pop();
+            }
+            while (leaf != kNoEntry) {
+                visit_leaf<false, COUNT>(S, r, leaf, tcur, hslot, hu, hv, &tc);
+                leaf = kNoEntry;
+                if (cur != kNoEntry && entry_is_leaf(cur)) {
+                    leaf = cur;
+                    cur = pop();
+                }
+            }
+            if (cur == kNoEntry) break;  // the ray is done
+            if (__popc(__activemask()) < kRefillLanes) break;
+        }
+        if (cur == kNoEntry && leaf == kNoEntry) {
+            HitD hit;
+            hit.t = tcur;
+            hit.slot = hslot;
+            hit.u = hu;
+            hit.v = hv;
+            const bool cont = i < ncont;
+            const int key = extend_finish(w, S, p, cont, r.o, r.d, hslot >= 0, hit);
+            grouped_push(qmat, cnt + 3, key, p);
+            i = -1;
+        }
+    }
+    count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
+}
+
 template <bool COUNT>
 __global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
@@ -564,11 +664,12 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
     const int ggen = grid_for(ctx, k_wf_generate, kBlock, paths);
     timed(ctx, CGPU_KERNEL_GENERATE, s, [&] { k_wf_generate<<<ggen, kBlock, 0, s>>>(a); });
-    const bool dyn = ctx->tuning.traversal == 1;
-    auto ext_kernel = dyn ? (counting ? k_wf_extend_dyn<true> : k_wf_extend_dyn<false>)
-                          : (counting ? k_wf_extend<true> : k_wf_extend<false>);
-    auto sh_kernel = dyn ? (counting ? k_wf_shadow_dyn<true> : k_wf_shadow_dyn<false>)
-                         : (counting ? k_wf_shadow<true> : k_wf_shadow<false>);
+    const int trav = ctx->tuning.traversal;
+    auto ext_kernel = trav == 1   ? (counting ? k_wf_extend_dyn<true> : k_wf_extend_dyn<false>)
+                      : trav == 2 ? (counting ? k_wf_extend_pww<true> : k_wf_extend_pww<false>)
+                                  : (counting ? k_wf_extend<true> : k_wf_extend<false>);
+    auto sh_kernel = trav == 1 ? (counting ? k_wf_shadow_dyn<true> : k_wf_shadow_dyn<false>)
+                               : (counting ? k_wf_shadow<true> : k_wf_shadow<false>);
     const int gext = grid_for(ctx, ext_kernel, bt, paths);
     const int gsh = grid_for(ctx, sh_kernel, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
@@ -898,9 +999,9 @@ cgpu_status noalloc_base(cgpu_ctx* ctx, char** out) {
 void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_t paths, uint32_t npix) {
     cudaStream_t s = ctx->stream;
     const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
-    const bool dyn = ctx->tuning.traversal == 1;
-    auto ext = dyn ? k_wf_extend_dyn<false> : k_wf_extend<false>;
-    auto sh = dyn ? k_wf_shadow_dyn<false> : k_wf_shadow<false>;
+    const int trav = ctx->tuning.traversal;
+    auto ext = trav == 1 ? k_wf_extend_dyn<false> : trav == 2 ? k_wf_extend_pww<false> : k_wf_extend<false>;
+    auto sh = trav == 1 ? k_wf_shadow_dyn<false> : k_wf_shadow<false>;
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
     const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, sh, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),

@@ -79,16 +79,18 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
         gpu_ctx.film_clear(s)
     gpu_ctx.render(sids, 0, 4, seed=5)
     ref = films(gpu_ctx, sids)
-    gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=1)  # small batches, persistent ray replacement
-    for s in sids:
-        gpu_ctx.film_clear(s)
-    gpu_ctx.render(sids, 0, 4, seed=5)
-    got = films(gpu_ctx, sids)
-    assert gpu_ctx.stats().batches > 1
+    # small batches; persistent ray replacement (1) and persistent while-while (2)
+    for traversal in (1, 2):
+        gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal)
+        for s in sids:
+            gpu_ctx.film_clear(s)
+        gpu_ctx.render(sids, 0, 4, seed=5)
+        got = films(gpu_ctx, sids)
+        assert gpu_ctx.stats().batches > 1
+        for a, b in zip(ref, got):
+            for x, y in zip(a, b):
+                assert np.array_equal(x, y)
     gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], base["traversal"])
-    for a, b in zip(ref, got):
-        for x, y in zip(a, b):
-            assert np.array_equal(x, y)
 
 
 def test_autotune_picks_and_caches(gpu_ctx, uneven, tmp_path):
