@@ -281,7 +281,7 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
 // the warp still hold an unfinished ray, the finished lanes store their hits
 // and take the next rays of the queue, so lanes do not idle until the warp's
 // longest ray is done.  Same hits as the other extend kernels (closer_hit).
-constexpr int kRefillLanes = 16;
+constexpr int kRefillLanes = 12;
 
 template <bool COUNT>
 __global__ void k_wf_extend_pww(RenderArgs a, int b) {

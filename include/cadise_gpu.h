@@ -283,7 +283,7 @@ typedef struct cgpu_tuning {
     uint32_t max_paths;    /* paths in flight per wavefront batch; 0 = automatic (2^21, at least one frame) */
     int32_t traversal;     /* 0: one ray per thread per grid-stride step; 1: persistent warps that hand a
                               finished lane the next ray at once; 2: persistent while-while closest-hit
-                              pass that refills a warp's finished lanes once half of them are done */
+                              pass that refills a warp's finished lanes once 20 of them are done */
 } cgpu_tuning;
 cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out_tuning);
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* tuning);
