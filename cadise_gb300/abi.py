@@ -67,7 +67,7 @@ class cgpu_scene_desc(C.Structure):
                 ("num_materials", C.c_uint32), ("materials", C.POINTER(cgpu_material)),
                 ("num_textures", C.c_uint32), ("textures", C.POINTER(cgpu_texture)),
                 ("num_lights", C.c_uint32), ("lights", C.POINTER(cgpu_area_light)),
-                ("environment_texture", C.c_int32)]
+                ("environment_texture", C.c_int32), ("light_cluster", C.c_int32)]
 
 
 class cgpu_scene_info(C.Structure):
@@ -227,4 +227,5 @@ def flatten(spec: "S.SceneSpec") -> FlatScene:
     d.num_lights = len(spec.lights)
     d.lights = lights
     d.environment_texture = tex_index[spec.environment] + 1 if spec.environment else 0
+    d.light_cluster = {"uniform": 0, "power": 1}[spec.light_cluster]
     return FlatScene(d, kind, verts, mat, normals, uvws, mats, lights, texs, tex_arrays, names, mat_index)

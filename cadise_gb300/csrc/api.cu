@@ -206,6 +206,8 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     if (st == CGPU_OK && d->prim_normals) st = upload(ctx, sl, d->prim_normals, size_t(np) * 9, &dnorm);
     if (st == CGPU_OK && d->prim_uvws) st = upload(ctx, sl, d->prim_uvws, size_t(np) * 9, &duvw);
     if (st == CGPU_OK) st = upload(ctx, sl, hs.rect_frames.data(), hs.rect_frames.size(), &drect);
+    float* dlcdf = nullptr;
+    if (st == CGPU_OK && !hs.light_cdf.empty()) st = upload(ctx, sl, hs.light_cdf.data(), hs.light_cdf.size(), &dlcdf);
     const size_t npix = size_t(d->width) * size_t(d->height);
     double* film = nullptr;
     if (st == CGPU_OK) {
@@ -237,6 +239,7 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.prim_normals = dnorm;
     S.prim_uvws = duvw;
     S.rect_frames = drect;
+    S.light_cdf = dlcdf;
     S.num_lights = int(hs.lights.size());
     S.env_light = hs.env_light;
     S.num_tris = int(hs.tris.size());

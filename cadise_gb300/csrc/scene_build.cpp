@@ -314,6 +314,56 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
                 }
         for (int k = 0; k < 3; ++k) { out->info.bounds_min[k] = lo[k]; out->info.bounds_max[k] = hi[k]; }
     }
+    // ---- power light cluster (powerLightCluster.cpp:9-27): pick distribution
+    // over the lights' approximate fluxes, Distribution1D's CDF
+    // (distribution1D.cpp:10-41), in the reference's FP32 order
+    if (d->light_cluster == CGPU_LIGHT_CLUSTER_POWER) {
+        // RgbSpectrum::luminance (rgbSpectrum.cpp:33-37), weights as the reference has them
+        auto luminance = [](float3 c) { return 0.0126f * c.x + 0.7152f * c.y + 0.0722f * c.z; };
+        const size_t n = out->lights.size();
+        std::vector<float> flux(n);
+        for (size_t i = 0; i < n; ++i) {
+            const LightD& L = out->lights[i];
+            if (L.kind == 2) {
+                // EnvironmentLight::approximateFlux (environmentLight.cpp:32-50, 125-139):
+                // sum of texel luminance x sin(theta) x 4 pi x R^2, R half the scene diagonal
+                const cgpu_texture& et = d->textures[L.tex];
+                float background = 0.0f;
+                for (int y = 0; y < et.height; ++y) {
+                    const float v = (float(y) + 0.5f) / float(et.height);
+                    const float st = std::sin((1.0f - v) * 3.1415926535897932f);
+                    for (int x = 0; x < et.width; ++x) {
+                        const float* t = et.texels + 3 * (size_t(y) * et.width + x);
+                        background += luminance(make_float3(t[0], t[1], t[2])) * st;
+                    }
+                }
+                float e2 = 0.0f;
+                for (int k = 0; k < 3; ++k) {
+                    const float e = out->info.bounds_max[k] - out->info.bounds_min[k];
+                    e2 += e * e;
+                }
+                const float R = std::sqrt(e2) * 0.5f;
+                flux[i] = background * 12.566370614359172f * R * R;
+            } else {
+                // SingleAreaLight::approximateFlux (singleAreaLight.cpp:170-187)
+                const float f = luminance(L.radiance) * L.area * 3.1415926535897932f;
+                flux[i] = f > 0.0f ? f : 1.0f;  // AreaLight::_defaultFlux
+            }
+        }
+        std::vector<float> cdf(n + 1);
+        const float delta = 1.0f / float(n);
+        cdf[0] = 0.0f;
+        for (size_t i = 1; i <= n; ++i) cdf[i] = cdf[i - 1] + flux[i - 1] * delta;
+        const float sum = cdf[n];
+        if (sum > 0.0f) {
+            const float inv = 1.0f / sum;
+            for (size_t i = 1; i <= n; ++i) cdf[i] *= inv;
+        } else {
+            for (size_t i = 1; i <= n; ++i) cdf[i] = float(i) * delta;
+        }
+        cdf[n] = 1.0f;
+        out->light_cdf = std::move(cdf);
+    }
     return CGPU_OK;
 }
 
@@ -331,6 +381,7 @@ SceneD host_view(HostScene& hs, const cgpu_scene_desc* d) {
     S.prim_normals = d->prim_normals;
     S.prim_uvws = d->prim_uvws;
     S.rect_frames = hs.rect_frames.data();
+    S.light_cdf = hs.light_cdf.empty() ? nullptr : hs.light_cdf.data();
     S.num_lights = int(hs.lights.size());
     S.env_light = hs.env_light;
     S.num_tris = int(hs.tris.size());

@@ -24,6 +24,7 @@ struct HostScene {
     std::vector<float> env_marg, env_cond;
     std::vector<TextureD> textures;  // texel pointers into the caller's desc
     std::vector<float> rect_frames;  // vB, eA, eB per rectangle
+    std::vector<float> light_cdf;    // power light cluster: num_lights + 1 CDF values; empty: uniform
     CameraD cam{};
     cgpu_scene_info info{};
     int wide_depth = 0;

@@ -99,6 +99,7 @@ struct SceneD {
     const float* prim_normals;  // 9 per primitive or null
     const float* prim_uvws;     // 9 per primitive or null
     const float* rect_frames;   // 9 per rectangle (vB, eA, eB), indexed by the rectangle index
+    const float* light_cdf;     // power light cluster: num_lights + 1 CDF values; null: uniform pick
     int num_lights;  // area lights + environment
     int env_light;   // index of the environment light, -1 if none
     int num_tris;

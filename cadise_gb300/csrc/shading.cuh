@@ -624,6 +624,30 @@ CG_D float light_pdfW(const LightD& l, const SurfaceD& si, float3 target) {
     return l.pdf_area * len2(target - si.P) / c;
 }
 
+// LightCluster::sampleOneLight: uniform (uniformLightCluster.cpp:15-24,
+// Random::nextIndex) or by flux (powerLightCluster.cpp:29-36: one draw,
+// Distribution1D::sampleDiscrete, distribution1D.cpp:83-94 / 115-125 - the
+// largest index whose CDF value is <= the draw, found here by bisection).
+CG_D int pick_light(const SceneD& S, Rng& rng, float* pdf) {
+    if (!S.light_cdf) {
+        *pdf = 1.0f / float(S.num_lights);
+        return rng.index(S.num_lights);
+    }
+    const float u = rng.next();
+    int lo = 0, hi = S.num_lights - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(S.light_cdf + mid) <= u) lo = mid; else hi = mid - 1;
+    }
+    *pdf = __ldg(S.light_cdf + lo + 1) - __ldg(S.light_cdf + lo);
+    return lo;
+}
+// LightCluster::evaluatePickLightPdf of light `li`
+CG_D float light_pick_pdf(const SceneD& S, int li) {
+    if (!S.light_cdf) return 1.0f / float(S.num_lights);
+    return __ldg(S.light_cdf + li + 1) - __ldg(S.light_cdf + li);
+}
+
 CG_D float mis_power(float a, float b) {  // TMis<POWER>::weight (tMis.h:21-47)
     const float a2 = a * a, b2 = b * b;
     return a2 / (a2 + b2);
@@ -661,8 +685,8 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
     if (si.light >= 0 && count_emission) p.emit = T * light_emittance(S.lights[si.light], si);
     if (!bsdf_is_specular(m.type)) {
         p.count_emission = 0;
-        const int li = rng.index(S.num_lights);
-        const float pick = 1.0f / float(S.num_lights);
+        float pick;
+        const int li = pick_light(S, rng, &pick);
         if (m.type != BSDF_ABSORBER) {
             const LightD& l = S.lights[li];
             const LightS ls = light_sample(S, l, si.P, rng);
@@ -719,7 +743,7 @@ CG_D float3 mis_resolve(const SceneD& S, const SurfaceD& hit, float3 origin, flo
     const float3 rad = light_emittance(l, hit);
     const float lp = light_pdfW(l, hit, origin);
     const float w = mis_power(pdf, lp);
-    const float pick = 1.0f / float(S.num_lights);
+    const float pick = light_pick_pdf(S, hit.light);
     if (x_out) *x_out = can_emit(l, hit.wi, hit.Ns) ? T * divs(divs(factor * w, pdf), pick) : splat3(0.0f);
     return T * divs(divs(rad * w * factor, pdf), pick);
 }
@@ -736,7 +760,7 @@ CG_D float3 mis_resolve_env(const SceneD& S, float3 dir, float3 T, float3 factor
     const LightD& l = S.lights[S.env_light];
     const float3 rad = env_radiance(S, dir);
     const float w = mis_power(pdf, env_pdfW(l, dir));
-    const float pick = 1.0f / float(S.num_lights);
+    const float pick = light_pick_pdf(S, S.env_light);
     if (x_out) *x_out = T * divs(divs(factor * w, pdf), pick);
     return T * divs(divs(rad * w * factor, pdf), pick);
 }

@@ -413,8 +413,10 @@ struct cgpu_crsd_scene {
             else if (b.cls == "light") light_block(b);
         }
         if (!film || !camera || !renderer) fail(CGPU_ERR_PARSE, "scene needs film, camera and renderer blocks");
-        if (cluster && find_str(*cluster, "type", "uniform") != "uniform")
-            fail(CGPU_ERR_UNSUPPORTED, "light cluster '" + find_str(*cluster, "type", "") + "' (uniform only)");
+        const std::string cluster_type = cluster ? find_str(*cluster, "type", "uniform") : "uniform";
+        if (cluster_type == "power") desc.light_cluster = CGPU_LIGHT_CLUSTER_POWER;
+        else if (cluster_type == "uniform") desc.light_cluster = CGPU_LIGHT_CLUSTER_UNIFORM;
+        else fail(CGPU_ERR_UNSUPPORTED, "light cluster '" + cluster_type + "' (uniform or power)");
         if (accel) {
             const std::string t = find_str(*accel, "type", "bvh");
             if (t != "bvh" && t != "bruteForce" && t != "kd-tree") fail(CGPU_ERR_UNSUPPORTED, "accelerator '" + t + "'");

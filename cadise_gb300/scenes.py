@@ -114,6 +114,8 @@ class SceneSpec:
     textures: List[ImageTexture] = field(default_factory=list)
     # name of an ImageTexture used as a latitude-longitude environment light
     environment: Optional[str] = None
+    # light selection: "uniform" (the reference's default) or "power"
+    light_cluster: str = "uniform"
 
     # ------------------------------------------------------------------ sizes
     def num_primitives(self) -> int:
@@ -166,7 +168,7 @@ class SceneSpec:
           "    [sampler string \"stratified\"]\n    [estimator string \"pt\"]\n"
           "    [max-depth int32 \"%d\"]\n}\n" % (self.spp, self.max_depth))
         w("accelerator {\n    [type string \"bvh\"]\n}\n")
-        w("light-cluster {\n    [type string \"uniform\"]\n}\n")
+        w("light-cluster {\n    [type string \"%s\"]\n}\n" % self.light_cluster)
         for m in self.materials:
             w("material {\n    [type string \"%s\"]\n    [name string \"%s\"]\n" % (m.type, m.name))
             if m.type == LAMBERT:
@@ -483,6 +485,15 @@ def diff_scene(width: int = 512, height: int = 512, spp: int = 32, max_depth: in
         s.primitives.append(Rectangle(name, "lightBase", (cx + h, 14.0, cz - h), (cx - h, 14.0, cz - h),
                                       (cx - h, 14.0, cz + h)))
         s.lights.append(AreaLight(name, col, _quad_light_watt(col, (2 * h) ** 2)))
+    return s
+
+
+def power_field(width: int = 48, height: int = 36, spp: int = 16, max_depth: int = 8, seed: int = 21) -> SceneSpec:
+    """Small icosphere field (glass, conductors, Lambert) under 6 quad lights
+    of log-uniform emission, lights picked by the power light cluster."""
+    s = icosphere_field(n_spheres=10, subdivision=2, n_lights=6, seed=seed, width=width, height=height, spp=spp,
+                        max_depth=max_depth, dielectric=GLASS, box=30.0, radius_range=(2.0, 6.0))
+    s.light_cluster = "power"
     return s
 
 

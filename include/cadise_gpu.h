@@ -138,7 +138,15 @@ typedef struct cgpu_scene_desc {
      * from infinity, 0 for none.  It joins the uniform light pick after the
      * area lights. */
     int32_t environment_texture;
+
+    /* Light selection (CRSD light-cluster block, lightClusterInstantiator.cpp:21-45):
+     * CGPU_LIGHT_CLUSTER_UNIFORM picks every light with the same probability
+     * (uniformLightCluster.cpp:15-24); CGPU_LIGHT_CLUSTER_POWER in proportion to
+     * its approximate flux, computed once at upload (powerLightCluster.cpp:9-48). */
+    int32_t light_cluster;
 } cgpu_scene_desc;
+
+enum { CGPU_LIGHT_CLUSTER_UNIFORM = 0, CGPU_LIGHT_CLUSTER_POWER = 1 };
 
 typedef struct cgpu_scene_info {
     uint32_t num_primitives;

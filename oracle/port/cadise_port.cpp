@@ -153,6 +153,9 @@ struct Scene {
     // environment light (no reference parity: see env* below)
     int envLight = -1, envTex = -1;
     std::vector<float> envMarg, envCond;
+    // power light cluster: Distribution1D CDF over the lights' approximate
+    // fluxes (powerLightCluster.cpp:9-27); empty for the uniform cluster
+    std::vector<float> lightCdf;
     V3 camPos, camX, camY, camZ;
     float sx = 0, sy = 0, tx = 0, ty = 0, offset = 0;
 };
@@ -860,6 +863,22 @@ float lightPdfW(const Scene& s, const Light& l, const Surface& si, const V3& tar
     return pdfA * emitVec.lengthSquared() / c;
 }
 
+// Scene::sampleOneLight through the light cluster: UniformLightCluster
+// (uniformLightCluster.cpp:15-24, Random::nextIndex) or PowerLightCluster
+// (powerLightCluster.cpp:29-36: Distribution1D::sampleDiscrete, whose
+// continuousToDiscrete scans the CDF from the top, distribution1D.cpp:115-125).
+std::size_t pickLight(const Scene& s, Rng& rng, float* pdf) {
+    if (s.lightCdf.empty()) {
+        *pdf = 1.0f / static_cast<float>(s.lights.size());
+        return rng.index(0, s.lights.size());
+    }
+    const float u = rng.next();
+    std::size_t i = s.lights.size() - 1;
+    while (i > 0 && !(s.lightCdf[i] <= u)) --i;
+    *pdf = s.lightCdf[i + 1] - s.lightCdf[i];
+    return i;
+}
+
 float misPower(float a, float b) {  // tMis.h:21-47
     const float a2 = a * a, b2 = b * b;
     return a2 / (a2 + b2);
@@ -933,8 +952,8 @@ V3 estimate(const Scene& s, Ray ray, Rng& rng) {
         }
         if (!isSpecular(m.type)) {
             countEmission = false;
-            const std::size_t li = rng.index(0, s.lights.size());
-            const float pick = 1.0f / static_cast<float>(s.lights.size());
+            float pick;
+            const std::size_t li = pickLight(s, rng, &pick);
             const V3 direct = directLight(s, si, m, static_cast<int>(li), rng) / pick;
             L += T * direct;
         } else {
@@ -1096,6 +1115,55 @@ Scene* create(const cgpu_scene_desc* d) {
         s->envLight = static_cast<int>(s->lights.size());
         s->lights.push_back(env);
     }
+    if (d->light_cluster == CGPU_LIGHT_CLUSTER_POWER) {
+        // approximate fluxes: SingleAreaLight::approximateFlux (singleAreaLight.cpp:170-187),
+        // luminance with the weights of rgbSpectrum.cpp:33-37; the sky as
+        // EnvironmentLight::approximateFlux (environmentLight.cpp:32-50, 125-139) with R
+        // half the diagonal of the primitives' bounds
+        auto luminance = [](const V3& c) { return 0.0126f * c.x + 0.7152f * c.y + 0.0722f * c.z; };
+        const std::size_t n = s->lights.size();
+        std::vector<float> flux(n);
+        for (std::size_t i = 0; i < n; ++i) {
+            const Light& L = s->lights[i];
+            if (static_cast<int>(i) == s->envLight) {
+                const Texture& t = s->textures[size_t(s->envTex)];
+                float background = 0.0f;
+                for (int y = 0; y < t.h; ++y) {
+                    const float v = (static_cast<float>(y) + 0.5f) / static_cast<float>(t.h);
+                    const float st = std::sin((1.0f - v) * kPi);
+                    for (int x = 0; x < t.w; ++x) {
+                        const float* p = &t.texels[3 * (size_t(y) * t.w + x)];
+                        background += luminance(V3(p[0], p[1], p[2])) * st;
+                    }
+                }
+                V3 lo(std::numeric_limits<float>::infinity()), hi(-std::numeric_limits<float>::infinity());
+                auto grow = [&](const V3& q) {
+                    for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], q[k]); hi[k] = std::max(hi[k], q[k]); }
+                };
+                for (const Triangle& tr : s->tris) { grow(tr.a); grow(tr.b); grow(tr.c); }
+                for (const Rectangle& r : s->rects) { grow(r.vA); grow(r.vB); grow(r.vC); grow(r.vD); }
+                const V3 e = hi - lo;
+                const float R = std::sqrt(e.x * e.x + e.y * e.y + e.z * e.z) * 0.5f;
+                flux[i] = background * 12.566370614359172f * R * R;
+            } else {
+                const float f = luminance(L.radiance) * lightArea(*s, L) * kPi;
+                flux[i] = f > 0.0f ? f : 1.0f;  // AreaLight::_defaultFlux (areaLight.cpp:30-32)
+            }
+        }
+        // Distribution1D (distribution1D.cpp:10-41)
+        std::vector<float>& cdf = s->lightCdf;
+        cdf.assign(n + 1, 0.0f);
+        const float delta = 1.0f / static_cast<float>(n);
+        for (std::size_t i = 1; i <= n; ++i) cdf[i] = cdf[i - 1] + flux[i - 1] * delta;
+        const float sum = cdf[n];
+        if (sum > 0.0f) {
+            const float inv = 1.0f / sum;
+            for (std::size_t i = 1; i <= n; ++i) cdf[i] *= inv;
+        } else {
+            for (std::size_t i = 1; i <= n; ++i) cdf[i] = static_cast<float>(i) * delta;
+        }
+        cdf[n] = 1.0f;
+    }
     std::vector<BuildItem> items(s->prims.size());
     for (std::size_t i = 0; i < s->prims.size(); ++i) {
         primBound(*s, static_cast<int>(i), &items[i].lo, &items[i].hi);
@@ -1239,8 +1307,9 @@ D3 estimateDual(const Scene& s, Ray ray, Rng& rng) {
             L = L + T * radianceDual(s, pr.light);
         if (!isSpecular(m.type)) {
             countEmission = false;
-            const std::size_t li = rng.index(0, s.lights.size());
-            const double pick = 1.0 / double(s.lights.size());
+            float pickf;
+            const std::size_t li = pickLight(s, rng, &pickf);
+            const double pick = s.lightCdf.empty() ? 1.0 / double(s.lights.size()) : double(pickf);
             if (m.type != CGPU_BSDF_ABSORBER) {
                 const Light& l = s.lights[li];
                 const LightSample ls = lightSample(s, l, si.P, rng);

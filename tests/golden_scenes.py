@@ -16,6 +16,7 @@ def specs():
                                         spp=16, max_depth=8, dielectric=scenes.GLASS, box=30.0,
                                         radius_range=(2.0, 6.0)),
         "features": scenes.feature_scene(),
+        "power": scenes.power_field(),
     }
 
 

@@ -88,7 +88,7 @@ class Host:
         self.L.khc_destroy(self.h)
 
 
-NAMES = ["cornell", "field", "features"]
+NAMES = ["cornell", "field", "features", "power"]
 
 
 @pytest.mark.parametrize("name", NAMES)
