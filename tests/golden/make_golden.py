@@ -50,7 +50,7 @@ def golden_scenes():
                                          height=36, spp=16, max_depth=8, dielectric=scenes.GLASS,
                                          box=30.0, radius_range=(2.0, 6.0)), 2048),
         "features": (scenes.feature_scene(), 32768),
-        "power": (scenes.power_field(), 8192),
+        "power": (scenes.power_field(), 131072),
     }
 
 
