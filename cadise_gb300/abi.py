@@ -18,12 +18,16 @@ from . import scenes as S
 
 CGPU_PRIM_TRIANGLE = 0
 CGPU_PRIM_RECTANGLE = 1
+CGPU_PRIM_SPHERE = 2
 
 CGPU_BSDF_LAMBERTIAN = 0
 CGPU_BSDF_CONDUCTOR_GGX = 1
 CGPU_BSDF_GLASS = 2
 CGPU_BSDF_ABSORBER = 3
 CGPU_BSDF_DIELECTRIC_GGX = 4
+CGPU_BSDF_MIRROR = 5
+CGPU_BSDF_PHONG = 6
+CGPU_BSDF_PLASTIC = 7
 
 CGPU_MODE_MEGAKERNEL = 0
 CGPU_MODE_WAVEFRONT = 1
@@ -34,6 +38,9 @@ BSDF_OF_TYPE = {
     S.GLASS: CGPU_BSDF_GLASS,
     S.ROUGH_DIELECTRIC: CGPU_BSDF_DIELECTRIC_GGX,
     "absorb": CGPU_BSDF_ABSORBER,
+    S.MIRROR: CGPU_BSDF_MIRROR,
+    S.PHONG: CGPU_BSDF_PHONG,
+    S.PLASTIC: CGPU_BSDF_PLASTIC,
 }
 
 STATUS_NAMES = {0: "CGPU_OK", 1: "CGPU_ERR_INVALID_ARGUMENT", 2: "CGPU_ERR_CUDA",
@@ -44,7 +51,8 @@ STATUS_NAMES = {0: "CGPU_OK", 1: "CGPU_ERR_INVALID_ARGUMENT", 2: "CGPU_ERR_CUDA"
 class cgpu_material(C.Structure):
     _fields_ = [("type", C.c_int32), ("albedo_texture", C.c_int32), ("albedo", C.c_float * 3),
                 ("f0", C.c_float * 3), ("roughness", C.c_float), ("ior_outer", C.c_float),
-                ("ior_inner", C.c_float), ("reserved", C.c_float)]
+                ("ior_inner", C.c_float), ("exponent", C.c_float), ("diffuse_ratio", C.c_float),
+                ("fresnel", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class cgpu_texture(C.Structure):
@@ -173,6 +181,12 @@ def flatten(spec: "S.SceneSpec") -> FlatScene:
             mat[i] = mat_index[p.material]
             names.setdefault(p.name, i)
             i += 1
+        elif isinstance(p, S.Sphere):
+            kind[i] = CGPU_PRIM_SPHERE
+            verts[i, :4] = np.array([*p.center, p.radius], dtype=np.float32)
+            mat[i] = mat_index[p.material]
+            names.setdefault(p.name, i)
+            i += 1
         else:
             m = p.positions.shape[0]
             kind[i:i + m] = CGPU_PRIM_TRIANGLE
@@ -194,6 +208,9 @@ def flatten(spec: "S.SceneSpec") -> FlatScene:
         mats[j].roughness = float(m.roughness)
         mats[j].ior_outer = float(m.ior_outer)
         mats[j].ior_inner = float(m.ior_inner)
+        mats[j].exponent = float(m.exponent)
+        mats[j].diffuse_ratio = float(m.diffuse_ratio)
+        mats[j].fresnel = 1 if m.fresnel == "dielectric" else 0
     lights = (cgpu_area_light * max(1, len(spec.lights)))()
     for j, lt in enumerate(spec.lights):
         lights[j].primitive = names[lt.primitive]

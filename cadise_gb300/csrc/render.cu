@@ -109,7 +109,7 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
     if (cont) {
         if (hitp) {
             w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
-            return S.materials[material_of_slot(S, hit.slot)].type;
+            return shade_queue(S.materials[material_of_slot(S, hit.slot)].type);
         }
         if (S.env_light >= 0) {
             const float4 tw = w.thr[p];

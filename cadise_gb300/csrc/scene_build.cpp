@@ -64,15 +64,19 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
     }
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const int t = d->materials[i].type;
-        if (t < 0 || t >= kNumBsdfKinds) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "unknown BSDF type");
+        if (t < 0 || t >= kNumBsdfTypes) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "unknown BSDF type");
         const int tex = d->materials[i].albedo_texture;
         if (tex >= int(d->num_textures)) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "texture index out of range");
     }
     uint32_t ntris = 0, nrects = 0;
     for (uint32_t i = 0; i < np; ++i) {
         const int k = d->prim_kind ? d->prim_kind[i] : CGPU_PRIM_TRIANGLE;
-        if (k != CGPU_PRIM_TRIANGLE && k != CGPU_PRIM_RECTANGLE)
+        if (k != CGPU_PRIM_TRIANGLE && k != CGPU_PRIM_RECTANGLE && k != CGPU_PRIM_SPHERE)
             return fail(err, CGPU_ERR_INVALID_ARGUMENT, "unknown primitive kind");
+        if (k == CGPU_PRIM_SPHERE && light_of[i] >= 0)
+            return fail(err, CGPU_ERR_UNSUPPORTED, "sphere light (the reference cannot sample sphere positions)");
+        if (k == CGPU_PRIM_SPHERE && !(d->prim_vertices[9 * size_t(i) + 3] > 0.0f))
+            return fail(err, CGPU_ERR_INVALID_ARGUMENT, "sphere radius must be positive");
         if (d->prim_material[i] < 0 || uint32_t(d->prim_material[i]) >= d->num_materials)
             return fail(err, CGPU_ERR_INVALID_ARGUMENT, "material index out of range");
         ntris += k == CGPU_PRIM_RECTANGLE ? 2 : 1;
@@ -90,7 +94,19 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
             if (k == CGPU_PRIM_TRIANGLE) {
                 std::memcpy(&tv[9 * size_t(t)], v, 9 * sizeof(float));
                 tprim[t] = i;
-                tflags[t] = 0;
+                tflags[t] = kRecTriangle;
+                ++t;
+            } else if (k == CGPU_PRIM_SPHERE) {
+                // the build sees the sphere's box as a degenerate "triangle" (lo, hi, lo),
+                // widened by a few ulps of its coordinates
+                const float r = v[3];
+                for (int a = 0; a < 3; ++a) {
+                    const float pad = 1e-5f * (std::fabs(v[a]) + r);
+                    tv[9 * size_t(t) + a] = tv[9 * size_t(t) + 6 + a] = v[a] - r - pad;
+                    tv[9 * size_t(t) + 3 + a] = v[a] + r + pad;
+                }
+                tprim[t] = i;
+                tflags[t] = kRecSphere;
                 ++t;
             } else {
                 // rectangle v1 v2 v3 = vA vB vC; eA = vA - vB, eB = vC - vB, vD = vB + eA + eB
@@ -106,7 +122,7 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
                         tv[9 * size_t(t) + 3 * j + 2] = hv[j].z;
                     }
                     tprim[t] = i;
-                    tflags[t] = 1u | (r << 1);
+                    tflags[t] = kRecRectHalf | (r << 2);
                     ++t;
                 }
                 float* fr = &rect_frames[9 * size_t(r)];
@@ -133,9 +149,16 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         const uint32_t mat = uint32_t(d->prim_material[prim]);
         const uint32_t packed = mat | (uint32_t(light_of[prim] + 1) << 16);
         TriRecord& R = recs[s];
-        R.v0 = make_float4(v[0], v[1], v[2], 0.0f);
-        R.v1 = make_float4(v[3], v[4], v[5], 0.0f);
-        R.v2 = make_float4(v[6], v[7], v[8], 0.0f);
+        if (tflags[t] == kRecSphere) {
+            const float* c = d->prim_vertices + 9 * size_t(prim);
+            R.v0 = make_float4(c[0], c[1], c[2], 0.0f);
+            R.v1 = make_float4(c[3], 0.0f, 0.0f, 0.0f);
+            R.v2 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else {
+            R.v0 = make_float4(v[0], v[1], v[2], 0.0f);
+            R.v1 = make_float4(v[3], v[4], v[5], 0.0f);
+            R.v2 = make_float4(v[6], v[7], v[8], 0.0f);
+        }
         std::memcpy(&R.v0.w, &prim, 4);
         std::memcpy(&R.v1.w, &packed, 4);
         std::memcpy(&R.v2.w, &tflags[t], 4);
@@ -155,6 +178,10 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         M.f0 = make_float3(m.f0[0], m.f0[1], m.f0[2]);
         M.ior_outer = m.ior_outer;
         M.ior_inner = m.ior_inner;
+        M.exponent = m.exponent;
+        M.ratio = m.diffuse_ratio;
+        M.fresnel = m.fresnel;
+        M.pad = 0;
     }
     // ---- lights (singleAreaLight.cpp:20-37)
     std::vector<LightD> lights(d->num_lights);

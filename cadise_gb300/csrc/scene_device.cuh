@@ -39,12 +39,31 @@ constexpr int kStackSize = 96;
 struct __align__(16) TriRecord {
     float4 v0;  // xyz = vertex A, w = primitive index (int bits)
     float4 v1;  // xyz = vertex B, w = (material index) | ((light index + 1) << 16)
-    float4 v2;  // xyz = vertex C, w = flags (bit 0: half of a rectangle, bits 1..31: rectangle index)
+    float4 v2;  // xyz = vertex C, w = flags (kRec* kind in bits 0-1, rectangle index in bits 2-31)
+    // a sphere: v0.xyz = centre, v1.x = radius
 };
 static_assert(sizeof(TriRecord) == 48, "TriRecord is 48 bytes");
 
-enum : int { BSDF_LAMBERTIAN = 0, BSDF_CONDUCTOR = 1, BSDF_GLASS = 2, BSDF_ABSORBER = 3, BSDF_DIELECTRIC_GGX = 4 };
+enum : int {
+    BSDF_LAMBERTIAN = 0,
+    BSDF_CONDUCTOR = 1,
+    BSDF_GLASS = 2,
+    BSDF_ABSORBER = 3,
+    BSDF_DIELECTRIC_GGX = 4,
+    BSDF_MIRROR = 5,
+    BSDF_PHONG = 6,
+    BSDF_PLASTIC = 7
+};
+constexpr int kNumBsdfTypes = 8;
+// Shade queues (one shade kernel each): materials that cost alike share one.
 constexpr int kNumBsdfKinds = 5;
+CG_HD int shade_queue(int type) {
+    return type == BSDF_MIRROR ? BSDF_GLASS : (type == BSDF_PHONG || type == BSDF_PLASTIC) ? BSDF_LAMBERTIAN : type;
+}
+
+// Record flags (TriRecord::v2.w): bits 0-1 the kind, bits 2-31 the
+// rectangle index of a rectangle half.
+constexpr uint32_t kRecTriangle = 0u, kRecRectHalf = 1u, kRecSphere = 2u;
 
 struct __align__(16) MaterialD {
     int type;
@@ -55,6 +74,10 @@ struct __align__(16) MaterialD {
     float ior_outer;
     float3 f0;
     float ior_inner;
+    float exponent;   // phong / plastic specular exponent
+    float ratio;      // plastic diffuse ratio
+    int fresnel;      // mirror: 0 conductor (f0), 1 dielectric (iors)
+    int pad;
 };
 
 struct __align__(16) LightD {

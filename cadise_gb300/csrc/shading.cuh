@@ -46,6 +46,16 @@ CG_D void stratum_jitter(int spp, uint32_t s, Rng& rng, float* jx, float* jy) {
     }
 }
 
+// SphericalMapper::mappingToUvw (sphericalMapper.cpp:14-28): y up,
+// phi = atan2(x, z), u = phi / 2 pi, v = (pi - theta) / pi.
+CG_D float3 env_uvw(float3 d) {
+    const float3 n = normalize(d);
+    const float theta = acosf(fminf(fmaxf(n.y, -1.0f), 1.0f));
+    float phi = atan2f(n.x, n.z);
+    if (phi < 0.0f) phi += 2.0f * kPi;
+    return mk(phi * 0.1591549430918953f, (kPi - theta) * kInvPi, 0.0f);
+}
+
 // ----------------------------------------------------------------- surface --
 struct SurfaceD {
     float3 P, Ng, Ns, uvw, wi;
@@ -96,7 +106,8 @@ struct HitPoint {
     float3 P;
     float b0, b1, b2;  // triangle barycentrics (b1 of B, b2 of C)
     float p1, p2;      // rectangle coordinates
-    int rect;          // rectangle index, -1 for a triangle
+    int rect;          // rectangle index, -1 for a triangle or a sphere
+    int sphere;        // 1 for a sphere (its t is the traversal's, already the reference's)
 };
 
 CG_D void rect_frame(const SceneD& S, int rect, float3* vB, float3* eA, float3* eB) {
@@ -111,8 +122,16 @@ CG_D HitPoint hit_point(const SceneD& S, float3 o, float3 d, const HitD& h) {
     const float4* tp = reinterpret_cast<const float4*>(S.tris + h.slot);
     const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
     const uint32_t flags = __float_as_uint(c.w);
-    if (flags & 1u) {
-        hp.rect = int(flags >> 1);
+    hp.sphere = (flags & 3u) == kRecSphere;
+    if (hp.sphere) {
+        hp.rect = -1;
+        hp.t = h.t;
+        hp.P = o + d * hp.t;
+        hp.b0 = hp.b1 = hp.b2 = hp.p1 = hp.p2 = 0.0f;
+        return hp;
+    }
+    if ((flags & 3u) == kRecRectHalf) {
+        hp.rect = int(flags >> 2);
         float3 vB, eA, eB;
         rect_frame(S, hp.rect, &vB, &eA, &eB);
         hp.t = ref_rect_t(o, d, vB, eA, eB, h.t);
@@ -156,6 +175,15 @@ CG_D SurfaceD surface_at(const SceneD& S, float3 o, float3 d, const HitD& h) {
     const HitPoint hp = hit_point(S, o, d, h);
     si.P = hp.P;
     si.wi = -d;
+    if (hp.sphere) {
+        // Sphere::evaluateSurfaceDetail (sphere.cpp:106-135): the normal from
+        // the centre, uvw from SphericalMapper (sphericalMapper.cpp:14-28)
+        const float3 N = normalize(hp.P - f3(a));
+        si.Ng = N;
+        si.Ns = N;
+        si.uvw = env_uvw(N);
+        return si;
+    }
     if (hp.rect >= 0) {
         // normal and uvw from the rectangle's own frame; the uvw is the
         // bilinear blend of the corner uvws (1,0) (0,0) (0,1) (1,1) as the
@@ -267,7 +295,39 @@ CG_D bool refract_dir(float3 v, float3 n, float etaI, float etaT, float3* out) {
 }
 
 // -------------------------------------------------------------------- BSDF --
-CG_HD bool bsdf_is_specular(int type) { return type == BSDF_GLASS; }
+// A BSDF with a specular lobe: no next-event estimation at its vertices
+// (ptEstimator.cpp:64-72 tests the lobes for SPECULAR_REFLECTION / _TRANSMISSION).
+CG_HD bool bsdf_is_specular(int type) { return type == BSDF_GLASS || type == BSDF_MIRROR; }
+
+// PhongBsdf (phongBsdf.cpp:14-98): pow(max(R.V, 0), e) with R = L.reflect(Ns),
+// value factor (e + 2) / 2 pi, pdf factor (e + 1) / 2 pi.  Zero when V and L
+// are on different sides.
+CG_D float phong_power(const MaterialD& m, float3 V, float3 L, float3 N) {
+    if (dot(V, N) * dot(L, N) <= 0.0f) return -1.0f;
+    const float3 R = reflect(L, N);
+    const float RdotV = fmaxf(dot(R, V), 0.0f);
+    return powf(RdotV, m.exponent);
+}
+CG_D float phong_value_factor(const MaterialD& m) { return (m.exponent + 2.0f) * 0.1591549430918953f; }
+CG_D float phong_pdf_factor(const MaterialD& m) { return (m.exponent + 1.0f) * 0.1591549430918953f; }
+
+// LambertianDiffuse::evaluate / evaluatePdfW (lambertianDiffuse.cpp:27-44, 83-96)
+CG_D float3 lambert_eval(const SceneD& S, const MaterialD& m, const SurfaceD& si, float3 L) {
+    if (dot(si.wi, si.Ns) * dot(L, si.Ns) <= 0.0f) return splat3(0.0f);
+    return albedo_of(S, m, si.uvw) * kInvPi;
+}
+CG_D float lambert_pdf(const SurfaceD& si, float3 L) {
+    if (dot(si.wi, si.Ns) * dot(L, si.Ns) <= 0.0f) return 0.0f;
+    return absdot(L, si.Ns) * kInvPi;
+}
+CG_D float3 phong_eval(const MaterialD& m, const SurfaceD& si, float3 L) {
+    const float p = phong_power(m, si.wi, L, si.Ns);
+    return splat3(p < 0.0f ? 0.0f : p * phong_value_factor(m));
+}
+CG_D float phong_pdf(const MaterialD& m, const SurfaceD& si, float3 L) {
+    const float p = phong_power(m, si.wi, L, si.Ns);
+    return p < 0.0f ? 0.0f : p * phong_pdf_factor(m);
+}
 
 // Rough dielectric (no reference counterpart): GGX BRDF + BTDF of Walter,
 // Marschner, Li & Torrance, "Microfacet Models for Refraction through Rough
@@ -339,7 +399,11 @@ CG_D float3 bsdf_eval(const SceneD& S, const MaterialD& m, const SurfaceD& si, f
         rough_dielectric_eval(m, albedo_of(S, m, si.uvw), V, L, N, &f, &pdf);
         return f;
     }
-    return splat3(0.0f);
+    if (m.type == BSDF_PHONG) return phong_eval(m, si, L);
+    if (m.type == BSDF_PLASTIC) {  // MixedBsdf::evaluate (mixedBsdf.cpp:33-57), A Lambert, B Phong
+        return lambert_eval(S, m, si, L) * m.ratio + phong_eval(m, si, L) * (1.0f - m.ratio);
+    }
+    return splat3(0.0f);  // glass, mirror, absorber: no non-delta part
 }
 
 // Bsdf::evaluatePdfW (lambertianDiffuse.cpp:83-96, conductorMicrofacet.cpp:126-163)
@@ -365,6 +429,11 @@ CG_D float bsdf_pdf(const SceneD& S, const MaterialD& m, const SurfaceD& si, flo
         rough_dielectric_eval(m, splat3(1.0f), V, L, N, &f, &pdf);
         return pdf;
     }
+    if (m.type == BSDF_PHONG) return phong_pdf(m, si, L);
+    if (m.type == BSDF_PLASTIC) {  // MixedBsdf::evaluatePdfW (mixedBsdf.cpp:157-185)
+        const float avg = (m.ratio + m.ratio + m.ratio) / 3.0f;
+        return lambert_pdf(si, L) * avg + phong_pdf(m, si, L) * (1.0f - avg);
+    }
     return 0.0f;
 }
 
@@ -374,6 +443,56 @@ struct BsdfS {
     CG_D bool valid() const { return !is_zero(f) && pdf > 0.0f; }  // bsdfSample.cpp:39-41
 };
 
+// LambertianDiffuse::evaluateSample (lambertianDiffuse.cpp:46-81) with
+// Hemisphere::cosineWeightedSampling (hemisphere.cpp:30-48):
+// theta = acos(1 - 2 u1) / 2, i.e. cos(theta) = sqrt(1 - u1)
+CG_D BsdfS lambert_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, Rng& rng) {
+    BsdfS out;
+    const float3 N = si.Ns, V = si.wi;
+    float3 z, x;
+    frame_from_y(N, &z, &x);
+    float u0, u1;
+    rng.next2(&u0, &u1);
+    float sp, cp;
+    sincospif(2.0f * u0, &sp, &cp);
+    const float c = sqrtf(1.0f - u1);
+    const float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
+    float3 L = x * (sp * s) + N * c + z * (cp * s);
+    L = normalize(L);
+    if (dot(V, N) <= 0.0f) L = -L;
+    out.f = albedo_of(S, m, si.uvw) * kInvPi;
+    out.L = L;
+    out.pdf = c * kInvPi;
+    return out;
+}
+
+// PhongBsdf::evaluateSample (phongBsdf.cpp:38-81) with
+// Hemisphere::cosineExpWeightedSampling (hemisphere.cpp:50-69): the lobe
+// sampled around the shading normal, its value and pdf evaluated around the
+// mirror direction, as the reference does.
+CG_D BsdfS phong_sample(const MaterialD& m, const SurfaceD& si, Rng& rng) {
+    BsdfS out;
+    out.f = splat3(0.0f);
+    out.L = mk(0.0f, 1.0f, 0.0f);
+    out.pdf = 0.0f;
+    const float3 N = si.Ns, V = si.wi;
+    float3 z, x;
+    frame_from_y(N, &z, &x);
+    float u0, u1;
+    rng.next2(&u0, &u1);
+    float sp, cp;
+    sincospif(2.0f * u0, &sp, &cp);
+    const float c = powf(u1, 1.0f / (m.exponent + 1.0f));
+    const float s = sqrtf(1.0f - c * c);
+    const float3 L = normalize(x * (sp * s) + N * c + z * (cp * s));
+    const float p = phong_power(m, V, L, N);
+    if (p < 0.0f) return out;
+    out.f = splat3(p * phong_value_factor(m));
+    out.L = L;
+    out.pdf = p * phong_pdf_factor(m);
+    return out;
+}
+
 // Bsdf::evaluateSample (lambertianDiffuse.cpp:46-81, conductorMicrofacet.cpp:68-124,
 // specularDielectric.cpp:35-127)
 CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, Rng& rng) {
@@ -382,23 +501,41 @@ CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, 
     out.L = mk(0.0f, 1.0f, 0.0f);
     out.pdf = 0.0f;
     const float3 N = si.Ns, V = si.wi;
-    if (m.type == BSDF_LAMBERTIAN) {
-        float3 z, x;
-        frame_from_y(N, &z, &x);
-        float u0, u1;
-        rng.next2(&u0, &u1);
-        // Hemisphere::cosineWeightedSampling (hemisphere.cpp:30-48):
-        // theta = acos(1 - 2 u1) / 2, i.e. cos(theta) = sqrt(1 - u1)
-        float sp, cp;
-        sincospif(2.0f * u0, &sp, &cp);
-        const float c = sqrtf(1.0f - u1);
-        const float s = sqrtf(fmaxf(0.0f, 1.0f - c * c));
-        float3 L = x * (sp * s) + N * c + z * (cp * s);
-        L = normalize(L);
-        if (dot(V, N) <= 0.0f) L = -L;
-        out.f = albedo_of(S, m, si.uvw) * kInvPi;
+    if (m.type == BSDF_LAMBERTIAN) return lambert_sample(S, m, si, rng);
+    if (m.type == BSDF_PHONG) return phong_sample(m, si, rng);
+    if (m.type == BSDF_PLASTIC) {
+        // MixedBsdf::evaluateSample (mixedBsdf.cpp:59-155): one draw picks the
+        // lobe by the average ratio; the other lobe is evaluated at the
+        // sampled direction.  When Phong (B) is sampled the reference weights
+        // its value by the ratio and Lambert's by its complement, as written
+        // there (mixedBsdf.cpp:123-128); so does this.
+        const float avg = (m.ratio + m.ratio + m.ratio) / 3.0f;
+        const float u = rng.next();
+        if (u < avg) {
+            const BsdfS a = lambert_sample(S, m, si, rng);
+            if (!a.valid()) return out;
+            out.L = a.L;
+            out.f = a.f * m.ratio + phong_eval(m, si, a.L) * (1.0f - m.ratio);
+            out.pdf = avg * a.pdf + (1.0f - avg) * phong_pdf(m, si, a.L);
+        } else {
+            const BsdfS b = phong_sample(m, si, rng);
+            if (!b.valid()) return out;
+            out.L = b.L;
+            out.f = b.f * m.ratio + lambert_eval(S, m, si, b.L) * (1.0f - m.ratio);
+            out.pdf = avg * b.pdf + (1.0f - avg) * lambert_pdf(si, b.L);
+        }
+        return out;
+    }
+    if (m.type == BSDF_MIRROR) {
+        // SpecularReflection::evaluateSample (specularReflection.cpp:32-57), pdf 1
+        const float VdotN = dot(V, N);
+        const float3 L = reflect(V, N * (VdotN > 0.0f ? 1.0f : -1.0f));
+        const float LdotN = dot(L, N);
+        const float3 R = m.fresnel == 0 ? schlick(m.f0, LdotN)
+                                        : splat3(fresnel_dielectric(m.ior_outer, m.ior_inner, LdotN));
+        out.f = divs(R * albedo_of(S, m, si.uvw), fabsf(LdotN));
         out.L = L;
-        out.pdf = c * kInvPi;
+        out.pdf = 1.0f;
         return out;
     }
     if (m.type == BSDF_CONDUCTOR) {
@@ -506,13 +643,6 @@ CG_D float3 env_dir(float u, float v) {
     sincospif(1.0f - v, &st, &ct);
     (void)theta;
     return mk(st * sp, ct, st * cp);
-}
-CG_D float3 env_uvw(float3 d) {
-    const float3 n = normalize(d);
-    const float theta = acosf(fminf(fmaxf(n.y, -1.0f), 1.0f));
-    float phi = atan2f(n.x, n.z);
-    if (phi < 0.0f) phi += 2.0f * kPi;
-    return mk(phi * (0.5f / kPi), (kPi - theta) * kInvPi, 0.0f);
 }
 CG_D int cdf_find(const float* cdf, int n, float u) {
     int lo = 0, hi = n - 1;  // largest i with cdf[i] <= u, in [0, n-1]

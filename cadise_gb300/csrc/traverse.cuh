@@ -190,7 +190,32 @@ CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcu
     return nearest;
 }
 
-// Tests the triangles of leaf `e`; returns true when an any-hit query is
+// Sphere::isIntersecting / isOccluded (sphere.cpp:43-104): the root pair of
+// Haines et al., "Precision Improvements for Ray/Sphere Intersection" (Ray
+// Tracing Gems 2019) - t0 = c / q, t1 = q - and _isSolutionValid's choice
+// (sphere.cpp:150-170), in the reference's FP32 order; the traversal's t is
+// the reference's t.
+CG_D bool sphere_test(const RayPre& r, float3 G, float rad, float tmax, float* tout) {
+    const float3 f = r.o - G;
+    const float b = -dot(f, r.d);
+    const float3 l = f + r.d * b;
+    const float disc = rad * rad - absdot(l, l);
+    if (disc < 0.0f) return false;
+    const float signB = b > 0.0f ? 1.0f : -1.0f;
+    const float q = b + signB * sqrtf(disc);
+    const float c = absdot(f, f) - rad * rad;
+    const float t0 = c / q, t1 = q;
+    if (t0 > tmax || t1 < r.tmin) return false;
+    float t = t0;
+    if (t < r.tmin) {
+        t = t1;
+        if (t > tmax) return false;
+    }
+    *tout = t;
+    return true;
+}
+
+// Tests the primitives of leaf `e`; returns true when an any-hit query is
 // answered (the hit is in slot / tcur).
 template <bool ANY, bool COUNT>
 CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, int& hslot, float& hu, float& hv,
@@ -200,10 +225,12 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
         const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
         const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
         if (COUNT) cnt->tris++;
-        float t, u, v;
+        float t, u = 0.0f, v = 0.0f;
         // closest hit: a bound one rounding wider than tcur, so that every
         // triangle whose t rounds to <= tcur reaches closer_hit
-        if (tri_test(r, f3(a), f3(b), f3(c), ANY ? tcur : tcur * 1.00000036f, &t, &u, &v)) {
+        const bool sphere = (__float_as_uint(c.w) & 3u) == kRecSphere;
+        if (sphere ? sphere_test(r, f3(a), b.x, tcur, &t)
+                   : tri_test(r, f3(a), f3(b), f3(c), ANY ? tcur : tcur * 1.00000036f, &t, &u, &v)) {
             const int slot = int(first + k);
             if (ANY) {
                 hslot = slot;

@@ -276,6 +276,29 @@ struct cgpu_crsd_scene {
             m.roughness = roughness_of(b);
         } else if (type == "absorb") {
             m.type = CGPU_BSDF_ABSORBER;
+        } else if (type == "mirror") {  // bsdfInstantiator.cpp:38-64
+            m.type = CGPU_BSDF_MIRROR;
+            albedo_of(b, "albedo", &m);
+            const std::string fr = find_str(b, "fresnel-type", "conductor");
+            if (fr == "conductor") {
+                m.fresnel = CGPU_FRESNEL_CONDUCTOR;
+                const V3f f0 = find_vec3(b, "f0", V3f{1, 1, 1});
+                m.f0[0] = f0.x; m.f0[1] = f0.y; m.f0[2] = f0.z;
+            } else if (fr == "dielectric") {
+                m.fresnel = CGPU_FRESNEL_DIELECTRIC;
+                m.ior_outer = find_real(b, "ior-outer", 1.0f);
+                m.ior_inner = find_real(b, "ior-inner", 1.5f);
+            } else {
+                fail(CGPU_ERR_UNSUPPORTED, "mirror fresnel type '" + fr + "'");
+            }
+        } else if (type == "phong") {  // bsdfInstantiator.cpp:94-102
+            m.type = CGPU_BSDF_PHONG;
+            m.exponent = find_real(b, "exponent", 32.0f);
+        } else if (type == "plastic") {  // bsdfInstantiator.cpp:104-116
+            m.type = CGPU_BSDF_PLASTIC;
+            albedo_of(b, "diffuse-albedo", &m);
+            m.exponent = find_real(b, "specular-exponent", 32.0f);
+            m.diffuse_ratio = find_real(b, "diffuse-ratio", 0.7f);
         } else {
             fail(CGPU_ERR_UNSUPPORTED, "material type '" + type + "'");
         }
@@ -360,8 +383,10 @@ struct cgpu_crsd_scene {
             for (size_t t = 0; t < nt; ++t)
                 add_prim(CGPU_PRIM_TRIANGLE, &pos[9 * t], mat, nrm.empty() ? nullptr : &nrm[9 * t],
                          uvw.empty() ? nullptr : &uvw[9 * t]);
-        } else if (type == "sphere") {
-            fail(CGPU_ERR_UNSUPPORTED, "analytic sphere primitives (tessellate to a triangle-mesh)");
+        } else if (type == "sphere") {  // primitiveInstantiator.cpp:17-28
+            const V3f c = find_vec3(b, "center", V3f{});
+            const float v[9] = {c.x, c.y, c.z, find_real(b, "radius", 0.0f), 0, 0, 0, 0, 0};
+            add_prim(CGPU_PRIM_SPHERE, v, material_for(b, false), nullptr, nullptr);
         } else {
             fail(CGPU_ERR_UNSUPPORTED, "primitive type '" + type + "'");
         }

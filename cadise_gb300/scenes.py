@@ -39,6 +39,9 @@ GLASS = "glass"
 # Rough (GGX) dielectric after Walter et al. 2007.  The reference has no rough
 # dielectric, so this type exists only in this library.
 ROUGH_DIELECTRIC = "dielectric-microfacet"
+MIRROR = "mirror"
+PHONG = "phong"
+PLASTIC = "plastic"
 
 
 @dataclass
@@ -51,6 +54,9 @@ class Material:
     ior_outer: float = 1.0
     ior_inner: float = 1.5
     albedo_texture: Optional[str] = None  # name of a texture-spectrum block
+    exponent: float = 32.0            # phong "exponent", plastic "specular-exponent"
+    diffuse_ratio: float = 0.7        # plastic "diffuse-ratio"
+    fresnel: str = "conductor"        # mirror "fresnel-type": conductor (f0) or dielectric (iors)
 
 
 @dataclass
@@ -70,6 +76,14 @@ class Triangle:
     v1: tuple
     v2: tuple
     v3: tuple
+
+
+@dataclass
+class Sphere:
+    name: str
+    material: str
+    center: tuple
+    radius: float
 
 
 @dataclass
@@ -123,7 +137,7 @@ class SceneSpec:
         mesh triangle), i.e. the length of its intersector list."""
         n = 0
         for p in self.primitives:
-            n += 1 if isinstance(p, (Rectangle, Triangle)) else int(p.positions.shape[0])
+            n += 1 if isinstance(p, (Rectangle, Triangle, Sphere)) else int(p.positions.shape[0])
         return n
 
     def num_triangles(self) -> int:
@@ -184,6 +198,17 @@ class SceneSpec:
                   % (v3(m.albedo), m.ior_outer, m.ior_inner))
                 if m.type == ROUGH_DIELECTRIC:
                     w("    [roughness real \"%.9g\"]\n" % m.roughness)
+            elif m.type == MIRROR:
+                w("    [albedo rgb \"%s\"]\n    [fresnel-type string \"%s\"]\n" % (v3(m.albedo), m.fresnel))
+                if m.fresnel == "conductor":
+                    w("    [f0 rgb \"%s\"]\n" % v3(m.f0))
+                else:
+                    w("    [ior-outer real \"%.9g\"]\n    [ior-inner real \"%.9g\"]\n" % (m.ior_outer, m.ior_inner))
+            elif m.type == PHONG:
+                w("    [exponent real \"%.9g\"]\n" % m.exponent)
+            elif m.type == PLASTIC:
+                w("    [diffuse-albedo rgb \"%s\"]\n    [specular-exponent real \"%.9g\"]\n"
+                  "    [diffuse-ratio real \"%.9g\"]\n" % (v3(m.albedo), m.exponent, m.diffuse_ratio))
             w("}\n")
         for p in self.primitives:
             if isinstance(p, Triangle):
@@ -194,6 +219,10 @@ class SceneSpec:
                 w("primitive {\n    [type string \"rectangle\"]\n    [name string \"%s\"]\n"
                   "    [bsdf material \"%s\"]\n    [v1 vector3r \"%s\"]\n    [v2 vector3r \"%s\"]\n"
                   "    [v3 vector3r \"%s\"]\n}\n" % (p.name, p.material, v3(p.v1), v3(p.v2), v3(p.v3)))
+            elif isinstance(p, Sphere):
+                w("primitive {\n    [type string \"sphere\"]\n    [name string \"%s\"]\n"
+                  "    [bsdf material \"%s\"]\n    [center vector3r \"%s\"]\n    [radius real \"%.9g\"]\n}\n"
+                  % (p.name, p.material, v3(p.center), p.radius))
             elif sidecar is not None and p.positions.shape[0] >= sidecar[2]:
                 import os
                 base, stem, _ = sidecar
@@ -485,6 +514,44 @@ def diff_scene(width: int = 512, height: int = 512, spp: int = 32, max_depth: in
         s.primitives.append(Rectangle(name, "lightBase", (cx + h, 14.0, cz - h), (cx - h, 14.0, cz - h),
                                       (cx - h, 14.0, cz + h)))
         s.lights.append(AreaLight(name, col, _quad_light_watt(col, (2 * h) ** 2)))
+    return s
+
+
+def sphere_box(width: int = 64, height: int = 48, spp: int = 16, max_depth: int = 8) -> SceneSpec:
+    """Open-front box of rectangles with analytic spheres in every non-GGX
+    material the reference has besides Lambert: plastic (Lambert + Phong mix),
+    Phong, mirror with a conductor and with a dielectric Fresnel term, a
+    smooth conductor, and glass; one rectangular ceiling light."""
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth, cam_position=(280.0, 270.0, 780.0),
+                  cam_direction=(0.0, 0.0, -1.0), cam_up=(0.0, 1.0, 0.0), fov=50.0)
+    s.materials = [
+        Material("white", LAMBERT, albedo=(0.72, 0.72, 0.70)),
+        Material("red", LAMBERT, albedo=(0.70, 0.28, 0.25)),
+        Material("blue", LAMBERT, albedo=(0.25, 0.30, 0.72)),
+        Material("plastic", PLASTIC, albedo=(0.70, 0.55, 0.05), exponent=16.0, diffuse_ratio=0.8),
+        Material("phong", PHONG, exponent=24.0),
+        Material("chrome", MIRROR, albedo=(0.95, 0.95, 0.95), fresnel="conductor", f0=(0.9, 0.85, 0.8)),
+        Material("glassMirror", MIRROR, albedo=(1.0, 1.0, 1.0), fresnel="dielectric", ior_outer=1.0,
+                 ior_inner=1.6),
+        Material("steel", CONDUCTOR, roughness=0.0, f0=(1.0, 1.0, 1.0)),
+        Material("glass", GLASS, albedo=(1.0, 1.0, 1.0), ior_outer=1.0, ior_inner=1.5),
+    ]
+    W, H, D = 560.0, 550.0, -650.0
+    s.primitives = [
+        Rectangle("left", "red", (-80.0, 0.0, D), (-80.0, 0.0, 0.0), (-80.0, H, 0.0)),
+        Rectangle("right", "blue", (640.0, 0.0, 0.0), (640.0, 0.0, D), (640.0, H, D)),
+        Rectangle("top", "white", (645.0, H, 0.0), (-85.0, H, 0.0), (-85.0, H, D)),
+        Rectangle("back", "white", (-85.0, H, D), (645.0, H, D), (645.0, 0.0, D)),
+        Rectangle("floor", "white", (645.0, 0.0, 0.0), (-85.0, 0.0, 0.0), (-85.0, 0.0, D)),
+        Sphere("plasticBall", "plastic", (100.0, 100.0, -360.0), 100.0),
+        Sphere("steelBall", "steel", (420.0, 110.0, -220.0), 110.0),
+        Sphere("phongBall", "phong", (300.0, 60.0, -470.0), 60.0),
+        Sphere("chromeBall", "chrome", (520.0, 300.0, -520.0), 70.0),
+        Sphere("mirrorBall", "glassMirror", (60.0, 330.0, -560.0), 55.0),
+        Sphere("glassBall", "glass", (250.0, 260.0, -300.0), 45.0),
+        Rectangle("light", "white", (370.0, H - 10.0, -170.0), (370.0, H - 10.0, -330.0), (185.0, H - 10.0, -330.0)),
+    ]
+    s.lights = [AreaLight("light", (1.0, 1.0, 1.0), 5.0e6)]
     return s
 
 

@@ -66,8 +66,11 @@ typedef struct cgpu_ctx cgpu_ctx;
 
 /* ---------------------------------------------------------------- scene -- */
 
-/* Primitive kinds, one per reference intersector (primitiveInstantiator.cpp:92-129). */
-enum { CGPU_PRIM_TRIANGLE = 0, CGPU_PRIM_RECTANGLE = 1 };
+/* Primitive kinds, one per reference intersector (primitiveInstantiator.cpp:92-129).
+ * A sphere (sphere.cpp) stores centre and radius in the first 4 of its 9 vertex
+ * floats; spheres cannot emit (the reference leaves their position sampling
+ * unimplemented, sphere.cpp:137-141). */
+enum { CGPU_PRIM_TRIANGLE = 0, CGPU_PRIM_RECTANGLE = 1, CGPU_PRIM_SPHERE = 2 };
 
 /* BSDF kinds keyed like the reference's CRSD material types (bsdfInstantiator.cpp:177-221). */
 enum {
@@ -75,18 +78,27 @@ enum {
     CGPU_BSDF_CONDUCTOR_GGX = 1,    /* "conductor-microfacet"  conductorMicrofacet.cpp      */
     CGPU_BSDF_GLASS = 2,            /* "glass"                 specularDielectric.cpp       */
     CGPU_BSDF_ABSORBER = 3,         /* "absorb"                absorberBsdf.cpp             */
-    CGPU_BSDF_DIELECTRIC_GGX = 4    /* "dielectric-microfacet" (no reference counterpart)   */
+    CGPU_BSDF_DIELECTRIC_GGX = 4,   /* "dielectric-microfacet" (no reference counterpart)   */
+    CGPU_BSDF_MIRROR = 5,           /* "mirror"                specularReflection.cpp       */
+    CGPU_BSDF_PHONG = 6,            /* "phong"                 phongBsdf.cpp                */
+    CGPU_BSDF_PLASTIC = 7           /* "plastic": MixedBsdf(Lambertian, Phong, ratio)
+                                                               mixedBsdf.cpp, bsdfInstantiator.cpp:104-116 */
 };
+/* Fresnel term of a mirror (bsdfInstantiator.cpp:38-64). */
+enum { CGPU_FRESNEL_CONDUCTOR = 0, CGPU_FRESNEL_DIELECTRIC = 1 };
 
 typedef struct cgpu_material {
     int32_t type;            /* CGPU_BSDF_* */
     int32_t albedo_texture;  /* index into cgpu_scene_desc.textures, or -1 for constant albedo */
-    float albedo[3];
-    float f0[3];             /* Schlick F0 of the conductor */
+    float albedo[3];         /* albedo; plastic: diffuse albedo */
+    float f0[3];             /* Schlick F0 of the conductor (and of a conductor-Fresnel mirror) */
     float roughness;         /* CRSD "roughness"; alpha = max(max(r, 1e-3)^2, 1e-3) */
     float ior_outer;
     float ior_inner;
-    float reserved;
+    float exponent;          /* phong "exponent", plastic "specular-exponent" */
+    float diffuse_ratio;     /* plastic "diffuse-ratio" */
+    int32_t fresnel;         /* mirror: CGPU_FRESNEL_* */
+    int32_t reserved[2];
 } cgpu_material;
 
 /* RGB float texture, nearest texel with repeat wrap (rgbImageTexture.cpp:8-15). */

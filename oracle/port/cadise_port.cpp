@@ -127,6 +127,12 @@ struct Material {
     V3 albedo, f0;
     float roughness, iorOuter, iorInner;
     int tex;
+    float exponent = 32.0f, ratio = 0.7f;  // phong / plastic
+    int fresnel = CGPU_FRESNEL_CONDUCTOR;  // mirror
+};
+struct Sphere {  // sphere.cpp:18-31
+    V3 c;
+    float r;
 };
 struct Light {
     int prim;
@@ -141,6 +147,7 @@ struct Scene {
     std::vector<Prim> prims;
     std::vector<Triangle> tris;
     std::vector<Rectangle> rects;
+    std::vector<Sphere> spheres;
     std::vector<Material> mats;
     std::vector<Texture> textures;
     std::vector<Light> lights;
@@ -207,8 +214,35 @@ bool rectHit(const Rectangle& r, const Ray& ray, float* tOut) {
     return true;
 }
 
+// sphere.cpp:43-78 (Haines et al., Ray Tracing Gems 2019) and _isSolutionValid :150-170
+bool sphereHit(const Sphere& sp, const Ray& ray, float* tOut) {
+    const V3& O = ray.o;
+    const V3 G = sp.c;
+    const V3 f = O - G;
+    const V3& d = ray.d;
+    const float b = -f.dot(d);
+    const float r = sp.r;
+    const V3 l = f + b * d;
+    const float discriminant = r * r - l.absDot(l);
+    if (discriminant < 0.0f) return false;
+    const float signB = (b > 0.0f) ? 1.0f : -1.0f;
+    const float q = b + signB * std::sqrt(discriminant);
+    const float c = f.absDot(f) - r * r;
+    const float t0 = c / q;
+    const float t1 = q;
+    if (t0 > ray.maxT || t1 < ray.minT) return false;
+    float t = t0;
+    if (t < ray.minT) {
+        t = t1;
+        if (t > ray.maxT) return false;
+    }
+    *tOut = t;
+    return true;
+}
+
 bool primHit(const Scene& s, int p, const Ray& ray, float* t) {
     const Prim& pr = s.prims[p];
+    if (pr.kind == CGPU_PRIM_SPHERE) return sphereHit(s.spheres[pr.slot], ray, t);
     return pr.kind == CGPU_PRIM_TRIANGLE ? triHit(s.tris[pr.slot], ray, t) : rectHit(s.rects[pr.slot], ray, t);
 }
 
@@ -216,6 +250,12 @@ void primBound(const Scene& s, int p, V3* lo, V3* hi) {
     const Prim& pr = s.prims[p];
     V3 vs[4];
     int n = 3;
+    if (pr.kind == CGPU_PRIM_SPHERE) {  // sphere.cpp:33-40: (c - r, c + r) expanded by 0.0001
+        const Sphere& sp = s.spheres[pr.slot];
+        *lo = sp.c - sp.r - 0.0001f;
+        *hi = sp.c + sp.r + 0.0001f;
+        return;
+    }
     if (pr.kind == CGPU_PRIM_TRIANGLE) {
         const Triangle& t = s.tris[pr.slot];
         vs[0] = t.a; vs[1] = t.b; vs[2] = t.c;
@@ -384,7 +424,9 @@ V3 barycentric(const Triangle& t, const V3& p) {
     return V3(1.0f - u - v, u, v);
 }
 
-// scene.cpp:30-65 + triangle.cpp:125-160 + rectangle.cpp:102-132
+V3 envUvw(const V3& d);
+
+// scene.cpp:30-65 + triangle.cpp:125-160 + rectangle.cpp:102-132 + sphere.cpp:106-135
 bool intersect(const Scene& s, Ray& ray, Surface* si) {
     const int p = traverse(s, ray, false);
     if (p < 0) return false;
@@ -392,6 +434,13 @@ bool intersect(const Scene& s, Ray& ray, Surface* si) {
     si->wi = -ray.d;
     si->P = ray.o + ray.d * ray.maxT;
     const Prim& pr = s.prims[p];
+    if (pr.kind == CGPU_PRIM_SPHERE) {
+        const V3 N = (si->P - s.spheres[pr.slot].c).normalize();
+        si->Ng = N;
+        si->Ns = N;
+        si->uvw = envUvw(N);  // SphericalMapper::mappingToUvw of the shading normal
+        return true;
+    }
     if (pr.kind == CGPU_PRIM_TRIANGLE) {
         const Triangle& t = s.tris[pr.slot];
         const V3 Ng = triNormal(t);
@@ -425,7 +474,8 @@ bool occluded(const Scene& s, Ray ray) { return traverse(s, ray, true) >= 0; }
 // ----------------------------------------------------------------- BSDF ---
 struct BsdfSample { V3 f, L; float pdf = 0.0f; bool valid() const { return !f.isZero() && pdf > 0.0f; } };
 
-bool isSpecular(int type) { return type == CGPU_BSDF_GLASS; }
+// ptEstimator.cpp:64-72: no NEE at a BSDF with a specular lobe
+bool isSpecular(int type) { return type == CGPU_BSDF_GLASS || type == CGPU_BSDF_MIRROR; }
 
 // tRoughnessMapper.h:18-40 (SQUARE)
 float roughnessToAlpha(float r) {
@@ -555,8 +605,36 @@ void roughDielectric(const Material& m, const V3& alb, const V3& V, const V3& L,
     if (!std::isfinite(*pdf)) { *pdf = 0.0f; *f = V3(0.0f); }
 }
 
-// lambertianDiffuse.cpp:27-44 / conductorMicrofacet.cpp:32-66
+// PhongBsdf (phongBsdf.cpp:14-98)
+float phongPdfFactor(const Material& m) { return (m.exponent + 1.0f) * 0.1591549430918953f; }
+float phongBrdfFactor(const Material& m) { return (m.exponent + 2.0f) * 0.1591549430918953f; }
+V3 phongEval(const Material& m, const Surface& si, const V3& L) {
+    const V3& Ns = si.Ns;
+    const V3& V = si.wi;
+    const V3 R = L.reflect(Ns);
+    if (V.dot(Ns) * L.dot(Ns) <= 0.0f) return V3(0.0f);
+    const float RdotV = std::max(R.dot(V), 0.0f);
+    return V3(std::pow(RdotV, m.exponent) * phongBrdfFactor(m));
+}
+float phongPdf(const Material& m, const Surface& si, const V3& L) {
+    const V3& Ns = si.Ns;
+    const V3& V = si.wi;
+    const V3 R = L.reflect(Ns);
+    if (V.dot(Ns) * L.dot(Ns) <= 0.0f) return 0.0f;
+    const float RdotV = std::max(R.dot(V), 0.0f);
+    return std::pow(RdotV, m.exponent) * phongPdfFactor(m);
+}
+V3 lambertEval(const Material& m, const Surface& si, const V3& L);
+float lambertPdf(const Surface& si, const V3& L);
+
+// lambertianDiffuse.cpp:27-44 / conductorMicrofacet.cpp:32-66 / phongBsdf.cpp /
+// mixedBsdf.cpp:33-57 (plastic = Mixed(Lambertian, Phong, ratio))
 V3 bsdfEval(const Material& m, const Surface& si, const V3& L) {
+    if (m.type == CGPU_BSDF_PHONG) return phongEval(m, si, L);
+    if (m.type == CGPU_BSDF_PLASTIC) {
+        const V3 ratio(m.ratio);
+        return lambertEval(m, si, L) * ratio + phongEval(m, si, L) * ratio.complement();
+    }
     const V3& Ns = si.Ns;
     const V3& V = si.wi;
     if (m.type == CGPU_BSDF_LAMBERTIAN) {
@@ -585,8 +663,13 @@ V3 bsdfEval(const Material& m, const Surface& si, const V3& L) {
     return V3(0.0f);
 }
 
-// lambertianDiffuse.cpp:83-96 / conductorMicrofacet.cpp:126-163
+// lambertianDiffuse.cpp:83-96 / conductorMicrofacet.cpp:126-163 / mixedBsdf.cpp:157-185
 float bsdfPdf(const Material& m, const Surface& si, const V3& L) {
+    if (m.type == CGPU_BSDF_PHONG) return phongPdf(m, si, L);
+    if (m.type == CGPU_BSDF_PLASTIC) {
+        const float avg = V3(m.ratio).average();
+        return lambertPdf(si, L) * avg + phongPdf(m, si, L) * (1.0f - avg);
+    }
     const V3& Ns = si.Ns;
     const V3& V = si.wi;
     if (m.type == CGPU_BSDF_LAMBERTIAN) {
@@ -615,10 +698,82 @@ float bsdfPdf(const Material& m, const Surface& si, const V3& L) {
     return 0.0f;
 }
 
+V3 lambertEval(const Material& m, const Surface& si, const V3& L) {
+    if (si.wi.dot(si.Ns) * L.dot(si.Ns) <= 0.0f) return V3(0.0f);
+    return albedoAt(m, si.uvw) * kInvPi;
+}
+float lambertPdf(const Surface& si, const V3& L) {
+    if (si.wi.dot(si.Ns) * L.dot(si.Ns) <= 0.0f) return 0.0f;
+    return L.absDot(si.Ns) * kInvPi;
+}
+
+BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng);
+
+// phongBsdf.cpp:38-81 with hemisphere.cpp:50-69 (lobe around the normal)
+BsdfSample phongSample(const Material& m, const Surface& si, Rng& rng) {
+    BsdfSample out;
+    const V3& Ns = si.Ns;
+    const V3& V = si.wi;
+    V3 z, x;
+    buildCoordinateSystem(Ns, &z, &x);
+    float u0, u1;
+    rng.next2(&u0, &u1);
+    const float phi = kTwoPi * u0;
+    const float cosTheta = std::pow(u1, 1.0f / (m.exponent + 1.0f));
+    const float sinTheta = std::sqrt(1.0f - cosTheta * cosTheta);
+    V3 L(std::sin(phi) * sinTheta, cosTheta, std::cos(phi) * sinTheta);
+    L = x * L.x + Ns * L.y + z * L.z;
+    L = L.normalize();
+    if (V.dot(Ns) * L.dot(Ns) <= 0.0f) return out;
+    const V3 R = L.reflect(Ns);
+    const float RdotV = std::max(R.dot(V), 0.0f);
+    const float powerTerm = std::pow(RdotV, m.exponent);
+    out.f = V3(powerTerm * phongBrdfFactor(m));
+    out.L = L;
+    out.pdf = powerTerm * phongPdfFactor(m);
+    return out;
+}
+
 BsdfSample bsdfSample(const Material& m, const Surface& si, Rng& rng) {
     BsdfSample out;
     const V3& Ns = si.Ns;
     const V3& V = si.wi;
+    if (m.type == CGPU_BSDF_PHONG) return phongSample(m, si, rng);
+    if (m.type == CGPU_BSDF_PLASTIC) {  // mixedBsdf.cpp:59-155 (A Lambertian, B Phong)
+        const V3 ratio(m.ratio);
+        const float averageRatio = ratio.average();
+        const float sample = rng.next();
+        if (sample < ratio.average()) {
+            Material a = m;
+            a.type = CGPU_BSDF_LAMBERTIAN;
+            const BsdfSample ls = bsdfSample(a, si, rng);
+            if (!ls.valid()) return out;
+            const V3 fA = ls.f, fB = phongEval(m, si, ls.L);
+            out.f = ratio * fA + ratio.complement() * fB;
+            out.L = ls.L;
+            out.pdf = averageRatio * ls.pdf + (1.0f - averageRatio) * phongPdf(m, si, ls.L);
+        } else {
+            const BsdfSample ls = phongSample(m, si, rng);
+            if (!ls.valid()) return out;
+            const V3 fB = ls.f, fA = lambertEval(m, si, ls.L);
+            out.f = ratio * fB + ratio.complement() * fA;  // as mixedBsdf.cpp:123-128 writes it
+            out.L = ls.L;
+            out.pdf = averageRatio * ls.pdf + (1.0f - averageRatio) * lambertPdf(si, ls.L);
+        }
+        return out;
+    }
+    if (m.type == CGPU_BSDF_MIRROR) {  // specularReflection.cpp:32-57
+        const float VdotN = V.dot(Ns);
+        const float NFactor = (VdotN > 0.0f) ? 1.0f : -1.0f;
+        const V3 L = V.reflect(Ns * NFactor);
+        const float LdotN = L.dot(Ns);
+        const V3 reflectance = m.fresnel == CGPU_FRESNEL_CONDUCTOR ? schlick(m.f0, LdotN)
+                                                                   : V3(dielectricFresnel(m.iorOuter, m.iorInner, LdotN));
+        out.f = reflectance * albedoAt(m, si.uvw) / std::abs(LdotN);
+        out.L = L;
+        out.pdf = 1.0f;
+        return out;
+    }
     if (m.type == CGPU_BSDF_LAMBERTIAN) {  // lambertianDiffuse.cpp:46-81
         V3 z, x;
         buildCoordinateSystem(Ns, &z, &x);
@@ -745,7 +900,7 @@ V3 envUvw(const V3& d) {
     const float theta = std::acos(std::min(std::max(n.y, -1.0f), 1.0f));
     float phi = std::atan2(n.x, n.z);
     if (phi < 0.0f) phi += kTwoPi;
-    return V3(phi * (0.5f / kPi), (kPi - theta) * kInvPi, 0.0f);
+    return V3(phi * 0.1591549430918953f, (kPi - theta) * kInvPi, 0.0f);  // constant::inv_two_pi
 }
 V3 texel(const Scene& s, int tex, const V3& uvw) {
     const Texture& t = s.textures[size_t(tex)];
@@ -1018,7 +1173,8 @@ Scene* create(const cgpu_scene_desc* d) {
     s->W = d->width; s->H = d->height; s->maxDepth = d->max_depth; s->spp = d->spp > 0 ? d->spp : 1;
     for (uint32_t i = 0; i < d->num_materials; ++i) {
         const cgpu_material& m = d->materials[i];
-        s->mats.push_back({m.type, vload(m.albedo), vload(m.f0), m.roughness, m.ior_outer, m.ior_inner, m.albedo_texture});
+        s->mats.push_back({m.type, vload(m.albedo), vload(m.f0), m.roughness, m.ior_outer, m.ior_inner, m.albedo_texture,
+                           m.exponent, m.diffuse_ratio, m.fresnel});
     }
     for (uint32_t i = 0; i < d->num_textures; ++i) {
         Texture t;
@@ -1051,6 +1207,9 @@ Scene* create(const cgpu_scene_desc* d) {
             }
             p.slot = static_cast<int>(s->tris.size());
             s->tris.push_back(t);
+        } else if (kind == CGPU_PRIM_SPHERE) {
+            p.slot = static_cast<int>(s->spheres.size());
+            s->spheres.push_back(Sphere{vload(v), v[3]});
         } else {
             Rectangle r;
             r.vA = vload(v); r.vB = vload(v + 3); r.vC = vload(v + 6);
@@ -1291,7 +1450,7 @@ D3 bsdfDual(const Scene& s, int mi, const Surface& si, const V3& L) {
         const V3 F = schlick(m.f0, L.dot(H));
         return d3(F) * (ggxDG(s, mi, m, V, L, N, H) * (1.0 / (4.0 * std::abs(double(VdotN) * LdotN))));
     }
-    return d3(V3(0.0f));  // glass: no differentiable parameter here
+    return d3(bsdfEval(m, si, L));  // no differentiable parameter of this BSDF here
 }
 
 D3 estimateDual(const Scene& s, Ray ray, Rng& rng) {
@@ -1351,8 +1510,10 @@ D3 estimateDual(const Scene& s, Ray ray, Rng& rng) {
         if (!bs.valid()) break;
         const float LdotN = bs.L.absDot(si.Ns);
         Tf *= bs.f * LdotN / bs.pdf;
-        if (m.type == CGPU_BSDF_GLASS) T = T * d3(bs.f * LdotN / bs.pdf);
-        else T = T * (bsdfDual(s, pr.material, si, bs.L) * (double(LdotN) / bs.pdf));
+        if (m.type == CGPU_BSDF_LAMBERTIAN || m.type == CGPU_BSDF_CONDUCTOR_GGX)
+            T = T * (bsdfDual(s, pr.material, si, bs.L) * (double(LdotN) / bs.pdf));
+        else
+            T = T * d3(bs.f * LdotN / bs.pdf);
         if (bounce > 2) {
             const float q = std::min(std::max(1.0f - Tf.maxComponent(), 0.05f), 1.0f);
             const float u = rng.next();

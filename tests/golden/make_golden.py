@@ -51,6 +51,7 @@ def golden_scenes():
                                          box=30.0, radius_range=(2.0, 6.0)), 2048),
         "features": (scenes.feature_scene(), 32768),
         "power": (scenes.power_field(), 131072),
+        "spheres": (scenes.sphere_box(), 16384),
     }
 
 

@@ -17,6 +17,7 @@ def specs():
                                         radius_range=(2.0, 6.0)),
         "features": scenes.feature_scene(),
         "power": scenes.power_field(),
+        "spheres": scenes.sphere_box(),
     }
 
 

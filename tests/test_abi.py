@@ -59,6 +59,6 @@ def test_create_without_a_device_reports_no_device(lib):
 def test_struct_layouts_match_header():
     assert C.sizeof(abi.cgpu_ray) == 32
     assert C.sizeof(abi.cgpu_hit) == 16
-    assert C.sizeof(abi.cgpu_material) == 48
+    assert C.sizeof(abi.cgpu_material) == 64
     assert C.sizeof(abi.cgpu_area_light) == 24
     assert C.sizeof(abi.cgpu_render_params) == 48

@@ -16,7 +16,7 @@ def built():
     cg.build()
 
 
-@pytest.mark.parametrize("name", ["cornell", "field", "features", "power"])
+@pytest.mark.parametrize("name", ["cornell", "field", "features", "power", "spheres"])
 def test_golden_crsd_loads_to_the_generator_arrays(name):
     sc = cg.CrsdScene(path=os.path.join(GOLDEN, name + ".crsd"))
     flat = abi.flatten(specs()[name])
@@ -36,10 +36,17 @@ def test_golden_crsd_loads_to_the_generator_arrays(name):
         assert a.type == b.type
         if a.type == abi.CGPU_BSDF_CONDUCTOR_GGX:
             assert list(a.f0) == list(b.f0) and a.roughness == b.roughness
-        else:
+        elif a.type != abi.CGPU_BSDF_PHONG:  # phong has no albedo
             assert list(a.albedo) == list(b.albedo)
-        if a.type in (abi.CGPU_BSDF_GLASS, abi.CGPU_BSDF_DIELECTRIC_GGX):
+        if a.type in (abi.CGPU_BSDF_GLASS, abi.CGPU_BSDF_DIELECTRIC_GGX) or \
+                (a.type == abi.CGPU_BSDF_MIRROR and a.fresnel == 1):
             assert a.ior_inner == b.ior_inner and a.ior_outer == b.ior_outer
+        if a.type == abi.CGPU_BSDF_MIRROR:
+            assert a.fresnel == b.fresnel and (a.fresnel == 1 or list(a.f0) == list(b.f0))
+        if a.type in (abi.CGPU_BSDF_PHONG, abi.CGPU_BSDF_PLASTIC):
+            assert a.exponent == b.exponent
+        if a.type == abi.CGPU_BSDF_PLASTIC:
+            assert a.diffuse_ratio == b.diffuse_ratio
     if flat.normals is not None:
         n = np.ctypeslib.as_array(d.prim_normals, shape=(d.num_primitives, 9))
         assert np.array_equal(n, flat.normals)
@@ -79,7 +86,7 @@ def test_mesh_name_maps_to_its_first_triangle():
 
 @pytest.mark.parametrize("bad,status", [
     ("film { [image-width int32 \"4\"] }", 7),                                   # no camera / renderer
-    ("material { [type string \"phong\"] [name string \"x\"] }", 5),              # unsupported BSDF
+    ("material { [type string \"cloth\"] [name string \"x\"] }", 5),              # unsupported BSDF
     ("camera { [fov real \"abc\"] }", 7),                                         # not a number
 ])
 def test_errors_are_status_codes(bad, status):

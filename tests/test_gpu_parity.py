@@ -27,7 +27,7 @@ from golden_scenes import image, specs, vectors
 
 pytestmark = pytest.mark.gpu
 
-NAMES = ["cornell", "field", "features", "power"]
+NAMES = ["cornell", "field", "features", "power", "spheres"]
 
 
 @pytest.fixture(scope="module")
@@ -47,6 +47,8 @@ def edge_margin(flat, prim, P):
         if p < 0:
             continue
         v = flat.vertices[p].reshape(3, 3).astype(np.float64)
+        if flat.kind[p] == abi.CGPU_PRIM_SPHERE:
+            continue  # no edges: the sphere test is the reference's own formula
         if flat.kind[p] == abi.CGPU_PRIM_TRIANGLE:
             e0, e1, w = v[1] - v[0], v[2] - v[0], x - v[0]
             d00, d01, d11 = e0 @ e0, e0 @ e1, e1 @ e1

@@ -88,7 +88,7 @@ class Host:
         self.L.khc_destroy(self.h)
 
 
-NAMES = ["cornell", "field", "features", "power"]
+NAMES = ["cornell", "field", "features", "power", "spheres"]
 
 
 @pytest.mark.parametrize("name", NAMES)

@@ -17,7 +17,7 @@ from cadise_gb300 import abi
 from golden_scenes import crsd_text, specs, vectors
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
-NAMES = ["cornell", "field", "features", "power"]
+NAMES = ["cornell", "field", "features", "power", "spheres"]
 
 
 @pytest.fixture(scope="module")
