@@ -180,7 +180,7 @@ def rel_mse(x, ref):
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("field", 8192), ("features", 32768), ("power", 131072)])
+@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("field", 8192), ("features", 32768), ("power", 131072), ("spheres", 65536)])
 def test_image_converges_to_reference(name, spp, gpu_ctx, uploaded):
     spec, flat, sid = uploaded[name]
     ref = image(name)
