@@ -252,6 +252,7 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     sl.height = d->height;
     sl.spp = S.spp;
     sl.max_depth = d->max_depth;
+    sl.has_spheres = hs.has_spheres;
     sl.live = true;
     sl.info.build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     int id = -1;

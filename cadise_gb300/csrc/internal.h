@@ -146,6 +146,7 @@ struct SceneSlot {
     cgpu_scene_info info{};
     cg::FilmD film{};
     int width = 0, height = 0, spp = 1, max_depth = 1;
+    bool has_spheres = false;  // renders of this scene use the kernels with the sphere test
 };
 
 struct cgpu_ctx {
@@ -181,6 +182,8 @@ struct cgpu_ctx {
     cudaGraphExec_t graph = nullptr;
     int graph_depth = -1;
     uint32_t graph_paths = 0;
+    bool graph_spheres = false;
+    bool batch_spheres = false;  // a scene of the current render holds spheres
 
     cgpu_render_stats stats{};
 

@@ -69,7 +69,7 @@ CG_D void count_flush(unsigned long long* counters, const TraceCounters& cc, con
 // Three accumulators, as the wavefront keeps them: L (emission and the
 // BSDF-sampled half of NEE), Le (the sky seen by an escaping continuation
 // ray) and Ls (the light-sampled half of NEE); the sample is (L + Le) + Ls.
-template <bool COUNT>
+template <bool COUNT, bool SPH = true>
 CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, float3* Leout, float3* Lsout,
                   TraceCounters* tc, TraceCounters* ta, uint32_t* nclosest, uint32_t* nany) {
     float3 L = splat3(0.0f), Le = splat3(0.0f), Ls = splat3(0.0f), T = splat3(1.0f);
@@ -78,7 +78,7 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
         const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
         HitD hit;
         if (COUNT) ++*nclosest;
-        if (!traverse<false, COUNT>(S, r, &hit, tc)) {
+        if (!traverse<false, COUNT, SPH>(S, r, &hit, tc)) {
             if (S.env_light >= 0 && ce) Le = T * env_radiance(S, d);
             break;
         }
@@ -89,13 +89,13 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
             const RayPre sr = ray_prep(si.P, pl.sdir, kRayEps, pl.stmax);
             HitD sh;
             if (COUNT) ++*nany;
-            if (!traverse<true, COUNT>(S, sr, &sh, ta)) Ls += pl.scontrib;
+            if (!traverse<true, COUNT, SPH>(S, sr, &sh, ta)) Ls += pl.scontrib;
         }
         if (pl.mis) {
             const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
             HitD mh;
             if (COUNT) ++*nclosest;
-            if (traverse<false, COUNT>(S, mr, &mh, tc)) {
+            if (traverse<false, COUNT, SPH>(S, mr, &mh, tc)) {
                 if (light_of_slot(S, mh.slot) == pl.mlight) {
                     const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
                     L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);

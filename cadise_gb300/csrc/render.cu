@@ -23,7 +23,7 @@
 
 namespace cg {
 
-template <bool COUNT>
+template <bool COUNT, bool SPH>
 __global__ void k_megakernel(RenderArgs a) {
     const BatchHeader h = *a.header;
     TraceCounters tc{0, 0}, ta{0, 0};
@@ -35,7 +35,7 @@ __global__ void k_megakernel(RenderArgs a) {
         float3 o, d;
         primary_ray(S, id, h.seed, rng, &o, &d);
         float3 L, Le, Ls;
-        mk_path<COUNT>(S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
+        mk_path<COUNT, SPH>(S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
         a.wf.L[p] = make_float4(L.x, L.y, L.z, 0.0f);
         a.wf.Le[p] = make_float4(Le.x, Le.y, Le.z, 0.0f);
         a.wf.Ls[p] = make_float4(Ls.x, Ls.y, Ls.z, 0.0f);
@@ -156,7 +156,7 @@ CG_D void shadow_finish(const WfBuffers& w, int p, bool occluded) {
     w.Ls[p] = Ls;
 }
 
-template <bool COUNT>
+template <bool COUNT, bool SPH>
 __global__ void k_wf_extend(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -176,14 +176,14 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
         const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
         HitD hit;
         if (COUNT) ++nclosest;
-        const bool hitp = traverse_warp<COUNT>(S, r, &hit, &tc);
+        const bool hitp = traverse_warp<COUNT, SPH>(S, r, &hit, &tc);
         const int key = extend_finish(w, S, p, cont, o, d, hitp, hit);
         grouped_push(qmat, cnt + 3, key, p);
     }
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
 }
 
-template <bool COUNT>
+template <bool COUNT, bool SPH>
 __global__ void k_wf_shadow(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     const int n = w.cnt[b * kCntStride + 2];
@@ -197,7 +197,7 @@ __global__ void k_wf_shadow(RenderArgs a, int b) {
         const RayPre r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
         HitD hit;
         if (COUNT) ++nany;
-        shadow_finish(w, p, traverse<true, COUNT>(S, r, &hit, &tc));
+        shadow_finish(w, p, traverse<true, COUNT, SPH>(S, r, &hit, &tc));
     }
     count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
 }
@@ -223,7 +223,7 @@ CG_D int warp_take(int* work, bool need, int n) {
     return k < n ? k : -1;
 }
 
-template <bool COUNT>
+template <bool COUNT, bool SPH>
 __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -259,7 +259,7 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
         if (__all_sync(__activemask(), i < 0)) break;
         if (i >= 0) {
             const SceneD& S = a.scenes[w.meta[p].x];
-            for (int s = 0; s < kStepsPerFetch && !st.done; ++s) trav_step<false, COUNT>(S, r, st, &tc);
+            for (int s = 0; s < kStepsPerFetch && !st.done; ++s) trav_step<false, COUNT, SPH>(S, r, st, &tc);
             if (st.done) {
                 HitD hit;
                 hit.slot = st.hslot;
@@ -283,7 +283,7 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
 // longest ray is done.  Same hits as the other extend kernels (closer_hit).
 constexpr int kRefillLanes = 12;
 
-template <bool COUNT>
+template <bool COUNT, bool SPH>
 __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -350,7 +350,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 cur = pop();
             }
             while (leaf != kNoEntry) {
-                visit_leaf<false, COUNT>(S, r, leaf, tcur, hslot, hu, hv, &tc);
+                visit_leaf<false, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, &tc);
                 leaf = kNoEntry;
                 if (cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
@@ -375,7 +375,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
 }
 
-template <bool COUNT>
+template <bool COUNT, bool SPH>
 __global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -405,7 +405,7 @@ __global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
         if (__all_sync(__activemask(), i < 0)) break;
         if (i >= 0) {
             const SceneD& S = a.scenes[w.meta[p].x];
-            for (int s = 0; s < kStepsPerFetch && !st.done; ++s) trav_step<true, COUNT>(S, r, st, &tc);
+            for (int s = 0; s < kStepsPerFetch && !st.done; ++s) trav_step<true, COUNT, SPH>(S, r, st, &tc);
             if (st.done) {
                 shadow_finish(w, p, st.hslot >= 0);
                 i = -1;
@@ -665,11 +665,11 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int ggen = grid_for(ctx, k_wf_generate, kBlock, paths);
     timed(ctx, CGPU_KERNEL_GENERATE, s, [&] { k_wf_generate<<<ggen, kBlock, 0, s>>>(a); });
     const int trav = ctx->tuning.traversal;
-    auto ext_kernel = trav == 1   ? (counting ? k_wf_extend_dyn<true> : k_wf_extend_dyn<false>)
-                      : trav == 2 ? (counting ? k_wf_extend_pww<true> : k_wf_extend_pww<false>)
-                                  : (counting ? k_wf_extend<true> : k_wf_extend<false>);
-    auto sh_kernel = trav == 1 ? (counting ? k_wf_shadow_dyn<true> : k_wf_shadow_dyn<false>)
-                               : (counting ? k_wf_shadow<true> : k_wf_shadow<false>);
+    const bool sph = ctx->batch_spheres;
+#define CG_PICK(K) (sph ? (counting ? K<true, true> : K<false, true>) : (counting ? K<true, false> : K<false, false>))
+    auto ext_kernel = trav == 1 ? CG_PICK(k_wf_extend_dyn) : trav == 2 ? CG_PICK(k_wf_extend_pww) : CG_PICK(k_wf_extend);
+    auto sh_kernel = trav == 1 ? CG_PICK(k_wf_shadow_dyn) : CG_PICK(k_wf_shadow);
+#undef CG_PICK
     const int gext = grid_for(ctx, ext_kernel, bt, paths);
     const int gsh = grid_for(ctx, sh_kernel, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
@@ -708,13 +708,15 @@ cgpu_status run_batch(cgpu_ctx* ctx, int mode, int depth, uint32_t paths, bool s
     const bool counting = ctx->counting;
     if (mode == CGPU_MODE_MEGAKERNEL) {
         RenderArgs a = make_args(ctx);
+        const int bt = ctx->tuning.block_trace;
+        const bool sph = ctx->batch_spheres;
         if (counting) {
-            const int bt = ctx->tuning.block_trace;
-            k_megakernel<true><<<grid_for(ctx, k_megakernel<true>, bt, paths), bt, 0, ctx->stream>>>(a);
+            auto k = sph ? k_megakernel<true, true> : k_megakernel<true, false>;
+            k<<<grid_for(ctx, k, bt, paths), bt, 0, ctx->stream>>>(a);
         } else {
-            const int bt = ctx->tuning.block_trace;
-            const int g = grid_for(ctx, k_megakernel<false>, bt, paths);
-            timed(ctx, CGPU_KERNEL_MEGAKERNEL, ctx->stream, [&] { k_megakernel<false><<<g, bt, 0, ctx->stream>>>(a); });
+            auto k = sph ? k_megakernel<false, true> : k_megakernel<false, false>;
+            const int g = grid_for(ctx, k, bt, paths);
+            timed(ctx, CGPU_KERNEL_MEGAKERNEL, ctx->stream, [&] { k<<<g, bt, 0, ctx->stream>>>(a); });
         }
         ctx->stats.kernel_launches += 1;
         if (splat) {
@@ -725,8 +727,9 @@ cgpu_status run_batch(cgpu_ctx* ctx, int mode, int depth, uint32_t paths, bool s
         return cg_cuda(ctx, cudaGetLastError(), "megakernel launch");
     }
     if (!use_graph || counting || !splat || ctx->profiling) return enqueue_wavefront(ctx, depth, paths, splat, counting);
-    // one graph per (depth, path capacity); the batch itself lives in device memory
-    if (!ctx->graph || ctx->graph_depth != depth || ctx->graph_paths != ctx->path_cap) {
+    // one graph per (depth, path capacity, sphere kernels); the batch itself lives in device memory
+    if (!ctx->graph || ctx->graph_depth != depth || ctx->graph_paths != ctx->path_cap ||
+        ctx->graph_spheres != ctx->batch_spheres) {
         if (ctx->graph) {
             cudaGraphExecDestroy(ctx->graph);
             ctx->graph = nullptr;
@@ -745,6 +748,7 @@ cgpu_status run_batch(cgpu_ctx* ctx, int mode, int depth, uint32_t paths, bool s
         if (e != cudaSuccess) return cg_cuda(ctx, e, "graph instantiate");
         ctx->graph_depth = depth;
         ctx->graph_paths = ctx->path_cap;
+        ctx->graph_spheres = ctx->batch_spheres;
         ctx->stats.kernel_launches = before;
     }
     ctx->stats.kernel_launches += uint32_t(2 + (depth + 1) * 2 + depth * kNumBsdfKinds);
@@ -784,6 +788,9 @@ cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p) {
         max_npix = std::max<uint32_t>(max_npix, uint32_t(sl.width) * uint32_t(sl.height));
         depth = std::max(depth, sl.max_depth);
     }
+    bool spheres = false;
+    for (uint32_t i = 0; i < p->num_scenes; ++i) spheres |= ctx->scenes[p->scenes[i]].has_spheres;
+    ctx->batch_spheres = spheres;
     cgpu_status st = cg_sync_tables(ctx);
     if (st != CGPU_OK) return st;
     st = ensure_path_buffers(ctx, paths_capacity(ctx, max_npix), depth);
@@ -861,6 +868,7 @@ cgpu_status cg_render_paths_raw(cgpu_ctx* ctx, int scene, int mode, uint32_t fir
         return cg_fail(ctx, CGPU_ERR_NOT_FOUND, "render_paths: unknown scene id");
     const SceneSlot& sl = ctx->scenes[scene];
     const uint32_t npix = uint32_t(sl.width) * uint32_t(sl.height);
+    ctx->batch_spheres = sl.has_spheres;
     cgpu_status st = cg_sync_tables(ctx);
     if (st != CGPU_OK) return st;
     st = ensure_path_buffers(ctx, paths_capacity(ctx, npix), sl.max_depth);
@@ -1000,8 +1008,12 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
     cudaStream_t s = ctx->stream;
     const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
     const int trav = ctx->tuning.traversal;
-    auto ext = trav == 1 ? k_wf_extend_dyn<false> : trav == 2 ? k_wf_extend_pww<false> : k_wf_extend<false>;
-    auto sh = trav == 1 ? k_wf_shadow_dyn<false> : k_wf_shadow<false>;
+    const bool sph = ctx->batch_spheres;
+    auto ext = trav == 1   ? (sph ? k_wf_extend_dyn<false, true> : k_wf_extend_dyn<false, false>)
+               : trav == 2 ? (sph ? k_wf_extend_pww<false, true> : k_wf_extend_pww<false, false>)
+                           : (sph ? k_wf_extend<false, true> : k_wf_extend<false, false>);
+    auto sh = trav == 1 ? (sph ? k_wf_shadow_dyn<false, true> : k_wf_shadow_dyn<false, false>)
+                        : (sph ? k_wf_shadow<false, true> : k_wf_shadow<false, false>);
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
     const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, sh, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
@@ -1063,6 +1075,7 @@ extern "C" cgpu_status cgpu_render_noalloc(cgpu_ctx* ctx, int32_t scene, uint32_
     const uint32_t n = uint32_t(npix);
     const uint32_t per = kNoAllocMaxPaths / n;  // samples per batch
     const int depth = sl.max_depth;
+    ctx->batch_spheres = sl.has_spheres;
     ctx->stats = cgpu_render_stats{};
     for (uint32_t done = 0; done < num_samples;) {
         const uint32_t k = std::min(per, num_samples - done);

@@ -108,6 +108,7 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
                 tprim[t] = i;
                 tflags[t] = kRecSphere;
                 ++t;
+                out->has_spheres = true;
             } else {
                 // rectangle v1 v2 v3 = vA vB vC; eA = vA - vB, eB = vC - vB, vD = vB + eA + eB
                 const HostV3 vA = v3(v), vB = v3(v + 3), vC = v3(v + 6);

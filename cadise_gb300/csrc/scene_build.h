@@ -28,6 +28,7 @@ struct HostScene {
     CameraD cam{};
     cgpu_scene_info info{};
     int wide_depth = 0;
+    bool has_spheres = false;
 };
 
 // Returns CGPU_OK or an error status with a message in *err.

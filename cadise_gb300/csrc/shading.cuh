@@ -493,6 +493,49 @@ CG_D BsdfS phong_sample(const MaterialD& m, const SurfaceD& si, Rng& rng) {
     return out;
 }
 
+// MixedBsdf::evaluateSample (mixedBsdf.cpp:59-155) of plastic: one draw picks
+// the lobe by the average ratio; the other lobe is evaluated at the sampled
+// direction.  When Phong (B) is sampled the reference weights its value by
+// the ratio and Lambert's by its complement, as written there
+// (mixedBsdf.cpp:123-128); so does this.
+CG_D BsdfS plastic_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, Rng& rng) {
+    BsdfS out;
+    out.f = splat3(0.0f);
+    out.L = mk(0.0f, 1.0f, 0.0f);
+    out.pdf = 0.0f;
+    const float avg = (m.ratio + m.ratio + m.ratio) / 3.0f;
+    const float u = rng.next();
+    if (u < avg) {
+        const BsdfS a = lambert_sample(S, m, si, rng);
+        if (!a.valid()) return out;
+        out.L = a.L;
+        out.f = a.f * m.ratio + phong_eval(m, si, a.L) * (1.0f - m.ratio);
+        out.pdf = avg * a.pdf + (1.0f - avg) * phong_pdf(m, si, a.L);
+    } else {
+        const BsdfS b = phong_sample(m, si, rng);
+        if (!b.valid()) return out;
+        out.L = b.L;
+        out.f = b.f * m.ratio + lambert_eval(S, m, si, b.L) * (1.0f - m.ratio);
+        out.pdf = avg * b.pdf + (1.0f - avg) * lambert_pdf(si, b.L);
+    }
+    return out;
+}
+
+// SpecularReflection::evaluateSample (specularReflection.cpp:32-57), pdf 1
+CG_D BsdfS mirror_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si) {
+    BsdfS out;
+    const float3 N = si.Ns, V = si.wi;
+    const float VdotN = dot(V, N);
+    const float3 L = reflect(V, N * (VdotN > 0.0f ? 1.0f : -1.0f));
+    const float LdotN = dot(L, N);
+    const float3 R = m.fresnel == 0 ? schlick(m.f0, LdotN)
+                                    : splat3(fresnel_dielectric(m.ior_outer, m.ior_inner, LdotN));
+    out.f = divs(R * albedo_of(S, m, si.uvw), fabsf(LdotN));
+    out.L = L;
+    out.pdf = 1.0f;
+    return out;
+}
+
 // Bsdf::evaluateSample (lambertianDiffuse.cpp:46-81, conductorMicrofacet.cpp:68-124,
 // specularDielectric.cpp:35-127)
 CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, Rng& rng) {
@@ -503,41 +546,8 @@ CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, 
     const float3 N = si.Ns, V = si.wi;
     if (m.type == BSDF_LAMBERTIAN) return lambert_sample(S, m, si, rng);
     if (m.type == BSDF_PHONG) return phong_sample(m, si, rng);
-    if (m.type == BSDF_PLASTIC) {
-        // MixedBsdf::evaluateSample (mixedBsdf.cpp:59-155): one draw picks the
-        // lobe by the average ratio; the other lobe is evaluated at the
-        // sampled direction.  When Phong (B) is sampled the reference weights
-        // its value by the ratio and Lambert's by its complement, as written
-        // there (mixedBsdf.cpp:123-128); so does this.
-        const float avg = (m.ratio + m.ratio + m.ratio) / 3.0f;
-        const float u = rng.next();
-        if (u < avg) {
-            const BsdfS a = lambert_sample(S, m, si, rng);
-            if (!a.valid()) return out;
-            out.L = a.L;
-            out.f = a.f * m.ratio + phong_eval(m, si, a.L) * (1.0f - m.ratio);
-            out.pdf = avg * a.pdf + (1.0f - avg) * phong_pdf(m, si, a.L);
-        } else {
-            const BsdfS b = phong_sample(m, si, rng);
-            if (!b.valid()) return out;
-            out.L = b.L;
-            out.f = b.f * m.ratio + lambert_eval(S, m, si, b.L) * (1.0f - m.ratio);
-            out.pdf = avg * b.pdf + (1.0f - avg) * lambert_pdf(si, b.L);
-        }
-        return out;
-    }
-    if (m.type == BSDF_MIRROR) {
-        // SpecularReflection::evaluateSample (specularReflection.cpp:32-57), pdf 1
-        const float VdotN = dot(V, N);
-        const float3 L = reflect(V, N * (VdotN > 0.0f ? 1.0f : -1.0f));
-        const float LdotN = dot(L, N);
-        const float3 R = m.fresnel == 0 ? schlick(m.f0, LdotN)
-                                        : splat3(fresnel_dielectric(m.ior_outer, m.ior_inner, LdotN));
-        out.f = divs(R * albedo_of(S, m, si.uvw), fabsf(LdotN));
-        out.L = L;
-        out.pdf = 1.0f;
-        return out;
-    }
+    if (m.type == BSDF_PLASTIC) return plastic_sample(S, m, si, rng);
+    if (m.type == BSDF_MIRROR) return mirror_sample(S, m, si);
     if (m.type == BSDF_CONDUCTOR) {
         const float nf = dot(V, N) > 0.0f ? 1.0f : -1.0f;
         float3 z, x;

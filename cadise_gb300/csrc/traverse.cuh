@@ -217,7 +217,10 @@ CG_D bool sphere_test(const RayPre& r, float3 G, float rad, float tmax, float* t
 
 // Tests the primitives of leaf `e`; returns true when an any-hit query is
 // answered (the hit is in slot / tcur).
-template <bool ANY, bool COUNT>
+// SPH = false: the scene holds no spheres, and the sphere test is compiled out
+// of the hot kernels (a sphere record would then be misread as a triangle, so
+// the host picks SPH from the scenes it renders).
+template <bool ANY, bool COUNT, bool SPH = true>
 CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, int& hslot, float& hu, float& hv,
                      TraceCounters* cnt) {
     const uint32_t first = leaf_first(e), n = leaf_count(e);
@@ -228,7 +231,7 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
         float t, u = 0.0f, v = 0.0f;
         // closest hit: a bound one rounding wider than tcur, so that every
         // triangle whose t rounds to <= tcur reaches closer_hit
-        const bool sphere = (__float_as_uint(c.w) & 3u) == kRecSphere;
+        const bool sphere = SPH && (__float_as_uint(c.w) & 3u) == kRecSphere;
         if (sphere ? sphere_test(r, f3(a), b.x, tcur, &t)
                    : tri_test(r, f3(a), f3(b), f3(c), ANY ? tcur : tcur * 1.00000036f, &t, &u, &v)) {
             const int slot = int(first + k);
@@ -252,7 +255,7 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
 // megakernel's traversal (its threads are at different bounces anyway) and
 // every any-hit query (the first hit ends the walk, so there is nothing to
 // gain from holding leaves back).
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool SPH = true>
 CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
     uint32_t stack_e[kStackSize];
     float stack_t[kStackSize];
@@ -264,7 +267,7 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
     for (;;) {
         uint32_t next = kNoEntry;
         if (entry_is_leaf(cur)) {
-            if (visit_leaf<ANY, COUNT>(S, r, cur, tcur, hslot, hu, hv, cnt)) {
+            if (visit_leaf<ANY, COUNT, SPH>(S, r, cur, tcur, hslot, hu, hv, cnt)) {
                 hit->slot = hslot;
                 hit->t = tcur;
                 return true;
@@ -295,7 +298,7 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
 // together, so inner-node and triangle work run with more lanes in step.
 // Finds the same hit as traverse<false> (closer_hit does not depend on the
 // visiting order).
-template <bool COUNT>
+template <bool COUNT, bool SPH = true>
 CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
     uint32_t stack_e[kStackSize];
     float stack_t[kStackSize];
@@ -329,7 +332,7 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
             cur = pop();
         }
         while (leaf != kNoEntry) {
-            visit_leaf<false, COUNT>(S, r, leaf, tcur, hslot, hu, hv, cnt);
+            visit_leaf<false, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, cnt);
             leaf = kNoEntry;
             if (cur != kNoEntry && entry_is_leaf(cur)) {
                 leaf = cur;
@@ -370,10 +373,10 @@ CG_D void trav_begin(TravState& st, const RayPre& r) {
     st.done = false;
 }
 
-template <bool ANY, bool COUNT>
+template <bool ANY, bool COUNT, bool SPH = true>
 CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounters* cnt) {
     if (entry_is_leaf(st.cur)) {
-        if (visit_leaf<ANY, COUNT>(S, r, st.cur, st.tcur, st.hslot, st.hu, st.hv, cnt)) {
+        if (visit_leaf<ANY, COUNT, SPH>(S, r, st.cur, st.tcur, st.hslot, st.hu, st.hv, cnt)) {
             st.done = true;
             return;
         }
