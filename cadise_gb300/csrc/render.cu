@@ -439,7 +439,7 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
         Rng rng;
         rng.key = path_key(seed, meta.x, meta.y, meta.z);
         rng.ctr = meta.w;
-        const VertexPlan pl = plan_vertex(S, si, f3(tw), (__float_as_int(tw.w) & 1) != 0, b, rng);
+        const VertexPlan pl = plan_vertex<KIND>(S, si, f3(tw), (__float_as_int(tw.w) & 1) != 0, b, rng);
         if (!is_zero(pl.emit)) {
             float4 L = w.L[p];
             L.x += pl.emit.x;

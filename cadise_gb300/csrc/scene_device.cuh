@@ -57,9 +57,13 @@ enum : int {
 constexpr int kNumBsdfTypes = 8;
 // Shade queues (one shade kernel each): materials that cost alike share one.
 constexpr int kNumBsdfKinds = 5;
-CG_HD int shade_queue(int type) {
+constexpr CG_HD int shade_queue(int type) {
     return type == BSDF_MIRROR ? BSDF_GLASS : (type == BSDF_PHONG || type == BSDF_PLASTIC) ? BSDF_LAMBERTIAN : type;
 }
+// Whether the shading code compiled for shade queue Q (-1: every queue, the
+// megakernel and the adjoint) includes BSDF `type`.
+template <int Q>
+constexpr CG_HD bool queue_has(int type) { return Q < 0 || shade_queue(type) == Q; }
 
 // Record flags (TriRecord::v2.w): bits 0-1 the kind, bits 2-31 the
 // rectangle index of a rectangle half.

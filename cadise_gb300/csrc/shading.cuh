@@ -376,13 +376,14 @@ CG_D void rough_dielectric_eval(const MaterialD& m, float3 albedo, float3 V, flo
 }
 
 // Bsdf::evaluate (lambertianDiffuse.cpp:27-44, conductorMicrofacet.cpp:32-66)
+template <int Q = -1>
 CG_D float3 bsdf_eval(const SceneD& S, const MaterialD& m, const SurfaceD& si, float3 L) {
     const float3 N = si.Ns, V = si.wi;
-    if (m.type == BSDF_LAMBERTIAN) {
+    if (queue_has<Q>(BSDF_LAMBERTIAN) && m.type == BSDF_LAMBERTIAN) {
         if (dot(V, N) * dot(L, N) <= 0.0f) return splat3(0.0f);
         return albedo_of(S, m, si.uvw) * kInvPi;
     }
-    if (m.type == BSDF_CONDUCTOR) {
+    if (queue_has<Q>(BSDF_CONDUCTOR) && m.type == BSDF_CONDUCTOR) {
         const float VdotN = dot(V, N), LdotN = dot(L, N);
         if (VdotN * LdotN <= 0.0f) return splat3(0.0f);
         float3 H = (V + L) * (VdotN > 0.0f ? 1.0f : -1.0f);
@@ -393,27 +394,28 @@ CG_D float3 bsdf_eval(const SceneD& S, const MaterialD& m, const SurfaceD& si, f
         const float G = ggx_G(m.alpha, V, L, N, H);
         return F * G * D * (1.0f / (4.0f * fabsf(VdotN * LdotN)));
     }
-    if (m.type == BSDF_DIELECTRIC_GGX) {
+    if (queue_has<Q>(BSDF_DIELECTRIC_GGX) && m.type == BSDF_DIELECTRIC_GGX) {
         float3 f;
         float pdf;
         rough_dielectric_eval(m, albedo_of(S, m, si.uvw), V, L, N, &f, &pdf);
         return f;
     }
-    if (m.type == BSDF_PHONG) return phong_eval(m, si, L);
-    if (m.type == BSDF_PLASTIC) {  // MixedBsdf::evaluate (mixedBsdf.cpp:33-57), A Lambert, B Phong
+    if (queue_has<Q>(BSDF_PHONG) && m.type == BSDF_PHONG) return phong_eval(m, si, L);
+    if (queue_has<Q>(BSDF_PLASTIC) && m.type == BSDF_PLASTIC) {  // MixedBsdf::evaluate (mixedBsdf.cpp:33-57), A Lambert, B Phong
         return lambert_eval(S, m, si, L) * m.ratio + phong_eval(m, si, L) * (1.0f - m.ratio);
     }
     return splat3(0.0f);  // glass, mirror, absorber: no non-delta part
 }
 
 // Bsdf::evaluatePdfW (lambertianDiffuse.cpp:83-96, conductorMicrofacet.cpp:126-163)
+template <int Q = -1>
 CG_D float bsdf_pdf(const SceneD& S, const MaterialD& m, const SurfaceD& si, float3 L) {
     const float3 N = si.Ns, V = si.wi;
-    if (m.type == BSDF_LAMBERTIAN) {
+    if (queue_has<Q>(BSDF_LAMBERTIAN) && m.type == BSDF_LAMBERTIAN) {
         if (dot(V, N) * dot(L, N) <= 0.0f) return 0.0f;
         return absdot(L, N) * kInvPi;
     }
-    if (m.type == BSDF_CONDUCTOR) {
+    if (queue_has<Q>(BSDF_CONDUCTOR) && m.type == BSDF_CONDUCTOR) {
         const float VdotN = dot(V, N), LdotN = dot(L, N);
         if (VdotN * LdotN <= 0.0f) return 0.0f;
         float3 H = (V + L) * (VdotN > 0.0f ? 1.0f : -1.0f);
@@ -423,14 +425,14 @@ CG_D float bsdf_pdf(const SceneD& S, const MaterialD& m, const SurfaceD& si, flo
         const float pdfL = fabsf(fabsf(D * dot(N, H)) / (4.0f * dot(L, H)));
         return isfinite(pdfL) ? pdfL : 0.0f;
     }
-    if (m.type == BSDF_DIELECTRIC_GGX) {
+    if (queue_has<Q>(BSDF_DIELECTRIC_GGX) && m.type == BSDF_DIELECTRIC_GGX) {
         float3 f;
         float pdf;
         rough_dielectric_eval(m, splat3(1.0f), V, L, N, &f, &pdf);
         return pdf;
     }
-    if (m.type == BSDF_PHONG) return phong_pdf(m, si, L);
-    if (m.type == BSDF_PLASTIC) {  // MixedBsdf::evaluatePdfW (mixedBsdf.cpp:157-185)
+    if (queue_has<Q>(BSDF_PHONG) && m.type == BSDF_PHONG) return phong_pdf(m, si, L);
+    if (queue_has<Q>(BSDF_PLASTIC) && m.type == BSDF_PLASTIC) {  // MixedBsdf::evaluatePdfW (mixedBsdf.cpp:157-185)
         const float avg = (m.ratio + m.ratio + m.ratio) / 3.0f;
         return lambert_pdf(si, L) * avg + phong_pdf(m, si, L) * (1.0f - avg);
     }
@@ -538,17 +540,18 @@ CG_D BsdfS mirror_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si
 
 // Bsdf::evaluateSample (lambertianDiffuse.cpp:46-81, conductorMicrofacet.cpp:68-124,
 // specularDielectric.cpp:35-127)
+template <int Q = -1>
 CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, Rng& rng) {
     BsdfS out;
     out.f = splat3(0.0f);
     out.L = mk(0.0f, 1.0f, 0.0f);
     out.pdf = 0.0f;
     const float3 N = si.Ns, V = si.wi;
-    if (m.type == BSDF_LAMBERTIAN) return lambert_sample(S, m, si, rng);
-    if (m.type == BSDF_PHONG) return phong_sample(m, si, rng);
-    if (m.type == BSDF_PLASTIC) return plastic_sample(S, m, si, rng);
-    if (m.type == BSDF_MIRROR) return mirror_sample(S, m, si);
-    if (m.type == BSDF_CONDUCTOR) {
+    if (queue_has<Q>(BSDF_LAMBERTIAN) && m.type == BSDF_LAMBERTIAN) return lambert_sample(S, m, si, rng);
+    if (queue_has<Q>(BSDF_PHONG) && m.type == BSDF_PHONG) return phong_sample(m, si, rng);
+    if (queue_has<Q>(BSDF_PLASTIC) && m.type == BSDF_PLASTIC) return plastic_sample(S, m, si, rng);
+    if (queue_has<Q>(BSDF_MIRROR) && m.type == BSDF_MIRROR) return mirror_sample(S, m, si);
+    if (queue_has<Q>(BSDF_CONDUCTOR) && m.type == BSDF_CONDUCTOR) {
         const float nf = dot(V, N) > 0.0f ? 1.0f : -1.0f;
         float3 z, x;
         frame_from_y(N, &z, &x);
@@ -569,7 +572,7 @@ CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, 
         out.pdf = pdfL;
         return out;
     }
-    if (m.type == BSDF_GLASS) {
+    if (queue_has<Q>(BSDF_GLASS) && m.type == BSDF_GLASS) {
         const float VdotN = dot(V, N);
         const float R = fresnel_dielectric(m.ior_outer, m.ior_inner, VdotN);
         const float pr = (R + R + R) / 3.0f;  // Spectrum::average of a grey reflectance
@@ -594,7 +597,7 @@ CG_D BsdfS bsdf_sample(const SceneD& S, const MaterialD& m, const SurfaceD& si, 
         }
         return out;
     }
-    if (m.type == BSDF_DIELECTRIC_GGX) {
+    if (queue_has<Q>(BSDF_DIELECTRIC_GGX) && m.type == BSDF_DIELECTRIC_GGX) {
         const float cv = dot(V, N);
         if (cv == 0.0f) return out;
         const float3 Nv = cv > 0.0f ? N : -N;
@@ -814,6 +817,9 @@ struct VertexPlan {
 // light-sampling half of DirectLightEvaluator::evaluate
 // (directLightEvaluator.cpp:36-76); random numbers in the reference's order:
 // light pick, light position, MIS BSDF sample, continuation sample, roulette.
+// Q: the shade queue the caller handles (-1: any material) - only that
+// queue's BSDFs are compiled in.
+template <int Q = -1>
 CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool count_emission, int bounce, Rng& rng) {
     VertexPlan p;
     p.emit = splat3(0.0f);
@@ -834,9 +840,9 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
                 const float3 Lv = ls.pos - si.P;
                 const float dist = len(Lv);
                 const float3 L = divs(Lv, dist);
-                const float3 f = bsdf_eval(S, m, si, L);
+                const float3 f = bsdf_eval<Q>(S, m, si, L);
                 const float3 factor = f * absdot(L, si.Ns);
-                const float bp = bsdf_pdf(S, m, si, L);
+                const float bp = bsdf_pdf<Q>(S, m, si, L);
                 const float w = mis_power(ls.pdfW, bp);
                 const float3 part = divs(divs(ls.radiance * w * factor, ls.pdfW), pick);
                 p.shadow = 1;
@@ -846,7 +852,7 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
                 p.sx = T * divs(divs(factor * w, ls.pdfW), pick);
                 p.slight = li;
             }
-            const BsdfS bs = bsdf_sample(S, m, si, rng);
+            const BsdfS bs = bsdf_sample<Q>(S, m, si, rng);
             if (bs.valid()) {
                 p.mis = 1;
                 p.mdir = normalize(bs.L);
@@ -858,7 +864,7 @@ CG_D VertexPlan plan_vertex(const SceneD& S, const SurfaceD& si, float3 T, bool 
     } else {
         p.count_emission = 1;
     }
-    const BsdfS bs = bsdf_sample(S, m, si, rng);
+    const BsdfS bs = bsdf_sample<Q>(S, m, si, rng);
     if (!bs.valid()) return p;
     T *= divs(bs.f * absdot(bs.L, si.Ns), bs.pdf);
     if (bounce > 2) {  // RussianRoulette::isSurvivedOnNextRound (russianRoulette.cpp:9-28)
