@@ -336,12 +336,20 @@ def adjoint_rate(ctx, args):
             times_f.append(t1 - t0)
             times_b.append(t2 - t1)
     nparams = gt.size + gr.size + gl.size
+    # the same backward on the one-thread-per-path schedule, for comparison
+    from cadise_gb300 import CGPU_MODE_MEGAKERNEL, CGPU_MODE_WAVEFRONT
+    ctx.set_adjoint_mode(CGPU_MODE_MEGAKERNEL)
+    ctx.adjoint_backward(sid, spec.spp, 1000, grad_img)
+    t0 = time.perf_counter()
+    ctx.adjoint_backward(sid, spec.spp, 1000, grad_img)
+    bwd_mk = time.perf_counter() - t0
+    ctx.set_adjoint_mode(CGPU_MODE_WAVEFRONT)
     ctx.release(sid)
     fwd, bwd = statistics.mean(times_f), statistics.mean(times_b)
     return {"workload": "diff-scene-102k-tris-%dx%d-%dspp" % (spec.width, spec.height, spec.spp),
             "iterations_per_s": 1.0 / (fwd + bwd), "grads_per_s": nparams / (fwd + bwd),
             "unit": "gradient evaluations/s (forward + adjoint)", "parameters": int(nparams),
-            "forward_ms": fwd * 1e3, "backward_ms": bwd * 1e3,
+            "forward_ms": fwd * 1e3, "backward_ms": bwd * 1e3, "backward_ms_megakernel_schedule": bwd_mk * 1e3,
             "backward_path_samples_per_s": npix * spec.spp / bwd}
 
 

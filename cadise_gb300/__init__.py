@@ -30,7 +30,7 @@ EXPORTED = [
     "cgpu_camera_rays", "cgpu_render", "cgpu_render_noalloc", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
     "cgpu_kernel_times_get", "cgpu_param_counts_get", "cgpu_params_get", "cgpu_params_set",
-    "cgpu_adjoint_forward", "cgpu_adjoint_backward", "cgpu_tuning_get", "cgpu_tuning_set", "cgpu_autotune",
+    "cgpu_adjoint_forward", "cgpu_adjoint_backward", "cgpu_set_adjoint_mode", "cgpu_tuning_get", "cgpu_tuning_set", "cgpu_autotune",
     # include/cadise_crsd.h
     "cgpu_crsd_load_file", "cgpu_crsd_load_text", "cgpu_crsd_desc", "cgpu_crsd_settings_get",
     "cgpu_crsd_primitive_index", "cgpu_crsd_free",
@@ -95,6 +95,7 @@ def load(path: Optional[str] = None):
     L.cgpu_params_set.argtypes = [vp, C.c_int32, vp, vp, vp]
     L.cgpu_adjoint_forward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp]
     L.cgpu_adjoint_backward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp, vp, vp, vp]
+    L.cgpu_set_adjoint_mode.argtypes = [vp, C.c_int32]
     L.cgpu_tuning_get.argtypes = [vp, C.POINTER(abi.cgpu_tuning)]
     L.cgpu_tuning_set.argtypes = [vp, C.POINTER(abi.cgpu_tuning)]
     L.cgpu_autotune.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_char_p, C.POINTER(abi.cgpu_tuning)]
@@ -292,6 +293,10 @@ class Context:
         img = np.zeros((flat.desc.height, flat.desc.width, 3), np.float32)
         self._check(self.L.cgpu_adjoint_forward(self.h, sid, spp, seed, _p(img)))
         return img
+
+    def set_adjoint_mode(self, mode: int) -> None:
+        """CGPU_MODE_WAVEFRONT (default) or CGPU_MODE_MEGAKERNEL schedule of adjoint_backward."""
+        self._check(self.L.cgpu_set_adjoint_mode(self.h, mode))
 
     def adjoint_backward(self, sid: int, spp: int, seed: int, d_loss_d_image: np.ndarray):
         nt, nm, nl = self.param_counts(sid)

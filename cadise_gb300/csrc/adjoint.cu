@@ -205,6 +205,14 @@ cgpu_status cgpu_adjoint_forward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uin
     return CGPU_OK;
 }
 
+cgpu_status cgpu_set_adjoint_mode(cgpu_ctx* ctx, int32_t mode) {
+    if (!ctx) return CGPU_ERR_INVALID_ARGUMENT;
+    if (mode != CGPU_MODE_MEGAKERNEL && mode != CGPU_MODE_WAVEFRONT)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "set_adjoint_mode: unknown mode");
+    ctx->adjoint_schedule = mode;
+    return CGPU_OK;
+}
+
 cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uint64_t seed, const float* dLdI,
                                   double* grad_texels, double* grad_roughness, double* grad_radiance) {
     if (!ctx) return CGPU_ERR_INVALID_ARGUMENT;
@@ -241,7 +249,27 @@ cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, ui
     if (e == cudaSuccess) e = cudaMemsetAsync(d_gt, 0, std::max<uint64_t>(ntex, 1) * sizeof(double), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_gr, 0, std::max(nmat, 1) * sizeof(double), ctx->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_gl, 0, std::max(3 * nlight, 1) * sizeof(double), ctx->stream);
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && ctx->adjoint_schedule == CGPU_MODE_WAVEFRONT) {
+        AdjBufs ab{};
+        ab.dLdI = d_dl;
+        ab.g_tex = d_gt;
+        ab.tex_offset = d_off;
+        ab.g_rough = d_gr;
+        ab.g_rad = d_gl;
+        ab.nmat = nmat;
+        ab.nlight = nlight;
+        ab.inv_spp = 1.0f / float(spp);
+        const cgpu_status ws = cg_adjoint_wavefront(ctx, scene, spp, seed, ab);
+        if (ws != CGPU_OK) {
+            cudaStreamSynchronize(ctx->stream);
+            cudaFree(d_dl);
+            cudaFree(d_gt);
+            cudaFree(d_gr);
+            cudaFree(d_gl);
+            cudaFree(d_off);
+            return ws;
+        }
+    } else if (e == cudaSuccess) {
         AdjArgs a;
         a.scenes = ctx->d_scenes;
         a.scene = scene;

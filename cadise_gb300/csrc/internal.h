@@ -43,7 +43,8 @@ struct FilmD {
 // Counters per bounce b at cnt[b * kCntStride + k]:
 //   k = 0 continuation rays to extend, 1 MIS rays to extend, 2 shadow rays,
 //   3 + kind: hits waiting for the shade kernel of that BSDF kind,
-//   8 / 9: rays handed out so far by the persistent extend / shadow kernels.
+//   8 / 9: rays handed out so far by the persistent extend / shadow kernels,
+//   10: adjoint vertices of bounce b - 1 (the wavefront adjoint's gradient kernel).
 constexpr int kCntStride = 16;
 
 struct WfBuffers {
@@ -121,6 +122,42 @@ inline size_t noalloc_layout(char* base, NoAllocView* v) {
     return off + wf_layout(base ? base + off : nullptr, kNoAllocMaxPaths, kNoAllocMaxDepth + 2, &v->wf);
 }
 
+// Wavefront adjoint (path replay in wavefront form): per path the radiance
+// of the whole path from a first wavefront pass (Ltot), the radiance of the
+// vertices replayed so far (acc), and what one vertex leaves for the gradient
+// kernel that runs once its shadow and MIS rays are traced: st_a = textured
+// albedo and texel index, st_b = d ln f / d roughness towards the shadow,
+// MIS and continuation directions + material | flags, st_c = the shadow
+// contribution without the light's radiance + the light; mis_B / mis_X = the
+// MIS half and its radiance derivative (with the light) once resolved.
+struct AdjBufs {
+    float4 *Ltot, *acc, *st_a, *st_b, *st_c, *mis_B, *mis_X;
+    int* q_vtx[2];          // paths with a vertex at bounce b, ping-pong on b
+    const float* dLdI;      // d loss / d pixel, 3 per pixel
+    double* g_tex;
+    const int* tex_offset;  // per texture: first float of its block in g_tex
+    double* g_rough;        // per material
+    double* g_rad;          // 3 per area light
+    int nmat, nlight;
+    float inv_spp;
+};
+// st_b.w bits above the 16-bit material index
+constexpr uint32_t kAdjShadow = 1u << 16, kAdjMis = 1u << 17, kAdjCont = 1u << 18, kAdjTexel = 1u << 19,
+                   kAdjGgx = 1u << 20;
+
+inline size_t adj_layout(char* base, size_t cap, AdjBufs* a) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        char* r = base ? base + off : nullptr;
+        off += (bytes + 255) & ~size_t(255);
+        return r;
+    };
+    float4** f4s[] = {&a->Ltot, &a->acc, &a->st_a, &a->st_b, &a->st_c, &a->mis_B, &a->mis_X};
+    for (float4** f : f4s) *f = reinterpret_cast<float4*>(take(cap * sizeof(float4)));
+    for (int k = 0; k < 2; ++k) a->q_vtx[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+    return off;
+}
+
 struct RenderArgs {
     const SceneD* scenes;
     const Chunk* chunks;
@@ -128,6 +165,7 @@ struct RenderArgs {
     FilmD* films;     // per scene id
     WfBuffers wf;
     unsigned long long* counters;  // closest rays, any rays, nodes, tris, paths
+    AdjBufs adj;      // wavefront adjoint only
 };
 
 }  // namespace cg
@@ -176,6 +214,11 @@ struct cgpu_ctx {
     uint32_t path_cap = 0;
     cg::WfBuffers wf{};
     void* wf_block = nullptr;
+    // wavefront adjoint state (allocated by the first wavefront adjoint)
+    uint32_t adj_cap = 0;
+    cg::AdjBufs adj{};
+    void* adj_block = nullptr;
+    int adjoint_schedule = CGPU_MODE_WAVEFRONT;
     unsigned long long* d_counters = nullptr;
 
     // captured wavefront graph
@@ -196,6 +239,7 @@ struct cgpu_ctx {
 
 // implemented in render.cu
 cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p);
+cgpu_status cg_adjoint_wavefront(cgpu_ctx* ctx, int scene, uint32_t spp, uint64_t seed, const cg::AdjBufs& params);
 cgpu_status cg_render_paths_raw(cgpu_ctx* ctx, int scene, int mode, uint32_t first, uint32_t count, uint64_t seed,
                                 float* host_rgb);
 cgpu_status cg_path_radiance(cgpu_ctx* ctx, int scene, int mode, const double* film_xy, const uint64_t* keys,

@@ -104,8 +104,11 @@ CG_D void grouped_push(int* const* queues, int* counters, int key, int p) {
 // continuation ray picks up the sky; a MIS ray that reaches its light adds
 // the BSDF-sampling half of the NEE estimate.  Returns -1 when nothing is
 // queued.
+// ADJ (wavefront adjoint): the MIS half and its derivative by the light's
+// radiance go to adj.mis_B / mis_X instead of L.
+template <bool ADJ = false>
 CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, float3 o, float3 d, bool hitp,
-                       const HitD& hit) {
+                       const HitD& hit, const AdjBufs* adj = nullptr) {
     if (cont) {
         if (hitp) {
             w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
@@ -122,19 +125,28 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
     }
     const float4 mb = w.mis_b[p];
     const int mlight = __float_as_int(mb.w);
-    float3 add = splat3(0.0f);
+    float3 add = splat3(0.0f), X = splat3(0.0f);
     bool has = false;
+    int xlight = -1;
     if (hitp) {
         if (light_of_slot(S, hit.slot) == mlight) {
             const SurfaceD hs = surface_at(S, o, d, hit);
             const float4 ma = w.mis_a[p];
-            add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w);
+            add = mis_resolve(S, hs, o, f3(mb), f3(ma), ma.w, ADJ ? &X : nullptr);
             has = true;
+            xlight = mlight;
         }
     } else if (mlight == S.env_light) {
         const float4 ma = w.mis_a[p];
         add = mis_resolve_env(S, d, f3(mb), f3(ma), ma.w);
         has = true;
+    }
+    if (ADJ) {
+        if (has) {
+            adj->mis_B[p] = make_float4(add.x, add.y, add.z, 1.0f);
+            adj->mis_X[p] = make_float4(X.x, X.y, X.z, __int_as_float(xlight));
+        }
+        return -1;
     }
     if (has) {
         float4 L = w.L[p];
@@ -146,9 +158,15 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
     return -1;
 }
 
+// ADJ: marks an unoccluded shadow ray in sh_c.w for the adjoint's gradient kernel.
+template <bool ADJ = false>
 CG_D void shadow_finish(const WfBuffers& w, int p, bool occluded) {
     if (occluded) return;
     const float4 c = w.sh_c[p];
+    if (ADJ) {
+        w.sh_c[p] = make_float4(c.x, c.y, c.z, 1.0f);
+        return;
+    }
     float4 Ls = w.Ls[p];
     Ls.x += c.x;
     Ls.y += c.y;
@@ -156,7 +174,7 @@ CG_D void shadow_finish(const WfBuffers& w, int p, bool occluded) {
     w.Ls[p] = Ls;
 }
 
-template <bool COUNT, bool SPH>
+template <bool COUNT, bool SPH, bool ADJ = false>
 __global__ void k_wf_extend(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -177,13 +195,13 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
         HitD hit;
         if (COUNT) ++nclosest;
         const bool hitp = traverse_warp<COUNT, SPH>(S, r, &hit, &tc);
-        const int key = extend_finish(w, S, p, cont, o, d, hitp, hit);
+        const int key = extend_finish<ADJ>(w, S, p, cont, o, d, hitp, hit, &a.adj);
         grouped_push(qmat, cnt + 3, key, p);
     }
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
 }
 
-template <bool COUNT, bool SPH>
+template <bool COUNT, bool SPH, bool ADJ = false>
 __global__ void k_wf_shadow(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     const int n = w.cnt[b * kCntStride + 2];
@@ -197,7 +215,7 @@ __global__ void k_wf_shadow(RenderArgs a, int b) {
         const RayPre r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
         HitD hit;
         if (COUNT) ++nany;
-        shadow_finish(w, p, traverse<true, COUNT, SPH>(S, r, &hit, &tc));
+        shadow_finish<ADJ>(w, p, traverse<true, COUNT, SPH>(S, r, &hit, &tc));
     }
     count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
 }
@@ -415,14 +433,159 @@ __global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
     count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
 }
 
-template <int KIND>
+// ------------------------------------------------------ wavefront adjoint --
+// FP64 block sums of the few roughness / radiance gradients in shared memory
+// ([0, nmat) roughness, then 3 per area light), flushed once per block.
+CG_D void adj_shared_zero(double* sh, const AdjBufs& A) {
+    for (int i = threadIdx.x; i < A.nmat + 3 * A.nlight; i += blockDim.x) sh[i] = 0.0;
+    __syncthreads();
+}
+CG_D void adj_shared_flush(double* sh, const AdjBufs& A) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < A.nmat; i += blockDim.x)
+        if (sh[i] != 0.0) atomicAdd(A.g_rough + i, sh[i]);
+    for (int i = threadIdx.x; i < 3 * A.nlight; i += blockDim.x)
+        if (sh[A.nmat + i] != 0.0) atomicAdd(A.g_rad + i, sh[A.nmat + i]);
+}
+CG_D void adj_add(double* sh, int i, double v) {
+    if (v != 0.0) atomicAdd(sh + i, v);
+}
+CG_D float3 adj_delta(const AdjBufs& A, uint32_t pixel) {
+    return mk(A.dLdI[3 * pixel] * A.inv_spp, A.dLdI[3 * pixel + 1] * A.inv_spp, A.dLdI[3 * pixel + 2] * A.inv_spp);
+}
+
+// The adjoint's part of shading vertex b of path p (the replay of adjoint.cuh,
+// split at the point where the vertex's shadow and MIS rays are traced): the
+// emission term's radiance gradient now, the rest kept for k_adj_vertex.
+// Returns whether the path carries gradient (finite total, nonzero weight).
+CG_D bool adj_vertex_begin(const RenderArgs& a, double* sh, const SceneD& S, const SurfaceD& si, const VertexPlan& pl,
+                           float4 tw, int p, uint32_t pixel) {
+    const AdjBufs& A = a.adj;
+    const float3 delta = adj_delta(A, pixel);
+    if (!finite3(f3(A.Ltot[p])) || is_zero(delta)) return false;
+    const bool ce = (__float_as_int(tw.w) & 1) != 0;
+    if (si.light >= 0 && si.light < A.nlight && ce && can_emit(S.lights[si.light], si.wi, si.Ns)) {
+        const float3 gx = delta * f3(tw);
+        adj_add(sh + A.nmat, 3 * si.light + 0, gx.x);
+        adj_add(sh + A.nmat, 3 * si.light + 1, gx.y);
+        adj_add(sh + A.nmat, 3 * si.light + 2, gx.z);
+    }
+    const float4 acc = A.acc[p];
+    A.acc[p] = make_float4(acc.x + pl.emit.x, acc.y + pl.emit.y, acc.z + pl.emit.z, 0.0f);
+    const MaterialD& m = S.materials[si.material];
+    uint32_t bits = uint32_t(si.material) | (pl.shadow ? kAdjShadow : 0u) | (pl.mis ? kAdjMis : 0u) |
+                    (pl.cont ? kAdjCont : 0u);
+    if (m.type == BSDF_LAMBERTIAN && m.albedo_tex >= 0) {
+        const TextureD& tex = S.textures[m.albedo_tex];
+        const float3 alb = texture_rgb(tex, si.uvw);
+        A.st_a[p] = make_float4(alb.x, alb.y, alb.z, __int_as_float(3 * texel_index(tex, si.uvw)));
+        bits |= kAdjTexel;
+    }
+    float gs = 0.0f, gb = 0.0f, gc = 0.0f;
+    if (m.type == BSDF_CONDUCTOR || m.type == BSDF_DIELECTRIC_GGX) {
+        if (pl.shadow) gs = dlogf_droughness(m, si.wi, pl.sdir, si.Ns);
+        if (pl.mis) gb = dlogf_droughness(m, si.wi, pl.mdir, si.Ns);
+        if (pl.cont) gc = dlogf_droughness(m, si.wi, pl.cdir, si.Ns);
+        bits |= kAdjGgx;
+    }
+    A.st_b[p] = make_float4(gs, gb, gc, __uint_as_float(bits));
+    if (pl.shadow) A.st_c[p] = make_float4(pl.sx.x, pl.sx.y, pl.sx.z, __int_as_float(pl.slight));
+    if (pl.mis) A.mis_B[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    return true;
+}
+
+// Vertices of bounce b, once their shadow (bounce b + 1 shadow pass) and MIS
+// (bounce b + 1 extend pass) rays are traced: A, B and the radiance of the
+// vertices after this one (R = Ltot - acc - A - B) give the texel, roughness
+// and radiance terms of adjoint.cuh.
+__global__ void k_adj_vertex(RenderArgs a, int b) {
+    extern __shared__ double sh[];
+    const WfBuffers& w = a.wf;
+    const AdjBufs& A = a.adj;
+    adj_shared_zero(sh, A);
+    const int n = w.cnt[(b + 1) * kCntStride + 10];
+    const int* q = A.q_vtx[b & 1];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = q[i];
+        const uint4 meta = w.meta[p];
+        const SceneD& S = a.scenes[meta.x];
+        const float3 delta = adj_delta(A, meta.y);
+        const float4 sb = A.st_b[p];
+        const uint32_t bits = __float_as_uint(sb.w);
+        const int mat = int(bits & 0xFFFFu);
+        float3 Av = splat3(0.0f), Bv = splat3(0.0f);
+        if (bits & kAdjShadow) {
+            const float4 c = w.sh_c[p];
+            if (c.w != 0.0f) {
+                Av = f3(c);
+                const float4 sc = A.st_c[p];
+                const int slight = __float_as_int(sc.w);
+                if (slight < A.nlight) {
+                    const float3 gx = delta * f3(sc);
+                    adj_add(sh + A.nmat, 3 * slight + 0, gx.x);
+                    adj_add(sh + A.nmat, 3 * slight + 1, gx.y);
+                    adj_add(sh + A.nmat, 3 * slight + 2, gx.z);
+                }
+            }
+        }
+        if (bits & kAdjMis) {
+            const float4 mb = A.mis_B[p];
+            if (mb.w != 0.0f) {
+                Bv = f3(mb);
+                const float4 mx = A.mis_X[p];
+                const int xl = __float_as_int(mx.w);
+                if (xl >= 0 && xl < A.nlight) {
+                    const float3 gx = delta * f3(mx);
+                    adj_add(sh + A.nmat, 3 * xl + 0, gx.x);
+                    adj_add(sh + A.nmat, 3 * xl + 1, gx.y);
+                    adj_add(sh + A.nmat, 3 * xl + 2, gx.z);
+                }
+            }
+        }
+        const float3 acc = f3(A.acc[p]);
+        const float3 after = f3(A.Ltot[p]) - acc - Av - Bv;
+        if (bits & kAdjTexel) {
+            const float4 sa = A.st_a[p];
+            const float3 num = delta * (Av + Bv + after);
+            double* g = A.g_tex + A.tex_offset[S.materials[mat].albedo_tex] + __float_as_int(sa.w);
+            if (sa.x > 0.0f && num.x != 0.0f) atomicAdd(g + 0, double(num.x / sa.x));
+            if (sa.y > 0.0f && num.y != 0.0f) atomicAdd(g + 1, double(num.y / sa.y));
+            if (sa.z > 0.0f && num.z != 0.0f) atomicAdd(g + 2, double(num.z / sa.z));
+        }
+        if (bits & kAdjGgx) {
+            float gr = 0.0f;
+            if (!is_zero(Av)) gr += dot(delta, Av) * sb.x;
+            if (!is_zero(Bv)) gr += dot(delta, Bv) * sb.y;
+            if (bits & kAdjCont) gr += dot(delta, after) * sb.z;
+            adj_add(sh, mat, double(gr));
+        }
+        const float3 nacc = acc + (Av + Bv);
+        A.acc[p] = make_float4(nacc.x, nacc.y, nacc.z, 0.0f);
+    }
+    adj_shared_flush(sh, A);
+}
+
+// Between the two wavefront passes of the adjoint: every path's total
+// radiance from the first, and a zero replay accumulator for the second.
+__global__ void k_adj_ltot(RenderArgs a) {
+    const BatchHeader h = *a.header;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < h.total_paths; p += gridDim.x * blockDim.x) {
+        const float3 v = path_sample(f3(a.wf.L[p]), f3(a.wf.Le[p]), f3(a.wf.Ls[p]));
+        a.adj.Ltot[p] = make_float4(v.x, v.y, v.z, 0.0f);
+        a.adj.acc[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    }
+}
+
+template <int KIND, bool ADJ = false>
 __global__ void k_wf_shade(RenderArgs a, int b) {
+    extern __shared__ double adj_sh[];  // ADJ only: gradient block sums
     const WfBuffers& w = a.wf;
     const int n = w.cnt[b * kCntStride + 3 + KIND];
     int* next = w.cnt + (b + 1) * kCntStride;
     const int* q = w.q_mat[KIND];
     const int nb = (b + 1) & 1;
     const uint64_t seed = a.header->seed;
+    if (ADJ) adj_shared_zero(adj_sh, a.adj);
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const int p = q[i];
         uint4 meta = w.meta[p];
@@ -440,14 +603,19 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
         rng.key = path_key(seed, meta.x, meta.y, meta.z);
         rng.ctr = meta.w;
         const VertexPlan pl = plan_vertex<KIND>(S, si, f3(tw), (__float_as_int(tw.w) & 1) != 0, b, rng);
-        if (!is_zero(pl.emit)) {
+        bool adj_live = false;
+        if (ADJ) {
+            adj_live = adj_vertex_begin(a, adj_sh, S, si, pl, tw, p, meta.y);
+        } else if (!is_zero(pl.emit)) {
             float4 L = w.L[p];
             L.x += pl.emit.x;
             L.y += pl.emit.y;
             L.z += pl.emit.z;
             w.L[p] = L;
         }
-        const bool cont = pl.cont && (b + 1 < S.max_depth);
+        // the adjoint drops a path that carries no gradient
+        const bool live = !ADJ || adj_live;
+        const bool cont = live && pl.cont && (b + 1 < S.max_depth);
         if (pl.shadow || pl.mis || cont) w.ray_o[p] = make_float4(si.P.x, si.P.y, si.P.z, 0.0f);
         if (pl.shadow) {
             w.sh_d[p] = make_float4(pl.sdir.x, pl.sdir.y, pl.sdir.z, pl.stmax);
@@ -464,13 +632,18 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
         }
         meta.w = rng.ctr;
         w.meta[p] = meta;
-        const int s_slot = warp_append(next + 2, pl.shadow != 0);
+        const int s_slot = warp_append(next + 2, live && pl.shadow != 0);
         if (s_slot >= 0) w.q_shadow[nb][s_slot] = p;
-        const int m_slot = warp_append(next + 1, pl.mis != 0);
+        const int m_slot = warp_append(next + 1, live && pl.mis != 0);
         if (m_slot >= 0) w.q_mis[nb][m_slot] = p;
         const int c_slot = warp_append(next + 0, cont);
         if (c_slot >= 0) w.q_cont[nb][c_slot] = p;
+        if (ADJ) {
+            const int v_slot = warp_append(next + 10, adj_live);
+            if (v_slot >= 0) a.adj.q_vtx[b & 1][v_slot] = p;
+        }
     }
+    if (ADJ) adj_shared_flush(adj_sh, a.adj);
 }
 
 // FP64 accumulation of one batch into the scenes' films (box filter of
@@ -568,9 +741,9 @@ namespace {
 constexpr int kBlock = 128;  // fixed-size utility kernels
 
 template <typename K>
-int grid_for(cgpu_ctx* ctx, K kernel, int block, uint64_t work) {
+int grid_for(cgpu_ctx* ctx, K kernel, int block, uint64_t work, size_t shared_bytes = 0) {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, shared_bytes);
     if (per_sm < 1) per_sm = 1;
     const uint64_t full = uint64_t(ctx->num_sms) * uint64_t(per_sm);
     const uint64_t need = (work + block - 1) / block;
@@ -769,6 +942,12 @@ void cg_free_render_state(cgpu_ctx* ctx) {
     }
     ctx->wf = WfBuffers{};
     ctx->path_cap = 0;
+    if (ctx->adj_block) {
+        cudaFree(ctx->adj_block);
+        ctx->adj_block = nullptr;
+    }
+    ctx->adj = AdjBufs{};
+    ctx->adj_cap = 0;
 }
 
 // Split the requested samples of every scene into batches of at most
@@ -954,6 +1133,135 @@ cgpu_status cg_film_clear(cgpu_ctx* ctx, int scene) {
     cudaMemsetAsync(sl.film.sumsq, 0, npix * 3 * sizeof(double), ctx->stream);
     cudaMemsetAsync(sl.film.count, 0, npix * sizeof(double), ctx->stream);
     return cg_cuda(ctx, cudaGetLastError(), "film clear");
+}
+
+// ======================================================= wavefront adjoint ==
+// cgpu_adjoint_backward on the wavefront schedule.  Per batch of whole
+// samples of the scene: (A) the forward wavefront render of the batch without
+// the film splat, whose per-path radiance is the Ltot of each path; (B) the
+// same paths regenerated and replayed pass by pass with the adjoint variants
+// of the kernels (extend / shadow store the MIS and shadow outcomes instead of
+// adding them; shade keeps each vertex's state and queues it), and after each
+// traversal pass the gradient kernel of the vertices whose rays it traced.
+namespace {
+
+void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_t paths, size_t shared_bytes) {
+    cudaStream_t s = ctx->stream, side = ctx->side;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    cudaMemsetAsync(ctx->wf.cnt, 0, size_t(depth + 2) * kCntStride * sizeof(int), s);
+    const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
+    const bool sph = ctx->batch_spheres;
+    auto ext = sph ? k_wf_extend<false, true, true> : k_wf_extend<false, false, true>;
+    auto shd = sph ? k_wf_shadow<false, true, true> : k_wf_shadow<false, false, true>;
+    void (*shade[kNumBsdfKinds])(RenderArgs, int) = {k_wf_shade<0, true>, k_wf_shade<1, true>, k_wf_shade<2, true>,
+                                                     k_wf_shade<3, true>, k_wf_shade<4, true>};
+    k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
+    const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, shd, bt, paths);
+    const int gv = grid_for(ctx, k_adj_vertex, kBlock, paths, shared_bytes);
+    int gsd[kNumBsdfKinds];
+    for (int k = 0; k < kNumBsdfKinds; ++k) gsd[k] = grid_for(ctx, shade[k], bs, paths, shared_bytes);
+    uint32_t launches = 1;
+    for (int b = 0; b <= depth; ++b) {
+        cudaEventRecord(fork, s);
+        cudaStreamWaitEvent(side, fork, 0);
+        ext<<<gext, bt, 0, s>>>(a, b);
+        shd<<<gsh, bt, 0, side>>>(a, b);
+        cudaEventRecord(join, side);
+        cudaStreamWaitEvent(s, join, 0);
+        launches += 2;
+        if (b > 0) {
+            k_adj_vertex<<<gv, kBlock, shared_bytes, s>>>(a, b - 1);
+            launches += 1;
+        }
+        if (b == depth) break;
+        for (int k = 0; k < kNumBsdfKinds; ++k) shade[k]<<<gsd[k], bs, shared_bytes, s>>>(a, b);
+        launches += kNumBsdfKinds;
+    }
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
+    ctx->stats.kernel_launches += launches;
+}
+
+cgpu_status ensure_adj_buffers(cgpu_ctx* ctx) {
+    if (ctx->adj_cap >= ctx->path_cap && ctx->adj_block) return CGPU_OK;
+    if (ctx->adj_block) cudaFree(ctx->adj_block);
+    ctx->adj_block = nullptr;
+    ctx->adj_cap = 0;
+    AdjBufs tmp{};
+    const size_t bytes = adj_layout(nullptr, ctx->path_cap, &tmp);
+    cudaError_t e = cudaMalloc(&ctx->adj_block, bytes);
+    if (e != cudaSuccess) {
+        ctx->adj_block = nullptr;
+        return cg_fail(ctx, CGPU_ERR_OUT_OF_MEMORY, "adjoint buffers: " + std::string(cudaGetErrorString(e)));
+    }
+    adj_layout(static_cast<char*>(ctx->adj_block), ctx->path_cap, &ctx->adj);
+    ctx->adj_cap = ctx->path_cap;
+    return CGPU_OK;
+}
+
+}  // namespace
+
+cgpu_status cg_adjoint_wavefront(cgpu_ctx* ctx, int scene, uint32_t spp, uint64_t seed, const AdjBufs& params) {
+    const SceneSlot& sl = ctx->scenes[scene];
+    const uint32_t npix = uint32_t(sl.width) * uint32_t(sl.height);
+    ctx->batch_spheres = sl.has_spheres;
+    cgpu_status st = cg_sync_tables(ctx);
+    if (st != CGPU_OK) return st;
+    st = ensure_path_buffers(ctx, paths_capacity(ctx, npix), sl.max_depth);
+    if (st != CGPU_OK) return st;
+    st = ensure_adj_buffers(ctx);
+    if (st != CGPU_OK) return st;
+    const size_t shared_bytes = size_t(params.nmat + 3 * params.nlight) * sizeof(double);
+    if (shared_bytes > 48 * 1024) {
+        const int sb = int(shared_bytes);
+        cudaFuncSetAttribute(k_adj_vertex, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+        cudaFuncSetAttribute(k_wf_shade<0, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+        cudaFuncSetAttribute(k_wf_shade<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+        cudaFuncSetAttribute(k_wf_shade<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+        cudaFuncSetAttribute(k_wf_shade<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+        cudaFuncSetAttribute(k_wf_shade<4, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb);
+    }
+    RenderArgs a = make_args(ctx);
+    a.adj = params;
+    a.adj.Ltot = ctx->adj.Ltot;
+    a.adj.acc = ctx->adj.acc;
+    a.adj.st_a = ctx->adj.st_a;
+    a.adj.st_b = ctx->adj.st_b;
+    a.adj.st_c = ctx->adj.st_c;
+    a.adj.mis_B = ctx->adj.mis_B;
+    a.adj.mis_X = ctx->adj.mis_X;
+    a.adj.q_vtx[0] = ctx->adj.q_vtx[0];
+    a.adj.q_vtx[1] = ctx->adj.q_vtx[1];
+    ctx->stats = cgpu_render_stats{};
+    const uint32_t per = std::max<uint32_t>(1, ctx->path_cap / npix);
+    const int depth = sl.max_depth;
+    for (uint32_t done = 0; done < spp;) {
+        const uint32_t k = std::min(per, spp - done);
+        const uint32_t paths = k * npix;
+        cudaStreamSynchronize(ctx->stream);
+        ctx->h_chunks[0] = Chunk{scene, 0, npix, uint32_t(sl.width), done, k, 0, 0};
+        BatchHeader& h = *ctx->h_header;
+        h.num_chunks = 1;
+        h.total_paths = paths;
+        h.total_pixels = npix;
+        h.max_depth = depth;
+        h.seed = seed;
+        cudaMemcpyAsync(ctx->d_chunks, ctx->h_chunks, sizeof(Chunk), cudaMemcpyHostToDevice, ctx->stream);
+        cudaMemcpyAsync(ctx->d_header, ctx->h_header, sizeof(BatchHeader), cudaMemcpyHostToDevice, ctx->stream);
+        st = enqueue_wavefront(ctx, depth, paths, false, false);
+        if (st != CGPU_OK) return st;
+        k_adj_ltot<<<grid_for(ctx, k_adj_ltot, 256, paths), 256, 0, ctx->stream>>>(a);
+        ctx->stats.kernel_launches += 1;
+        enqueue_adjoint_pass(ctx, a, depth, paths, shared_bytes);
+        st = cg_cuda(ctx, cudaGetLastError(), "adjoint wavefront launch");
+        if (st != CGPU_OK) return st;
+        ctx->stats.batches += 1;
+        done += k;
+    }
+    ctx->stats.paths = uint64_t(spp) * npix;
+    return CGPU_OK;
 }
 
 // =========================================================== no-alloc render ==

@@ -338,6 +338,12 @@ cgpu_status cgpu_adjoint_forward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uin
 cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uint64_t seed,
                                   const float* d_loss_d_image, double* grad_texels, double* grad_roughness,
                                   double* grad_radiance);
+/* Schedule of cgpu_adjoint_backward: CGPU_MODE_WAVEFRONT (default; a forward
+ * wavefront pass for each path's radiance, then a wavefront replay with a
+ * gradient kernel after each traversal pass) or CGPU_MODE_MEGAKERNEL (one
+ * thread replays one path twice).  Both compute the same estimator on the
+ * same path samples; they differ in FP64 summation order only. */
+cgpu_status cgpu_set_adjoint_mode(cgpu_ctx* ctx, int32_t mode);
 
 /* Per-kernel CUDA-event timing of the following renders (launches are made
  * one by one instead of through the captured graph while it is on, and the
