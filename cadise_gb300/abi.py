@@ -64,6 +64,33 @@ class cgpu_area_light(C.Structure):
                 ("back_face_emit", C.c_int32)]
 
 
+CGPU_FILTER_BOX = 0
+CGPU_FILTER_GAUSSIAN = 1
+CGPU_FILTER_MITCHELL = 2
+CGPU_FILTER_CONE = 3
+FILTER_OF_NAME = {"box": CGPU_FILTER_BOX, "gaussian": CGPU_FILTER_GAUSSIAN, "mitchell": CGPU_FILTER_MITCHELL,
+                  "cone": CGPU_FILTER_CONE}
+
+
+class cgpu_film_filter(C.Structure):
+    _fields_ = [("type", C.c_int32), ("width", C.c_float), ("height", C.c_float),
+                ("sigma_x", C.c_float), ("sigma_y", C.c_float), ("amplitude", C.c_float),
+                ("b", C.c_float), ("c", C.c_float), ("tile_width", C.c_int32), ("tile_height", C.c_int32)]
+
+
+def film_filter_struct(f) -> "cgpu_film_filter":
+    """cgpu_film_filter of a scenes.FilmFilter (None: the default box)."""
+    out = cgpu_film_filter()
+    if f is None:
+        return out
+    out.type = FILTER_OF_NAME[f.type]
+    out.width, out.height = f.size()
+    out.sigma_x, out.sigma_y, out.amplitude = f.sigma_x, f.sigma_y, f.amplitude
+    out.b, out.c = f.b, f.c
+    out.tile_width, out.tile_height = f.tile
+    return out
+
+
 class cgpu_scene_desc(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32),
                 ("cam_position", C.c_float * 3), ("cam_direction", C.c_float * 3), ("cam_up", C.c_float * 3),
@@ -75,7 +102,8 @@ class cgpu_scene_desc(C.Structure):
                 ("num_materials", C.c_uint32), ("materials", C.POINTER(cgpu_material)),
                 ("num_textures", C.c_uint32), ("textures", C.POINTER(cgpu_texture)),
                 ("num_lights", C.c_uint32), ("lights", C.POINTER(cgpu_area_light)),
-                ("environment_texture", C.c_int32), ("light_cluster", C.c_int32)]
+                ("environment_texture", C.c_int32), ("light_cluster", C.c_int32),
+                ("filter", cgpu_film_filter)]
 
 
 class cgpu_scene_info(C.Structure):
@@ -245,4 +273,5 @@ def flatten(spec: "S.SceneSpec") -> FlatScene:
     d.lights = lights
     d.environment_texture = tex_index[spec.environment] + 1 if spec.environment else 0
     d.light_cluster = {"uniform": 0, "power": 1}[spec.light_cluster]
+    d.filter = film_filter_struct(spec.film_filter)
     return FlatScene(d, kind, verts, mat, normals, uvws, mats, lights, texs, tex_arrays, names, mat_index)

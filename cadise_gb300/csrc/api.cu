@@ -248,6 +248,7 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.max_depth = d->max_depth;
     S.spp = d->spp > 0 ? d->spp : 1;
     S.cam = hs.cam;
+    S.filter = hs.filter;
     sl.width = d->width;
     sl.height = d->height;
     sl.spp = S.spp;

@@ -48,6 +48,8 @@ struct FilmD {
 constexpr int kCntStride = 16;
 
 struct WfBuffers {
+    // L.w and Ls.w hold the sample's film position (x, y) for the film filter;
+    // the passes update L and Ls in place and leave .w as it is.
     float4 *ray_o, *ray_d, *hit, *thr, *L, *Ls, *mis_a, *mis_b, *mis_d, *sh_d, *sh_c;
     // Sky radiance picked up by an escaped continuation ray.  Kept apart from
     // L: the MIS ray of the same path's last vertex adds to L in the same

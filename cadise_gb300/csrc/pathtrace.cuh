@@ -32,7 +32,9 @@ CG_D PathId path_id(const Chunk* chunks, int nchunks, uint32_t p) {
     return id;
 }
 
-CG_D void primary_ray(const SceneD& S, const PathId& id, uint64_t seed, Rng& rng, float3* o, float3* d) {
+// fxy (optional): the sample's film position, for the film filter.
+CG_D void primary_ray(const SceneD& S, const PathId& id, uint64_t seed, Rng& rng, float3* o, float3* d,
+                      float2* fxy = nullptr) {
     rng.key = path_key(seed, uint32_t(id.scene), id.pixel, id.sample);
     rng.ctr = 0;
     float jx, jy;
@@ -40,6 +42,7 @@ CG_D void primary_ray(const SceneD& S, const PathId& id, uint64_t seed, Rng& rng
     const float fx = float(id.pixel % id.width) + jx;
     const float fy = float(id.pixel / id.width) + jy;
     camera_ray(S.cam, fx, fy, o, d);
+    if (fxy) *fxy = make_float2(fx, fy);
 }
 
 CG_D int light_of_slot(const SceneD& S, int slot) {

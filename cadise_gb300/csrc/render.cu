@@ -13,6 +13,7 @@
 //            -> extend(max_depth) || shadow(max_depth) -> splat
 // Queues hold path ids; per-path state lives in SoA arrays indexed by path.
 // Queue appends are warp-aggregated (ballot / match + one atomic per group).
+#include "film.cuh"
 #include "internal.h"
 #include "pathtrace.cuh"
 
@@ -33,12 +34,13 @@ __global__ void k_megakernel(RenderArgs a) {
         const SceneD& S = a.scenes[id.scene];
         Rng rng;
         float3 o, d;
-        primary_ray(S, id, h.seed, rng, &o, &d);
+        float2 fxy;
+        primary_ray(S, id, h.seed, rng, &o, &d, &fxy);
         float3 L, Le, Ls;
         mk_path<COUNT, SPH>(S, o, d, rng, &L, &Le, &Ls, &tc, &ta, &nc, &na);
-        a.wf.L[p] = make_float4(L.x, L.y, L.z, 0.0f);
+        a.wf.L[p] = make_float4(L.x, L.y, L.z, fxy.x);
         a.wf.Le[p] = make_float4(Le.x, Le.y, Le.z, 0.0f);
-        a.wf.Ls[p] = make_float4(Ls.x, Ls.y, Ls.z, 0.0f);
+        a.wf.Ls[p] = make_float4(Ls.x, Ls.y, Ls.z, fxy.y);
     }
     count_flush<COUNT>(a.counters, tc, ta, nc, na);
 }
@@ -73,13 +75,14 @@ __global__ void k_wf_generate(RenderArgs a) {
         const SceneD& S = a.scenes[id.scene];
         Rng rng;
         float3 o, d;
-        primary_ray(S, id, h.seed, rng, &o, &d);
+        float2 fxy;
+        primary_ray(S, id, h.seed, rng, &o, &d, &fxy);
         w.ray_o[p] = make_float4(o.x, o.y, o.z, 0.0f);
         w.ray_d[p] = make_float4(d.x, d.y, d.z, 0.0f);
         w.thr[p] = make_float4(1.0f, 1.0f, 1.0f, __int_as_float(1));
-        w.L[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.L[p] = make_float4(0.0f, 0.0f, 0.0f, fxy.x);
         w.Le[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        w.Ls[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        w.Ls[p] = make_float4(0.0f, 0.0f, 0.0f, fxy.y);
         w.meta[p] = make_uint4(uint32_t(id.scene), id.pixel, id.sample, rng.ctr);
         w.q_cont[0][p] = int(p);
     }
@@ -646,10 +649,10 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
     if (ADJ) adj_shared_flush(adj_sh, a.adj);
 }
 
-// FP64 accumulation of one batch into the scenes' films (box filter of
-// width 1: a sample at (ix + fx, iy + fy) lands in pixel (ix, iy) only);
-// NaN / Inf samples are dropped as FilmTile::addSample does
-// (source/core/film/filmTile.cpp:21-28).
+// FP64 accumulation of one batch into the scenes' films.  With the default
+// box filter of size 1 a sample at (ix + fx, iy + fy) lands in pixel (ix, iy)
+// only; other filters go through splat_filtered.  NaN / Inf samples are
+// dropped as FilmTile::addSample does (source/core/film/filmTile.cpp:21-28).
 __global__ void k_splat(RenderArgs a) {
     const BatchHeader h = *a.header;
     for (uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < h.total_pixels; idx += gridDim.x * blockDim.x) {
@@ -660,6 +663,27 @@ __global__ void k_splat(RenderArgs a) {
         }
         const Chunk c = a.chunks[lo];
         const uint32_t pixel = idx - c.pix_begin;
+        const FilterD& F = a.scenes[c.scene].filter;
+        if (!F.pixel_only) {
+            double s[3] = {0, 0, 0}, q[3] = {0, 0, 0}, n = 0;
+            const int W = int(c.width);
+            auto fetch = [&](uint32_t k, int sx, int sy, float3* v, float2* pos) {
+                const uint32_t p = c.path_begin + k * c.npix + uint32_t(sy * W + sx);
+                const float4 L = a.wf.L[p], Ls = a.wf.Ls[p];
+                *v = path_sample(f3(L), f3(a.wf.Le[p]), f3(Ls));
+                *pos = make_float2(L.w, Ls.w);
+                return isfinite(v->x) && isfinite(v->y) && isfinite(v->z);
+            };
+            filter_gather(F, W, int(c.npix / c.width), int(pixel % c.width), int(pixel / c.width), c.nsamples, fetch, s,
+                          q, &n);
+            const FilmD f = a.films[c.scene];
+            for (int k = 0; k < 3; ++k) {
+                f.sum[3 * pixel + k] += s[k];
+                f.sumsq[3 * pixel + k] += q[k];
+            }
+            f.count[pixel] += n;
+            continue;
+        }
         double s0 = 0, s1 = 0, s2 = 0, q0 = 0, q1 = 0, q2 = 0, n = 0;
         for (uint32_t k = 0; k < c.nsamples; ++k) {
             const uint32_t p = c.path_begin + k * c.npix + pixel;

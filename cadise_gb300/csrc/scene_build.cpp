@@ -37,8 +37,48 @@ bool zeroh(HostV3 a) { return a.x == 0.0f && a.y == 0.0f && a.z == 0.0f; }
 
 }  // namespace
 
+// The filter constants are computed here in FP32 with the C library's exp,
+// as the reference's filter constructors compute them
+// (gaussianFilter.cpp:9-25, filter.cpp:19-21).
+cgpu_status resolve_filter(const cgpu_film_filter& f, FilterD* out, std::string* err) {
+    FilterD F{};
+    F.type = f.type;
+    float w = f.width, h = f.height;
+    if (f.type == CGPU_FILTER_BOX) {
+        if (w == 0.0f) w = 1.0f;
+        if (h == 0.0f) h = 1.0f;
+    } else if (f.type != CGPU_FILTER_GAUSSIAN && f.type != CGPU_FILTER_MITCHELL && f.type != CGPU_FILTER_CONE) {
+        return fail(err, CGPU_ERR_INVALID_ARGUMENT, "unknown film filter");
+    }
+    if (!(w > 0.0f) || !(h > 0.0f) || !std::isfinite(w) || !std::isfinite(h) || w > 64.0f || h > 64.0f)
+        return fail(err, CGPU_ERR_INVALID_ARGUMENT, "film filter size must be in (0, 64]");
+    F.tile_w = f.tile_width == 0 ? 16 : f.tile_width;
+    F.tile_h = f.tile_height == 0 ? 16 : f.tile_height;
+    if (F.tile_w <= 0 || F.tile_h <= 0) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "film tile size must be positive");
+    F.hx = w / 2.0f;
+    F.hy = h / 2.0f;
+    F.pixel_only = (f.type == CGPU_FILTER_BOX && w == 1.0f && h == 1.0f) ? 1 : 0;
+    if (f.type == CGPU_FILTER_GAUSSIAN) {
+        if (!(f.sigma_x > 0.0f) || !(f.sigma_y > 0.0f))
+            return fail(err, CGPU_ERR_INVALID_ARGUMENT, "gaussian filter sigma must be positive");
+        F.p0 = -1.0f / (2.0f * f.sigma_x * f.sigma_x);
+        F.p1 = -1.0f / (2.0f * f.sigma_y * f.sigma_y);
+        F.p3 = f.amplitude;
+        F.p2 = f.amplitude * std::exp(F.p0 * F.hx * F.hx + F.p1 * F.hy * F.hy);
+    } else if (f.type == CGPU_FILTER_MITCHELL) {
+        F.p0 = f.b;
+        F.p1 = f.c;
+    }
+    *out = F;
+    return CGPU_OK;
+}
+
 cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err) {
     if (!d) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "null scene description");
+    {
+        const cgpu_status fs = resolve_filter(d->filter, &out->filter, err);
+        if (fs != CGPU_OK) return fs;
+    }
     if (d->num_primitives == 0 || !d->prim_vertices || !d->prim_material)
         return fail(err, CGPU_ERR_INVALID_ARGUMENT, "no primitives");
     if (d->width <= 0 || d->height <= 0 || d->max_depth < 0)
@@ -418,6 +458,7 @@ SceneD host_view(HostScene& hs, const cgpu_scene_desc* d) {
     S.max_depth = d->max_depth;
     S.spp = d->spp > 0 ? d->spp : 1;
     S.cam = hs.cam;
+    S.filter = hs.filter;
     return S;
 }
 

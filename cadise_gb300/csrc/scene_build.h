@@ -26,10 +26,15 @@ struct HostScene {
     std::vector<float> rect_frames;  // vB, eA, eB per rectangle
     std::vector<float> light_cdf;    // power light cluster: num_lights + 1 CDF values; empty: uniform
     CameraD cam{};
+    FilterD filter{};
     cgpu_scene_info info{};
     int wide_depth = 0;
     bool has_spheres = false;
 };
+
+// Resolves a cgpu_film_filter (defaults, derived constants); CGPU_OK or an
+// error status with a message in *err.
+cgpu_status resolve_filter(const cgpu_film_filter& f, FilterD* out, std::string* err);
 
 // Returns CGPU_OK or an error status with a message in *err.
 cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err);

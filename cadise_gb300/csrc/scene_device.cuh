@@ -117,6 +117,18 @@ struct CameraD {
     float sx, sy, tx, ty, offset;
 };
 
+// Film filter of a scene (cgpu_film_filter resolved at upload).  pixel_only:
+// the default box of size 1, whose footprint is the sample's own pixel.
+// Gaussian: p0 / p1 = -1 / (2 sigma^2) in x / y, p2 = the value at the corner
+// of the footprint, p3 = amplitude.  Mitchell: p0 = b, p1 = c.
+struct FilterD {
+    int type;
+    int pixel_only;
+    float hx, hy;  // half the filter's size
+    float p0, p1, p2, p3;
+    int tile_w, tile_h;
+};
+
 struct SceneD {
     const Bvh4Node* nodes;
     const TriRecord* tris;
@@ -134,6 +146,7 @@ struct SceneD {
     int max_depth;
     int spp;
     CameraD cam;
+    FilterD filter;
 };
 
 }  // namespace cg

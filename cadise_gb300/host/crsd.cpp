@@ -446,9 +446,26 @@ struct cgpu_crsd_scene {
             const std::string t = find_str(*accel, "type", "bvh");
             if (t != "bvh" && t != "bruteForce" && t != "kd-tree") fail(CGPU_ERR_UNSUPPORTED, "accelerator '" + t + "'");
         }
-        if (find_str(*film, "filter", "box") != "box") fail(CGPU_ERR_UNSUPPORTED, "film filter (box only)");
-        if (find_real(*film, "filter-width", 1.0f) != 1.0f || find_real(*film, "filter-height", 1.0f) != 1.0f)
-            fail(CGPU_ERR_UNSUPPORTED, "box filter size other than 1");
+        {
+            // filterInstantiator.cpp:16-57 (defaults), filmInstantiator.cpp:22-23 (tile size)
+            const std::string ft = find_str(*film, "filter", "box");
+            cgpu_film_filter& f = desc.filter;
+            const float size_default = ft == "box" ? 1.0f : 4.0f;
+            if (ft == "box") f.type = CGPU_FILTER_BOX;
+            else if (ft == "gaussian") f.type = CGPU_FILTER_GAUSSIAN;
+            else if (ft == "mitchell") f.type = CGPU_FILTER_MITCHELL;
+            else if (ft == "cone") f.type = CGPU_FILTER_CONE;
+            else fail(CGPU_ERR_UNSUPPORTED, "film filter '" + ft + "'");
+            f.width = find_real(*film, "filter-width", size_default);
+            f.height = find_real(*film, "filter-height", size_default);
+            f.sigma_x = find_real(*film, "sigma-x", 0.5f);
+            f.sigma_y = find_real(*film, "sigma-y", 0.5f);
+            f.amplitude = find_real(*film, "amplitude", 1.0f);
+            f.b = find_real(*film, "b", 1.0f / 3.0f);
+            f.c = find_real(*film, "c", 1.0f / 3.0f);
+            f.tile_width = find_int(*film, "tile-size-x", 16);
+            f.tile_height = find_int(*film, "tile-size-y", 16);
+        }
         if (find_str(*camera, "type", "") != "perspective-pinhole") fail(CGPU_ERR_UNSUPPORTED, "camera type");
         desc.width = find_int(*film, "image-width", 1024);
         desc.height = find_int(*film, "image-height", 768);

@@ -111,6 +111,26 @@ class ImageTexture:
 
 
 @dataclass
+class FilmFilter:
+    """Film reconstruction filter, CRSD film block keys (filterInstantiator.cpp:16-57):
+    type box | gaussian | mitchell | cone; width / height default 1 for the box,
+    4 for the others; tile = the film tile size clipping each sample's footprint."""
+    type: str = "box"
+    width: Optional[float] = None
+    height: Optional[float] = None
+    sigma_x: float = 0.5
+    sigma_y: float = 0.5
+    amplitude: float = 1.0
+    b: float = 1.0 / 3.0
+    c: float = 1.0 / 3.0
+    tile: tuple = (16, 16)
+
+    def size(self):
+        d = 1.0 if self.type == "box" else 4.0
+        return (self.width if self.width is not None else d, self.height if self.height is not None else d)
+
+
+@dataclass
 class SceneSpec:
     width: int
     height: int
@@ -130,6 +150,8 @@ class SceneSpec:
     environment: Optional[str] = None
     # light selection: "uniform" (the reference's default) or "power"
     light_cluster: str = "uniform"
+    # film filter; None: the box of size 1
+    film_filter: Optional[FilmFilter] = None
 
     # ------------------------------------------------------------------ sizes
     def num_primitives(self) -> int:
@@ -170,8 +192,20 @@ class SceneSpec:
         def v3(v):
             return "%.9g %.9g %.9g" % (float(v[0]), float(v[1]), float(v[2]))
 
+        f = self.film_filter or FilmFilter()
+        fw, fh = f.size()
         w("film {\n    [image-width int32 \"%d\"]\n    [image-height int32 \"%d\"]\n"
-          "    [filter string \"box\"]\n}\n" % (self.width, self.height))
+          "    [filter string \"%s\"]\n" % (self.width, self.height, f.type))
+        if (fw, fh) != ((1.0, 1.0) if f.type == "box" else (4.0, 4.0)):
+            w("    [filter-width real \"%.9g\"]\n    [filter-height real \"%.9g\"]\n" % (fw, fh))
+        if f.type == "gaussian":
+            w("    [sigma-x real \"%.9g\"]\n    [sigma-y real \"%.9g\"]\n    [amplitude real \"%.9g\"]\n"
+              % (f.sigma_x, f.sigma_y, f.amplitude))
+        if f.type == "mitchell":
+            w("    [b real \"%.9g\"]\n    [c real \"%.9g\"]\n" % (f.b, f.c))
+        if tuple(f.tile) != (16, 16):
+            w("    [tile-size-x int32 \"%d\"]\n    [tile-size-y int32 \"%d\"]\n" % tuple(f.tile))
+        w("}\n")
         w("camera {\n    [type string \"perspective-pinhole\"]\n"
           "    [position vector3r \"%s\"]\n    [direction vector3r \"%s\"]\n"
           "    [up vector3r \"%s\"]\n    [fov real \"%.9g\"]\n"

@@ -48,7 +48,7 @@
 extern "C" {
 #endif
 
-#define CGPU_ABI_VERSION 2
+#define CGPU_ABI_VERSION 3
 
 typedef enum cgpu_status {
     CGPU_OK = 0,
@@ -117,6 +117,30 @@ typedef struct cgpu_area_light {
     int32_t back_face_emit;
 } cgpu_area_light;
 
+/* Film reconstruction filter (filterInstantiator.cpp:16-57, filters under
+ * core/film/filter/).  As FilmTile::addSample does (filmTile.cpp:36-66), a
+ * sample at film position (x, y) adds weight w = filter(pixel centre - (x, y))
+ * to every pixel within half the filter's size of it, clipped to the film
+ * tile (tile_width x tile_height pixels, from the film's origin) its own pixel
+ * lies in; the film then holds sum w L, sum w L^2 and sum w per pixel.
+ * A zero-initialised filter is the reference's default box of size 1 (the
+ * sample's own pixel, weight 1): width / height 0 mean 1 for CGPU_FILTER_BOX,
+ * tile sizes 0 mean 16.  Gaussian, Mitchell and cone filters use the fields as
+ * given (the CRSD loader fills in the reference's defaults). */
+enum {
+    CGPU_FILTER_BOX = 0,       /* weight 1 (boxFilter.cpp:9-11) */
+    CGPU_FILTER_GAUSSIAN = 1,  /* max(0, a exp(-x^2 / 2 sx^2 - y^2 / 2 sy^2) - edge value) (gaussianFilter.cpp:9-38) */
+    CGPU_FILTER_MITCHELL = 2,  /* Mitchell-Netravali (b, c), separable (mitchellFilter.cpp:17-42) */
+    CGPU_FILTER_CONE = 3       /* max(w/2 - |x|, 0) max(h/2 - |y|, 0) (coneFilter.cpp:11-15) */
+};
+typedef struct cgpu_film_filter {
+    int32_t type;                       /* CGPU_FILTER_* */
+    float width, height;                /* full size in pixels */
+    float sigma_x, sigma_y, amplitude;  /* gaussian */
+    float b, c;                         /* mitchell */
+    int32_t tile_width, tile_height;    /* film tile clipping the footprint */
+} cgpu_film_filter;
+
 typedef struct cgpu_scene_desc {
     /* film + camera (filmInstantiator.cpp:13-30, cameraInstantiator.cpp:27-45) */
     int32_t width;
@@ -156,6 +180,8 @@ typedef struct cgpu_scene_desc {
      * (uniformLightCluster.cpp:15-24); CGPU_LIGHT_CLUSTER_POWER in proportion to
      * its approximate flux, computed once at upload (powerLightCluster.cpp:9-48). */
     int32_t light_cluster;
+
+    cgpu_film_filter filter;
 } cgpu_scene_desc;
 
 enum { CGPU_LIGHT_CLUSTER_UNIFORM = 0, CGPU_LIGHT_CLUSTER_POWER = 1 };

@@ -70,7 +70,21 @@ def lib():
                                   C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
         L.port_adjoint_fp64.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_int32, C.c_int32, C.c_void_p]
+        L.port_filter_splat.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_uint64, C.c_void_p, C.c_void_p,
+                                        C.c_void_p]
+        L.port_sample_positions.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
     return _lib
+
+
+def filter_splat(film_filter, width: int, height: int, xy: np.ndarray, rgb: np.ndarray) -> np.ndarray:
+    """FilmTile::addSample restated: samples (N x 2 positions, N x 3 radiance,
+    in this order) through `film_filter` (a cadise_gb300.abi.cgpu_film_filter)
+    into an H x W x 7 FP64 film {sum w rgb, sum w rgb^2, sum w}."""
+    xy = np.ascontiguousarray(xy, dtype=np.float32).reshape(-1, 2)
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32).reshape(-1, 3)
+    film = np.zeros((height, width, 7), np.float64)
+    lib().port_filter_splat(C.byref(film_filter), width, height, xy.shape[0], _p(xy), _p(rgb), _p(film))
+    return film
 
 
 def _p(a):
@@ -126,6 +140,12 @@ class PortScene:
         lib().port_render(self.handle, seed, scene_index, first, count, r0, r1, threads, _p(film), _p(paths))
         return film, paths
 
+
+    def sample_positions(self, seed: int, first: int, count: int, scene_index: int = 0) -> np.ndarray:
+        """Film positions (count x H x W x 2, float32) of samples [first, first + count)."""
+        xy = np.zeros((count, self.height, self.width, 2), np.float32)
+        lib().port_sample_positions(self.handle, seed, scene_index, first, count, _p(xy))
+        return xy
 
     def adjoint_fp64(self, seed: int, spp: int, d_loss_d_image: np.ndarray, params, threads: int = 8,
                      scene_index: int = 0) -> np.ndarray:

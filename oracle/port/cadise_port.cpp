@@ -1534,7 +1534,114 @@ D3 estimateDual(const Scene& s, Ray ray, Rng& rng) {
 
 }  // namespace port
 
+// ---------------------------------------------------------- film filters --
+// Filters (core/film/filter/*.cpp) and FilmTile::addSample
+// (core/film/filmTile.cpp:36-66) restated: the filter constants as the
+// constructors compute them, the footprint clipped to the tile of the
+// sample's own pixel (Film::getTileBound, core/film/film.cpp:204-211).
+struct FilmFilter {
+    int type = CGPU_FILTER_BOX;
+    float hx = 0.5f, hy = 0.5f;
+    float expX = 0.0f, expY = 0.0f, edge = 0.0f, amp = 1.0f;  // gaussianFilter.cpp:9-25
+    float b = 0.0f, c = 0.0f;                                 // mitchellFilter.cpp:7-15
+    int tw = 16, th = 16;
+};
+
+FilmFilter makeFilmFilter(const cgpu_film_filter& f) {
+    FilmFilter F;
+    F.type = f.type;
+    float w = f.width, h = f.height;
+    if (f.type == CGPU_FILTER_BOX) {
+        if (w == 0.0f) w = 1.0f;
+        if (h == 0.0f) h = 1.0f;
+    }
+    F.hx = w / 2.0f;  // Filter::filterHalfSize (filter.cpp:19-21)
+    F.hy = h / 2.0f;
+    F.tw = f.tile_width ? f.tile_width : 16;
+    F.th = f.tile_height ? f.tile_height : 16;
+    if (f.type == CGPU_FILTER_GAUSSIAN) {
+        F.expX = -1.0f / (2.0f * f.sigma_x * f.sigma_x);
+        F.expY = -1.0f / (2.0f * f.sigma_y * f.sigma_y);
+        F.amp = f.amplitude;
+        F.edge = F.amp * std::exp(F.expX * F.hx * F.hx + F.expY * F.hy * F.hy);
+    }
+    F.b = f.b;
+    F.c = f.c;
+    return F;
+}
+
+float mitchell1D(const FilmFilter& F, float d) {  // mitchellFilter.cpp:21-42
+    const float a = std::fabs(d);
+    const float den = 1.0f / 6.0f;
+    if (a < 1.0f) return ((12.0f - 9.0f * F.b - 6.0f * F.c) * a * a * a + (-18.0f + 12.0f * F.b + 6.0f * F.c) * a * a +
+                          (6.0f - 2.0f * F.b)) * den;
+    if (a < 2.0f) return ((-F.b - 6.0f * F.c) * a * a * a + (6.0f * F.b + 30.0f * F.c) * a * a +
+                          (-12.0f * F.b - 48.0f * F.c) * a + (8.0f * F.b + 24.0f * F.c)) * den;
+    return 0.0f;
+}
+
+float filterEval(const FilmFilter& F, float x, float y) {
+    switch (F.type) {
+        case CGPU_FILTER_GAUSSIAN: {  // gaussianFilter.cpp:27-32
+            const float v = F.amp * std::exp(F.expX * x * x + F.expY * y * y);
+            return std::max(0.0f, v - F.edge);
+        }
+        case CGPU_FILTER_MITCHELL: return mitchell1D(F, x) * mitchell1D(F, y);  // mitchellFilter.cpp:17-19
+        case CGPU_FILTER_CONE:  // coneFilter.cpp:11-15
+            return std::max(F.hx - std::fabs(x), 0.0f) * std::max(F.hy - std::fabs(y), 0.0f);
+        default: return 1.0f;  // boxFilter.cpp:9-11
+    }
+}
+
+// One sample into an H x W x 7 FP64 film {sum w r,g,b; sum w r^2,g^2,b^2; sum w}.
+void filterSplat(const FilmFilter& F, int W, int H, float x, float y, const float* rgb, double* film) {
+    if (!(std::isfinite(rgb[0]) && std::isfinite(rgb[1]) && std::isfinite(rgb[2]))) return;  // filmTile.cpp:21-28
+    const int ix = static_cast<int>(std::floor(x)), iy = static_cast<int>(std::floor(y));
+    const int tx0 = ix / F.tw * F.tw, ty0 = iy / F.th * F.th;
+    const int tx1 = std::min(tx0 + F.tw, W), ty1 = std::min(ty0 + F.th, H);
+    const float minX = std::max(x - F.hx, static_cast<float>(tx0)), minY = std::max(y - F.hy, static_cast<float>(ty0));
+    const float maxX = std::min(x + F.hx, static_cast<float>(tx1)), maxY = std::min(y + F.hy, static_cast<float>(ty1));
+    const int x0 = static_cast<int>(std::ceil(minX - 0.5f)), y0 = static_cast<int>(std::ceil(minY - 0.5f));
+    const int x1 = static_cast<int>(std::floor(maxX - 0.5f) + 1), y1 = static_cast<int>(std::floor(maxY - 0.5f) + 1);
+    for (int py = y0; py < y1; ++py)
+        for (int px = x0; px < x1; ++px) {
+            const float w = filterEval(F, px - (x - 0.5f), py - (y - 0.5f));
+            double* o = film + 7 * static_cast<std::size_t>(py * W + px);
+            for (int k = 0; k < 3; ++k) {
+                o[k] += static_cast<double>(rgb[k] * w);
+                o[3 + k] += static_cast<double>(w) * rgb[k] * rgb[k];
+            }
+            o[6] += w;
+        }
+}
+
 extern "C" {
+
+// n samples {x, y} / {r, g, b} in the given order into `film` (H x W x 7).
+void port_filter_splat(const cgpu_film_filter* f, int32_t W, int32_t H, uint64_t n, const float* xy, const float* rgb,
+                       double* film) {
+    const FilmFilter F = makeFilmFilter(*f);
+    for (uint64_t i = 0; i < n; ++i) filterSplat(F, W, H, xy[2 * i], xy[2 * i + 1], rgb + 3 * i, film);
+}
+
+// Film positions of samples [first, first + count) of every pixel, sample-major
+// (count x H x W x 2): pixel + the stratified jitter of the path stream.
+void port_sample_positions(void* sp, uint64_t seed, uint32_t scene_index, uint32_t first, uint32_t count, float* xy) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    for (uint32_t k = 0; k < count; ++k)
+        for (int iy = 0; iy < s.H; ++iy)
+            for (int ix = 0; ix < s.W; ++ix) {
+                const uint32_t pixel = static_cast<uint32_t>(iy * s.W + ix);
+                port::Rng rng;
+                rng.s.key = oracle_rng::path_key(seed, scene_index, pixel, first + k);
+                rng.s.counter = 0;
+                float jx, jy;
+                port::jitter(s.spp, first + k, rng, &jx, &jy);
+                float* o = xy + 2 * (static_cast<std::size_t>(k) * s.W * s.H + pixel);
+                o[0] = static_cast<float>(ix) + jx;
+                o[1] = static_cast<float>(iy) + jy;
+            }
+}
 
 void* port_scene_create(const cgpu_scene_desc* desc) { return port::create(desc); }
 void port_scene_destroy(void* s) { delete static_cast<port::Scene*>(s); }

@@ -22,10 +22,22 @@
 //   paths  <scene.crsd> <in: N x {f64 fx, f64 fy, u64 key}>   <out: N x {f32 r, g, b, u32 draws}>
 //   render <scene.crsd> <out: H x W x 7 f64> <spp> <seed> <threads>
 //          (sum r,g,b, sum of squares r,g,b, accepted sample count)
+//   filmtile <scene.crsd> <in: N x {f32 x, f32 y, f32 r, g, b}> <out: H x W x 4 f64>
+//          the scene's film filter through FilmTile::addSample
+//          (core/film/filmTile.cpp:36-66) on the 16 x 16 (tile-size-x/y) tiles
+//          of Film::getTileBound (core/film/film.cpp:204-211): per pixel the
+//          sensor's sum of w r, w g, w b and sum of w
+//   render-tiles <scene.crsd> <out: H x W x 7 f64> <spp> <seed> <threads>
+//          the render loop above with the scene's film filter: every pass of up
+//          to 256 samples per pixel goes through a fresh FilmTile per tile, whose
+//          sensors are then added in FP64 (sum w r,g,b, zeros, sum w)
 
 #include "core/camera/camera.h"
 #include "core/estimator/energyEstimator.h"
 #include "core/film/film.h"
+#include "core/film/filmTile.h"
+#include "core/film/filter/filter.h"
+#include "core/film/rgbRadianceSensor.h"
 #include "core/instantiator/instantiator.h"
 #include "core/intersector/accelerator/accelerator.h"
 #include "core/intersector/accelerator/bruteForceAccelerator.h"
@@ -324,6 +336,123 @@ int cmdRender(const LoadedScene& ls, const char* out, int spp, uint64_t seed, in
     return 0;
 }
 
+// The film's tiles with the scene's filter, as the reference's Film lays them out.
+struct TileSet {
+    int W = 0, H = 0, tw = 16, th = 16, ntx = 0, nty = 0;
+    std::shared_ptr<Filter> filter;
+    std::vector<std::unique_ptr<FilmTile>> tiles;
+
+    explicit TileSet(const LoadedScene& ls) {
+        W = ls.width;
+        H = ls.height;
+        tw = ls.film->findInt32("tile-size-x", 16);
+        th = ls.film->findInt32("tile-size-y", 16);
+        ntx = (W + tw - 1) / tw;
+        nty = (H + th - 1) / th;
+        filter = instantiator::makeFilter(ls.film);
+        reset();
+    }
+    void reset() {
+        tiles.clear();
+        for (int ty = 0; ty < nty; ++ty)
+            for (int tx = 0; tx < ntx; ++tx) {
+                const Vector2I lo(tx * tw, ty * th);
+                const Vector2I hi(std::min(lo.x() + tw, W), std::min(lo.y() + th, H));
+                tiles.push_back(std::make_unique<FilmTile>(AABB2I(lo, hi), filter.get()));
+            }
+    }
+    FilmTile& tileOfPixel(int ix, int iy) { return *tiles[static_cast<std::size_t>((iy / th) * ntx + ix / tw)]; }
+    // adds tile `t`'s sensors to an H x W x stride FP64 film at channels {0,1,2} and `wchan`
+    void drain(std::size_t t, double* film, int stride, int wchan) const {
+        const FilmTile& ft = *tiles[t];
+        const Vector2I& a = ft.tileBound().minVertex();
+        const Vector2I& b = ft.tileBound().maxVertex();
+        for (int iy = a.y(); iy < b.y(); ++iy)
+            for (int ix = a.x(); ix < b.x(); ++ix) {
+                const RgbRadianceSensor& s = ft.getSensor(ix - a.x(), iy - a.y());
+                double* px = film + static_cast<std::size_t>(iy * W + ix) * stride;
+                px[0] += s.r();
+                px[1] += s.g();
+                px[2] += s.b();
+                px[wchan] += s.weight();
+            }
+    }
+};
+
+int cmdFilmTile(const LoadedScene& ls, const char* in, const char* out) {
+    const auto v = readAll<float>(in);
+    const std::size_t n = v.size() / 5;
+    TileSet ts(ls);
+    for (std::size_t i = 0; i < n; ++i) {
+        const float* r = &v[5 * i];
+        const int ix = static_cast<int>(std::floor(r[0])), iy = static_cast<int>(std::floor(r[1]));
+        // the Spectrum overload, which drops NaN / Inf samples as the render loop's does
+        ts.tileOfPixel(ix, iy).addSample(Vector2R(r[0], r[1]), Spectrum(Vector3R(r[2], r[3], r[4])));
+    }
+    std::vector<double> film(static_cast<std::size_t>(ts.W) * ts.H * 4, 0.0);
+    for (std::size_t t = 0; t < ts.tiles.size(); ++t) ts.drain(t, film.data(), 4, 3);
+    writeAll(out, film.data(), film.size() * sizeof(double));
+    return 0;
+}
+
+int cmdRenderTiles(const LoadedScene& ls, const char* out, int spp, uint64_t seed, int threads) {
+    const int W = ls.width, H = ls.height;
+    TileSet ts(ls);
+    std::vector<double> film(static_cast<std::size_t>(W) * H * 7, 0.0);
+    const int per = std::min(spp, 256), passes = (spp + per - 1) / per;
+    std::atomic<int> nextTile{0};
+    auto worker = [&]() {
+        for (;;) {
+            const int t = nextTile.fetch_add(1);
+            if (t >= static_cast<int>(ts.tiles.size())) break;
+            FilmTile& base = *ts.tiles[static_cast<std::size_t>(t)];
+            const AABB2I bound = base.tileBound();
+            for (int pass = 0; pass < passes; ++pass) {
+                FilmTile ft(bound, ts.filter.get());
+                const uint64_t pseed = seed + static_cast<uint64_t>(pass);
+                for (int iy = bound.minVertex().y(); iy < bound.maxVertex().y(); ++iy)
+                    for (int ix = bound.minVertex().x(); ix < bound.maxVertex().x(); ++ix) {
+                        const uint32_t pixel = static_cast<uint32_t>(iy * W + ix);
+                        g_stream.key = oracle_rng::path_key(pseed, 0, pixel, 0xFFFFFFFFu);
+                        g_stream.counter = 0;
+                        auto s = ls.sampler->clone(static_cast<std::size_t>(per));
+                        auto rec = s->requestSample2D();
+                        for (int si = 0; si < per; ++si) {
+                            const Vector2R pos = Vector2I(ix, iy).asType<real>() + rec->nextSample();
+                            const uint64_t pixelKey = g_stream.key;
+                            const uint32_t pixelCtr = g_stream.counter;
+                            g_stream.key = oracle_rng::path_key(pseed, 0, pixel, static_cast<uint32_t>(si));
+                            g_stream.counter = 0;
+                            Ray primary;
+                            ls.cam->spawnPrimaryRay(pos.asType<float64>(), &primary);
+                            Spectrum radiance;
+                            ls.estimator->estimate(*ls.scene, primary, &radiance);
+                            g_stream.key = pixelKey;
+                            g_stream.counter = pixelCtr;
+                            ft.addSample(pos, radiance);
+                        }
+                    }
+                const Vector2I& a = bound.minVertex();
+                const Vector2I& b = bound.maxVertex();
+                for (int iy = a.y(); iy < b.y(); ++iy)
+                    for (int ix = a.x(); ix < b.x(); ++ix) {
+                        const RgbRadianceSensor& sn = ft.getSensor(ix - a.x(), iy - a.y());
+                        double* px = &film[static_cast<std::size_t>(iy * W + ix) * 7];
+                        px[0] += sn.r();
+                        px[1] += sn.g();
+                        px[2] += sn.b();
+                        px[6] += sn.weight();
+                    }
+            }
+        }
+    };
+    std::vector<std::thread> pool;
+    for (int t = 0; t < threads; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    writeAll(out, film.data(), film.size() * sizeof(double));
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -336,6 +465,10 @@ int main(int argc, char** argv) {
     if (cmd == "camera" && argc >= 5) return cmdCamera(*ls, argv[3], argv[4]);
     if (cmd == "trace" && argc >= 5) return cmdTrace(*ls, argv[3], argv[4]);
     if (cmd == "paths" && argc >= 5) return cmdPaths(*ls, argv[3], argv[4]);
+    if (cmd == "filmtile" && argc >= 5) return cmdFilmTile(*ls, argv[3], argv[4]);
+    if (cmd == "render-tiles" && argc >= 7) {
+        return cmdRenderTiles(*ls, argv[3], std::atoi(argv[4]), std::strtoull(argv[5], nullptr, 10), std::atoi(argv[6]));
+    }
     if (cmd == "render" && argc >= 7) {
         return cmdRender(*ls, argv[3], std::atoi(argv[4]), std::strtoull(argv[5], nullptr, 10), std::atoi(argv[6]));
     }

@@ -16,7 +16,11 @@ next to this script, and records what the reference computes for it:
                number of random draws the path consumed
 * ``<scene>_image.npz`` - an FP64 box-filtered film rendered with the
   reference tile loop (reference StratifiedSampler + PtEstimator): per-pixel
-  sum, sum of squares and sample count, for statistical image parity.
+  sum, sum of squares and sample count, for statistical image parity (for a
+  scene with another film filter: sums of w L and of w through the
+  reference's FilmTile, sum_sq zero).
+* ``filter_vectors.npz`` - the reference's FilmTile::addSample with each
+  filter of FILTER_CASES on one set of samples: per-pixel sensor sums.
 
 Primitive indices are the reference's intersector creation order.  Path keys
 follow oracle/oracle_rng.h.
@@ -38,6 +42,9 @@ sys.path.insert(0, ROOT)
 from cadise_gb300 import scenes  # noqa: E402
 import oracle  # noqa: E402
 
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+from golden_scenes import FILTER_CASES, filtered_scene  # noqa: E402
+
 TRACE_SEED = 1234
 PATH_SEED = 77
 
@@ -52,7 +59,34 @@ def golden_scenes():
         "features": (scenes.feature_scene(), 32768),
         "power": (scenes.power_field(), 131072),
         "spheres": (scenes.sphere_box(), 16384),
+        "filtered": (filtered_scene(), 32768),
     }
+
+
+def make_filter_vectors(harness, work, n=4000):
+    """FilmTile::addSample of the reference with each filter on the same
+    samples (uniform positions over a 40 x 30 film, some on exact pixel
+    edges, a few NaN / Inf radiances)."""
+    rng = np.random.default_rng(99)
+    W, H = 40, 30
+    xy = rng.uniform(0, 1, (n, 2)) * [W, H]
+    xy[:100] = np.floor(xy[:100])          # exactly on a pixel corner
+    xy = np.minimum(xy, [W - 1e-3, H - 1e-3]).astype(np.float32)
+    rgb = rng.uniform(0, 2, (n, 3)).astype(np.float32)
+    rgb[200, 0] = np.nan
+    rgb[201, 2] = np.inf
+    samples = np.concatenate([xy, rgb], 1).astype(np.float32)
+    samples.tofile(os.path.join(work, "samples.bin"))
+    out = {"xy": xy, "rgb": rgb, "width": W, "height": H}
+    for name, f in FILTER_CASES:
+        spec = scenes.cornell_box(W, H, 1, 2)
+        spec.film_filter = f
+        crsd = os.path.join(work, "filter.crsd")
+        with open(crsd, "w") as fh:
+            fh.write(spec.to_crsd())
+        run(harness, ["filmtile", crsd, os.path.join(work, "samples.bin"), os.path.join(work, "ft.bin")])
+        out["sensor_" + name] = np.fromfile(os.path.join(work, "ft.bin"), dtype=np.float64).reshape(H, W, 4)
+    np.savez_compressed(os.path.join(HERE, "filter_vectors.npz"), **out)
 
 
 def trace_rays(lo, hi, n, rng):
@@ -124,7 +158,9 @@ def make_vectors(name, spec, harness, work, n_camera=512, n_trace=3000, n_paths=
 def make_image(name, spec, harness, work, spp, seed=2024, threads=8):
     crsd = os.path.join(HERE, name + ".crsd")
     path = os.path.join(work, "film.bin")
-    run(harness, ["render", crsd, path, spp, seed, threads])
+    # a filtered film goes through the reference's FilmTile (no sums of squares)
+    cmd = "render" if spec.film_filter is None else "render-tiles"
+    run(harness, [cmd, crsd, path, spp, seed, threads])
     film = np.fromfile(path, dtype=np.float64).reshape(spec.height, spec.width, 7)
     np.savez_compressed(os.path.join(HERE, name + "_image.npz"), sum=film[..., :3], sum_sq=film[..., 3:6],
                         count=film[..., 6], spp=spp, seed=seed)
@@ -140,6 +176,9 @@ def main():
     if harness is None:
         sys.exit("reference sources not found at %s" % args.ref)
     with tempfile.TemporaryDirectory() as work:
+        if args.only in (None, "filters"):
+            make_filter_vectors(harness, work)
+            print("golden filters done")
         for name, (spec, spp) in golden_scenes().items():
             if args.only and name != args.only:
                 continue

@@ -6,6 +6,7 @@
 // host C++, so their logic is checked against the golden vectors before any
 // GPU time is spent.
 #include "../../cadise_gb300/csrc/adjoint.cuh"
+#include "../../cadise_gb300/csrc/film.cuh"
 #include "../../cadise_gb300/csrc/scene_build.h"
 
 #include <cstdio>
@@ -162,6 +163,30 @@ void khc_adjoint(void* p, uint64_t seed, uint32_t scene_index, uint32_t spp, con
 // The path-state layout of the wavefront (wf_layout) for `cap` paths and
 // `rows` counter rows: 0 when every array lies inside the measured size,
 // 256-byte aligned and disjoint from the others, else the failing array + 1.
+// The splat kernel's filtered gather (film.cuh filter_gather) for every pixel
+// of a W x H film over `count` samples per pixel (sample-major arrays:
+// positions count x H x W x 2, radiance count x H x W x 3); film H x W x 7
+// {sum w rgb, sum w rgb^2, sum w}.  Returns 0, or -1 if the filter is invalid.
+int khc_filter_gather(const cgpu_film_filter* f, int W, int H, uint32_t count, const float* xy, const float* rgb,
+                      double* film) {
+    cg::FilterD F;
+    std::string err;
+    if (cg::resolve_filter(*f, &F, &err) != CGPU_OK) return -1;
+    const size_t npix = size_t(W) * H;
+    auto fetch = [&](uint32_t k, int sx, int sy, float3* v, float2* pos) {
+        const size_t i = size_t(k) * npix + size_t(sy) * W + sx;
+        *v = make_float3(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+        *pos = make_float2(xy[2 * i], xy[2 * i + 1]);
+        return std::isfinite(v->x) && std::isfinite(v->y) && std::isfinite(v->z);
+    };
+    for (int iy = 0; iy < H; ++iy)
+        for (int ix = 0; ix < W; ++ix) {
+            double* o = film + 7 * (size_t(iy) * W + ix);
+            cg::filter_gather(F, W, H, ix, iy, count, fetch, o, o + 3, o + 6);
+        }
+    return 0;
+}
+
 int khc_wf_layout_check(uint64_t cap, int rows) {
     cg::WfBuffers w{};
     const size_t total = cg::wf_layout(nullptr, size_t(cap), rows, &w);

@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.cgpu_abi_version() == 2
+    assert lib.cgpu_abi_version() == 3
     for code, name in abi.STATUS_NAMES.items():
         assert lib.cgpu_status_string(code).decode() == name
 
@@ -62,3 +62,4 @@ def test_struct_layouts_match_header():
     assert C.sizeof(abi.cgpu_material) == 64
     assert C.sizeof(abi.cgpu_area_light) == 24
     assert C.sizeof(abi.cgpu_render_params) == 48
+    assert C.sizeof(abi.cgpu_film_filter) == 40

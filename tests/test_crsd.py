@@ -16,7 +16,7 @@ def built():
     cg.build()
 
 
-@pytest.mark.parametrize("name", ["cornell", "field", "features", "power", "spheres"])
+@pytest.mark.parametrize("name", ["cornell", "field", "features", "power", "spheres", "filtered"])
 def test_golden_crsd_loads_to_the_generator_arrays(name):
     sc = cg.CrsdScene(path=os.path.join(GOLDEN, name + ".crsd"))
     flat = abi.flatten(specs()[name])

@@ -14,7 +14,7 @@ import pytest
 
 import oracle
 from cadise_gb300 import abi, scenes
-from golden_scenes import specs, vectors
+from golden_scenes import FILTER_CASES, specs, vectors
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 BUILD = os.path.join(ROOT, "tests", "native", "_build")
@@ -47,6 +47,7 @@ def khc():
     L.khc_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
     L.khc_adjoint.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
     L.khc_wf_layout_check.argtypes = [C.c_uint64, C.c_int]
+    L.khc_filter_gather.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
     L.khc_noalloc_layout_bytes.restype = C.c_uint64
     L.khc_noalloc_scratch_bytes.restype = C.c_uint64
     return L
@@ -195,3 +196,40 @@ def test_noalloc_scratch_holds_its_layout(khc):
     need, have = khc.khc_noalloc_layout_bytes(), khc.khc_noalloc_scratch_bytes()
     assert have == 64 << 20
     assert 0 < need <= have, (need, have)
+
+
+@pytest.mark.parametrize("case", [c[0] for c in FILTER_CASES])
+def test_kernel_filter_gather_matches_oracle(khc, case):
+    """The splat kernel's gather over the pixels of each tile (film.cuh) and
+    the oracle's scatter restatement of FilmTile::addSample add the same
+    weights to the same pixels: equal up to the order of the FP64 sums.
+    Samples include positions on exact pixel edges (where the footprint
+    reaches one pixel further) and NaN / Inf radiance."""
+    import oracle
+    f = abi.film_filter_struct(dict(FILTER_CASES)[case])
+    W, H, count = 37, 29, 3
+    rng = np.random.default_rng(5)
+    pix = np.stack(np.meshgrid(np.arange(W), np.arange(H)), -1).astype(np.float32)  # H x W x 2 (x, y)
+    jit = rng.uniform(0, 1, (count, H, W, 2)).astype(np.float32)
+    jit[0, ::3, ::2] = 0.0  # exact pixel corners
+    xy = (pix[None] + jit).astype(np.float32)
+    rgb = rng.uniform(0, 3, (count, H, W, 3)).astype(np.float32)
+    rgb[1, 4, 5, 0] = np.nan
+    rgb[2, 10, 11, 1] = np.inf
+    film = np.zeros((H, W, 7), np.float64)
+    assert khc.khc_filter_gather(C.byref(f), W, H, count, _p(xy), _p(rgb), _p(film)) == 0
+    ref = oracle.filter_splat(f, W, H, xy.reshape(-1, 2), rgb.reshape(-1, 3))
+    scale = np.abs(ref).max(axis=(0, 1))
+    np.testing.assert_allclose(film, ref, rtol=1e-12, atol=1e-12 * scale.max())
+    assert ref[..., 6].min() != ref[..., 6].max()
+
+
+def test_invalid_film_filter_is_rejected(khc):
+    spec = scenes.cornell_box(8, 8, 1, 2)
+    flat = abi.flatten(spec)
+    for bad in (dict(type=7), dict(type=abi.CGPU_FILTER_GAUSSIAN, width=4.0, height=4.0, sigma_x=0.0, sigma_y=0.5),
+                dict(type=abi.CGPU_FILTER_CONE, width=-1.0, height=2.0), dict(type=0, tile_width=-3)):
+        flat.desc.filter = abi.cgpu_film_filter(**bad)
+        err = C.create_string_buffer(256)
+        assert not khc.khc_create(C.addressof(flat.desc), err, 256)
+        assert b"filter" in err.value or b"tile" in err.value, err.value
