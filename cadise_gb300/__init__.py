@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libcadise_gpu.so")
 # Every symbol include/cadise_gpu.h declares.
 EXPORTED = [
     "cgpu_create", "cgpu_destroy", "cgpu_last_error", "cgpu_status_string", "cgpu_abi_version",
-    "cgpu_synchronize", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
+    "cgpu_synchronize", "cgpu_set_bvh_builder", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
     "cgpu_trace_closest", "cgpu_trace_any", "cgpu_trace_closest_device", "cgpu_trace_any_device",
     "cgpu_camera_rays", "cgpu_render", "cgpu_render_noalloc", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
@@ -96,6 +96,7 @@ def load(path: Optional[str] = None):
     L.cgpu_adjoint_forward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp]
     L.cgpu_adjoint_backward.argtypes = [vp, C.c_int32, C.c_uint32, C.c_uint64, vp, vp, vp, vp]
     L.cgpu_set_adjoint_mode.argtypes = [vp, C.c_int32]
+    L.cgpu_set_bvh_builder.argtypes = [vp, C.c_int32]
     L.cgpu_tuning_get.argtypes = [vp, C.POINTER(abi.cgpu_tuning)]
     L.cgpu_tuning_set.argtypes = [vp, C.POINTER(abi.cgpu_tuning)]
     L.cgpu_autotune.argtypes = [vp, vp, C.c_uint32, C.c_uint32, C.c_char_p, C.POINTER(abi.cgpu_tuning)]
@@ -293,6 +294,10 @@ class Context:
         img = np.zeros((flat.desc.height, flat.desc.width, 3), np.float32)
         self._check(self.L.cgpu_adjoint_forward(self.h, sid, spp, seed, _p(img)))
         return img
+
+    def set_bvh_builder(self, builder: int) -> None:
+        """abi.CGPU_BVH_BUILDER_AUTO (default), _HOST_SAH or _GPU_PLOC for the following uploads."""
+        self._check(self.L.cgpu_set_bvh_builder(self.h, builder))
 
     def set_adjoint_mode(self, mode: int) -> None:
         """CGPU_MODE_WAVEFRONT (default) or CGPU_MODE_MEGAKERNEL schedule of adjoint_backward."""

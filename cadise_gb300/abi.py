@@ -110,7 +110,14 @@ class cgpu_scene_info(C.Structure):
     _fields_ = [("num_primitives", C.c_uint32), ("num_triangles", C.c_uint32),
                 ("num_bvh_nodes", C.c_uint32), ("num_lights", C.c_uint32),
                 ("device_bytes", C.c_uint64), ("build_ms", C.c_double),
-                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3)]
+                ("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("bvh_ms", C.c_double), ("bvh_builder", C.c_int32), ("reserved", C.c_int32)]
+
+
+CGPU_BVH_BUILDER_AUTO = 0
+CGPU_BVH_BUILDER_HOST_SAH = 1
+CGPU_BVH_BUILDER_GPU_PLOC = 2
+CGPU_BVH_GPU_MIN_PRIMITIVES = 65536
 
 
 class cgpu_options(C.Structure):

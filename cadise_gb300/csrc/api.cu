@@ -164,6 +164,20 @@ cgpu_status cgpu_synchronize(cgpu_ctx* ctx) {
     return cg_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
 }
 
+cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder) {
+    if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
+    if (builder != CGPU_BVH_BUILDER_AUTO && builder != CGPU_BVH_BUILDER_HOST_SAH && builder != CGPU_BVH_BUILDER_GPU_PLOC)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "set_bvh_builder: unknown builder");
+    ctx->bvh_builder = builder;
+    return CGPU_OK;
+}
+
+namespace {
+bool gpu_bvh_builder(const float* tv, uint32_t n, Bvh4Result* out, std::string* err, void* user) {
+    return build_bvh4_gpu(tv, n, static_cast<cgpu_ctx*>(user)->stream, out, err);
+}
+}  // namespace
+
 cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* out_scene) {
     if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
     if (!d || !out_scene) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "scene_upload: null argument");
@@ -171,8 +185,11 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     const auto t0 = std::chrono::steady_clock::now();
     HostScene hs;
     std::string err;
-    cgpu_status st = build_host_scene(d, &hs, &err);
+    const bool gpu_bvh = ctx->bvh_builder == CGPU_BVH_BUILDER_GPU_PLOC ||
+                         (ctx->bvh_builder == CGPU_BVH_BUILDER_AUTO && d->num_primitives >= CGPU_BVH_GPU_MIN_PRIMITIVES);
+    cgpu_status st = gpu_bvh ? build_host_scene(d, &hs, &err, gpu_bvh_builder, ctx) : build_host_scene(d, &hs, &err);
     if (st != CGPU_OK) return cg_fail(ctx, st, "scene_upload: " + err);
+    hs.info.bvh_builder = gpu_bvh ? CGPU_BVH_BUILDER_GPU_PLOC : CGPU_BVH_BUILDER_HOST_SAH;
     if (3 * hs.wide_depth + 1 > kStackSize)
         return cg_fail(ctx, CGPU_ERR_UNSUPPORTED, "scene_upload: BVH too deep for the traversal stack");
     SceneSlot sl;

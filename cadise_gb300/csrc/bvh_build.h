@@ -20,4 +20,13 @@ struct Bvh4Result {
 // empty or oversized input.
 bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, std::string* err);
 
+// The same result from the GPU build (bvh_gpu.cu): tri_vertices in host
+// memory, work on `stream`, nodes and leaf order copied back to `out`.
+bool build_bvh4_gpu(const float* tri_vertices, uint32_t num_tris, cudaStream_t stream, Bvh4Result* out,
+                    std::string* err);
+
+// A BVH builder the scene build can be handed instead of build_bvh4.
+using BvhBuildFn = bool (*)(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, std::string* err,
+                            void* user);
+
 }  // namespace cg

@@ -221,6 +221,7 @@ struct cgpu_ctx {
     cg::AdjBufs adj{};
     void* adj_block = nullptr;
     int adjoint_schedule = CGPU_MODE_WAVEFRONT;
+    int bvh_builder = CGPU_BVH_BUILDER_AUTO;
     unsigned long long* d_counters = nullptr;
 
     // captured wavefront graph

@@ -4,6 +4,7 @@
 #include "bvh_build.h"
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 
@@ -73,7 +74,8 @@ cgpu_status resolve_filter(const cgpu_film_filter& f, FilterD* out, std::string*
     return CGPU_OK;
 }
 
-cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err) {
+cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err, BvhBuildFn bvh_builder,
+                             void* bvh_user) {
     if (!d) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "null scene description");
     {
         const cgpu_status fs = resolve_filter(d->filter, &out->filter, err);
@@ -179,7 +181,11 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
     }
     Bvh4Result bvh;
     std::string berr;
-    if (!build_bvh4(tv.data(), ntris, &bvh, &berr)) return fail(err, CGPU_ERR_INVALID_ARGUMENT, berr);
+    const auto tb = std::chrono::steady_clock::now();
+    const bool built = bvh_builder ? bvh_builder(tv.data(), ntris, &bvh, &berr, bvh_user)
+                                   : build_bvh4(tv.data(), ntris, &bvh, &berr);
+    out->info.bvh_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tb).count();
+    if (!built) return fail(err, CGPU_ERR_INVALID_ARGUMENT, berr);
     if (3 * bvh.wide_depth + 1 > kStackSize)
         return fail(err, CGPU_ERR_UNSUPPORTED, "BVH too deep for the traversal stack");
     std::vector<TriRecord> recs(ntris);

@@ -6,6 +6,7 @@
 #pragma once
 
 #include "../../include/cadise_gpu.h"
+#include "bvh_build.h"
 #include "scene_device.cuh"
 
 #include <string>
@@ -36,8 +37,10 @@ struct HostScene {
 // error status with a message in *err.
 cgpu_status resolve_filter(const cgpu_film_filter& f, FilterD* out, std::string* err);
 
-// Returns CGPU_OK or an error status with a message in *err.
-cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err);
+// Returns CGPU_OK or an error status with a message in *err.  `bvh_builder`
+// (optional) builds the BVH in place of the host builder.
+cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err,
+                             BvhBuildFn bvh_builder = nullptr, void* bvh_user = nullptr);
 
 // A SceneD whose pointers are the host arrays (for running the kernel logic on the CPU).
 SceneD host_view(HostScene& hs, const cgpu_scene_desc* d);

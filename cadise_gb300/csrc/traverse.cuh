@@ -144,10 +144,15 @@ constexpr uint32_t kNoEntry = 0xFFFFFFFFu;  // never a node or leaf entry (28-bi
 
 // Which of two hits a closest-hit query keeps: the smaller distance, and on
 // an exact tie (a ray through an edge shared by two triangles hits both at
-// the same t) the lower triangle slot, so that the answer does not depend on
-// the order in which the traversal met them.
-CG_D bool closer_hit(float t, int slot, float tcur, int hslot) {
-    return hslot < 0 ? t <= tcur : (t < tcur || (t == tcur && slot < hslot));
+// the same t) the lower primitive index, so that the answer depends neither
+// on the order in which the traversal met them nor on the BVH (which builder,
+// which leaf order).  The two halves of a rectangle share a primitive and give
+// the same hit point, so between them either will do.  `prim` is the
+// candidate's primitive; the kept hit's is loaded only on a tie.
+CG_D bool closer_hit(const SceneD& S, float t, int prim, float tcur, int hslot) {
+    if (hslot < 0) return t <= tcur;
+    if (t != tcur) return t < tcur;
+    return prim < __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + hslot)).w);
 }
 
 // Visits inner node `e`: pushes the children the ray enters, farthest first,
@@ -240,7 +245,7 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
                 tcur = t;
                 return true;
             }
-            if (closer_hit(t, slot, tcur, hslot)) {
+            if (closer_hit(S, t, __float_as_int(a.w), tcur, hslot)) {
                 hslot = slot;
                 tcur = t;
                 hu = u;

@@ -192,10 +192,22 @@ typedef struct cgpu_scene_info {
     uint32_t num_bvh_nodes;   /* 4-wide nodes of 128 B */
     uint32_t num_lights;
     uint64_t device_bytes;    /* scene + BVH bytes resident on the device */
-    double build_ms;          /* host BVH build time */
+    double build_ms;          /* whole scene build + upload time */
     float bounds_min[3];
     float bounds_max[3];
+    double bvh_ms;            /* BVH build alone */
+    int32_t bvh_builder;      /* CGPU_BVH_BUILDER_HOST_SAH or CGPU_BVH_BUILDER_GPU_PLOC: the one used */
+    int32_t reserved;
 } cgpu_scene_info;
+
+/* BVH builder of the following uploads (cgpu_set_bvh_builder):
+ *   AUTO      the GPU build from CGPU_BVH_GPU_MIN_PRIMITIVES primitives up, else the host build (default)
+ *   HOST_SAH  binned SAH on the host threads (bvh_build.cpp)
+ *   GPU_PLOC  parallel locally-ordered clustering on the GPU (bvh_gpu.cu)
+ * Renders do not depend on the builder: closest hits keep, on an exact tie
+ * of distance, the lower primitive index, whatever the tree. */
+enum { CGPU_BVH_BUILDER_AUTO = 0, CGPU_BVH_BUILDER_HOST_SAH = 1, CGPU_BVH_BUILDER_GPU_PLOC = 2 };
+#define CGPU_BVH_GPU_MIN_PRIMITIVES 65536
 
 /* -------------------------------------------------------------- context -- */
 
@@ -213,6 +225,7 @@ const char* cgpu_status_string(cgpu_status status);
 int32_t cgpu_abi_version(void);
 cgpu_status cgpu_synchronize(cgpu_ctx* ctx);
 
+cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder);
 cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* desc, int32_t* out_scene);
 cgpu_status cgpu_scene_release(cgpu_ctx* ctx, int32_t scene);
 cgpu_status cgpu_scene_info_get(cgpu_ctx* ctx, int32_t scene, cgpu_scene_info* out_info);
