@@ -39,6 +39,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--bvh", default="auto", choices=["auto", "host", "gpu"],
+                    help="BVH builder of the uploads (auto: the GPU build for large scenes)")
     ap.add_argument("--profile-case", action="store_true",
                     help="for ncu: upload the frame and run --steps wavefront passes of 1 spp, nothing else")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
@@ -148,6 +150,7 @@ def run_gpu(args, rank, world, local):
         dist.init_process_group("nccl")
     stream = torch.cuda.Stream()
     ctx = cg.Context(device=local, stream=stream.cuda_stream)
+    ctx.set_bvh_builder(BVH_BUILDERS[args.bvh])
     spec = make_scene(args)
     flat = abi.flatten(spec)
     sid = ctx.upload(flat)
@@ -273,6 +276,7 @@ def run_gpu(args, rank, world, local):
         "config": {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": spec.width,
                    "height": spec.height, "spp": spp, "max_depth": spec.max_depth,
                    "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
+                   "bvh": {"builder": {1: "host-sah", 2: "gpu-ploc"}[info.bvh_builder], "build_ms": info.bvh_ms},
                    "schedule": "wavefront, CUDA graph per batch", "l2": "256 MB buffer written between steps",
                    "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
         "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value},
@@ -399,6 +403,9 @@ CONFIGS = {
 }
 
 
+BVH_BUILDERS = {"auto": 0, "host": 1, "gpu": 2}
+
+
 def run_config(args):
     """The other configurations, one JSON line each: wavefront and
     megakernel path samples/s on the GPU, the oracle's CPU rate on a bounded
@@ -411,6 +418,7 @@ def run_config(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.Stream()
     ctx = cg.Context(device=0, stream=stream.cuda_stream)
+    ctx.set_bvh_builder(BVH_BUILDERS[args.bvh])
     t0 = time.perf_counter()
     if args.config == "c1":
         specs = [scenes.cornell_box()]
@@ -476,7 +484,8 @@ def run_config(args):
         "megakernel": {"value": mk, "unit": UNIT, "speedup_wavefront": wf / mk,
                        "samples_per_step": int(sum(n * c for n, c in zip(npix, mk_counts)))},
         "setup_s": {"scene_generation": gen_s, "upload_with_bvh_build": upload_s,
-                    "bvh_build": sum(i.build_ms for i in infos) / 1e3},
+                    "bvh_build": sum(i.bvh_ms for i in infos) / 1e3,
+                    "bvh_builders": sorted({{1: "host-sah", 2: "gpu-ploc"}[i.bvh_builder] for i in infos})},
         "clocks": clk,
         "cpu_baseline": cpu,
     }
