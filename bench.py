@@ -41,8 +41,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--bvh", default="auto", choices=["auto", "host", "gpu"],
                     help="BVH builder of the uploads (auto: the GPU build for large scenes)")
+    ap.add_argument("--profile-spp", type=int, default=8, help="samples per pixel per --profile-case render")
     ap.add_argument("--profile-case", action="store_true",
-                    help="for ncu: upload the frame and run --steps wavefront passes of 1 spp, nothing else")
+                    help="for ncu: the frame with the bench tuning, --steps renders of --profile-spp in a profiler range")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2: the headline line (default); c1 Cornell box, c3 64 batched scenes, "
                          "c4 differentiable scene forward, c5 20.48 M-triangle stress frame: one JSON line each")
@@ -494,15 +495,30 @@ def run_config(args):
 
 
 def run_profile_case(args):
+    """The bench frame's wavefront passes for ncu, with the tuning the bench
+    uses (autotuned the same way first) and direct launches instead of the
+    graph; the profiled range (cudaProfilerStart / Stop, for ncu
+    --profile-from-start off) holds only the `--steps` renders of
+    `--profile-spp` samples per pixel."""
+    import torch
+
     import cadise_gb300 as cg
     from cadise_gb300 import abi
+    torch.cuda.set_device(0)
     ctx = cg.Context()
+    ctx.set_bvh_builder(BVH_BUILDERS[args.bvh])
     spec = make_scene(args)
     sid = ctx.upload(abi.flatten(spec))
+    tuning = ctx.tuning() if args.no_autotune else ctx.autotune([sid], samples=8)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
     for i in range(args.steps):
-        ctx.render([sid], i, 1, seed=2024, mode=cg.CGPU_MODE_WAVEFRONT, graph=False)
-    print(json.dumps({"profile_case": WORKLOAD if not args.quick else "quick", "passes": args.steps,
-                      "kernel_launches_last_pass": ctx.stats().kernel_launches}))
+        ctx.render([sid], i * args.profile_spp, args.profile_spp, seed=2024, mode=cg.CGPU_MODE_WAVEFRONT, graph=False)
+    torch.cuda.synchronize()
+    torch.cuda.profiler.stop()
+    print(json.dumps({"profile_case": WORKLOAD if not args.quick else "quick", "renders": args.steps,
+                      "spp_per_render": args.profile_spp, "tuning": tuning,
+                      "kernel_launches_last_render": ctx.stats().kernel_launches}))
     ctx.close()
 
 

@@ -36,7 +36,7 @@ EXPORTED = [
     "cgpu_crsd_primitive_index", "cgpu_crsd_free",
 ]
 
-KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel"]
+KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel", "reorder"]
 
 _lib = None
 
@@ -317,11 +317,12 @@ class Context:
         t = abi.cgpu_tuning()
         self._check(self.L.cgpu_tuning_get(self.h, C.byref(t)))
         return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths,
-                "traversal": t.traversal}
+                "traversal": t.traversal, "reorder": t.reorder}
 
-    def set_tuning(self, block_trace: int, block_shade: int, max_paths: int = 0, traversal: int = 0):
+    def set_tuning(self, block_trace: int, block_shade: int, max_paths: int = 0, traversal: int = 0,
+                   reorder: int = 0):
         t = abi.cgpu_tuning(block_trace=block_trace, block_shade=block_shade, max_paths=max_paths,
-                            traversal=traversal)
+                            traversal=traversal, reorder=reorder)
         self._check(self.L.cgpu_tuning_set(self.h, C.byref(t)))
 
     def autotune(self, sids, samples: int = 1, cache_path: Optional[str] = None) -> dict:
@@ -330,7 +331,7 @@ class Context:
         self._check(self.L.cgpu_autotune(self.h, arr, len(sids), samples,
                                          cache_path.encode() if cache_path else None, C.byref(t)))
         return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths,
-                "traversal": t.traversal}
+                "traversal": t.traversal, "reorder": t.reorder}
 
     def set_profiling(self, on: bool):
         self._check(self.L.cgpu_set_profiling(self.h, 1 if on else 0))

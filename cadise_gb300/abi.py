@@ -154,7 +154,7 @@ class cgpu_crsd_settings(C.Structure):
 
 class cgpu_tuning(C.Structure):
     _fields_ = [("block_trace", C.c_int32), ("block_shade", C.c_int32), ("max_paths", C.c_uint32),
-                ("traversal", C.c_int32)]
+                ("traversal", C.c_int32), ("reorder", C.c_int32)]
 
 
 class cgpu_param_counts(C.Structure):

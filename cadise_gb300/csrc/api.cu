@@ -266,6 +266,15 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.spp = d->spp > 0 ? d->spp : 1;
     S.cam = hs.cam;
     S.filter = hs.filter;
+    S.bounds_lo = make_float3(hs.info.bounds_min[0], hs.info.bounds_min[1], hs.info.bounds_min[2]);
+    {
+        float inv[3];
+        for (int k = 0; k < 3; ++k) {
+            const float e = hs.info.bounds_max[k] - hs.info.bounds_min[k];
+            inv[k] = e > 0.0f ? 1.0f / e : 0.0f;
+        }
+        S.bounds_inv = make_float3(inv[0], inv[1], inv[2]);
+    }
     sl.width = d->width;
     sl.height = d->height;
     sl.spp = S.spp;

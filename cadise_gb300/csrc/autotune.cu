@@ -15,7 +15,8 @@ namespace {
 
 bool valid_tuning(const cgpu_tuning& t) {
     auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
-    return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal >= 0 && t.traversal <= 2);
+    return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal >= 0 && t.traversal <= 2) &&
+           (t.reorder >= 0 && t.reorder <= 3);
 }
 
 void apply(cgpu_ctx* ctx, const cgpu_tuning& t) {
@@ -61,9 +62,11 @@ bool cache_lookup(const char* path, const std::string& key, cgpu_tuning* out) {
         const char* q = std::strstr(line.c_str(), "\"block_shade\":");
         const char* r = std::strstr(line.c_str(), "\"max_paths\":");
         const char* tv = std::strstr(line.c_str(), "\"traversal\":");
+        const char* ro = std::strstr(line.c_str(), "\"reorder\":");
         if (!p || !q || !r) continue;
-        int trav = 0;
+        int trav = 0, reord = 0;
         if (tv) std::sscanf(tv, "\"traversal\": %d", &trav);
+        if (ro) std::sscanf(ro, "\"reorder\": %d", &reord);
         if (std::sscanf(p, "\"block_trace\": %d", &a) != 1 || std::sscanf(q, "\"block_shade\": %d", &b) != 1 ||
             std::sscanf(r, "\"max_paths\": %u", &c) != 1)
             continue;
@@ -71,6 +74,7 @@ bool cache_lookup(const char* path, const std::string& key, cgpu_tuning* out) {
         t.block_shade = b;
         t.max_paths = c;
         t.traversal = trav;
+        t.reorder = reord;
         if (valid_tuning(t)) {
             *out = t;
             found = true;  // the last matching line wins
@@ -91,7 +95,7 @@ cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out) {
 
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* t) {
     if (!ctx || !t) return CGPU_ERR_INVALID_ARGUMENT;
-    if (!valid_tuning(*t)) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0, 1 or 2");
+    if (!valid_tuning(*t)) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0, 1 or 2, reorder 0 to 3");
     cudaStreamSynchronize(ctx->stream);
     apply(ctx, *t);
     return CGPU_OK;
@@ -157,14 +161,15 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     // paths in flight: larger batches hold several samples per pixel and
     // share one tail of short late-bounce queues among them
     const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
-    const int options[] = {3, 3, 3, 5};
-    for (int pass = 0; pass < 4 && st == CGPU_OK; ++pass) {
+    const int options[] = {3, 3, 3, 5, 4};
+    for (int pass = 0; pass < 5 && st == CGPU_OK; ++pass) {
         for (int k = 0; k < options[pass] && st == CGPU_OK; ++k) {
             cgpu_tuning t = best;
             if (pass == 0) t.traversal = k;
             if (pass == 1) t.block_trace = blocks[k];
             if (pass == 2) t.block_shade = blocks[k];
             if (pass == 3) t.max_paths = caps[k];
+            if (pass == 4) t.reorder = k;
             if (std::memcmp(&t, &best, sizeof(t)) == 0) continue;
             float ms = 0.0f;
             st = time_one(t, &ms);
@@ -186,7 +191,7 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
         std::ofstream f(cache_path, std::ios::app);
         f << "{\"key\": \"" << key << "\", \"block_trace\": " << best.block_trace << ", \"block_shade\": "
           << best.block_shade << ", \"max_paths\": " << best.max_paths << ", \"traversal\": " << best.traversal
-          << ", \"ms\": " << best_ms << "}\n";
+          << ", \"reorder\": " << best.reorder << ", \"ms\": " << best_ms << "}\n";
     }
     if (out) *out = best;
     return CGPU_OK;

@@ -24,6 +24,7 @@
 //      entries whose triangles are laid out contiguously in DFS order.
 // No kernel waits on another thread: every loop is bounded by the data.
 #include "bvh_build.h"
+#include "radix.cuh"
 
 #include <cuda_runtime.h>
 
@@ -34,9 +35,7 @@
 namespace cg {
 namespace {
 
-constexpr int kBlock = 256;
-constexpr int kItems = 8;                    // keys (or scan elements) per thread per tile
-constexpr int kTile = kBlock * kItems;       // 2048
+constexpr int kBlock = kRadixBlock;
 // PLOC search radius.  On the 1,024,018-triangle icosphere field closest-hit
 // rays visit 21.9 / 21.7 / 21.0 wide nodes with radius 16 / 32 / 64 (the
 // host SAH tree: 18.9) for 9.5 / 9.9 / 10.4 ms of build.
@@ -121,98 +120,6 @@ __global__ void k_morton(const float4* lo, const float4* hi, uint32_t n, const u
         keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
         vals[i] = i;
     }
-}
-
-// --------------------------------------------------------------- radix sort --
-// Digit counts of each block's tile, digit-major: hist[d * blocks + b].
-__global__ void k_radix_hist(const uint64_t* keys, uint32_t n, int shift, uint32_t* hist) {
-    __shared__ uint32_t h[256];
-    h[threadIdx.x] = 0;
-    __syncthreads();
-    const uint32_t base = blockIdx.x * kTile;
-    for (int r = 0; r < kItems; ++r) {
-        const uint32_t i = base + r * kBlock + threadIdx.x;
-        if (i < n) atomicAdd(&h[(keys[i] >> shift) & 255u], 1u);
-    }
-    __syncthreads();
-    hist[threadIdx.x * gridDim.x + blockIdx.x] = h[threadIdx.x];
-}
-
-// Stable scatter of one tile: rounds of 256 consecutive keys, ranked within
-// each warp by match_any and across the block's warps by per-digit counts.
-__global__ void k_radix_scatter(const uint64_t* kin, const uint32_t* vin, uint64_t* kout, uint32_t* vout, uint32_t n,
-                                int shift, const uint32_t* offs) {
-    __shared__ uint32_t wc[kBlock / 32][256];
-    __shared__ uint32_t run[256];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    run[t] = offs[t * gridDim.x + blockIdx.x];
-    for (int w = 0; w < kBlock / 32; ++w) wc[w][t] = 0;
-    __syncthreads();
-    const uint32_t base = blockIdx.x * kTile;
-    for (int r = 0; r < kItems; ++r) {
-        const uint32_t i = base + r * kBlock + t;
-        const bool valid = i < n;
-        const uint64_t k = valid ? kin[i] : 0ull;
-        const uint32_t v = valid ? vin[i] : 0u;
-        const int d = valid ? int((k >> shift) & 255u) : 256;
-        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
-        const int rank = __popc(peers & ((1u << lane) - 1u));
-        if (valid && lane == __ffs(peers) - 1) wc[warp][d] = __popc(peers);
-        __syncthreads();
-        {
-            uint32_t acc = run[t];
-            for (int w = 0; w < kBlock / 32; ++w) {
-                const uint32_t c = wc[w][t];
-                wc[w][t] = acc;
-                acc += c;
-            }
-            run[t] = acc;
-        }
-        __syncthreads();
-        if (valid) {
-            const uint32_t pos = wc[warp][d] + uint32_t(rank);
-            kout[pos] = k;
-            vout[pos] = v;
-        }
-        __syncthreads();
-        for (int w = 0; w < kBlock / 32; ++w) wc[w][t] = 0;
-        __syncthreads();
-    }
-}
-
-// ----------------------------------------------------------- exclusive scan --
-__global__ void k_scan_tile(uint32_t* data, uint32_t n, uint32_t* sums) {
-    __shared__ uint32_t warp_tot[kBlock / 32];
-    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-    const uint32_t base = blockIdx.x * kTile + uint32_t(t) * kItems;
-    uint32_t v[kItems], local = 0;
-    for (int k = 0; k < kItems; ++k) {
-        v[k] = base + k < n ? data[base + k] : 0u;
-        local += v[k];
-    }
-    uint32_t incl = local;
-    for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) warp_tot[warp] = incl;
-    __syncthreads();
-    uint32_t wpre = 0, total = 0;
-    for (int w = 0; w < kBlock / 32; ++w) {
-        if (w < warp) wpre += warp_tot[w];
-        total += warp_tot[w];
-    }
-    uint32_t run = wpre + incl - local;
-    for (int k = 0; k < kItems; ++k) {
-        if (base + k < n) data[base + k] = run;
-        run += v[k];
-    }
-    if (t == 0) sums[blockIdx.x] = total;
-}
-
-__global__ void k_scan_add(uint32_t* data, uint32_t n, const uint32_t* offs) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        data[i] += offs[i / kTile];
 }
 
 // ---------------------------------------------------------------------- PLOC --
@@ -440,26 +347,6 @@ int grid_of(uint64_t work, int block = kBlock) {
     return int(std::max<uint64_t>(1, std::min<uint64_t>((work + block - 1) / block, 1u << 20)));
 }
 
-// In-place exclusive scan of n values; `sums` holds ceil(n / kTile) + ceil(.. / kTile) + ... words.
-void exclusive_scan(uint32_t* data, uint32_t n, uint32_t* sums, cudaStream_t s) {
-    if (n == 0) return;
-    const uint32_t nb = (n + kTile - 1) / kTile;
-    k_scan_tile<<<nb, kBlock, 0, s>>>(data, n, sums);
-    if (nb > 1) {
-        exclusive_scan(sums, nb, sums + nb, s);
-        k_scan_add<<<grid_of(n), kBlock, 0, s>>>(data, n, sums);
-    }
-}
-
-size_t scan_scratch(uint32_t n) {
-    size_t total = 0;
-    while (n > 1) {
-        n = (n + kTile - 1) / kTile;
-        total += n;
-    }
-    return total + 1;
-}
-
 }  // namespace
 
 bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4Result* out, std::string* err) {
@@ -474,7 +361,7 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
         return false;
     }
     Pool P;
-    const uint32_t nb = (n + kTile - 1) / kTile;
+    const uint32_t nb = radix_tiles(n);
     float* tv = P.get<float>(size_t(n) * 9);
     float4* tlo = P.get<float4>(n);
     float4* thi = P.get<float4>(n);
@@ -518,12 +405,7 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     cudaMemcpyAsync(cb, cb_init, sizeof(cb_init), cudaMemcpyHostToDevice, s);
     k_tri_boxes<<<grid_of(n), kBlock, 0, s>>>(tv, n, tlo, thi, cb);
     k_morton<<<grid_of(n), kBlock, 0, s>>>(tlo, thi, n, cb, keys[0], vals[0]);
-    for (int pass = 0; pass < 8; ++pass) {
-        const int cur = pass & 1;
-        k_radix_hist<<<nb, kBlock, 0, s>>>(keys[cur], n, 8 * pass, hist);
-        exclusive_scan(hist, nb * 256, sums, s);
-        k_radix_scatter<<<nb, kBlock, 0, s>>>(keys[cur], vals[cur], keys[cur ^ 1], vals[cur ^ 1], n, 8 * pass, hist);
-    }
+    radix_sort_pairs(keys, vals, n, nullptr, nb, 8, hist, sums, s);
     if (fail_cuda("sort")) return false;
     // 8 passes: the sorted pairs are back in keys[0] / vals[0]
     k_ploc_init<<<grid_of(n), kBlock, 0, s>>>(tlo, thi, vals[0], n, clo[0], chi[0], blo, bhi);

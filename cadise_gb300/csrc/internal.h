@@ -168,6 +168,19 @@ struct RenderArgs {
     WfBuffers wf;
     unsigned long long* counters;  // closest rays, any rays, nodes, tris, paths
     AdjBufs adj;      // wavefront adjoint only
+    // reordered closest-hit queue (tuning.reorder): path | 0x80000000 for a MIS ray
+    const uint32_t* sorted;
+};
+
+// Buffers of the ray reordering: keys / values ping-pong for 2 * path_cap
+// queue entries, digit counts, scan scratch, the entry count.
+struct SortBufs {
+    uint32_t* keys[2];
+    uint32_t* vals[2];
+    uint32_t* hist;
+    uint32_t* sums;
+    uint32_t* n;
+    uint32_t tiles;
 };
 
 }  // namespace cg
@@ -198,7 +211,7 @@ struct cgpu_ctx {
     std::vector<SceneSlot> scenes;
     int num_sms = 0;
     bool counting = false;
-    cgpu_tuning tuning{128, 128, 0, 0};
+    cgpu_tuning tuning{128, 128, 0, 0, 0};
 
     // device tables (rebuilt when the scene set changes)
     cg::SceneD* d_scenes = nullptr;
@@ -217,6 +230,10 @@ struct cgpu_ctx {
     cg::WfBuffers wf{};
     void* wf_block = nullptr;
     // wavefront adjoint state (allocated by the first wavefront adjoint)
+    // ray reordering buffers (allocated while tuning.reorder is on)
+    uint32_t sort_cap = 0;
+    cg::SortBufs sort{};
+    void* sort_block = nullptr;
     uint32_t adj_cap = 0;
     cg::AdjBufs adj{};
     void* adj_block = nullptr;
@@ -229,6 +246,7 @@ struct cgpu_ctx {
     int graph_depth = -1;
     uint32_t graph_paths = 0;
     bool graph_spheres = false;
+    uint32_t graph_launches = 0;  // kernel launches one replay of the graph makes
     bool batch_spheres = false;  // a scene of the current render holds spheres
 
     cgpu_render_stats stats{};

@@ -16,6 +16,7 @@
 #include "film.cuh"
 #include "internal.h"
 #include "pathtrace.cuh"
+#include "radix.cuh"
 
 #include <algorithm>
 #include <cstring>
@@ -177,7 +178,58 @@ CG_D void shadow_finish(const WfBuffers& w, int p, bool occluded) {
     w.Ls[p] = Ls;
 }
 
-template <bool COUNT, bool SPH, bool ADJ = false>
+// Queue entry i of a closest-hit pass: its path and whether it is a
+// continuation ray (else a MIS ray); SORTED reads the reordered queue.
+template <bool SORTED>
+CG_D int extend_entry(const RenderArgs& a, const int* qc, const int* qm, int ncont, int i, bool* cont) {
+    if (SORTED) {
+        const uint32_t e = a.sorted[i];
+        *cont = (e >> 31) == 0u;
+        return int(e & 0x7FFFFFFFu);
+    }
+    *cont = i < ncont;
+    return *cont ? qc[i] : qm[i - ncont];
+}
+
+CG_D uint32_t spread9(uint32_t v) {
+    uint32_t x = v & 0x1FFu;
+    x = (x | (x << 16)) & 0x030000FFu;
+    x = (x | (x << 8)) & 0x0300F00Fu;
+    x = (x | (x << 4)) & 0x030C30C3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// Sort keys of a closest-hit pass's queue (tuning.reorder): the direction's
+// octant above the Morton code of the origin in the scene bounds (`bits` per
+// axis, at most 9), so that sorted neighbours leave nearby points in similar
+// directions.  Values: path | 0x80000000 for a MIS ray.  Writes the entry
+// count for the sort.
+__global__ void k_ray_keys(RenderArgs a, int b, int bits, uint32_t* keys, uint32_t* vals, uint32_t* n_out) {
+    const WfBuffers& w = a.wf;
+    const int* cnt = w.cnt + b * kCntStride;
+    const int ncont = cnt[0], n = ncont + cnt[1];
+    const int* qc = w.q_cont[b & 1];
+    const int* qm = w.q_mis[b & 1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *n_out = uint32_t(n);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const bool cont = i < ncont;
+        const int p = cont ? qc[i] : qm[i - ncont];
+        const float3 o = f3(w.ray_o[p]);
+        const float3 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+        const SceneD& S = a.scenes[w.meta[p].x];
+        const float u[3] = {(o.x - S.bounds_lo.x) * S.bounds_inv.x, (o.y - S.bounds_lo.y) * S.bounds_inv.y,
+                            (o.z - S.bounds_lo.z) * S.bounds_inv.z};
+        const float cells = float((1 << bits) - 1);
+        uint32_t q[3];
+        for (int k = 0; k < 3; ++k) q[k] = uint32_t(fminf(fmaxf(u[k], 0.0f), 1.0f) * cells);
+        const uint32_t oct = (d.x < 0.0f ? 4u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 1u : 0u);
+        keys[i] = (oct << (3 * bits)) | (spread9(q[0]) << 2) | (spread9(q[1]) << 1) | spread9(q[2]);
+        vals[i] = uint32_t(p) | (cont ? 0u : 0x80000000u);
+    }
+}
+
+template <bool COUNT, bool SPH, bool ADJ = false, bool SORTED = false>
 __global__ void k_wf_extend(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -189,8 +241,8 @@ __global__ void k_wf_extend(RenderArgs a, int b) {
     uint32_t nclosest = 0;
     int* const* qmat = w.q_mat;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const bool cont = i < ncont;
-        const int p = cont ? qc[i] : qm[i - ncont];
+        bool cont;
+        const int p = extend_entry<SORTED>(a, qc, qm, ncont, i, &cont);
         const SceneD& S = a.scenes[w.meta[p].x];
         const float3 o = f3(w.ray_o[p]);
         const float3 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
@@ -304,7 +356,7 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
 // longest ray is done.  Same hits as the other extend kernels (closer_hit).
 constexpr int kRefillLanes = 12;
 
-template <bool COUNT, bool SPH>
+template <bool COUNT, bool SPH, bool SORTED = false>
 __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -323,6 +375,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     int hslot = -1;
     uint32_t cur = kNoEntry, leaf = kNoEntry;
     int i = -1, p = -1;  // queue entry and path of this lane's ray (i < 0: none)
+    bool cont = false;   // continuation ray (else MIS ray)
     bool drained = false;
     auto pop = [&]() -> uint32_t {
         while (sp > 0) {
@@ -339,9 +392,9 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 drained = true;
             } else {
                 i = k;
-                p = i < ncont ? qc[i] : qm[i - ncont];
+                p = extend_entry<SORTED>(a, qc, qm, ncont, i, &cont);
                 const float3 o = f3(w.ray_o[p]);
-                const float3 d = i < ncont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+                const float3 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
                 r = ray_prep(o, d, kRayEps, kFloatMax);
                 tcur = r.tmax;
                 hslot = -1;
@@ -387,7 +440,6 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
             hit.slot = hslot;
             hit.u = hu;
             hit.v = hv;
-            const bool cont = i < ncont;
             const int key = extend_finish(w, S, p, cont, r.o, r.d, hslot >= 0, hit);
             grouped_push(qmat, cnt + 3, key, p);
             i = -1;
@@ -805,14 +857,50 @@ cgpu_status ensure_path_buffers(cgpu_ctx* ctx, uint32_t cap, int depth) {
     return CGPU_OK;
 }
 
+uint32_t scan_launches(uint32_t n) {
+    const uint32_t nb = radix_tiles(n);
+    return 1 + (nb > 1 ? scan_launches(nb) + 1 : 0);
+}
+
+// Ray reordering buffers for 2 * path_cap queue entries (continuation + MIS
+// rays of a pass), kept while tuning.reorder is on.
+cgpu_status ensure_sort_buffers(cgpu_ctx* ctx) {
+    if (!ctx->tuning.reorder) return CGPU_OK;
+    const uint64_t cap = uint64_t(ctx->path_cap) * 2;
+    if (ctx->sort_block && ctx->sort_cap >= cap) return CGPU_OK;
+    if (ctx->sort_block) cudaFree(ctx->sort_block);
+    ctx->sort_block = nullptr;
+    ctx->sort_cap = 0;
+    const uint32_t tiles = radix_tiles(cap);
+    const size_t words[] = {cap, cap, cap, cap, size_t(tiles) * 256, scan_scratch(uint64_t(tiles) * 256), 1};
+    size_t total = 0;
+    for (size_t w : words) total += (w * sizeof(uint32_t) + 255) & ~size_t(255);
+    cudaError_t e = cudaMalloc(&ctx->sort_block, total);
+    if (e != cudaSuccess) {
+        ctx->sort_block = nullptr;
+        return cg_fail(ctx, CGPU_ERR_OUT_OF_MEMORY, "reorder buffers: " + std::string(cudaGetErrorString(e)));
+    }
+    uint32_t* ptr[7];
+    char* base = static_cast<char*>(ctx->sort_block);
+    for (int i = 0; i < 7; ++i) {
+        ptr[i] = reinterpret_cast<uint32_t*>(base);
+        base += (words[i] * sizeof(uint32_t) + 255) & ~size_t(255);
+    }
+    ctx->sort = SortBufs{{ptr[0], ptr[1]}, {ptr[2], ptr[3]}, ptr[4], ptr[5], ptr[6], tiles};
+    ctx->sort_cap = uint32_t(cap);
+    return CGPU_OK;
+}
+
 RenderArgs make_args(cgpu_ctx* ctx) {
-    RenderArgs a;
+    RenderArgs a{};
     a.scenes = ctx->d_scenes;
     a.chunks = ctx->d_chunks;
     a.header = ctx->d_header;
     a.films = ctx->d_films;
     a.wf = ctx->wf;
     a.counters = ctx->d_counters;
+    a.adj = AdjBufs{};
+    a.sorted = nullptr;
     return a;
 }
 
@@ -867,6 +955,18 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     auto ext_kernel = trav == 1 ? CG_PICK(k_wf_extend_dyn) : trav == 2 ? CG_PICK(k_wf_extend_pww) : CG_PICK(k_wf_extend);
     auto sh_kernel = trav == 1 ? CG_PICK(k_wf_shadow_dyn) : CG_PICK(k_wf_shadow);
 #undef CG_PICK
+    // reordered closest-hit passes after the first (the primary rays are in pixel order already)
+    const bool reorder = ctx->tuning.reorder != 0 && trav != 1 && ctx->sort_block != nullptr;
+#define CG_PICK_SORTED(C, S) (trav == 2 ? k_wf_extend_pww<C, S, true> : k_wf_extend<C, S, false, true>)
+    auto ext_sorted = sph ? (counting ? CG_PICK_SORTED(true, true) : CG_PICK_SORTED(false, true))
+                          : (counting ? CG_PICK_SORTED(true, false) : CG_PICK_SORTED(false, false));
+#undef CG_PICK_SORTED
+    // reorder 1 / 2 / 3: 9 / 7 / 4 Morton bits per axis, 4 / 3 / 2 sort passes of 8 bits; an odd
+    // pass count leaves the sorted values in the second buffer
+    const int sort_bits = ctx->tuning.reorder == 1 ? 9 : ctx->tuning.reorder == 2 ? 7 : 4;
+    const int sort_passes = (3 + 3 * sort_bits + 7) / 8;
+    if (reorder) a.sorted = ctx->sort.vals[sort_passes & 1];
+    const int gkeys = grid_for(ctx, k_ray_keys, 256, uint64_t(paths) * 2);
     const int gext = grid_for(ctx, ext_kernel, bt, paths);
     const int gsh = grid_for(ctx, sh_kernel, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
@@ -875,7 +975,17 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     for (int b = 0; b <= depth; ++b) {
         cudaEventRecord(fork, s);
         cudaStreamWaitEvent(side, fork, 0);
-        timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, 0, s>>>(a, b); });
+        if (reorder && b > 0) {
+            const SortBufs& q = ctx->sort;
+            timed(ctx, CGPU_KERNEL_REORDER, s, [&] {
+                k_ray_keys<<<gkeys, 256, 0, s>>>(a, b, sort_bits, q.keys[0], q.vals[0], q.n);
+                radix_sort_pairs<uint32_t>(q.keys, q.vals, 0, q.n, q.tiles, sort_passes, q.hist, q.sums, s);
+            });
+            launches += 1 + sort_passes * (2 + scan_launches(q.tiles * 256));
+            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_sorted<<<gext, bt, 0, s>>>(a, b); });
+        } else {
+            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, 0, s>>>(a, b); });
+        }
         timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, 0, side>>>(a, b); });
         cudaEventRecord(join, side);
         cudaStreamWaitEvent(s, join, 0);
@@ -946,9 +1056,10 @@ cgpu_status run_batch(cgpu_ctx* ctx, int mode, int depth, uint32_t paths, bool s
         ctx->graph_depth = depth;
         ctx->graph_paths = ctx->path_cap;
         ctx->graph_spheres = ctx->batch_spheres;
+        ctx->graph_launches = ctx->stats.kernel_launches - before;
         ctx->stats.kernel_launches = before;
     }
-    ctx->stats.kernel_launches += uint32_t(2 + (depth + 1) * 2 + depth * kNumBsdfKinds);
+    ctx->stats.kernel_launches += ctx->graph_launches;
     return cg_cuda(ctx, cudaGraphLaunch(ctx->graph, ctx->stream), "graph launch");
 }
 
@@ -972,6 +1083,12 @@ void cg_free_render_state(cgpu_ctx* ctx) {
     }
     ctx->adj = AdjBufs{};
     ctx->adj_cap = 0;
+    if (ctx->sort_block) {
+        cudaFree(ctx->sort_block);
+        ctx->sort_block = nullptr;
+    }
+    ctx->sort = SortBufs{};
+    ctx->sort_cap = 0;
 }
 
 // Split the requested samples of every scene into batches of at most
@@ -997,6 +1114,8 @@ cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p) {
     cgpu_status st = cg_sync_tables(ctx);
     if (st != CGPU_OK) return st;
     st = ensure_path_buffers(ctx, paths_capacity(ctx, max_npix), depth);
+    if (st != CGPU_OK) return st;
+    st = ensure_sort_buffers(ctx);
     if (st != CGPU_OK) return st;
     ctx->stats = cgpu_render_stats{};
     ctx->times = cgpu_kernel_times{};
@@ -1075,6 +1194,8 @@ cgpu_status cg_render_paths_raw(cgpu_ctx* ctx, int scene, int mode, uint32_t fir
     cgpu_status st = cg_sync_tables(ctx);
     if (st != CGPU_OK) return st;
     st = ensure_path_buffers(ctx, paths_capacity(ctx, npix), sl.max_depth);
+    if (st != CGPU_OK) return st;
+    st = ensure_sort_buffers(ctx);
     if (st != CGPU_OK) return st;
     float* d_out = nullptr;
     const uint32_t per = std::max<uint32_t>(1, ctx->path_cap / npix);
@@ -1397,7 +1518,7 @@ extern "C" cgpu_status cgpu_render_noalloc(cgpu_ctx* ctx, int32_t scene, uint32_
     NoAllocView v;
     if (noalloc_layout(base, &v) > kNoAllocScratchBytes)
         return cg_fail(ctx, CGPU_ERR_UNSUPPORTED, "render_noalloc: scratch layout exceeds the static array");
-    RenderArgs a;
+    RenderArgs a{};
     a.scenes = v.scenes;
     a.chunks = v.chunk;
     a.header = v.header;

@@ -147,6 +147,7 @@ struct SceneD {
     int spp;
     CameraD cam;
     FilterD filter;
+    float3 bounds_lo, bounds_inv;  // scene bounds: lower corner, 1 / extent (0 for a flat axis)
 };
 
 }  // namespace cg

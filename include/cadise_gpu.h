@@ -344,6 +344,10 @@ typedef struct cgpu_tuning {
     int32_t traversal;     /* 0: one ray per thread per grid-stride step; 1: persistent warps that hand a
                               finished lane the next ray at once; 2: persistent while-while closest-hit
                               pass that refills a warp's finished lanes once 20 of them are done */
+    int32_t reorder;       /* 1, 2, 3: before each closest-hit pass after the first, sort its rays by
+                              direction octant and origin (Morton order of 9, 7 or 4 bits per axis in the
+                              scene bounds; 4, 3 or 2 radix passes), so that a warp traces neighbouring
+                              rays (traversal 0 and 2); 0: queue order */
 } cgpu_tuning;
 cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out_tuning);
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* tuning);
@@ -396,6 +400,7 @@ enum {
     CGPU_KERNEL_SHADE = 3,      /* all shade-by-BSDF kernels */
     CGPU_KERNEL_SPLAT = 4,
     CGPU_KERNEL_MEGAKERNEL = 5,
+    CGPU_KERNEL_REORDER = 6,    /* sort keys + radix sort of a closest-hit queue (tuning.reorder) */
     CGPU_KERNEL_CLASSES = 8
 };
 typedef struct cgpu_kernel_times {

@@ -79,9 +79,10 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
         gpu_ctx.film_clear(s)
     gpu_ctx.render(sids, 0, 4, seed=5)
     ref = films(gpu_ctx, sids)
-    # small batches; persistent ray replacement (1) and persistent while-while (2)
-    for traversal in (1, 2):
-        gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal)
+    # small batches; persistent ray replacement (1) and persistent while-while (2);
+    # closest-hit queues sorted by direction octant and origin (reorder) with traversals 0 and 2
+    for traversal, reorder in ((1, 0), (2, 0), (0, 1), (2, 2), (2, 3)):
+        gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal, reorder=reorder)
         for s in sids:
             gpu_ctx.film_clear(s)
         gpu_ctx.render(sids, 0, 4, seed=5)
@@ -90,7 +91,7 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
         for a, b in zip(ref, got):
             for x, y in zip(a, b):
                 assert np.array_equal(x, y)
-    gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], base["traversal"])
+    gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], base["traversal"], base["reorder"])
 
 
 def test_autotune_picks_and_caches(gpu_ctx, uneven, tmp_path):
