@@ -42,6 +42,8 @@ def parse():
     ap.add_argument("--bvh", default="auto", choices=["auto", "host", "gpu"],
                     help="BVH builder of the uploads (auto: the GPU build for large scenes)")
     ap.add_argument("--profile-spp", type=int, default=8, help="samples per pixel per --profile-case render")
+    ap.add_argument("--tuning", default=None,
+                    help="--profile-case: this cgpu_tuning (JSON, as the bench line prints it) instead of autotuning")
     ap.add_argument("--profile-case", action="store_true",
                     help="for ncu: the frame with the bench tuning, --steps renders of --profile-spp in a profiler range")
     ap.add_argument("--config", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
@@ -509,7 +511,12 @@ def run_profile_case(args):
     ctx.set_bvh_builder(BVH_BUILDERS[args.bvh])
     spec = make_scene(args)
     sid = ctx.upload(abi.flatten(spec))
-    tuning = ctx.tuning() if args.no_autotune else ctx.autotune([sid], samples=8)
+    if args.tuning:
+        t = json.loads(args.tuning)
+        ctx.set_tuning(t["block_trace"], t["block_shade"], t["max_paths"], t["traversal"], t.get("reorder", 0))
+        tuning = ctx.tuning()
+    else:
+        tuning = ctx.tuning() if args.no_autotune else ctx.autotune([sid], samples=8)
     torch.cuda.synchronize()
     torch.cuda.profiler.start()
     for i in range(args.steps):
