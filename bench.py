@@ -373,13 +373,15 @@ def run_reference(args, rank, world, local):
     threads = os.cpu_count() or 1
     ps = oracle.PortScene(flat)
     w, h = spec.width, spec.height
-    rows = 4
+    # whole rows are the unit of the port's thread pool: a step of 3 rows per
+    # thread keeps every host thread busy (~0.1 s of work per step)
+    rows = min(h, 3 * threads)
     mid = h // 2
     for i in range(args.warmup):
         ps.render(seed=i, first=0, count=1, rows=(mid, mid + 1), threads=threads)
     t0 = time.perf_counter()
     for i in range(args.steps):
-        r0 = (mid + i * rows) % (h - rows)
+        r0 = (mid + i * rows) % max(1, h - rows)
         ps.render(seed=100 + i, first=i, count=1, rows=(r0, r0 + rows), threads=threads)
     dt = time.perf_counter() - t0
     samples = rows * w * args.steps
