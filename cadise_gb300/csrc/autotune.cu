@@ -15,7 +15,7 @@ namespace {
 
 bool valid_tuning(const cgpu_tuning& t) {
     auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
-    return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal >= 0 && t.traversal <= 2) &&
+    return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal >= 0 && t.traversal <= 3) &&
            (t.reorder >= 0 && t.reorder <= 3);
 }
 
@@ -95,7 +95,7 @@ cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out) {
 
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* t) {
     if (!ctx || !t) return CGPU_ERR_INVALID_ARGUMENT;
-    if (!valid_tuning(*t)) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0, 1 or 2, reorder 0 to 3");
+    if (!valid_tuning(*t)) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0 to 3, reorder 0 to 3");
     cudaStreamSynchronize(ctx->stream);
     apply(ctx, *t);
     return CGPU_OK;
@@ -163,7 +163,7 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
     // (ray reordering is not searched: on the 1 M-triangle field its sort costs about what it saves in
     // the closest-hit passes, so the search would pick it by noise)
-    const int options[] = {3, 3, 3, 5};
+    const int options[] = {4, 3, 3, 5};
     for (int pass = 0; pass < 4 && st == CGPU_OK; ++pass) {
         for (int k = 0; k < options[pass] && st == CGPU_OK; ++k) {
             cgpu_tuning t = best;

@@ -448,6 +448,92 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
 }
 
+// Persistent any-hit pass: k_wf_extend_pww's while-while traversal with
+// dynamic ray fetch for the shadow rays; a ray ends at its first hit.
+constexpr int kRefillLanesAny = 12;
+
+template <bool COUNT, bool SPH>
+__global__ void k_wf_shadow_pww(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    int* cnt = w.cnt + b * kCntStride;
+    const int n = cnt[2];
+    const int* q = w.q_shadow[b & 1];
+    TraceCounters tc{0, 0};
+    uint32_t nany = 0;
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    RayPre r{};
+    float tcur = 0.0f, hu = 0.0f, hv = 0.0f;
+    int hslot = -1;
+    uint32_t cur = kNoEntry, leaf = kNoEntry;
+    int i = -1, p = -1;
+    bool occluded = false, drained = false;
+    auto pop = [&]() -> uint32_t {
+        if (sp > 0) return stack_e[--sp];
+        return kNoEntry;
+    };
+    for (;;) {
+        const bool need = i < 0 && !drained;
+        const int k = warp_take(cnt + 9, need, n);
+        if (need) {
+            if (k < 0) {
+                drained = true;
+            } else {
+                i = k;
+                p = q[i];
+                const float4 sd = w.sh_d[p];
+                r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
+                tcur = r.tmax;
+                hslot = -1;
+                cur = 0;
+                leaf = kNoEntry;
+                sp = 0;
+                occluded = false;
+                if (COUNT) ++nany;
+            }
+        }
+        if (__all_sync(__activemask(), i < 0)) break;
+        if (i < 0) continue;
+        const SceneD& S = a.scenes[w.meta[p].x];
+        for (;;) {
+            while (cur != kNoEntry && !entry_is_leaf(cur)) {
+                cur = visit_node<true, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, &tc);
+                if (cur == kNoEntry) cur = pop();
+                if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
+                    leaf = cur;
+                    cur = pop();
+                }
+                if (!__any_sync(__activemask(), leaf == kNoEntry)) break;
+            }
+            if (leaf == kNoEntry) {
+                if (cur == kNoEntry) break;  // the ray is done: unoccluded
+                leaf = cur;
+                cur = pop();
+            }
+            while (leaf != kNoEntry) {
+                if (visit_leaf<true, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, &tc)) {
+                    occluded = true;
+                    cur = leaf = kNoEntry;
+                    break;
+                }
+                leaf = kNoEntry;
+                if (cur != kNoEntry && entry_is_leaf(cur)) {
+                    leaf = cur;
+                    cur = pop();
+                }
+            }
+            if (cur == kNoEntry) break;  // the ray is done
+            if (__popc(__activemask()) < kRefillLanesAny) break;
+        }
+        if (cur == kNoEntry && leaf == kNoEntry) {
+            shadow_finish(w, p, occluded);
+            i = -1;
+        }
+    }
+    count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
+}
+
 template <bool COUNT, bool SPH>
 __global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
@@ -952,12 +1038,13 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int trav = ctx->tuning.traversal;
     const bool sph = ctx->batch_spheres;
 #define CG_PICK(K) (sph ? (counting ? K<true, true> : K<false, true>) : (counting ? K<true, false> : K<false, false>))
-    auto ext_kernel = trav == 1 ? CG_PICK(k_wf_extend_dyn) : trav == 2 ? CG_PICK(k_wf_extend_pww) : CG_PICK(k_wf_extend);
-    auto sh_kernel = trav == 1 ? CG_PICK(k_wf_shadow_dyn) : CG_PICK(k_wf_shadow);
+    auto ext_kernel = trav == 1 ? CG_PICK(k_wf_extend_dyn)
+                      : (trav == 2 || trav == 3) ? CG_PICK(k_wf_extend_pww) : CG_PICK(k_wf_extend);
+    auto sh_kernel = trav == 1 ? CG_PICK(k_wf_shadow_dyn) : trav == 3 ? CG_PICK(k_wf_shadow_pww) : CG_PICK(k_wf_shadow);
 #undef CG_PICK
     // reordered closest-hit passes after the first (the primary rays are in pixel order already)
     const bool reorder = ctx->tuning.reorder != 0 && trav != 1 && ctx->sort_block != nullptr;
-#define CG_PICK_SORTED(C, S) (trav == 2 ? k_wf_extend_pww<C, S, true> : k_wf_extend<C, S, false, true>)
+#define CG_PICK_SORTED(C, S) (trav >= 2 ? k_wf_extend_pww<C, S, true> : k_wf_extend<C, S, false, true>)
     auto ext_sorted = sph ? (counting ? CG_PICK_SORTED(true, true) : CG_PICK_SORTED(false, true))
                           : (counting ? CG_PICK_SORTED(true, false) : CG_PICK_SORTED(false, false));
 #undef CG_PICK_SORTED
@@ -1463,10 +1550,11 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
     const int trav = ctx->tuning.traversal;
     const bool sph = ctx->batch_spheres;
     auto ext = trav == 1   ? (sph ? k_wf_extend_dyn<false, true> : k_wf_extend_dyn<false, false>)
-               : trav == 2 ? (sph ? k_wf_extend_pww<false, true> : k_wf_extend_pww<false, false>)
+               : trav >= 2 ? (sph ? k_wf_extend_pww<false, true> : k_wf_extend_pww<false, false>)
                            : (sph ? k_wf_extend<false, true> : k_wf_extend<false, false>);
-    auto sh = trav == 1 ? (sph ? k_wf_shadow_dyn<false, true> : k_wf_shadow_dyn<false, false>)
-                        : (sph ? k_wf_shadow<false, true> : k_wf_shadow<false, false>);
+    auto sh = trav == 1   ? (sph ? k_wf_shadow_dyn<false, true> : k_wf_shadow_dyn<false, false>)
+              : trav == 3 ? (sph ? k_wf_shadow_pww<false, true> : k_wf_shadow_pww<false, false>)
+                          : (sph ? k_wf_shadow<false, true> : k_wf_shadow<false, false>);
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
     const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, sh, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),

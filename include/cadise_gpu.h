@@ -343,7 +343,8 @@ typedef struct cgpu_tuning {
     uint32_t max_paths;    /* paths in flight per wavefront batch; 0 = automatic (2^21, at least one frame) */
     int32_t traversal;     /* 0: one ray per thread per grid-stride step; 1: persistent warps that hand a
                               finished lane the next ray at once; 2: persistent while-while closest-hit
-                              pass that refills a warp's finished lanes once 20 of them are done */
+                              pass that refills a warp's finished lanes once 20 of them are done;
+                              3: 2 plus the same persistent while-while form for the any-hit pass */
     int32_t reorder;       /* 1, 2, 3: before each closest-hit pass after the first, sort its rays by
                               direction octant and origin (Morton order of 9, 7 or 4 bits per axis in the
                               scene bounds; 4, 3 or 2 radix passes), so that a warp traces neighbouring

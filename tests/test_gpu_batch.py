@@ -81,7 +81,7 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
     ref = films(gpu_ctx, sids)
     # small batches; persistent ray replacement (1) and persistent while-while (2);
     # closest-hit queues sorted by direction octant and origin (reorder) with traversals 0 and 2
-    for traversal, reorder in ((1, 0), (2, 0), (0, 1), (2, 2), (2, 3)):
+    for traversal, reorder in ((1, 0), (2, 0), (3, 0), (0, 1), (2, 2), (3, 3)):
         gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal, reorder=reorder)
         for s in sids:
             gpu_ctx.film_clear(s)
