@@ -356,7 +356,7 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
 // longest ray is done.  Same hits as the other extend kernels (closer_hit).
 constexpr int kRefillLanes = 12;
 
-template <bool COUNT, bool SPH, bool SORTED = false>
+template <bool COUNT, bool SPH, bool SORTED = false, bool ADJ = false>
 __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -440,7 +440,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
             hit.slot = hslot;
             hit.u = hu;
             hit.v = hv;
-            const int key = extend_finish(w, S, p, cont, r.o, r.d, hslot >= 0, hit);
+            const int key = extend_finish<ADJ>(w, S, p, cont, r.o, r.d, hslot >= 0, hit, &a.adj);
             grouped_push(qmat, cnt + 3, key, p);
             i = -1;
         }
@@ -452,7 +452,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
 // dynamic ray fetch for the shadow rays; a ray ends at its first hit.
 constexpr int kRefillLanesAny = 12;
 
-template <bool COUNT, bool SPH>
+template <bool COUNT, bool SPH, bool ADJ = false>
 __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     int* cnt = w.cnt + b * kCntStride;
@@ -527,7 +527,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
             if (__popc(__activemask()) < kRefillLanesAny) break;
         }
         if (cur == kNoEntry && leaf == kNoEntry) {
-            shadow_finish(w, p, occluded);
+            shadow_finish<ADJ>(w, p, occluded);
             i = -1;
         }
     }
@@ -1385,8 +1385,12 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
     cudaMemsetAsync(ctx->wf.cnt, 0, size_t(depth + 2) * kCntStride * sizeof(int), s);
     const int bt = ctx->tuning.block_trace, bs = ctx->tuning.block_shade;
     const bool sph = ctx->batch_spheres;
-    auto ext = sph ? k_wf_extend<false, true, true> : k_wf_extend<false, false, true>;
-    auto shd = sph ? k_wf_shadow<false, true, true> : k_wf_shadow<false, false, true>;
+    // the persistent passes when the tuning uses them (traversal 2 / 3), else the per-ray loops
+    const int trav = ctx->tuning.traversal;
+    auto ext = trav >= 2 ? (sph ? k_wf_extend_pww<false, true, false, true> : k_wf_extend_pww<false, false, false, true>)
+                         : (sph ? k_wf_extend<false, true, true> : k_wf_extend<false, false, true>);
+    auto shd = trav == 3 ? (sph ? k_wf_shadow_pww<false, true, true> : k_wf_shadow_pww<false, false, true>)
+                         : (sph ? k_wf_shadow<false, true, true> : k_wf_shadow<false, false, true>);
     void (*shade[kNumBsdfKinds])(RenderArgs, int) = {k_wf_shade<0, true>, k_wf_shade<1, true>, k_wf_shade<2, true>,
                                                      k_wf_shade<3, true>, k_wf_shade<4, true>};
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);

@@ -184,11 +184,17 @@ def test_wavefront_and_megakernel_schedules_agree(gpu_ctx, diff, name):
         gpu_ctx.set_adjoint_mode(CGPU_MODE_MEGAKERNEL)
         mk = gpu_ctx.adjoint_backward(sid, spp, seed, W)
         gpu_ctx.set_adjoint_mode(CGPU_MODE_WAVEFRONT)
-        wf = gpu_ctx.adjoint_backward(sid, spp, seed, W)
         assert sum(np.count_nonzero(g) for g in mk) > 0
-        for a, b in zip(wf, mk):
-            scale = np.abs(b).max() if b.size else 0.0
-            np.testing.assert_allclose(a, b, rtol=1e-7, atol=1e-10 * scale + 1e-30)
+        base = gpu_ctx.tuning()
+        # per-ray traversal passes, and the persistent while-while passes (traversal 3)
+        for traversal in (0, 3):
+            gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], traversal)
+            wf = gpu_ctx.adjoint_backward(sid, spp, seed, W)
+            for a, b in zip(wf, mk):
+                scale = np.abs(b).max() if b.size else 0.0
+                np.testing.assert_allclose(a, b, rtol=1e-7, atol=1e-10 * scale + 1e-30)
+        gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], base["traversal"],
+                           base["reorder"])
     finally:
         gpu_ctx.set_adjoint_mode(CGPU_MODE_WAVEFRONT)
         if release:
