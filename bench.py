@@ -87,10 +87,29 @@ class ClockSampler:
                                          stdout=self.file, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # wait (up to 3 s) until the sampler is live, so a short timed region still gets samples
+        t0 = time.perf_counter()
+        while time.perf_counter() - t0 < 3.0:
+            self.file.flush()
+            if os.path.getsize(self.file.name) > 0:
+                break
+            time.sleep(0.02)
+
+    def sample_once(self):
+        """One more sample at the end of a timed region shorter than the sampling period."""
+        try:
+            out = subprocess.run(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                  "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=10)
+            with open(self.file.name, "a") as f:
+                f.write(out.stdout)
+        except Exception:
+            pass
 
     def stop(self):
         if not self.proc:
             return None
+        self.sample_once()
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
