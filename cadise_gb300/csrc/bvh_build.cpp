@@ -6,8 +6,8 @@
 // copies its BvhBoundInfo vectors at every level.  Here: 32 bins per axis on
 // all three axes, leaves of up to 4 triangles (8 when the SAH cannot split),
 // in-place partition of one index array, subtrees above 32k triangles built
-// on separate host threads, then a greedy collapse (open the child with the
-// largest surface area until four children) into 128-byte 4-wide nodes.
+// on separate host threads, then an SAH-optimal collapse (wide_costs) into
+// 128-byte 4-wide nodes.
 #include "bvh_build.h"
 
 #include <algorithm>
@@ -145,7 +145,8 @@ struct Builder {
         const int l = alloc(), r = alloc();
         node.left = l;
         node.right = r;
-        node.count = 0;
+        node.first = begin;  // an inner node's triangles are idx[first, first + count) too
+        node.count = n;
         const bool spawn = (mid - begin) >= kParallelMin && (end - mid) >= kParallelMin &&
                            threads_live.fetch_add(1) < max_threads;
         if (spawn) {
@@ -165,6 +166,104 @@ void set_empty(Bvh4Node& n, int i) {
     n.lox[i] = n.loy[i] = n.loz[i] = INFINITY;
     n.hix[i] = n.hiy[i] = n.hiz[i] = -INFINITY;
     n.child[i] = 0;
+}
+
+// SAH-optimal conversion of the binary tree into 4-wide nodes (the dynamic
+// programme of Ylitie, Karras & Laine, "Efficient Incoherent Ray Traversal on
+// GPUs Through Compressed Wide BVHs", HPG 2017, for width 4): cost[i - 1] is
+// the least SAH cost of a binary subtree that may fill at most i child slots
+// of its parent - as one leaf (at most kMaxLeafTris triangles), as one inner
+// wide node, or (i > 1) split between its two children's subtrees.
+constexpr float kCostNode = 1.0f;  // one wide-node visit (four box tests)
+constexpr float kCostTri = 1.0f;   // one triangle test (at 0.3 or 0.5 the trees trace slower)
+constexpr float kInf = FLT_MAX;
+
+struct WideCost {
+    float cost[4];
+    int8_t split[4];  // i > 1: slots of the left child when distributing, 0 = use i - 1 slots
+    bool leaf;        // one slot: a leaf (else an inner wide node)
+};
+
+void wide_costs(const std::vector<BinNode>& bn, int count, std::vector<WideCost>* out) {
+    std::vector<WideCost>& wc = *out;
+    wc.assign(size_t(count), WideCost{});
+    // children have larger ids than their parent: one pass from the back
+    for (int n = count - 1; n >= 0; --n) {
+        const BinNode& b = bn[size_t(n)];
+        WideCost& w = wc[size_t(n)];
+        const float A = b.box.half_area();
+        const float leaf_cost = b.count <= kMaxLeafTris ? A * float(b.count) * kCostTri : kInf;
+        if (b.left < 0) {
+            for (int i = 0; i < 4; ++i) {
+                w.cost[i] = leaf_cost;
+                w.split[i] = 0;
+            }
+            w.leaf = true;
+            continue;
+        }
+        const WideCost& L = wc[size_t(b.left)];
+        const WideCost& R = wc[size_t(b.right)];
+        float dist[5];
+        int8_t arg[5];
+        for (int j = 2; j <= 4; ++j) {
+            dist[j] = kInf;
+            arg[j] = 1;
+            for (int k = 1; k < j; ++k) {
+                const float c = L.cost[k - 1] + R.cost[j - k - 1];
+                if (c < dist[j]) {
+                    dist[j] = c;
+                    arg[j] = int8_t(k);
+                }
+            }
+        }
+        const float inner = A * kCostNode + dist[4];
+        w.leaf = leaf_cost <= inner;
+        w.cost[0] = w.leaf ? leaf_cost : inner;
+        w.split[0] = 0;
+        for (int i = 2; i <= 4; ++i) {
+            if (dist[i] < w.cost[i - 2]) {
+                w.cost[i - 1] = dist[i];
+                w.split[i - 1] = arg[i];
+            } else {
+                w.cost[i - 1] = w.cost[i - 2];
+                w.split[i - 1] = 0;
+            }
+        }
+    }
+}
+
+// The binary nodes that fill the slots of the wide node of inner node n.
+int wide_children(const std::vector<BinNode>& bn, const std::vector<WideCost>& wc, int n, int (&kids)[4]) {
+    int nk = 0;
+    // (node, slots) pairs still to place; at most 4 are ever open
+    int stack_n[8], stack_i[8], sp = 0;
+    const BinNode& b = bn[size_t(n)];
+    // the root of the wide node distributes its two children over 4 slots
+    int best_k = 1;
+    float best = kInf;
+    for (int k = 1; k < 4; ++k) {
+        const float c = wc[size_t(b.left)].cost[k - 1] + wc[size_t(b.right)].cost[4 - k - 1];
+        if (c < best) {
+            best = c;
+            best_k = k;
+        }
+    }
+    stack_n[sp] = b.right; stack_i[sp++] = 4 - best_k;
+    stack_n[sp] = b.left; stack_i[sp++] = best_k;
+    while (sp > 0) {
+        const int x = stack_n[--sp];
+        int i = stack_i[sp];
+        while (i > 1 && wc[size_t(x)].split[i - 1] == 0) --i;  // fewer slots do as well
+        if (i == 1) {
+            kids[nk++] = x;
+            continue;
+        }
+        const BinNode& c = bn[size_t(x)];
+        const int k = wc[size_t(x)].split[i - 1];
+        stack_n[sp] = c.right; stack_i[sp++] = i - k;
+        stack_n[sp] = c.left; stack_i[sp++] = k;
+    }
+    return nk;
 }
 
 }  // namespace
@@ -206,7 +305,9 @@ bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, s
     const std::vector<BinNode>& bn = B.nodes;
     out->binary_depth = B.max_depth.load();
 
-    // collapse into 4-wide nodes (breadth-first ids, root = 0)
+    // SAH-optimal collapse into 4-wide nodes (breadth-first ids, root = 0)
+    std::vector<WideCost> wc;
+    wide_costs(bn, B.next_node.load(), &wc);
     struct Item { int bin; int wide; int depth; };
     std::vector<Item> work;
     out->nodes.emplace_back();
@@ -219,26 +320,10 @@ bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, s
         int kids[4];
         int nk = 0;
         const BinNode& b = bn[it.bin];
-        if (b.left < 0) {
-            kids[nk++] = it.bin;  // a leaf root: one leaf child
+        if (b.left < 0 || wc[it.bin].leaf) {
+            kids[nk++] = it.bin;  // a root that is one leaf
         } else {
-            kids[nk++] = b.left;
-            kids[nk++] = b.right;
-            while (nk < 4) {
-                int pick = -1;
-                float area = -1.0f;
-                for (int k = 0; k < nk; ++k) {
-                    const BinNode& c = bn[kids[k]];
-                    if (c.left >= 0 && c.box.half_area() > area) {
-                        area = c.box.half_area();
-                        pick = k;
-                    }
-                }
-                if (pick < 0) break;
-                const BinNode& c = bn[kids[pick]];
-                kids[pick] = c.left;
-                kids[nk++] = c.right;
-            }
+            nk = wide_children(bn, wc, it.bin, kids);
         }
         Bvh4Node wn;
         std::memset(&wn, 0, sizeof(wn));
@@ -250,7 +335,7 @@ bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, s
             const BinNode& c = bn[kids[k]];
             wn.lox[k] = c.box.lo[0]; wn.loy[k] = c.box.lo[1]; wn.loz[k] = c.box.lo[2];
             wn.hix[k] = c.box.hi[0]; wn.hiy[k] = c.box.hi[1]; wn.hiz[k] = c.box.hi[2];
-            if (c.left < 0) {
+            if (c.left < 0 || wc[kids[k]].leaf) {
                 wn.child[k] = make_leaf(c.first, c.count);
             } else {
                 const int id = int(out->nodes.size());

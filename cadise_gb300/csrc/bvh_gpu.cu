@@ -16,12 +16,12 @@
 //      merge into a new binary node; prefix sums give the new node ids and
 //      compact the cluster array, so the build is deterministic;
 //   4. bottom-up (one thread per triangle, the second arrival at a node goes
-//      on): triangle counts and the SAH cost of each node as a leaf of up to
-//      four triangles or as a split;
+//      on): triangle counts and the SAH-optimal 4-wide collapse costs of the
+//      host builder (wide_costs in bvh_build.cpp);
 //   5. top-down, one level of the 4-wide tree per launch: each wide node
-//      takes the binary children, opening the one with the largest surface
-//      area until four (the host builder's rule); leaf subtrees become leaf
-//      entries whose triangles are laid out contiguously in DFS order.
+//      takes the binary subtrees those costs assign to its four slots; leaf
+//      subtrees (at most 8 triangles) become leaf entries whose triangles are
+//      laid out contiguously in DFS order.
 // No kernel waits on another thread: every loop is bounded by the data.
 #include "bvh_build.h"
 #include "radix.cuh"
@@ -40,7 +40,6 @@ constexpr int kBlock = kRadixBlock;
 // rays visit 21.9 / 21.7 / 21.0 wide nodes with radius 16 / 32 / 64 (the
 // host SAH tree: 18.9) for 9.5 / 9.9 / 10.4 ms of build.
 constexpr int kRadius = 64;
-constexpr uint32_t kLeafMax = 4;             // triangles per leaf
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr int kMaxIterations = 1 << 16;
 
@@ -205,12 +204,21 @@ __global__ void k_ploc_merge(const float4* clo, const float4* chi, const uint32_
     }
 }
 
-// ------------------------------------------------------ bottom-up SAH leaves --
+// ------------------------------------------------- bottom-up collapse costs --
+// The SAH-optimal 4-wide collapse of bvh_build.cpp (wide_costs): per binary
+// node the least cost of its subtree filling at most 1..4 child slots
+// (cost4), how a node spends i > 1 slots (split: byte i - 1 = slots of its
+// left child, 0 = fewer slots do as well) and whether one slot is a leaf.
+constexpr float kCostNode = 1.0f;
+constexpr float kCostTri = 1.0f;
+
 __global__ void k_bottom_up(uint32_t n, uint32_t root, const uint32_t* parent, const float4* blo, const float4* bhi,
-                            uint32_t* count, float* cost, uint8_t* leaf, uint32_t* visits) {
+                            uint32_t* count, float4* cost4, uint32_t* split, uint8_t* leaf, uint32_t* visits) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float c1 = half_area(blo[i], bhi[i]) * kCostTri;
         count[i] = 1;
-        cost[i] = 1.0f;
+        cost4[i] = make_float4(c1, c1, c1, c1);
+        split[i] = 0;
         leaf[i] = 1;
         uint32_t node = i;
         // each step climbs one level: at most the tree's node count
@@ -222,13 +230,39 @@ __global__ void k_bottom_up(uint32_t n, uint32_t root, const uint32_t* parent, c
             const float4 pl = blo[p], ph = bhi[p];
             const uint32_t l = __float_as_uint(pl.w), r = __float_as_uint(ph.w);
             const uint32_t c = __ldcg(count + l) + __ldcg(count + r);
+            const float4 L4 = __ldcg(cost4 + l), R4 = __ldcg(cost4 + r);
+            const float L[4] = {L4.x, L4.y, L4.z, L4.w}, R[4] = {R4.x, R4.y, R4.z, R4.w};
             const float A = half_area(pl, ph);
-            const float split = A > 0.0f ? 1.0f + (half_area(blo[l], bhi[l]) * __ldcg(cost + l) +
-                                                   half_area(blo[r], bhi[r]) * __ldcg(cost + r)) / A
-                                         : INFINITY;
-            const bool as_leaf = c <= kLeafMax && float(c) <= split;
+            const float leaf_cost = c <= kMaxLeafTris ? A * float(c) * kCostTri : INFINITY;
+            float dist[5];
+            uint32_t arg[5];
+            for (int j = 2; j <= 4; ++j) {
+                dist[j] = INFINITY;
+                arg[j] = 1;
+                for (int k = 1; k < j; ++k) {
+                    const float v = L[k - 1] + R[j - k - 1];
+                    if (v < dist[j]) {
+                        dist[j] = v;
+                        arg[j] = uint32_t(k);
+                    }
+                }
+            }
+            const float inner = A * kCostNode + dist[4];
+            const bool as_leaf = leaf_cost <= inner;
+            float cc[4];
+            uint32_t sp = 0;
+            cc[0] = as_leaf ? leaf_cost : inner;
+            for (int j = 2; j <= 4; ++j) {
+                if (dist[j] < cc[j - 2]) {
+                    cc[j - 1] = dist[j];
+                    sp |= arg[j] << (8 * (j - 1));
+                } else {
+                    cc[j - 1] = cc[j - 2];
+                }
+            }
             count[p] = c;
-            cost[p] = as_leaf ? float(c) : split;
+            cost4[p] = make_float4(cc[0], cc[1], cc[2], cc[3]);
+            split[p] = sp;
             leaf[p] = as_leaf ? 1 : 0;
             node = p;
         }
@@ -241,33 +275,46 @@ struct Item {
 };
 
 __global__ void k_collapse_select(const Item* items, uint32_t ni, const float4* blo, const float4* bhi,
-                                  const uint8_t* leaf, uint4* kids, uint32_t* nkids, uint32_t* inner) {
+                                  const uint8_t* leaf, const float4* cost4, const uint32_t* split, uint4* kids,
+                                  uint32_t* nkids, uint32_t* inner) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
         const uint32_t b = items[i].bnode;
         uint32_t k[4] = {kNone, kNone, kNone, kNone};
-        int nk;
+        int nk = 0;
         if (leaf[b]) {
-            k[0] = b;
-            nk = 1;
+            k[nk++] = b;  // a root that is one leaf
         } else {
-            k[0] = __float_as_uint(blo[b].w);
-            k[1] = __float_as_uint(bhi[b].w);
-            nk = 2;
-            while (nk < 4) {
-                int pick = -1;
-                float area = -1.0f;
-                for (int j = 0; j < nk; ++j) {
-                    if (leaf[k[j]]) continue;
-                    const float a = half_area(blo[k[j]], bhi[k[j]]);
-                    if (a > area) {
-                        area = a;
-                        pick = j;
-                    }
+            const uint32_t l = __float_as_uint(blo[b].w), r = __float_as_uint(bhi[b].w);
+            const float4 L4 = cost4[l], R4 = cost4[r];
+            const float L[4] = {L4.x, L4.y, L4.z, L4.w}, R[4] = {R4.x, R4.y, R4.z, R4.w};
+            uint32_t best_k = 1;
+            float best = INFINITY;
+            for (uint32_t q = 1; q < 4; ++q) {
+                const float v = L[q - 1] + R[4 - q - 1];
+                if (v < best) {
+                    best = v;
+                    best_k = q;
                 }
-                if (pick < 0) break;
-                const uint32_t c = k[pick];
-                k[pick] = __float_as_uint(blo[c].w);
-                k[nk++] = __float_as_uint(bhi[c].w);
+            }
+            // (node, slots) still to place; at most four are open at once
+            uint32_t st_n[8], st_i[8];
+            int sp = 0;
+            st_n[sp] = r; st_i[sp++] = 4 - best_k;
+            st_n[sp] = l; st_i[sp++] = best_k;
+            while (sp > 0 && nk < 4) {
+                --sp;
+                const uint32_t x = st_n[sp];
+                uint32_t slots = st_i[sp];
+                const uint32_t sx = split[x];
+                while (slots > 1 && ((sx >> (8 * (slots - 1))) & 255u) == 0u) --slots;
+                if (slots == 1) {
+                    k[nk++] = x;
+                    continue;
+                }
+                const uint32_t q = (sx >> (8 * (slots - 1))) & 255u;
+                if (sp + 2 > 8) break;  // cannot happen: at most four entries are open
+                st_n[sp] = __float_as_uint(bhi[x].w); st_i[sp++] = slots - q;
+                st_n[sp] = __float_as_uint(blo[x].w); st_i[sp++] = q;
             }
         }
         uint32_t in = 0;
@@ -303,14 +350,14 @@ __global__ void k_collapse_emit(const Item* items, uint32_t ni, const uint4* kid
             const uint32_t cnt = count[c];
             if (leaf[c]) {
                 wn.child[j] = make_leaf(off, cnt);
-                // the subtree's triangles (at most kLeafMax) in DFS order
-                uint32_t stack[2 * kLeafMax], sp = 0, w = off;
+                // the subtree's triangles (at most kMaxLeafTris) in DFS order
+                uint32_t stack[2 * kMaxLeafTris], sp = 0, w = off;
                 stack[sp++] = c;
                 while (sp > 0 && w < off + cnt) {
                     const uint32_t x = stack[--sp];
                     if (x < n) {
                         order[w++] = vals[x];
-                    } else if (sp + 2 <= 2 * kLeafMax) {
+                    } else if (sp + 2 <= 2 * kMaxLeafTris) {
                         stack[sp++] = __float_as_uint(bhi[x].w);
                         stack[sp++] = __float_as_uint(blo[x].w);
                     }
@@ -381,7 +428,8 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     float4* bhi = P.get<float4>(nnodes);
     uint32_t* parent = P.get<uint32_t>(nnodes);
     uint32_t* count = P.get<uint32_t>(nnodes);
-    float* cost = P.get<float>(nnodes);
+    float4* cost4 = P.get<float4>(nnodes);
+    uint32_t* split = P.get<uint32_t>(nnodes);
     uint8_t* leaf = P.get<uint8_t>(nnodes);
     uint32_t* visits = P.get<uint32_t>(nnodes);
     Item* items[2] = {P.get<Item>(n), P.get<Item>(n)};
@@ -438,7 +486,7 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     }
     const uint32_t root = node_base - 1;  // n == 1: the single triangle
     cudaMemsetAsync(visits, 0, nnodes * sizeof(uint32_t), s);
-    k_bottom_up<<<grid_of(n), kBlock, 0, s>>>(n, root, parent, blo, bhi, count, cost, leaf, visits);
+    k_bottom_up<<<grid_of(n), kBlock, 0, s>>>(n, root, parent, blo, bhi, count, cost4, split, leaf, visits);
     if (fail_cuda("bottom-up")) return false;
     // top-down, one wide level per round
     const Item first{root, 0, 0};
@@ -447,7 +495,8 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     int depth = 0, ci = 0;
     while (ni > 0) {
         ++depth;
-        k_collapse_select<<<grid_of(ni), kBlock, 0, s>>>(items[ci], ni, blo, bhi, leaf, kids, nkids, inner);
+        k_collapse_select<<<grid_of(ni), kBlock, 0, s>>>(items[ci], ni, blo, bhi, leaf, cost4, split, kids, nkids,
+                                                         inner);
         uint32_t last_inner = 0;
         cudaMemcpyAsync(&last_inner, inner + (ni - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         exclusive_scan(inner, ni, sums, s);
