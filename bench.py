@@ -261,8 +261,8 @@ def run_gpu(args, rank, world, local):
         e2e_value = float(npix) * spp * world / statistics.mean(e2e_t)
 
     # roofline of the dominant kernel (closest-hit traversal), algorithmic bytes:
-    # 32 B per 4-wide-node child slot (128 B node) + 48 B per triangle record + 64 B ray/hit queue I/O
-    ext_bytes = 128.0 * st.node_visits + 48.0 * st.triangle_tests + 64.0 * st.closest_rays
+    # 64 B per quantized 4-wide node + 48 B per triangle record + 64 B ray/hit queue I/O
+    ext_bytes = 64.0 * st.node_visits + 48.0 * st.triangle_tests + 64.0 * st.closest_rays
     ext_ms, ext_launches = kt["extend"]
     peaks = {}
     try:

@@ -7,7 +7,7 @@
 // all three axes, leaves of up to 4 triangles (8 when the SAH cannot split),
 // in-place partition of one index array, subtrees above 32k triangles built
 // on separate host threads, then an SAH-optimal collapse (wide_costs) into
-// 128-byte 4-wide nodes.
+// 64-byte quantized 4-wide nodes.
 #include "bvh_build.h"
 
 #include <algorithm>
@@ -161,12 +161,6 @@ struct Builder {
         }
     }
 };
-
-void set_empty(Bvh4Node& n, int i) {
-    n.lox[i] = n.loy[i] = n.loz[i] = INFINITY;
-    n.hix[i] = n.hiy[i] = n.hiz[i] = -INFINITY;
-    n.child[i] = 0;
-}
 
 // SAH-optimal conversion of the binary tree into 4-wide nodes (the dynamic
 // programme of Ylitie, Karras & Laine, "Efficient Incoherent Ray Traversal on
@@ -325,26 +319,24 @@ bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, s
         } else {
             nk = wide_children(bn, wc, it.bin, kids);
         }
-        Bvh4Node wn;
-        std::memset(&wn, 0, sizeof(wn));
-        for (int k = 0; k < 4; ++k) {
-            if (k >= nk) {
-                set_empty(wn, k);
-                continue;
-            }
+        float lo[4][3] = {}, hi[4][3] = {};
+        uint32_t child[4] = {0, 0, 0, 0};
+        for (int k = 0; k < nk; ++k) {
             const BinNode& c = bn[kids[k]];
-            wn.lox[k] = c.box.lo[0]; wn.loy[k] = c.box.lo[1]; wn.loz[k] = c.box.lo[2];
-            wn.hix[k] = c.box.hi[0]; wn.hiy[k] = c.box.hi[1]; wn.hiz[k] = c.box.hi[2];
+            for (int a = 0; a < 3; ++a) {
+                lo[k][a] = c.box.lo[a];
+                hi[k][a] = c.box.hi[a];
+            }
             if (c.left < 0 || wc[kids[k]].leaf) {
-                wn.child[k] = make_leaf(c.first, c.count);
+                child[k] = make_leaf(c.first, c.count);
             } else {
                 const int id = int(out->nodes.size());
                 out->nodes.emplace_back();
                 work.push_back({kids[k], id, it.depth + 1});
-                wn.child[k] = uint32_t(id);
+                child[k] = uint32_t(id);
             }
         }
-        out->nodes[size_t(it.wide)] = wn;
+        quantize_node(lo, hi, child, nk, &out->nodes[size_t(it.wide)]);
     }
     out->wide_depth = wide_depth;
     return true;

@@ -335,21 +335,16 @@ __global__ void k_collapse_emit(const Item* items, uint32_t ni, const uint4* kid
         const uint32_t k[4] = {k4.x, k4.y, k4.z, k4.w};
         const int nk = int(nkids[i]);
         uint32_t off = it.offset, slot = slots[i];
-        Bvh4Node wn;
-        for (int j = 0; j < 4; ++j) {
-            if (j >= nk) {
-                wn.lox[j] = wn.loy[j] = wn.loz[j] = INFINITY;
-                wn.hix[j] = wn.hiy[j] = wn.hiz[j] = -INFINITY;
-                wn.child[j] = 0;
-                continue;
-            }
+        float lo[4][3] = {}, hi[4][3] = {};
+        uint32_t child[4] = {0, 0, 0, 0};
+        for (int j = 0; j < nk; ++j) {
             const uint32_t c = k[j];
             const float4 l = blo[c], h = bhi[c];
-            wn.lox[j] = l.x; wn.loy[j] = l.y; wn.loz[j] = l.z;
-            wn.hix[j] = h.x; wn.hiy[j] = h.y; wn.hiz[j] = h.z;
+            lo[j][0] = l.x; lo[j][1] = l.y; lo[j][2] = l.z;
+            hi[j][0] = h.x; hi[j][1] = h.y; hi[j][2] = h.z;
             const uint32_t cnt = count[c];
             if (leaf[c]) {
-                wn.child[j] = make_leaf(off, cnt);
+                child[j] = make_leaf(off, cnt);
                 // the subtree's triangles (at most kMaxLeafTris) in DFS order
                 uint32_t stack[2 * kMaxLeafTris], sp = 0, w = off;
                 stack[sp++] = c;
@@ -363,13 +358,14 @@ __global__ void k_collapse_emit(const Item* items, uint32_t ni, const uint4* kid
                     }
                 }
             } else {
-                wn.child[j] = wide_base + slot;
+                child[j] = wide_base + slot;
                 next[slot] = Item{c, wide_base + slot, off};
                 ++slot;
             }
             off += cnt;
         }
-        for (int j = 0; j < 4; ++j) wn.pad[j] = 0;
+        Bvh4Node wn;
+        quantize_node(lo, hi, child, nk, &wn);
         nodes[it.wide] = wn;
     }
 }

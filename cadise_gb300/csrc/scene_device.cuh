@@ -1,11 +1,11 @@
 // Device-resident scene layout (one per uploaded scene, all in HBM).
 //
-//  * Bvh4Node, 128 B, one L2 line: four child boxes stored SoA
-//    (lo/hi x, y, z) + four 32-bit child entries.  A child entry is either an
-//    inner node index (bit 31 clear) or a leaf: bit 31 set, (count - 1) in
-//    bits 28..30, first triangle slot in bits 0..27.  Empty slots hold entry
-//    0 (the root can be no node's child) with an inverted box; the traversal
-//    tests the entry, not the box.
+//  * Bvh4Node, 64 B, half an L2 line: the four child boxes quantized to 8
+//    bits per plane in the node's own frame (see quantize_node) + four 32-bit
+//    child entries.  A child entry is either an inner node index (bit 31
+//    clear) or a leaf: bit 31 set, (count - 1) in bits 28..30, first triangle
+//    slot in bits 0..27.  Empty slots hold entry 0 (the root can be no node's
+//    child); the traversal tests the entry, not the box.
 //  * TriRecord, 48 B per triangle in leaf order: the three vertices in the
 //    primitive's own vertex order (so the geometric normal is the reference's
 //    eAB x eAC) with the primitive index, the packed material / light id and
@@ -20,11 +20,72 @@
 namespace cg {
 
 struct __align__(16) Bvh4Node {
-    float lox[4], hix[4], loy[4], hiy[4], loz[4], hiz[4];
+    float ox, oy, oz;   // frame origin
+    uint32_t exps;      // bytes 0..2: biased exponents e of the x, y, z steps 2^(e - 127)
     uint32_t child[4];
-    uint32_t pad[4];
+    uint32_t lox, hix, loy, hiy;  // byte i: child i's plane in steps from the origin
+    uint32_t loz, hiz, pad0, pad1;
 };
-static_assert(sizeof(Bvh4Node) == 128, "Bvh4Node must be one 128-byte line");
+static_assert(sizeof(Bvh4Node) == 64, "Bvh4Node is 64 bytes");
+
+// Encodes up to four child boxes (nk of them) conservatively: per axis a step
+// 2^e with the union of the boxes inside 254 steps (and no finer than two
+// float spacings of its coordinates), the origin at the union's lower plane,
+// every lower plane rounded down and every upper plane rounded up to a step.
+// The slab test computes (origin - o) / d + q * 2^e / d; its rounding error
+// is a few ulps of t, inside the traversal's 1 + 2 gamma(3) slack.  FP64
+// arithmetic, so host and device encode alike.
+CG_HD void quantize_node(const float (&lo)[4][3], const float (&hi)[4][3], const uint32_t (&child)[4], int nk,
+                         Bvh4Node* out) {
+    float org[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t ebits[3] = {127u, 127u, 127u};
+    uint32_t qlo[3] = {0u, 0u, 0u}, qhi[3] = {0u, 0u, 0u};
+    for (int a = 0; a < 3 && nk > 0; ++a) {
+        double ulo = lo[0][a], uhi = hi[0][a];
+        for (int i = 1; i < nk; ++i) {
+            ulo = ulo < lo[i][a] ? ulo : double(lo[i][a]);
+            uhi = uhi > hi[i][a] ? uhi : double(hi[i][a]);
+        }
+        const double mag = fabs(ulo) > fabs(uhi) ? fabs(ulo) : fabs(uhi);
+        double want = (uhi - ulo) / 254.0;
+        if (want < mag * 0x1p-22) want = mag * 0x1p-22;
+        if (want < 0x1p-120) want = 0x1p-120;
+        int e = 0;
+        frexp(want, &e);  // 2^e > want
+        for (;; ++e) {
+            const double step = ldexp(1.0, e);
+            const float o = float(ulo);  // a float already
+            uint32_t l4 = 0, h4 = 0;
+            bool fits = true;
+            for (int i = 0; i < nk; ++i) {
+                double ql = floor((double(lo[i][a]) - double(o)) / step);
+                double qh = ceil((double(hi[i][a]) - double(o)) / step);
+                if (ql < 0.0) ql = 0.0;
+                if (qh > 255.0 || qh < ql) fits = false;
+                l4 |= uint32_t(ql) << (8 * i);
+                h4 |= uint32_t(fits ? qh : 0.0) << (8 * i);
+            }
+            if (!fits && e < 126) continue;
+            org[a] = o;
+            ebits[a] = uint32_t(e + 127);
+            qlo[a] = l4;
+            qhi[a] = h4;
+            break;
+        }
+    }
+    out->ox = org[0];
+    out->oy = org[1];
+    out->oz = org[2];
+    out->exps = ebits[0] | (ebits[1] << 8) | (ebits[2] << 16);
+    for (int i = 0; i < 4; ++i) out->child[i] = i < nk ? child[i] : 0u;
+    out->lox = qlo[0];
+    out->hix = qhi[0];
+    out->loy = qlo[1];
+    out->hiy = qhi[1];
+    out->loz = qlo[2];
+    out->hiz = qhi[2];
+    out->pad0 = out->pad1 = 0u;
+}
 
 constexpr uint32_t kLeafBit = 0x80000000u;
 CG_HD bool entry_is_leaf(uint32_t e) { return (e & kLeafBit) != 0; }

@@ -99,41 +99,47 @@ struct TraceCounters {
 
 CG_D float4 ldg4(const float4* p) { return __ldg(p); }
 
-// Loads node `idx` as the ray sees it: q[0..2] the near slab planes of x, y,
-// z (lo, or hi for a ray running towards -axis), q[3..5] the far planes,
-// q[6] the four child entries.  Picking the planes by address leaves the
-// slab test without the per-child min / max that orders each plane pair.
-CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, const RayPre& r, float4 (&q)[7]) {
+// Loads node `idx`: q[0] the frame origin and step exponents, q[1] the four
+// child entries, q[2] / q[3] the quantized planes (lo / hi x, lo / hi y,
+// lo / hi z).
+CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, const RayPre& r, float4 (&q)[4]) {
     const float4* p = reinterpret_cast<const float4*>(nodes + idx);
-    // 1 where the ray runs towards -axis (the sign bit of 1 / d)
-    const int sx = int(__float_as_uint(r.inv.x) >> 31), sy = int(__float_as_uint(r.inv.y) >> 31),
-              sz = int(__float_as_uint(r.inv.z) >> 31);
-    q[0] = __ldg(p + 0 + sx);
-    q[3] = __ldg(p + 1 - sx);
-    q[1] = __ldg(p + 2 + sy);
-    q[4] = __ldg(p + 3 - sy);
-    q[2] = __ldg(p + 4 + sz);
-    q[5] = __ldg(p + 5 - sz);
-    q[6] = __ldg(p + 6);
+    q[0] = __ldg(p + 0);
+    q[1] = __ldg(p + 1);
+    q[2] = __ldg(p + 2);
+    q[3] = __ldg(p + 3);
 }
 
 // Child box distances; tnear = +inf marks a miss.  Empty child slots hold
-// entry 0 (the root, never anyone's child) and are always a miss.
-CG_D void child_hits(const RayPre& r, const float4 (&q)[7], float tcur, float (&tn)[4]) {
-    const uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
-                            __float_as_uint(q[6].w)};
-    const float nx[4] = {q[0].x, q[0].y, q[0].z, q[0].w};
-    const float ny[4] = {q[1].x, q[1].y, q[1].z, q[1].w};
-    const float nz[4] = {q[2].x, q[2].y, q[2].z, q[2].w};
-    const float fx[4] = {q[3].x, q[3].y, q[3].z, q[3].w};
-    const float fy[4] = {q[4].x, q[4].y, q[4].z, q[4].w};
-    const float fz[4] = {q[5].x, q[5].y, q[5].z, q[5].w};
+// entry 0 (the root, never anyone's child) and are always a miss.  Per axis
+// the slab distances are a + q * b with a = (origin - o) / d and b = step / d
+// (exact: the step is a power of two), the near plane picked by the sign of d.
+CG_D void child_hits(const RayPre& r, const float4 (&q)[4], float tcur, float (&tn)[4]) {
+    const uint32_t ce[4] = {__float_as_uint(q[1].x), __float_as_uint(q[1].y), __float_as_uint(q[1].z),
+                            __float_as_uint(q[1].w)};
+    const uint32_t exps = __float_as_uint(q[0].w);
+    const float bx = __uint_as_float((exps & 255u) << 23) * r.inv.x;
+    const float by = __uint_as_float(((exps >> 8) & 255u) << 23) * r.inv.y;
+    const float bz = __uint_as_float(((exps >> 16) & 255u) << 23) * r.inv.z;
+    const float ax = (q[0].x - r.o.x) * r.inv.x;
+    const float ay = (q[0].y - r.o.y) * r.inv.y;
+    const float az = (q[0].z - r.o.z) * r.inv.z;
+    // 1 where the ray runs towards -axis: the near plane is the upper one
+    const bool sx = (__float_as_uint(r.inv.x) >> 31) != 0u, sy = (__float_as_uint(r.inv.y) >> 31) != 0u,
+               sz = (__float_as_uint(r.inv.z) >> 31) != 0u;
+    const uint32_t lox = __float_as_uint(q[2].x), hix = __float_as_uint(q[2].y);
+    const uint32_t loy = __float_as_uint(q[2].z), hiy = __float_as_uint(q[2].w);
+    const uint32_t loz = __float_as_uint(q[3].x), hiz = __float_as_uint(q[3].y);
+    const uint32_t nx = sx ? hix : lox, fx = sx ? lox : hix;
+    const uint32_t ny = sy ? hiy : loy, fy = sy ? loy : hiy;
+    const uint32_t nz = sz ? hiz : loz, fz = sz ? loz : hiz;
     const float tlim = tcur * 1.00000036f;  // 1 + 2 gamma(3)
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-        const float tnx = (nx[i] - r.o.x) * r.inv.x, tfx = (fx[i] - r.o.x) * r.inv.x;
-        const float tny = (ny[i] - r.o.y) * r.inv.y, tfy = (fy[i] - r.o.y) * r.inv.y;
-        const float tnz = (nz[i] - r.o.z) * r.inv.z, tfz = (fz[i] - r.o.z) * r.inv.z;
+        const int sh = 8 * i;
+        const float tnx = fmaf(float((nx >> sh) & 255u), bx, ax), tfx = fmaf(float((fx >> sh) & 255u), bx, ax);
+        const float tny = fmaf(float((ny >> sh) & 255u), by, ay), tfy = fmaf(float((fy >> sh) & 255u), by, ay);
+        const float tnz = fmaf(float((nz >> sh) & 255u), bz, az), tfz = fmaf(float((fz >> sh) & 255u), bz, az);
         const float tnear = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, r.tmin));
         const float tfar = fminf(fminf(tfx, tfy), fminf(tfz, tlim));
         tn[i] = (ce[i] != 0u && tnear <= tfar * 1.00000036f) ? tnear : __int_as_float(0x7f800000);
@@ -161,13 +167,13 @@ template <bool ANY, bool COUNT>
 CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcur, uint32_t (&stack_e)[kStackSize],
                          float (&stack_t)[kStackSize], int& sp, TraceCounters* cnt) {
     const float kInf = __int_as_float(0x7f800000);
-    float4 q[7];
+    float4 q[4];
     load_node(S.nodes, e, r, q);
     if (COUNT) cnt->nodes++;
     float tn[4];
     child_hits(r, q, tcur, tn);
-    uint32_t ce[4] = {__float_as_uint(q[6].x), __float_as_uint(q[6].y), __float_as_uint(q[6].z),
-                      __float_as_uint(q[6].w)};
+    uint32_t ce[4] = {__float_as_uint(q[1].x), __float_as_uint(q[1].y), __float_as_uint(q[1].z),
+                      __float_as_uint(q[1].w)};
     if (!ANY) {
         // ascending by distance (misses sort last)
 #define CG_CSWAP(i, j)                                                      \
