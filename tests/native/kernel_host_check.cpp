@@ -187,6 +187,18 @@ int khc_filter_gather(const cgpu_film_filter* f, int W, int H, uint32_t count, c
     return 0;
 }
 
+// quantize_node on nk child boxes (lo / hi: nk x 3 floats each); out: the 64-byte node.
+void khc_quantize(const float* lo, const float* hi, int nk, void* out) {
+    float l[4][3] = {}, h[4][3] = {};
+    uint32_t child[4] = {1, 2, 3, 4};
+    for (int i = 0; i < nk; ++i)
+        for (int a = 0; a < 3; ++a) {
+            l[i][a] = lo[3 * i + a];
+            h[i][a] = hi[3 * i + a];
+        }
+    cg::quantize_node(l, h, child, nk, static_cast<cg::Bvh4Node*>(out));
+}
+
 int khc_wf_layout_check(uint64_t cap, int rows) {
     cg::WfBuffers w{};
     const size_t total = cg::wf_layout(nullptr, size_t(cap), rows, &w);

@@ -48,6 +48,7 @@ def khc():
     L.khc_adjoint.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32] + [C.c_void_p] * 4
     L.khc_wf_layout_check.argtypes = [C.c_uint64, C.c_int]
     L.khc_filter_gather.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+    L.khc_quantize.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]
     L.khc_noalloc_layout_bytes.restype = C.c_uint64
     L.khc_noalloc_scratch_bytes.restype = C.c_uint64
     return L
@@ -233,3 +234,45 @@ def test_invalid_film_filter_is_rejected(khc):
         err = C.create_string_buffer(256)
         assert not khc.khc_create(C.addressof(flat.desc), err, 256)
         assert b"filter" in err.value or b"tile" in err.value, err.value
+
+
+def decode_node(raw):
+    """The 64-byte quantized node (scene_device.cuh) to FP64 child boxes."""
+    org = np.frombuffer(raw[0:12], np.float32).astype(np.float64)
+    exps = np.frombuffer(raw[12:16], np.uint8)[:3].astype(int) - 127
+    planes = np.frombuffer(raw[32:56], np.uint8).reshape(6, 4).astype(np.float64)  # lox hix loy hiy loz hiz
+    step = np.ldexp(1.0, exps)
+    lo = org[None, :] + planes[0::2].T * step[None, :]
+    hi = org[None, :] + planes[1::2].T * step[None, :]
+    child = np.frombuffer(raw[16:32], np.uint32)
+    return lo, hi, step, child
+
+
+@pytest.mark.parametrize("scale", [1e-3, 1.0, 37.5, 1e4])
+def test_quantized_nodes_are_conservative_and_tight(khc, scale):
+    """Every decoded child box contains its box and exceeds it by less than
+    one step per plane; the union spans at most 254 steps; the steps are
+    powers of two no finer than the float spacing of the coordinates.
+    Boxes far from the origin, flat boxes and identical boxes included."""
+    rng = np.random.default_rng(int(scale * 7) + 1)
+    for trial in range(300):
+        nk = int(rng.integers(1, 5))
+        centre = rng.normal(0, 50 * scale, 3) if trial % 3 else rng.normal(0, 1e4 * scale, 3)
+        lo = centre + rng.uniform(-scale, scale, (nk, 3))
+        ext = rng.uniform(0, scale, (nk, 3)) * (rng.uniform(size=(nk, 3)) > 0.1)  # some flat axes
+        hi = lo + ext
+        if trial % 17 == 0:
+            lo[:] = lo[0]
+            hi[:] = hi[0]
+        lo32, hi32 = lo.astype(np.float32), hi.astype(np.float32)
+        hi32 = np.maximum(hi32, lo32)
+        raw = np.zeros(64, np.uint8)
+        khc.khc_quantize(_p(np.ascontiguousarray(lo32)), _p(np.ascontiguousarray(hi32)), nk, _p(raw))
+        dlo, dhi, step, child = decode_node(raw.tobytes())
+        assert list(child[:nk]) == [1, 2, 3, 4][:nk] and not child[nk:].any()
+        assert np.all(dlo[:nk] <= lo32) and np.all(dhi[:nk] >= hi32)
+        assert np.all(lo32 - dlo[:nk] < step) and np.all(dhi[:nk] - hi32 < step)
+        span = (hi32.max(0) - lo32.min(0)) / step
+        assert np.all(span <= 254.0)
+        mag = np.maximum(np.abs(lo32).max(0), np.abs(hi32).max(0))
+        assert np.all(step >= mag * 2.0 ** -22 * 0.999)
