@@ -1497,6 +1497,7 @@ cgpu_status cg_adjoint_wavefront(cgpu_ctx* ctx, int scene, uint32_t spp, uint64_
         done += k;
     }
     ctx->stats.paths = uint64_t(spp) * npix;
+    collect_profile(ctx);  // the forward passes' events, with profiling on
     return CGPU_OK;
 }
 
