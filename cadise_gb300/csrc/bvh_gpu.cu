@@ -2,9 +2,10 @@
 // collapse into the 4-wide layout of scene_device.cuh.
 //
 // Replaces BvhBuilder (source/core/intersector/accelerator/bvh/bvhBuilder.cpp:18-358,
-// serial recursive SAH) for very large scenes; the host builder
-// (bvh_build.cpp) stays the default below CGPU_BVH_GPU_MIN_PRIMITIVES: its
-// binned-SAH tree costs closest-hit rays ~10 % fewer node visits.  Method: Meister & Bittner, "Parallel
+// serial recursive SAH) where set-up time matters more than trace speed: the
+// host builder's (bvh_build.cpp) binned-SAH tree traces 12-25 % faster, so
+// CGPU_BVH_BUILDER_AUTO picks this build only for scenes with many primitives
+// per path sample.  Method: Meister & Bittner, "Parallel
 // Locally-Ordered Clustering for Bounding Volume Hierarchy Construction"
 // (IEEE TVCG 2018):
 //   1. triangle boxes and the bounds of their centroids;

@@ -201,14 +201,17 @@ typedef struct cgpu_scene_info {
 } cgpu_scene_info;
 
 /* BVH builder of the following uploads (cgpu_set_bvh_builder):
- *   AUTO      the GPU build from CGPU_BVH_GPU_MIN_PRIMITIVES primitives up (where the host build takes
- *             seconds), else the host build, whose tree traces ~10 % faster (default)
+ *   AUTO      the GPU build where the host build would cost more than the slower GPU tree: from
+ *             CGPU_BVH_GPU_MIN_PRIMITIVES primitives up and more than CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE
+ *             primitives per path sample of one full render (width * height * spp); else the host
+ *             build, whose tree traces 12-25 % faster (default)
  *   HOST_SAH  binned SAH on the host threads (bvh_build.cpp)
  *   GPU_PLOC  parallel locally-ordered clustering on the GPU (bvh_gpu.cu)
  * Renders do not depend on the builder: closest hits keep, on an exact tie
  * of distance, the lower primitive index, whatever the tree. */
 enum { CGPU_BVH_BUILDER_AUTO = 0, CGPU_BVH_BUILDER_HOST_SAH = 1, CGPU_BVH_BUILDER_GPU_PLOC = 2 };
-#define CGPU_BVH_GPU_MIN_PRIMITIVES 4194304
+#define CGPU_BVH_GPU_MIN_PRIMITIVES 1048576
+#define CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE 0.01
 
 /* -------------------------------------------------------------- context -- */
 

@@ -110,9 +110,15 @@ def test_million_triangle_field_identical_and_faster_to_build(gpu_ctx):
 
 
 def test_auto_builder_picks_by_size(gpu_ctx):
+    """AUTO: the host build for small scenes and for large ones rendered with
+    many samples; the GPU build for a large scene with few samples per primitive."""
     small = gpu_ctx.upload(scenes.cornell_box(8, 8, 1, 2))
     assert gpu_ctx.info(small).bvh_builder == HOST
     gpu_ctx.release(small)
+    for (w, h, spp), want in (((1920, 1080, 64), HOST), ((64, 64, 1), GPU)):
+        sid = gpu_ctx.upload(scenes.icosphere_field(width=w, height=h, spp=spp))
+        assert gpu_ctx.info(sid).bvh_builder == want, (w, h, spp)
+        gpu_ctx.release(sid)
     with pytest.raises(CgpuError) as e:
         gpu_ctx.set_bvh_builder(9)
     assert e.value.status == 1
