@@ -117,7 +117,7 @@ class cgpu_scene_info(C.Structure):
 CGPU_BVH_BUILDER_AUTO = 0
 CGPU_BVH_BUILDER_HOST_SAH = 1
 CGPU_BVH_BUILDER_GPU_PLOC = 2
-CGPU_BVH_GPU_MIN_PRIMITIVES = 1048576
+CGPU_BVH_GPU_MIN_PRIMITIVES = 1000000
 CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE = 0.01
 
 

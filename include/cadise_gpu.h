@@ -210,7 +210,7 @@ typedef struct cgpu_scene_info {
  * Renders do not depend on the builder: closest hits keep, on an exact tie
  * of distance, the lower primitive index, whatever the tree. */
 enum { CGPU_BVH_BUILDER_AUTO = 0, CGPU_BVH_BUILDER_HOST_SAH = 1, CGPU_BVH_BUILDER_GPU_PLOC = 2 };
-#define CGPU_BVH_GPU_MIN_PRIMITIVES 1048576
+#define CGPU_BVH_GPU_MIN_PRIMITIVES 1000000
 #define CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE 0.01
 
 /* -------------------------------------------------------------- context -- */
