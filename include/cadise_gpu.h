@@ -189,7 +189,7 @@ enum { CGPU_LIGHT_CLUSTER_UNIFORM = 0, CGPU_LIGHT_CLUSTER_POWER = 1 };
 typedef struct cgpu_scene_info {
     uint32_t num_primitives;
     uint32_t num_triangles;   /* rectangles count twice */
-    uint32_t num_bvh_nodes;   /* 4-wide nodes of 128 B */
+    uint32_t num_bvh_nodes;   /* 4-wide quantized nodes of 64 B */
     uint32_t num_lights;
     uint64_t device_bytes;    /* scene + BVH bytes resident on the device */
     double build_ms;          /* whole scene build + upload time */
