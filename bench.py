@@ -39,8 +39,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
-    ap.add_argument("--bvh", default="auto", choices=["auto", "host", "gpu"],
-                    help="BVH builder of the uploads (auto: the GPU build for large scenes)")
+    ap.add_argument("--bvh", default="auto", choices=["auto", "host", "gpu", "gpu-sah"],
+                    help="BVH builder of the uploads: host SAH, GPU PLOC (gpu), GPU SAH; auto picks by size")
     ap.add_argument("--profile-spp", type=int, default=8, help="samples per pixel per --profile-case render")
     ap.add_argument("--tuning", default=None,
                     help="--profile-case: this cgpu_tuning (JSON, as the bench line prints it) instead of autotuning")
@@ -298,7 +298,7 @@ def run_gpu(args, rank, world, local):
         "config": {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": spec.width,
                    "height": spec.height, "spp": spp, "max_depth": spec.max_depth,
                    "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
-                   "bvh": {"builder": {1: "host-sah", 2: "gpu-ploc"}[info.bvh_builder], "build_ms": info.bvh_ms},
+                   "bvh": {"builder": {1: "host-sah", 2: "gpu-ploc", 3: "gpu-sah"}[info.bvh_builder], "build_ms": info.bvh_ms},
                    "schedule": "wavefront, CUDA graph per batch", "l2": "256 MB buffer written between steps",
                    "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
         "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value},
@@ -427,7 +427,7 @@ CONFIGS = {
 }
 
 
-BVH_BUILDERS = {"auto": 0, "host": 1, "gpu": 2}
+BVH_BUILDERS = {"auto": 0, "host": 1, "gpu": 2, "gpu-sah": 3}
 
 
 def run_config(args):
@@ -509,7 +509,7 @@ def run_config(args):
                        "samples_per_step": int(sum(n * c for n, c in zip(npix, mk_counts)))},
         "setup_s": {"scene_generation": gen_s, "upload_with_bvh_build": upload_s,
                     "bvh_build": sum(i.bvh_ms for i in infos) / 1e3,
-                    "bvh_builders": sorted({{1: "host-sah", 2: "gpu-ploc"}[i.bvh_builder] for i in infos})},
+                    "bvh_builders": sorted({{1: "host-sah", 2: "gpu-ploc", 3: "gpu-sah"}[i.bvh_builder] for i in infos})},
         "clocks": clk,
         "cpu_baseline": cpu,
     }

@@ -117,8 +117,10 @@ class cgpu_scene_info(C.Structure):
 CGPU_BVH_BUILDER_AUTO = 0
 CGPU_BVH_BUILDER_HOST_SAH = 1
 CGPU_BVH_BUILDER_GPU_PLOC = 2
+CGPU_BVH_BUILDER_GPU_SAH = 3
 CGPU_BVH_GPU_MIN_PRIMITIVES = 1000000
 CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE = 0.01
+CGPU_BVH_GPU_SAH_MIN_PRIMITIVES = 65536
 
 
 class cgpu_options(C.Structure):

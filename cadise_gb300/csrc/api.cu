@@ -166,15 +166,18 @@ cgpu_status cgpu_synchronize(cgpu_ctx* ctx) {
 
 cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder) {
     if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
-    if (builder != CGPU_BVH_BUILDER_AUTO && builder != CGPU_BVH_BUILDER_HOST_SAH && builder != CGPU_BVH_BUILDER_GPU_PLOC)
+    if (builder < CGPU_BVH_BUILDER_AUTO || builder > CGPU_BVH_BUILDER_GPU_SAH)
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "set_bvh_builder: unknown builder");
     ctx->bvh_builder = builder;
     return CGPU_OK;
 }
 
 namespace {
-bool gpu_bvh_builder(const float* tv, uint32_t n, Bvh4Result* out, std::string* err, void* user) {
+bool gpu_ploc_builder(const float* tv, uint32_t n, Bvh4Result* out, std::string* err, void* user) {
     return build_bvh4_gpu(tv, n, static_cast<cgpu_ctx*>(user)->stream, out, err);
+}
+bool gpu_sah_builder(const float* tv, uint32_t n, Bvh4Result* out, std::string* err, void* user) {
+    return build_bvh4_gpu_sah(tv, n, static_cast<cgpu_ctx*>(user)->stream, out, err);
 }
 }  // namespace
 
@@ -185,15 +188,22 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     const auto t0 = std::chrono::steady_clock::now();
     HostScene hs;
     std::string err;
-    // AUTO: the host build costs ~0.35 us per primitive; the GPU tree renders 12-25 % slower, which
-    // outweighs that from ~0.01 primitives per path sample of a full render down
+    // AUTO: the PLOC tree renders 12-25 % slower, which its build time (0.08 s for 20 M triangles,
+    // against 0.5 s for the SAH build on the GPU) outweighs only above ~0.01 primitives per path
+    // sample of a full render; else the SAH tree, built on the GPU from 65,536 primitives up
     const double samples = double(d->width) * double(d->height) * double(d->spp > 0 ? d->spp : 1);
-    const bool gpu_bvh = ctx->bvh_builder == CGPU_BVH_BUILDER_GPU_PLOC ||
-                         (ctx->bvh_builder == CGPU_BVH_BUILDER_AUTO && d->num_primitives >= CGPU_BVH_GPU_MIN_PRIMITIVES &&
-                          double(d->num_primitives) > CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE * samples);
-    cgpu_status st = gpu_bvh ? build_host_scene(d, &hs, &err, gpu_bvh_builder, ctx) : build_host_scene(d, &hs, &err);
+    int builder = ctx->bvh_builder;
+    if (builder == CGPU_BVH_BUILDER_AUTO)
+        builder = d->num_primitives >= CGPU_BVH_GPU_MIN_PRIMITIVES &&
+                          double(d->num_primitives) > CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE * samples
+                      ? CGPU_BVH_BUILDER_GPU_PLOC
+                  : d->num_primitives >= CGPU_BVH_GPU_SAH_MIN_PRIMITIVES ? CGPU_BVH_BUILDER_GPU_SAH
+                                                                         : CGPU_BVH_BUILDER_HOST_SAH;
+    cgpu_status st = builder == CGPU_BVH_BUILDER_GPU_PLOC  ? build_host_scene(d, &hs, &err, gpu_ploc_builder, ctx)
+                     : builder == CGPU_BVH_BUILDER_GPU_SAH ? build_host_scene(d, &hs, &err, gpu_sah_builder, ctx)
+                                                           : build_host_scene(d, &hs, &err);
     if (st != CGPU_OK) return cg_fail(ctx, st, "scene_upload: " + err);
-    hs.info.bvh_builder = gpu_bvh ? CGPU_BVH_BUILDER_GPU_PLOC : CGPU_BVH_BUILDER_HOST_SAH;
+    hs.info.bvh_builder = builder;
     if (3 * hs.wide_depth + 1 > kStackSize)
         return cg_fail(ctx, CGPU_ERR_UNSUPPORTED, "scene_upload: BVH too deep for the traversal stack");
     SceneSlot sl;

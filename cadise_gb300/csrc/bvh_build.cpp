@@ -9,6 +9,7 @@
 // on separate host threads, then an SAH-optimal collapse (wide_costs) into
 // 64-byte quantized 4-wide nodes.
 #include "bvh_build.h"
+#include "wide_collapse.cuh"
 
 #include <algorithm>
 #include <atomic>
@@ -239,101 +240,26 @@ struct Builder {
     }
 };
 
-// SAH-optimal conversion of the binary tree into 4-wide nodes (the dynamic
-// programme of Ylitie, Karras & Laine, "Efficient Incoherent Ray Traversal on
-// GPUs Through Compressed Wide BVHs", HPG 2017, for width 4): cost[i - 1] is
-// the least SAH cost of a binary subtree that may fill at most i child slots
-// of its parent - as one leaf (at most kMaxLeafTris triangles), as one inner
-// wide node, or (i > 1) split between its two children's subtrees.
-constexpr float kCostNode = 1.0f;  // one wide-node visit (four box tests)
-constexpr float kCostTri = 1.0f;   // one triangle test (at 0.3 or 0.5 the trees trace slower)
-constexpr float kInf = FLT_MAX;
-
-struct WideCost {
-    float cost[4];
-    int8_t split[4];  // i > 1: slots of the left child when distributing, 0 = use i - 1 slots
-    bool leaf;        // one slot: a leaf (else an inner wide node)
-};
-
+// SAH-optimal collapse into 4-wide nodes (wide_collapse.cuh): costs of every
+// binary node, children before parents (children have larger ids).
 void wide_costs(const BinNode* bn, int count, std::vector<WideCost>* out) {
     std::vector<WideCost>& wc = *out;
-    wc.assign(size_t(count), WideCost{});
-    // children have larger ids than their parent: one pass from the back
+    wc.resize(size_t(count));
     for (int n = count - 1; n >= 0; --n) {
         const BinNode& b = bn[size_t(n)];
-        WideCost& w = wc[size_t(n)];
-        const float A = b.box.half_area();
-        const float leaf_cost = b.count <= kMaxLeafTris ? A * float(b.count) * kCostTri : kInf;
-        if (b.left < 0) {
-            for (int i = 0; i < 4; ++i) {
-                w.cost[i] = leaf_cost;
-                w.split[i] = 0;
-            }
-            w.leaf = true;
-            continue;
-        }
-        const WideCost& L = wc[size_t(b.left)];
-        const WideCost& R = wc[size_t(b.right)];
-        float dist[5];
-        int8_t arg[5];
-        for (int j = 2; j <= 4; ++j) {
-            dist[j] = kInf;
-            arg[j] = 1;
-            for (int k = 1; k < j; ++k) {
-                const float c = L.cost[k - 1] + R.cost[j - k - 1];
-                if (c < dist[j]) {
-                    dist[j] = c;
-                    arg[j] = int8_t(k);
-                }
-            }
-        }
-        const float inner = A * kCostNode + dist[4];
-        w.leaf = leaf_cost <= inner;
-        w.cost[0] = w.leaf ? leaf_cost : inner;
-        w.split[0] = 0;
-        for (int i = 2; i <= 4; ++i) {
-            if (dist[i] < w.cost[i - 2]) {
-                w.cost[i - 1] = dist[i];
-                w.split[i - 1] = arg[i];
-            } else {
-                w.cost[i - 1] = w.cost[i - 2];
-                w.split[i - 1] = 0;
-            }
-        }
+        wc[size_t(n)] = b.left < 0 ? wide_cost_leaf(b.box.half_area(), b.count)
+                                   : wide_cost_inner(b.box.half_area(), b.count, wc[size_t(b.left)],
+                                                     wc[size_t(b.right)]);
     }
 }
 
 // The binary nodes that fill the slots of the wide node of inner node n.
 int wide_children(const BinNode* bn, const std::vector<WideCost>& wc, int n, int (&kids)[4]) {
-    int nk = 0;
-    // (node, slots) pairs still to place; at most 4 are ever open
-    int stack_n[8], stack_i[8], sp = 0;
-    const BinNode& b = bn[size_t(n)];
-    // the root of the wide node distributes its two children over 4 slots
-    int best_k = 1;
-    float best = kInf;
-    for (int k = 1; k < 4; ++k) {
-        const float c = wc[size_t(b.left)].cost[k - 1] + wc[size_t(b.right)].cost[4 - k - 1];
-        if (c < best) {
-            best = c;
-            best_k = k;
-        }
-    }
-    stack_n[sp] = b.right; stack_i[sp++] = 4 - best_k;
-    stack_n[sp] = b.left; stack_i[sp++] = best_k;
-    while (sp > 0) {
-        const int x = stack_n[--sp];
-        int i = stack_i[sp];
-        while (i > 1 && wc[size_t(x)].split[i - 1] == 0) --i;  // fewer slots do as well
-        if (i == 1) {
-            kids[nk++] = x;
-            continue;
-        }
-        const BinNode& c = bn[size_t(x)];
-        const int k = wc[size_t(x)].split[i - 1];
-        stack_n[sp] = c.right; stack_i[sp++] = i - k;
-        stack_n[sp] = c.left; stack_i[sp++] = k;
-    }
+    uint32_t k[4];
+    const int nk = wide_slots(
+        uint32_t(bn[size_t(n)].left), uint32_t(bn[size_t(n)].right), [&](uint32_t x) { return wc[x]; },
+        [&](uint32_t x) { return uint32_t(bn[x].left); }, [&](uint32_t x) { return uint32_t(bn[x].right); }, k);
+    for (int i = 0; i < nk; ++i) kids[i] = int(k[i]);
     return nk;
 }
 

@@ -25,6 +25,11 @@ bool build_bvh4(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, s
 bool build_bvh4_gpu(const float* tri_vertices, uint32_t num_tris, cudaStream_t stream, Bvh4Result* out,
                     std::string* err);
 
+// The host build's binned SAH on the GPU (bvh_sah_gpu.cu): same inputs and
+// outputs as build_bvh4_gpu.
+bool build_bvh4_gpu_sah(const float* tri_vertices, uint32_t num_tris, cudaStream_t stream, Bvh4Result* out,
+                        std::string* err);
+
 // A BVH builder the scene build can be handed instead of build_bvh4.
 using BvhBuildFn = bool (*)(const float* tri_vertices, uint32_t num_tris, Bvh4Result* out, std::string* err,
                             void* user);

@@ -26,6 +26,7 @@
 // No kernel waits on another thread: every loop is bounded by the data.
 #include "bvh_build.h"
 #include "radix.cuh"
+#include "wide_collapse.cuh"
 
 #include <cuda_runtime.h>
 
@@ -206,21 +207,14 @@ __global__ void k_ploc_merge(const float4* clo, const float4* chi, const uint32_
 }
 
 // ------------------------------------------------- bottom-up collapse costs --
-// The SAH-optimal 4-wide collapse of bvh_build.cpp (wide_costs): per binary
-// node the least cost of its subtree filling at most 1..4 child slots
-// (cost4), how a node spends i > 1 slots (split: byte i - 1 = slots of its
-// left child, 0 = fewer slots do as well) and whether one slot is a leaf.
-constexpr float kCostNode = 1.0f;
-constexpr float kCostTri = 1.0f;
-
+// The SAH-optimal 4-wide collapse costs (wide_collapse.cuh) of every binary
+// node, from the triangle leaves up: the second thread to reach a node
+// computes it from its two children.
 __global__ void k_bottom_up(uint32_t n, uint32_t root, const uint32_t* parent, const float4* blo, const float4* bhi,
-                            uint32_t* count, float4* cost4, uint32_t* split, uint8_t* leaf, uint32_t* visits) {
+                            uint32_t* count, WideCost* cost, uint32_t* visits) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float c1 = half_area(blo[i], bhi[i]) * kCostTri;
         count[i] = 1;
-        cost4[i] = make_float4(c1, c1, c1, c1);
-        split[i] = 0;
-        leaf[i] = 1;
+        cost[i] = wide_cost_leaf(half_area(blo[i], bhi[i]), 1);
         uint32_t node = i;
         // each step climbs one level: at most the tree's node count
         for (uint32_t guard = 0; node != root && guard < 2 * n; ++guard) {
@@ -231,40 +225,16 @@ __global__ void k_bottom_up(uint32_t n, uint32_t root, const uint32_t* parent, c
             const float4 pl = blo[p], ph = bhi[p];
             const uint32_t l = __float_as_uint(pl.w), r = __float_as_uint(ph.w);
             const uint32_t c = __ldcg(count + l) + __ldcg(count + r);
-            const float4 L4 = __ldcg(cost4 + l), R4 = __ldcg(cost4 + r);
-            const float L[4] = {L4.x, L4.y, L4.z, L4.w}, R[4] = {R4.x, R4.y, R4.z, R4.w};
-            const float A = half_area(pl, ph);
-            const float leaf_cost = c <= kMaxLeafTris ? A * float(c) * kCostTri : INFINITY;
-            float dist[5];
-            uint32_t arg[5];
-            for (int j = 2; j <= 4; ++j) {
-                dist[j] = INFINITY;
-                arg[j] = 1;
-                for (int k = 1; k < j; ++k) {
-                    const float v = L[k - 1] + R[j - k - 1];
-                    if (v < dist[j]) {
-                        dist[j] = v;
-                        arg[j] = uint32_t(k);
-                    }
-                }
+            WideCost L, R;
+            for (int k = 0; k < 4; ++k) {
+                L.cost[k] = __ldcg(&cost[l].cost[k]);
+                R.cost[k] = __ldcg(&cost[r].cost[k]);
             }
-            const float inner = A * kCostNode + dist[4];
-            const bool as_leaf = leaf_cost <= inner;
-            float cc[4];
-            uint32_t sp = 0;
-            cc[0] = as_leaf ? leaf_cost : inner;
-            for (int j = 2; j <= 4; ++j) {
-                if (dist[j] < cc[j - 2]) {
-                    cc[j - 1] = dist[j];
-                    sp |= arg[j] << (8 * (j - 1));
-                } else {
-                    cc[j - 1] = cc[j - 2];
-                }
-            }
+            L.split = __ldcg(&cost[l].split);
+            R.split = __ldcg(&cost[r].split);
+            L.leaf = R.leaf = 0;
             count[p] = c;
-            cost4[p] = make_float4(cc[0], cc[1], cc[2], cc[3]);
-            split[p] = sp;
-            leaf[p] = as_leaf ? 1 : 0;
+            cost[p] = wide_cost_inner(half_area(pl, ph), c, L, R);
             node = p;
         }
     }
@@ -276,50 +246,21 @@ struct Item {
 };
 
 __global__ void k_collapse_select(const Item* items, uint32_t ni, const float4* blo, const float4* bhi,
-                                  const uint8_t* leaf, const float4* cost4, const uint32_t* split, uint4* kids,
-                                  uint32_t* nkids, uint32_t* inner) {
+                                  const WideCost* cost, uint4* kids, uint32_t* nkids, uint32_t* inner) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
         const uint32_t b = items[i].bnode;
         uint32_t k[4] = {kNone, kNone, kNone, kNone};
         int nk = 0;
-        if (leaf[b]) {
+        if (cost[b].leaf) {
             k[nk++] = b;  // a root that is one leaf
         } else {
-            const uint32_t l = __float_as_uint(blo[b].w), r = __float_as_uint(bhi[b].w);
-            const float4 L4 = cost4[l], R4 = cost4[r];
-            const float L[4] = {L4.x, L4.y, L4.z, L4.w}, R[4] = {R4.x, R4.y, R4.z, R4.w};
-            uint32_t best_k = 1;
-            float best = INFINITY;
-            for (uint32_t q = 1; q < 4; ++q) {
-                const float v = L[q - 1] + R[4 - q - 1];
-                if (v < best) {
-                    best = v;
-                    best_k = q;
-                }
-            }
-            // (node, slots) still to place; at most four are open at once
-            uint32_t st_n[8], st_i[8];
-            int sp = 0;
-            st_n[sp] = r; st_i[sp++] = 4 - best_k;
-            st_n[sp] = l; st_i[sp++] = best_k;
-            while (sp > 0 && nk < 4) {
-                --sp;
-                const uint32_t x = st_n[sp];
-                uint32_t slots = st_i[sp];
-                const uint32_t sx = split[x];
-                while (slots > 1 && ((sx >> (8 * (slots - 1))) & 255u) == 0u) --slots;
-                if (slots == 1) {
-                    k[nk++] = x;
-                    continue;
-                }
-                const uint32_t q = (sx >> (8 * (slots - 1))) & 255u;
-                if (sp + 2 > 8) break;  // cannot happen: at most four entries are open
-                st_n[sp] = __float_as_uint(bhi[x].w); st_i[sp++] = slots - q;
-                st_n[sp] = __float_as_uint(blo[x].w); st_i[sp++] = q;
-            }
+            nk = wide_slots(
+                __float_as_uint(blo[b].w), __float_as_uint(bhi[b].w), [&](uint32_t x) { return cost[x]; },
+                [&](uint32_t x) { return __float_as_uint(blo[x].w); }, [&](uint32_t x) { return __float_as_uint(bhi[x].w); },
+                k);
         }
         uint32_t in = 0;
-        for (int j = 0; j < nk; ++j) in += leaf[k[j]] ? 0u : 1u;
+        for (int j = 0; j < nk; ++j) in += cost[k[j]].leaf ? 0u : 1u;
         kids[i] = make_uint4(k[0], k[1], k[2], k[3]);
         nkids[i] = uint32_t(nk);
         inner[i] = in;
@@ -328,7 +269,7 @@ __global__ void k_collapse_select(const Item* items, uint32_t ni, const float4* 
 
 __global__ void k_collapse_emit(const Item* items, uint32_t ni, const uint4* kids, const uint32_t* nkids,
                                 const uint32_t* slots, uint32_t wide_base, Item* next, Bvh4Node* nodes,
-                                const uint32_t* count, const uint8_t* leaf, const float4* blo, const float4* bhi,
+                                const uint32_t* count, const WideCost* cost, const float4* blo, const float4* bhi,
                                 const uint32_t* vals, uint32_t n, uint32_t* order) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < ni; i += gridDim.x * blockDim.x) {
         const Item it = items[i];
@@ -344,7 +285,7 @@ __global__ void k_collapse_emit(const Item* items, uint32_t ni, const uint4* kid
             lo[j][0] = l.x; lo[j][1] = l.y; lo[j][2] = l.z;
             hi[j][0] = h.x; hi[j][1] = h.y; hi[j][2] = h.z;
             const uint32_t cnt = count[c];
-            if (leaf[c]) {
+            if (cost[c].leaf) {
                 child[j] = make_leaf(off, cnt);
                 // the subtree's triangles (at most kMaxLeafTris) in DFS order
                 uint32_t stack[2 * kMaxLeafTris], sp = 0, w = off;
@@ -425,9 +366,7 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     float4* bhi = P.get<float4>(nnodes);
     uint32_t* parent = P.get<uint32_t>(nnodes);
     uint32_t* count = P.get<uint32_t>(nnodes);
-    float4* cost4 = P.get<float4>(nnodes);
-    uint32_t* split = P.get<uint32_t>(nnodes);
-    uint8_t* leaf = P.get<uint8_t>(nnodes);
+    WideCost* cost = P.get<WideCost>(nnodes);
     uint32_t* visits = P.get<uint32_t>(nnodes);
     Item* items[2] = {P.get<Item>(n), P.get<Item>(n)};
     uint4* kids = P.get<uint4>(n);
@@ -483,7 +422,7 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     }
     const uint32_t root = node_base - 1;  // n == 1: the single triangle
     cudaMemsetAsync(visits, 0, nnodes * sizeof(uint32_t), s);
-    k_bottom_up<<<grid_of(n), kBlock, 0, s>>>(n, root, parent, blo, bhi, count, cost4, split, leaf, visits);
+    k_bottom_up<<<grid_of(n), kBlock, 0, s>>>(n, root, parent, blo, bhi, count, cost, visits);
     if (fail_cuda("bottom-up")) return false;
     // top-down, one wide level per round
     const Item first{root, 0, 0};
@@ -492,15 +431,14 @@ bool build_bvh4_gpu(const float* tri_vertices, uint32_t n, cudaStream_t s, Bvh4R
     int depth = 0, ci = 0;
     while (ni > 0) {
         ++depth;
-        k_collapse_select<<<grid_of(ni), kBlock, 0, s>>>(items[ci], ni, blo, bhi, leaf, cost4, split, kids, nkids,
-                                                         inner);
+        k_collapse_select<<<grid_of(ni), kBlock, 0, s>>>(items[ci], ni, blo, bhi, cost, kids, nkids, inner);
         uint32_t last_inner = 0;
         cudaMemcpyAsync(&last_inner, inner + (ni - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         exclusive_scan(inner, ni, sums, s);
         uint32_t last_slot = 0;
         cudaMemcpyAsync(&last_slot, inner + (ni - 1), sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         k_collapse_emit<<<grid_of(ni), kBlock, 0, s>>>(items[ci], ni, kids, nkids, inner, wide_count, items[ci ^ 1],
-                                                       nodes, count, leaf, blo, bhi, vals[0], n, order);
+                                                       nodes, count, cost, blo, bhi, vals[0], n, order);
         if (cudaStreamSynchronize(s) != cudaSuccess || fail_cuda("collapse")) {
             if (err->empty()) *err = "GPU BVH build: collapse failed";
             return false;

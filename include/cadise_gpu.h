@@ -196,22 +196,25 @@ typedef struct cgpu_scene_info {
     float bounds_min[3];
     float bounds_max[3];
     double bvh_ms;            /* BVH build alone */
-    int32_t bvh_builder;      /* CGPU_BVH_BUILDER_HOST_SAH or CGPU_BVH_BUILDER_GPU_PLOC: the one used */
+    int32_t bvh_builder;      /* CGPU_BVH_BUILDER_HOST_SAH, _GPU_PLOC or _GPU_SAH: the one used */
     int32_t reserved;
 } cgpu_scene_info;
 
 /* BVH builder of the following uploads (cgpu_set_bvh_builder):
- *   AUTO      the GPU build where the host build would cost more than the slower GPU tree: from
- *             CGPU_BVH_GPU_MIN_PRIMITIVES primitives up and more than CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE
- *             primitives per path sample of one full render (width * height * spp); else the host
- *             build, whose tree traces 12-25 % faster (default)
+ *   AUTO      GPU_PLOC from CGPU_BVH_GPU_MIN_PRIMITIVES primitives up with more than
+ *             CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE primitives per path sample of one full render
+ *             (width * height * spp), where its faster build outweighs its 12-25 % slower tree; else
+ *             GPU_SAH from CGPU_BVH_GPU_SAH_MIN_PRIMITIVES primitives up; else HOST_SAH (default)
  *   HOST_SAH  binned SAH on the host threads (bvh_build.cpp)
  *   GPU_PLOC  parallel locally-ordered clustering on the GPU (bvh_gpu.cu)
+ *   GPU_SAH   the host build's binned SAH run on the GPU (bvh_sah_gpu.cu): the same tree but below
+ *             the host's unstable-partition median splits, ~10x faster on large scenes
  * Renders do not depend on the builder: closest hits keep, on an exact tie
  * of distance, the lower primitive index, whatever the tree. */
-enum { CGPU_BVH_BUILDER_AUTO = 0, CGPU_BVH_BUILDER_HOST_SAH = 1, CGPU_BVH_BUILDER_GPU_PLOC = 2 };
+enum { CGPU_BVH_BUILDER_AUTO = 0, CGPU_BVH_BUILDER_HOST_SAH = 1, CGPU_BVH_BUILDER_GPU_PLOC = 2, CGPU_BVH_BUILDER_GPU_SAH = 3 };
 #define CGPU_BVH_GPU_MIN_PRIMITIVES 1000000
 #define CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE 0.01
+#define CGPU_BVH_GPU_SAH_MIN_PRIMITIVES 65536
 
 /* -------------------------------------------------------------- context -- */
 
