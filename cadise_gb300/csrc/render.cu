@@ -115,7 +115,7 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
                        const HitD& hit, const AdjBufs* adj = nullptr) {
     if (cont) {
         if (hitp) {
-            w.hit[p] = make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v);
+            __stcs(&w.hit[p], make_float4(hit.t, __int_as_float(hit.slot), hit.u, hit.v));
             return shade_queue(S.materials[material_of_slot(S, hit.slot)].type);
         }
         if (S.env_light >= 0) {
@@ -393,8 +393,8 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
             } else {
                 i = k;
                 p = extend_entry<SORTED>(a, qc, qm, ncont, i, &cont);
-                const float3 o = f3(w.ray_o[p]);
-                const float3 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+                const float3 o = f3(__ldcs(&w.ray_o[p]));
+                const float3 d = cont ? f3(__ldcs(&w.ray_d[p])) : f3(__ldcs(&w.mis_d[p]));
                 r = ray_prep(o, d, kRayEps, kFloatMax);
                 tcur = r.tmax;
                 hslot = -1;
@@ -407,7 +407,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
         }
         if (__all_sync(__activemask(), i < 0)) break;
         if (i < 0) continue;
-        const SceneD& S = a.scenes[w.meta[p].x];
+        const SceneD& S = a.scenes[__ldcs(&w.meta[p].x)];
         for (;;) {
             while (cur != kNoEntry && !entry_is_leaf(cur)) {
                 cur = visit_node<false, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, &tc);
@@ -482,8 +482,8 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
             } else {
                 i = k;
                 p = q[i];
-                const float4 sd = w.sh_d[p];
-                r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
+                const float4 sd = __ldcs(&w.sh_d[p]);
+                r = ray_prep(f3(__ldcs(&w.ray_o[p])), f3(sd), kRayEps, sd.w);
                 tcur = r.tmax;
                 hslot = -1;
                 cur = 0;
@@ -495,7 +495,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
         }
         if (__all_sync(__activemask(), i < 0)) break;
         if (i < 0) continue;
-        const SceneD& S = a.scenes[w.meta[p].x];
+        const SceneD& S = a.scenes[__ldcs(&w.meta[p].x)];
         for (;;) {
             while (cur != kNoEntry && !entry_is_leaf(cur)) {
                 cur = visit_node<true, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, &tc);
