@@ -44,7 +44,9 @@ struct FilmD {
 //   k = 0 continuation rays to extend, 1 MIS rays to extend, 2 shadow rays,
 //   3 + kind: hits waiting for the shade kernel of that BSDF kind,
 //   8 / 9: rays handed out so far by the persistent extend / shadow kernels,
-//   10: adjoint vertices of bounce b - 1 (the wavefront adjoint's gradient kernel).
+//   10: adjoint vertices of bounce b - 1 (the wavefront adjoint's gradient kernel),
+//   11: MIS rays whose direction meets the sampled light's primitive (or that
+//       sampled the environment), left for the MIS occlusion pass.
 constexpr int kCntStride = 16;
 
 struct WfBuffers {
@@ -55,10 +57,14 @@ struct WfBuffers {
     // L: the MIS ray of the same path's last vertex adds to L in the same
     // extend pass.  A path sample is (L + Le) + Ls.
     float4* Le;
+    // MIS ray resolved against its light at the vertex: (t, record slot, u, v)
+    // of the light's hit, slot -1 for the environment.
+    float4* mis_h;
     uint4* meta;      // scene, pixel, sample, rng counter
     int* q_cont[2];
     int* q_mis[2];
     int* q_shadow[2];
+    int* q_mocc[2];   // MIS occlusion queries, ping-pong on the bounce
     int* q_mat[kNumBsdfKinds];
     int* cnt;
     int cnt_depth;    // bounces the counter array covers
@@ -76,13 +82,14 @@ inline size_t wf_layout(char* base, size_t cap, int cnt_rows, WfBuffers* w) {
         return r;
     };
     float4** f4s[] = {&w->ray_o, &w->ray_d, &w->hit, &w->thr, &w->L, &w->Le, &w->Ls,
-                      &w->mis_a, &w->mis_b, &w->mis_d, &w->sh_d, &w->sh_c};
+                      &w->mis_a, &w->mis_b, &w->mis_d, &w->mis_h, &w->sh_d, &w->sh_c};
     for (float4** f : f4s) *f = reinterpret_cast<float4*>(take(cap * sizeof(float4)));
     w->meta = reinterpret_cast<uint4*>(take(cap * sizeof(uint4)));
     for (int k = 0; k < 2; ++k) {
         w->q_cont[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
         w->q_mis[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
         w->q_shadow[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+        w->q_mocc[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
     }
     for (int k = 0; k < kNumBsdfKinds; ++k) w->q_mat[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
     w->cnt = reinterpret_cast<int*>(take(size_t(cnt_rows) * kCntStride * sizeof(int)));
@@ -98,7 +105,7 @@ inline size_t wf_layout(char* base, size_t cap, int cnt_rows, WfBuffers* w) {
 constexpr uint32_t kNoAllocMaxPaths = 1u << 18;
 constexpr int kNoAllocMaxDepth = 62;
 constexpr int kNoAllocMaxScenes = 64;
-constexpr size_t kNoAllocScratchBytes = size_t(64) << 20;
+constexpr size_t kNoAllocScratchBytes = size_t(80) << 20;
 
 struct NoAllocView {
     BatchHeader* header;

@@ -162,6 +162,82 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
     return -1;
 }
 
+// A MIS ray adds its light's term only when its closest hit is the sampled
+// light (or, for the environment, when it hits nothing).  So the shade pass
+// tests the ray against that light's own records first, as the closest-hit
+// traversal tests them (the smaller t of a rectangle's two halves; a first
+// hit must lie within the ray's tmax): a ray that misses the light adds
+// nothing whatever else it meets and is not traced.  A ray that meets it is
+// left to k_wf_mis_occl, which asks only whether a primitive comes before
+// that hit in closest-hit order - the same answer as the closest-hit pass,
+// bit for bit, with an any-hit query bounded by the light's distance.
+// Writes (t, slot, u, v) of the light's hit; slot -1 for the environment.
+CG_D bool mis_light_hit(const SceneD& S, const RayPre& r, int mlight, float4* mh) {
+    if (mlight == S.env_light) {
+        *mh = make_float4(r.tmax, __int_as_float(-1), 0.0f, 0.0f);
+        return true;
+    }
+    const LightD& L = S.lights[mlight];
+    int best = -1;
+    float bt = 0.0f, bu = 0.0f, bv = 0.0f;
+    for (int k = 0; k < 2; ++k) {
+        const int slot = L.slot[k];
+        if (slot < 0) continue;
+        const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
+        const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+        float t, u, v;
+        if (tri_test(r, f3(a), f3(b), f3(c), r.tmax * 1.00000036f, &t, &u, &v) && t <= r.tmax &&
+            (best < 0 || t < bt)) {
+            best = slot;
+            bt = t;
+            bu = u;
+            bv = v;
+        }
+    }
+    *mh = make_float4(bt, __int_as_float(best), bu, bv);
+    return best >= 0;
+}
+
+// MIS rays that meet their light (mis_light_hit): unless a primitive comes
+// before the light's hit, the MIS term of extend_finish, added to L.
+template <bool COUNT, bool SPH>
+__global__ void k_wf_mis_occl(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    const int n = w.cnt[b * kCntStride + 11];
+    const int* q = w.q_mocc[b & 1];
+    TraceCounters tc{0, 0};
+    uint32_t nany = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int p = q[i];
+        const SceneD& S = a.scenes[w.meta[p].x];
+        const RayPre r = ray_prep(f3(w.ray_o[p]), f3(w.mis_d[p]), kRayEps, kFloatMax);
+        const float4 mh = w.mis_h[p];
+        const int slot = __float_as_int(mh.y);
+        const int prim_l = slot >= 0 ? __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + slot)).w) : 0x7FFFFFFF;
+        if (COUNT) ++nany;
+        if (occluded_before<COUNT, SPH>(S, r, mh.x, prim_l, &tc)) continue;
+        const float4 mb = w.mis_b[p], ma = w.mis_a[p];
+        float3 add;
+        if (slot >= 0) {
+            HitD hit;
+            hit.t = mh.x;
+            hit.slot = slot;
+            hit.u = mh.z;
+            hit.v = mh.w;
+            const SurfaceD hs = surface_at(S, r.o, r.d, hit);
+            add = mis_resolve(S, hs, r.o, f3(mb), f3(ma), ma.w, nullptr);
+        } else {
+            add = mis_resolve_env(S, r.d, f3(mb), f3(ma), ma.w);
+        }
+        float4 L = w.L[p];
+        L.x += add.x;
+        L.y += add.y;
+        L.z += add.z;
+        w.L[p] = L;
+    }
+    count_flush<COUNT>(a.counters, TraceCounters{0, 0}, tc, 0, nany);
+}
+
 // ADJ: marks an unoccluded shadow ray in sh_c.w for the adjoint's gradient kernel.
 template <bool ADJ = false>
 CG_D void shadow_finish(const WfBuffers& w, int p, bool occluded) {
@@ -762,10 +838,18 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
             w.sh_d[p] = make_float4(pl.sdir.x, pl.sdir.y, pl.sdir.z, pl.stmax);
             w.sh_c[p] = make_float4(pl.scontrib.x, pl.scontrib.y, pl.scontrib.z, 0.0f);
         }
+        // the adjoint traces every MIS ray in its closest-hit pass; the
+        // forward pass only those that meet their light (mis_light_hit)
+        bool mocc = false;
         if (pl.mis) {
-            w.mis_d[p] = make_float4(pl.mdir.x, pl.mdir.y, pl.mdir.z, 0.0f);
-            w.mis_a[p] = make_float4(pl.mfactor.x, pl.mfactor.y, pl.mfactor.z, pl.mpdf);
-            w.mis_b[p] = make_float4(tw.x, tw.y, tw.z, __int_as_float(pl.mlight));
+            float4 mh = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            mocc = !ADJ && mis_light_hit(S, ray_prep(si.P, pl.mdir, kRayEps, kFloatMax), pl.mlight, &mh);
+            if (ADJ || mocc) {
+                w.mis_d[p] = make_float4(pl.mdir.x, pl.mdir.y, pl.mdir.z, 0.0f);
+                w.mis_a[p] = make_float4(pl.mfactor.x, pl.mfactor.y, pl.mfactor.z, pl.mpdf);
+                w.mis_b[p] = make_float4(tw.x, tw.y, tw.z, __int_as_float(pl.mlight));
+            }
+            if (mocc) w.mis_h[p] = mh;
         }
         if (cont) {
             w.ray_d[p] = make_float4(pl.cdir.x, pl.cdir.y, pl.cdir.z, 0.0f);
@@ -775,8 +859,13 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
         w.meta[p] = meta;
         const int s_slot = warp_append(next + 2, live && pl.shadow != 0);
         if (s_slot >= 0) w.q_shadow[nb][s_slot] = p;
-        const int m_slot = warp_append(next + 1, live && pl.mis != 0);
-        if (m_slot >= 0) w.q_mis[nb][m_slot] = p;
+        if (ADJ) {
+            const int m_slot = warp_append(next + 1, live && pl.mis != 0);
+            if (m_slot >= 0) w.q_mis[nb][m_slot] = p;
+        } else {
+            const int o_slot = warp_append(next + 11, mocc);
+            if (o_slot >= 0) w.q_mocc[nb][o_slot] = p;
+        }
         const int c_slot = warp_append(next + 0, cont);
         if (c_slot >= 0) w.q_cont[nb][c_slot] = p;
         if (ADJ) {
@@ -1041,6 +1130,7 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     auto ext_kernel = trav == 1 ? CG_PICK(k_wf_extend_dyn)
                       : (trav == 2 || trav == 3) ? CG_PICK(k_wf_extend_pww) : CG_PICK(k_wf_extend);
     auto sh_kernel = trav == 1 ? CG_PICK(k_wf_shadow_dyn) : trav == 3 ? CG_PICK(k_wf_shadow_pww) : CG_PICK(k_wf_shadow);
+    auto mocc_kernel = CG_PICK(k_wf_mis_occl);
 #undef CG_PICK
     // reordered closest-hit passes after the first (the primary rays are in pixel order already)
     const bool reorder = ctx->tuning.reorder != 0 && trav != 1 && ctx->sort_block != nullptr;
@@ -1056,6 +1146,7 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int gkeys = grid_for(ctx, k_ray_keys, 256, uint64_t(paths) * 2);
     const int gext = grid_for(ctx, ext_kernel, bt, paths);
     const int gsh = grid_for(ctx, sh_kernel, bt, paths);
+    const int gmo = grid_for(ctx, mocc_kernel, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
                                     grid_for(ctx, k_wf_shade<4>, bs, paths)};
@@ -1074,6 +1165,11 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
             timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, 0, s>>>(a, b); });
         }
         timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, 0, side>>>(a, b); });
+        // the MIS rays of the vertices of bounce b - 1 that meet their light
+        if (b > 0) {
+            timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { mocc_kernel<<<gmo, bt, 0, side>>>(a, b); });
+            launches += 1;
+        }
         cudaEventRecord(join, side);
         cudaStreamWaitEvent(s, join, 0);
         launches += 2;
@@ -1565,9 +1661,12 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
                                     grid_for(ctx, k_wf_shade<4>, bs, paths)};
+    auto mocc = sph ? k_wf_mis_occl<false, true> : k_wf_mis_occl<false, false>;
+    const int gmo = grid_for(ctx, mocc, bt, paths);
     for (int b = 0; b <= depth; ++b) {
         ext<<<gext, bt, 0, s>>>(a, b);
         sh<<<gsh, bt, 0, s>>>(a, b);
+        if (b > 0) mocc<<<gmo, bt, 0, s>>>(a, b);
         if (b == depth) break;
         k_wf_shade<0><<<gsd[0], bs, 0, s>>>(a, b);
         k_wf_shade<1><<<gsd[1], bs, 0, s>>>(a, b);
@@ -1576,7 +1675,7 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
         k_wf_shade<4><<<gsd[4], bs, 0, s>>>(a, b);
     }
     k_splat<<<grid_for(ctx, k_splat, 256, npix), 256, 0, s>>>(a);
-    ctx->stats.kernel_launches += uint32_t(3 + 2 * (depth + 1) + kNumBsdfKinds * depth);
+    ctx->stats.kernel_launches += uint32_t(3 + 2 * (depth + 1) + depth + kNumBsdfKinds * depth);
 }
 
 }  // namespace

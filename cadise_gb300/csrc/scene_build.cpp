@@ -329,6 +329,15 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         }
         env_marg[size_t(H)] = 1.0f;
     }
+    // each area light's primitive records, in leaf order
+    for (LightD& L : lights) L.slot[0] = L.slot[1] = -1;
+    for (uint32_t s = 0; s < ntris; ++s) {
+        const int li = light_of[tprim[bvh.order[s]]];
+        if (li < 0) continue;
+        int* sl = lights[size_t(li)].slot;
+        if (sl[0] < 0) sl[0] = int(s);
+        else if (sl[1] < 0) sl[1] = int(s);
+    }
     out->nodes = std::move(bvh.nodes);
     out->tris = std::move(recs);
     out->mats = std::move(mats);
@@ -339,6 +348,7 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         std::memset(&E, 0, sizeof(E));
         E.prim = -1;
         E.kind = 2;
+        E.slot[0] = E.slot[1] = -1;
         E.tex = env_tex;
         E.ew = d->textures[env_tex].width;
         E.eh = d->textures[env_tex].height;

@@ -148,6 +148,7 @@ struct __align__(16) MaterialD {
 struct __align__(16) LightD {
     int prim;
     int kind;        // 0 triangle, 1 rectangle, 2 environment
+    int slot[2];     // its primitive records (leaf order): the triangle, or the two rectangle halves; -1 none
     int back_face;
     float pdf_area;  // 1 / area
     float3 radiance; // color / sum(color) * watt / (area * pi)

@@ -301,6 +301,50 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
     return hslot >= 0;
 }
 
+// Whether a primitive other than `prim_l` comes before the hit (t_l, prim_l)
+// in closest-hit order - a smaller t, or the same t and a lower primitive
+// index (closer_hit) - so that the closest hit of the ray is not prim_l.
+// Each primitive is tested as visit_leaf<false> tests it while its bound is
+// t_l, which every primitive that could come first passes; the nodes are
+// culled by t_l with the closest-hit slack.  prim_l = INT_MAX, t_l = the
+// ray's tmax: whether the ray hits anything at all.
+template <bool COUNT, bool SPH = true>
+CG_D bool visit_leaf_before(const SceneD& S, const RayPre& r, uint32_t e, float t_l, int prim_l, TraceCounters* cnt) {
+    const uint32_t first = leaf_first(e), n = leaf_count(e);
+    for (uint32_t k = 0; k < n; ++k) {
+        const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
+        const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+        if (COUNT) cnt->tris++;
+        float t, u, v;
+        const bool sphere = SPH && (__float_as_uint(c.w) & 3u) == kRecSphere;
+        if (sphere ? sphere_test(r, f3(a), b.x, t_l, &t)
+                   : tri_test(r, f3(a), f3(b), f3(c), t_l * 1.00000036f, &t, &u, &v)) {
+            const int prim = __float_as_int(a.w);
+            if (prim != prim_l && (t < t_l || (t == t_l && prim < prim_l))) return true;
+        }
+    }
+    return false;
+}
+
+template <bool COUNT, bool SPH = true>
+CG_D bool occluded_before(const SceneD& S, const RayPre& r, float t_l, int prim_l, TraceCounters* cnt) {
+    uint32_t stack_e[kStackSize];
+    float stack_t[kStackSize];
+    int sp = 0;
+    uint32_t cur = 0;
+    for (;;) {
+        uint32_t next = kNoEntry;
+        if (entry_is_leaf(cur)) {
+            if (visit_leaf_before<COUNT, SPH>(S, r, cur, t_l, prim_l, cnt)) return true;
+        } else {
+            next = visit_node<true, COUNT>(S, r, cur, t_l, stack_e, stack_t, sp, cnt);
+        }
+        if (next == kNoEntry && sp > 0) next = stack_e[--sp];
+        if (next == kNoEntry) return false;
+        cur = next;
+    }
+}
+
 // Closest hit for a warp of independent rays (the wavefront's extend pass and
 // the ray queries): while-while traversal with postponed leaves (Aila &
 // Laine, "Understanding the efficiency of ray traversal on GPUs", HPG 2009).

@@ -296,7 +296,7 @@ cgpu_status cgpu_film_read(cgpu_ctx* ctx, int32_t scene, double* sum_rgb, double
 /* Allocation-free variant of cgpu_render (no counterpart in the reference):
  * the wavefront render of samples [first_sample, first_sample + num_samples)
  * of one scene into its film, with every device buffer of the call in one
- * static 64 MiB array of this library instead of memory from cudaMalloc.
+ * static 80 MiB array of this library instead of memory from cudaMalloc.
  * For callers that must not allocate or free device memory at render time
  * (cudaMalloc / cudaFree synchronise the device and may fail under memory
  * pressure): a caller with its own memory budget, or one that keeps a render

@@ -192,10 +192,10 @@ def test_wavefront_buffer_layout_fits(khc, cap):
 
 
 def test_noalloc_scratch_holds_its_layout(khc):
-    """Header, batch tables and the path state of 262144 paths fit the 64 MiB
+    """Header, batch tables and the path state of 262144 paths fit the 80 MiB
     static array of cgpu_render_noalloc."""
     need, have = khc.khc_noalloc_layout_bytes(), khc.khc_noalloc_scratch_bytes()
-    assert have == 64 << 20
+    assert have == 80 << 20
     assert 0 < need <= have, (need, have)
 
 
