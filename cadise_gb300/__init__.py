@@ -36,7 +36,7 @@ EXPORTED = [
     "cgpu_crsd_primitive_index", "cgpu_crsd_free",
 ]
 
-KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel", "reorder"]
+KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel", "reorder", "mis_occl"]
 
 _lib = None
 

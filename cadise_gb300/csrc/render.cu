@@ -1167,7 +1167,7 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
         timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, 0, side>>>(a, b); });
         // the MIS rays of the vertices of bounce b - 1 that meet their light
         if (b > 0) {
-            timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { mocc_kernel<<<gmo, bt, 0, side>>>(a, b); });
+            timed(ctx, CGPU_KERNEL_MIS_OCCL, side, [&] { mocc_kernel<<<gmo, bt, 0, side>>>(a, b); });
             launches += 1;
         }
         cudaEventRecord(join, side);

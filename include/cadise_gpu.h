@@ -403,12 +403,13 @@ cgpu_status cgpu_set_adjoint_mode(cgpu_ctx* ctx, int32_t mode);
  * kernel is timed alone). */
 enum {
     CGPU_KERNEL_GENERATE = 0,
-    CGPU_KERNEL_EXTEND = 1,     /* closest-hit traversal (continuation + MIS rays) */
+    CGPU_KERNEL_EXTEND = 1,     /* closest-hit traversal (continuation rays; MIS rays too in the adjoint) */
     CGPU_KERNEL_SHADOW = 2,     /* any-hit traversal */
     CGPU_KERNEL_SHADE = 3,      /* all shade-by-BSDF kernels */
     CGPU_KERNEL_SPLAT = 4,
     CGPU_KERNEL_MEGAKERNEL = 5,
     CGPU_KERNEL_REORDER = 6,    /* sort keys + radix sort of a closest-hit queue (tuning.reorder) */
+    CGPU_KERNEL_MIS_OCCL = 7,   /* MIS rays that meet their light: is a primitive before the light's hit */
     CGPU_KERNEL_CLASSES = 8
 };
 typedef struct cgpu_kernel_times {
