@@ -199,8 +199,9 @@ CG_D bool mis_light_hit(const SceneD& S, const RayPre& r, int mlight, float4* mh
 }
 
 // MIS rays that meet their light (mis_light_hit): unless a primitive comes
-// before the light's hit, the MIS term of extend_finish, added to L.
-template <bool COUNT, bool SPH>
+// before the light's hit, the MIS term of extend_finish, added to L (ADJ:
+// stored with its radiance derivative for the adjoint's gradient kernel).
+template <bool COUNT, bool SPH, bool ADJ = false>
 __global__ void k_wf_mis_occl(RenderArgs a, int b) {
     const WfBuffers& w = a.wf;
     const int n = w.cnt[b * kCntStride + 11];
@@ -217,7 +218,8 @@ __global__ void k_wf_mis_occl(RenderArgs a, int b) {
         if (COUNT) ++nany;
         if (occluded_before<COUNT, SPH>(S, r, mh.x, prim_l, &tc)) continue;
         const float4 mb = w.mis_b[p], ma = w.mis_a[p];
-        float3 add;
+        float3 add, X = splat3(0.0f);
+        int xlight = -1;
         if (slot >= 0) {
             HitD hit;
             hit.t = mh.x;
@@ -225,9 +227,15 @@ __global__ void k_wf_mis_occl(RenderArgs a, int b) {
             hit.u = mh.z;
             hit.v = mh.w;
             const SurfaceD hs = surface_at(S, r.o, r.d, hit);
-            add = mis_resolve(S, hs, r.o, f3(mb), f3(ma), ma.w, nullptr);
+            add = mis_resolve(S, hs, r.o, f3(mb), f3(ma), ma.w, ADJ ? &X : nullptr);
+            xlight = __float_as_int(mb.w);
         } else {
             add = mis_resolve_env(S, r.d, f3(mb), f3(ma), ma.w);
+        }
+        if (ADJ) {
+            a.adj.mis_B[p] = make_float4(add.x, add.y, add.z, 1.0f);
+            a.adj.mis_X[p] = make_float4(X.x, X.y, X.z, __int_as_float(xlight));
+            continue;
         }
         float4 L = w.L[p];
         L.x += add.x;
@@ -838,18 +846,17 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
             w.sh_d[p] = make_float4(pl.sdir.x, pl.sdir.y, pl.sdir.z, pl.stmax);
             w.sh_c[p] = make_float4(pl.scontrib.x, pl.scontrib.y, pl.scontrib.z, 0.0f);
         }
-        // the adjoint traces every MIS ray in its closest-hit pass; the
-        // forward pass only those that meet their light (mis_light_hit)
+        // only MIS rays that meet their light are traced (mis_light_hit)
         bool mocc = false;
-        if (pl.mis) {
+        if (pl.mis && live) {
             float4 mh = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            mocc = !ADJ && mis_light_hit(S, ray_prep(si.P, pl.mdir, kRayEps, kFloatMax), pl.mlight, &mh);
-            if (ADJ || mocc) {
+            mocc = mis_light_hit(S, ray_prep(si.P, pl.mdir, kRayEps, kFloatMax), pl.mlight, &mh);
+            if (mocc) {
                 w.mis_d[p] = make_float4(pl.mdir.x, pl.mdir.y, pl.mdir.z, 0.0f);
                 w.mis_a[p] = make_float4(pl.mfactor.x, pl.mfactor.y, pl.mfactor.z, pl.mpdf);
                 w.mis_b[p] = make_float4(tw.x, tw.y, tw.z, __int_as_float(pl.mlight));
+                w.mis_h[p] = mh;
             }
-            if (mocc) w.mis_h[p] = mh;
         }
         if (cont) {
             w.ray_d[p] = make_float4(pl.cdir.x, pl.cdir.y, pl.cdir.z, 0.0f);
@@ -859,13 +866,8 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
         w.meta[p] = meta;
         const int s_slot = warp_append(next + 2, live && pl.shadow != 0);
         if (s_slot >= 0) w.q_shadow[nb][s_slot] = p;
-        if (ADJ) {
-            const int m_slot = warp_append(next + 1, live && pl.mis != 0);
-            if (m_slot >= 0) w.q_mis[nb][m_slot] = p;
-        } else {
-            const int o_slot = warp_append(next + 11, mocc);
-            if (o_slot >= 0) w.q_mocc[nb][o_slot] = p;
-        }
+        const int o_slot = warp_append(next + 11, mocc);
+        if (o_slot >= 0) w.q_mocc[nb][o_slot] = p;
         const int c_slot = warp_append(next + 0, cont);
         if (c_slot >= 0) w.q_cont[nb][c_slot] = p;
         if (ADJ) {
@@ -1487,10 +1489,12 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
                          : (sph ? k_wf_extend<false, true, true> : k_wf_extend<false, false, true>);
     auto shd = trav == 3 ? (sph ? k_wf_shadow_pww<false, true, true> : k_wf_shadow_pww<false, false, true>)
                          : (sph ? k_wf_shadow<false, true, true> : k_wf_shadow<false, false, true>);
+    auto mo = sph ? k_wf_mis_occl<false, true, true> : k_wf_mis_occl<false, false, true>;
     void (*shade[kNumBsdfKinds])(RenderArgs, int) = {k_wf_shade<0, true>, k_wf_shade<1, true>, k_wf_shade<2, true>,
                                                      k_wf_shade<3, true>, k_wf_shade<4, true>};
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
     const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, shd, bt, paths);
+    const int gmo = grid_for(ctx, mo, bt, paths);
     const int gv = grid_for(ctx, k_adj_vertex, kBlock, paths, shared_bytes);
     int gsd[kNumBsdfKinds];
     for (int k = 0; k < kNumBsdfKinds; ++k) gsd[k] = grid_for(ctx, shade[k], bs, paths, shared_bytes);
@@ -1500,6 +1504,10 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
         cudaStreamWaitEvent(side, fork, 0);
         ext<<<gext, bt, 0, s>>>(a, b);
         shd<<<gsh, bt, 0, side>>>(a, b);
+        if (b > 0) {
+            mo<<<gmo, bt, 0, side>>>(a, b);
+            launches += 1;
+        }
         cudaEventRecord(join, side);
         cudaStreamWaitEvent(s, join, 0);
         launches += 2;

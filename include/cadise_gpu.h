@@ -403,7 +403,7 @@ cgpu_status cgpu_set_adjoint_mode(cgpu_ctx* ctx, int32_t mode);
  * kernel is timed alone). */
 enum {
     CGPU_KERNEL_GENERATE = 0,
-    CGPU_KERNEL_EXTEND = 1,     /* closest-hit traversal (continuation rays; MIS rays too in the adjoint) */
+    CGPU_KERNEL_EXTEND = 1,     /* closest-hit traversal of continuation rays */
     CGPU_KERNEL_SHADOW = 2,     /* any-hit traversal */
     CGPU_KERNEL_SHADE = 3,      /* all shade-by-BSDF kernels */
     CGPU_KERNEL_SPLAT = 4,
