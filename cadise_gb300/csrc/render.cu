@@ -864,7 +864,10 @@ __global__ void k_wf_shade(RenderArgs a, int b) {
         }
         meta.w = rng.ctr;
         w.meta[p] = meta;
-        const int s_slot = warp_append(next + 2, live && pl.shadow != 0);
+        // a shadow ray whose contribution is zero in every channel adds
+        // nothing to Ls whatever its outcome (the adjoint still needs it: its
+        // radiance derivative need not be zero)
+        const int s_slot = warp_append(next + 2, live && pl.shadow != 0 && (ADJ || !is_zero(pl.scontrib)));
         if (s_slot >= 0) w.q_shadow[nb][s_slot] = p;
         const int o_slot = warp_append(next + 11, mocc);
         if (o_slot >= 0) w.q_mocc[nb][o_slot] = p;
