@@ -27,6 +27,16 @@ PORT_SO = os.path.join(BUILD, "libcadise_port.so")
 REF_HARNESS = os.path.join(HERE, "_ref", "ref_harness")
 
 
+def reference_dir() -> Optional[str]:
+    """Where the reference checkout is: $CADISE_REFERENCE_DIR, else a checkout
+    named ``reference`` next to this repository.  None when neither holds the
+    reference's ``source/`` tree (the oracle's pinned restatement and the
+    golden vectors need no checkout; only the harness build does)."""
+    cand = os.environ.get("CADISE_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                   "reference")
+    return cand if os.path.isdir(os.path.join(cand, "source")) else None
+
+
 def build_port(force: bool = False) -> str:
     src = os.path.join(HERE, "port", "cadise_port.cpp")
     deps = [src, os.path.join(HERE, "oracle_rng.h"),
@@ -42,10 +52,11 @@ def build_port(force: bool = False) -> str:
     return PORT_SO
 
 
-def build_reference_harness(ref_root: str = "/root/reference", jobs: int = 8) -> Optional[str]:
+def build_reference_harness(ref_root: Optional[str] = None, jobs: int = 8) -> Optional[str]:
     """Compile the reference harness from the reference sources (only where
     they exist; returns None elsewhere)."""
-    if not os.path.isdir(os.path.join(ref_root, "source")):
+    ref_root = ref_root or reference_dir()
+    if not ref_root or not os.path.isdir(os.path.join(ref_root, "source")):
         return None
     subprocess.check_call(["make", "-s", "-C", HERE, "-j%d" % jobs, "REF=" + ref_root])
     return REF_HARNESS

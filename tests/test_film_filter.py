@@ -12,7 +12,8 @@ import oracle
 from cadise_gb300 import abi, scenes
 from golden_scenes import FILTER_CASES, GOLDEN
 
-SHIPPED = "/root/reference/scene/cornell-box.crsd"
+_REF = oracle.reference_dir()
+SHIPPED = os.path.join(_REF, "scene", "cornell-box.crsd") if _REF else None
 
 
 @pytest.fixture(scope="module")
@@ -61,7 +62,7 @@ def test_crsd_filter_defaults_are_the_reference_defaults():
     assert e.value.status == 5
 
 
-@pytest.mark.skipif(not os.path.exists(SHIPPED), reason="reference checkout not present")
+@pytest.mark.skipif(not SHIPPED or not os.path.exists(SHIPPED), reason="reference checkout not present")
 def test_shipped_reference_scene_loads():
     """The reference's own scene file (Gaussian filter, plastic, GGX conductor,
     spheres, rectangles) loads without an unsupported feature."""
