@@ -534,7 +534,7 @@ def run_profile_case(args):
     sid = ctx.upload(abi.flatten(spec))
     if args.tuning:
         t = json.loads(args.tuning)
-        ctx.set_tuning(t["block_trace"], t["block_shade"], t["max_paths"], t["traversal"], t.get("reorder", 0))
+        ctx.set_tuning_dict(t)
         tuning = ctx.tuning()
     else:
         tuning = ctx.tuning() if args.no_autotune else ctx.autotune([sid], samples=8)

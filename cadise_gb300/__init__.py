@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libcadise_gpu.so")
 # Every symbol include/cadise_gpu.h declares.
 EXPORTED = [
     "cgpu_create", "cgpu_destroy", "cgpu_last_error", "cgpu_status_string", "cgpu_abi_version",
-    "cgpu_synchronize", "cgpu_set_bvh_builder", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
+    "cgpu_synchronize", "cgpu_set_visit_budget", "cgpu_set_bvh_builder", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
     "cgpu_trace_closest", "cgpu_trace_any", "cgpu_trace_closest_device", "cgpu_trace_any_device",
     "cgpu_camera_rays", "cgpu_render", "cgpu_render_noalloc", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
@@ -72,6 +72,7 @@ def load(path: Optional[str] = None):
     L.cgpu_status_string.restype = C.c_char_p
     L.cgpu_abi_version.restype = C.c_int32
     L.cgpu_synchronize.argtypes = [vp]
+    L.cgpu_set_visit_budget.argtypes = [vp, C.c_uint32]
     L.cgpu_scene_upload.argtypes = [vp, vp, C.POINTER(C.c_int32)]
     L.cgpu_scene_release.argtypes = [vp, C.c_int32]
     L.cgpu_scene_info_get.argtypes = [vp, C.c_int32, C.POINTER(cgpu_scene_info)]
@@ -115,6 +116,12 @@ def load(path: Optional[str] = None):
 
 def _p(a: np.ndarray):
     return a.ctypes.data_as(C.c_void_p)
+
+
+def _tuning_dict(t) -> dict:
+    return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths,
+            "traversal": t.traversal, "reorder": t.reorder, "refill_closest": t.refill_closest,
+            "refill_any": t.refill_any}
 
 
 class Context:
@@ -231,9 +238,6 @@ class Context:
         if sync:
             self.synchronize()
 
-    def synchronize(self):
-        self._check(self.L.cgpu_synchronize(self.h))
-
     def film_clear(self, sid: int):
         self._check(self.L.cgpu_film_clear(self.h, sid))
 
@@ -259,6 +263,15 @@ class Context:
         out = cgpu_render_stats()
         self._check(self.L.cgpu_render_stats_get(self.h, C.byref(out)))
         return out
+
+    def synchronize(self):
+        """Wait for the context stream; raises CgpuError (CGPU_ERR_TIMEOUT) if a
+        traversal ran out of its device-side visit budget since the last check."""
+        self._check(self.L.cgpu_synchronize(self.h))
+
+    def set_visit_budget(self, visits: int):
+        """Node and leaf visits per ray before a traversal stops (0: automatic)."""
+        self._check(self.L.cgpu_set_visit_budget(self.h, visits))
 
     def set_counting(self, on: bool):
         self._check(self.L.cgpu_set_counting(self.h, 1 if on else 0))
@@ -316,22 +329,26 @@ class Context:
     def tuning(self) -> dict:
         t = abi.cgpu_tuning()
         self._check(self.L.cgpu_tuning_get(self.h, C.byref(t)))
-        return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths,
-                "traversal": t.traversal, "reorder": t.reorder}
+        return _tuning_dict(t)
 
     def set_tuning(self, block_trace: int, block_shade: int, max_paths: int = 0, traversal: int = 0,
-                   reorder: int = 0):
+                   reorder: int = 0, refill_closest: int = 0, refill_any: int = 0):
         t = abi.cgpu_tuning(block_trace=block_trace, block_shade=block_shade, max_paths=max_paths,
-                            traversal=traversal, reorder=reorder)
+                            traversal=traversal, reorder=reorder, refill_closest=refill_closest,
+                            refill_any=refill_any)
         self._check(self.L.cgpu_tuning_set(self.h, C.byref(t)))
+
+    def set_tuning_dict(self, t: dict):
+        """set_tuning from a dict as tuning() / autotune() return it."""
+        self.set_tuning(t["block_trace"], t["block_shade"], t.get("max_paths", 0), t.get("traversal", 0),
+                        t.get("reorder", 0), t.get("refill_closest", 0), t.get("refill_any", 0))
 
     def autotune(self, sids, samples: int = 1, cache_path: Optional[str] = None) -> dict:
         arr = (C.c_int32 * len(sids))(*sids)
         t = abi.cgpu_tuning()
         self._check(self.L.cgpu_autotune(self.h, arr, len(sids), samples,
                                          cache_path.encode() if cache_path else None, C.byref(t)))
-        return {"block_trace": t.block_trace, "block_shade": t.block_shade, "max_paths": t.max_paths,
-                "traversal": t.traversal, "reorder": t.reorder}
+        return _tuning_dict(t)
 
     def set_profiling(self, on: bool):
         self._check(self.L.cgpu_set_profiling(self.h, 1 if on else 0))

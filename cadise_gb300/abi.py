@@ -157,7 +157,8 @@ class cgpu_crsd_settings(C.Structure):
 
 class cgpu_tuning(C.Structure):
     _fields_ = [("block_trace", C.c_int32), ("block_shade", C.c_int32), ("max_paths", C.c_uint32),
-                ("traversal", C.c_int32), ("reorder", C.c_int32)]
+                ("traversal", C.c_int32), ("reorder", C.c_int32), ("refill_closest", C.c_int32),
+                ("refill_any", C.c_int32)]
 
 
 class cgpu_param_counts(C.Structure):

@@ -202,7 +202,7 @@ cgpu_status cgpu_adjoint_forward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, uin
     if (e != cudaSuccess) return cg_cuda(ctx, e, "adjoint_forward readback");
     for (size_t i = 0; i < npix; ++i)
         for (int k = 0; k < 3; ++k) image_out[3 * i + k] = cnt[i] > 0.0 ? float(sum[3 * i + k] / cnt[i]) : 0.0f;
-    return CGPU_OK;
+    return cg_check_status(ctx);
 }
 
 cgpu_status cgpu_set_adjoint_mode(cgpu_ctx* ctx, int32_t mode) {
@@ -307,7 +307,8 @@ cgpu_status cgpu_adjoint_backward(cgpu_ctx* ctx, int32_t scene, uint32_t spp, ui
     cudaFree(d_gr);
     cudaFree(d_gl);
     cudaFree(d_off);
-    return cg_cuda(ctx, e, "adjoint_backward");
+    const cgpu_status fin = cg_cuda(ctx, e, "adjoint_backward");
+    return fin != CGPU_OK ? fin : cg_check_status(ctx);
 }
 
 }  // extern "C"

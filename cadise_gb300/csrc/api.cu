@@ -54,6 +54,23 @@ bool valid_scene(cgpu_ctx* ctx, int32_t s) { return s >= 0 && s < int32_t(ctx->s
 
 }  // namespace
 
+cgpu_status cg_check_status(cgpu_ctx* ctx) {
+    if (!ctx->d_status) return CGPU_OK;
+    uint32_t ran_out = 0;
+    cudaError_t e = cudaMemcpyAsync(&ran_out, ctx->d_status, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cg_cuda(ctx, e, "status read");
+    if (ran_out == 0) return CGPU_OK;
+    cudaMemsetAsync(ctx->d_status, 0, sizeof(uint32_t), ctx->stream);
+    cudaStreamSynchronize(ctx->stream);
+    const std::string budget =
+        ctx->visit_budget ? std::to_string(ctx->visit_budget) + " node and leaf visits per ray"
+                          : "the automatic budget of 5 x nodes + 64 node and leaf visits per ray";
+    return cg_fail(ctx, CGPU_ERR_TIMEOUT,
+                   std::to_string(ran_out) + " ray traversal(s) ran out of the device-side iteration budget (" +
+                       budget + ") and stopped early since the last check: their results are not valid");
+}
+
 cgpu_status cg_sync_tables(cgpu_ctx* ctx) {
     if (!ctx->tables_dirty) return CGPU_OK;
     const int n = int(ctx->scenes.size());
@@ -132,7 +149,12 @@ cgpu_status cgpu_create(cgpu_ctx** out_ctx, const cgpu_options* options) {
         }
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_status, 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_status, 0, 4 * sizeof(uint32_t));
     if (e != cudaSuccess) {
+        if (ctx->d_status) cudaFree(ctx->d_status);
+        if (ctx->side) cudaStreamDestroy(ctx->side);
+        if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
         return CGPU_ERR_CUDA;
     }
@@ -150,6 +172,7 @@ void cgpu_destroy(cgpu_ctx* ctx) {
     if (ctx->d_scenes) cudaFree(ctx->d_scenes);
     if (ctx->d_films) cudaFree(ctx->d_films);
     if (ctx->d_counters) cudaFree(ctx->d_counters);
+    if (ctx->d_status) cudaFree(ctx->d_status);
     if (ctx->d_chunks) cudaFree(ctx->d_chunks);
     if (ctx->d_header) cudaFree(ctx->d_header);
     if (ctx->h_chunks) cudaFreeHost(ctx->h_chunks);
@@ -161,7 +184,18 @@ void cgpu_destroy(cgpu_ctx* ctx) {
 
 cgpu_status cgpu_synchronize(cgpu_ctx* ctx) {
     if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
-    return cg_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
+    const cgpu_status st = cg_cuda(ctx, cudaStreamSynchronize(ctx->stream), "synchronize");
+    return st != CGPU_OK ? st : cg_check_status(ctx);
+}
+
+cgpu_status cgpu_set_visit_budget(cgpu_ctx* ctx, uint32_t visits) {
+    if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(ctx->stream);
+    ctx->visit_budget = visits;
+    for (SceneSlot& sl : ctx->scenes)
+        if (sl.live) sl.d.visit_budget = visits ? visits : auto_visit_budget(sl.info.num_bvh_nodes);
+    ctx->tables_dirty = true;
+    return CGPU_OK;
 }
 
 cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder) {
@@ -280,6 +314,8 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.spp = d->spp > 0 ? d->spp : 1;
     S.cam = hs.cam;
     S.filter = hs.filter;
+    S.visit_budget = ctx->visit_budget ? ctx->visit_budget : auto_visit_budget(hs.nodes.size());
+    S.status = ctx->d_status;
     S.bounds_lo = make_float3(hs.info.bounds_min[0], hs.info.bounds_min[1], hs.info.bounds_min[2]);
     {
         float inv[3];
@@ -349,7 +385,7 @@ static cgpu_status trace_host(cgpu_ctx* ctx, int32_t scene, const cgpu_ray* rays
     }
     cudaFree(dr);
     cudaFree(dout);
-    return st;
+    return st != CGPU_OK ? st : cg_check_status(ctx);
 }
 
 cgpu_status cgpu_trace_closest(cgpu_ctx* ctx, int32_t scene, const cgpu_ray* rays, uint32_t n, cgpu_hit* hits) {
@@ -419,7 +455,8 @@ cgpu_status cgpu_film_read(cgpu_ctx* ctx, int32_t scene, double* sum_rgb, double
         e = cudaMemcpyAsync(sum_sq_rgb, sl.film.sumsq, npix * 3 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess && count) e = cudaMemcpyAsync(count, sl.film.count, npix * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-    return cg_cuda(ctx, e, "film_read");
+    const cgpu_status st = cg_cuda(ctx, e, "film_read");
+    return st != CGPU_OK ? st : cg_check_status(ctx);
 }
 
 cgpu_status cgpu_path_radiance(cgpu_ctx* ctx, int32_t scene, int32_t mode, const double* film_xy, const uint64_t* keys,
@@ -429,7 +466,8 @@ cgpu_status cgpu_path_radiance(cgpu_ctx* ctx, int32_t scene, int32_t mode, const
     if (n == 0) return CGPU_OK;
     if (!film_xy || !keys || !out_rgb) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "path_radiance: null buffer");
     cudaSetDevice(ctx->device);
-    return cg_path_radiance(ctx, scene, mode, film_xy, keys, n, out_rgb);
+    const cgpu_status st = cg_path_radiance(ctx, scene, mode, film_xy, keys, n, out_rgb);
+    return st != CGPU_OK ? st : cg_check_status(ctx);
 }
 
 cgpu_status cgpu_render_paths(cgpu_ctx* ctx, int32_t scene, int32_t mode, uint32_t first_sample, uint32_t num_samples,
@@ -440,7 +478,8 @@ cgpu_status cgpu_render_paths(cgpu_ctx* ctx, int32_t scene, int32_t mode, uint32
     if (mode != CGPU_MODE_MEGAKERNEL && mode != CGPU_MODE_WAVEFRONT)
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "render_paths: unknown mode");
     cudaSetDevice(ctx->device);
-    return cg_render_paths_raw(ctx, scene, mode, first_sample, num_samples, seed, out_rgb);
+    const cgpu_status st = cg_render_paths_raw(ctx, scene, mode, first_sample, num_samples, seed, out_rgb);
+    return st != CGPU_OK ? st : cg_check_status(ctx);
 }
 
 cgpu_status cgpu_render_stats_get(cgpu_ctx* ctx, cgpu_render_stats* out) {

@@ -16,7 +16,8 @@ namespace {
 bool valid_tuning(const cgpu_tuning& t) {
     auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
     return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal >= 0 && t.traversal <= 3) &&
-           (t.reorder >= 0 && t.reorder <= 3);
+           (t.reorder >= 0 && t.reorder <= 3) && (t.refill_closest >= 0 && t.refill_closest <= 32) &&
+           (t.refill_any >= 0 && t.refill_any <= 32);
 }
 
 void apply(cgpu_ctx* ctx, const cgpu_tuning& t) {
@@ -63,10 +64,14 @@ bool cache_lookup(const char* path, const std::string& key, cgpu_tuning* out) {
         const char* r = std::strstr(line.c_str(), "\"max_paths\":");
         const char* tv = std::strstr(line.c_str(), "\"traversal\":");
         const char* ro = std::strstr(line.c_str(), "\"reorder\":");
+        const char* rc = std::strstr(line.c_str(), "\"refill_closest\":");
+        const char* ra = std::strstr(line.c_str(), "\"refill_any\":");
         if (!p || !q || !r) continue;
-        int trav = 0, reord = 0;
+        int trav = 0, reord = 0, refc = 0, refa = 0;
         if (tv) std::sscanf(tv, "\"traversal\": %d", &trav);
         if (ro) std::sscanf(ro, "\"reorder\": %d", &reord);
+        if (rc) std::sscanf(rc, "\"refill_closest\": %d", &refc);
+        if (ra) std::sscanf(ra, "\"refill_any\": %d", &refa);
         if (std::sscanf(p, "\"block_trace\": %d", &a) != 1 || std::sscanf(q, "\"block_shade\": %d", &b) != 1 ||
             std::sscanf(r, "\"max_paths\": %u", &c) != 1)
             continue;
@@ -75,6 +80,8 @@ bool cache_lookup(const char* path, const std::string& key, cgpu_tuning* out) {
         t.max_paths = c;
         t.traversal = trav;
         t.reorder = reord;
+        t.refill_closest = refc;
+        t.refill_any = refa;
         if (valid_tuning(t)) {
             *out = t;
             found = true;  // the last matching line wins
@@ -95,7 +102,10 @@ cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out) {
 
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* t) {
     if (!ctx || !t) return CGPU_ERR_INVALID_ARGUMENT;
-    if (!valid_tuning(*t)) return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0 to 3, reorder 0 to 3");
+    if (!valid_tuning(*t))
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT,
+                       "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0 to 3, reorder 0 to 3, "
+                       "refill thresholds 0 to 32");
     cudaStreamSynchronize(ctx->stream);
     apply(ctx, *t);
     return CGPU_OK;
@@ -163,14 +173,25 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     const uint32_t caps[] = {1u << 20, 1u << 21, 1u << 22, 1u << 23, 1u << 24};
     // (ray reordering is not searched: on the 1 M-triangle field its sort costs about what it saves in
     // the closest-hit passes, so the search would pick it by noise)
-    const int options[] = {4, 3, 3, 5};
-    for (int pass = 0; pass < 4 && st == CGPU_OK; ++pass) {
+    // queue compaction of the persistent passes: refill a warp's finished
+    // lanes once fewer than this many lanes still trace
+    const int refills[] = {6, 12, 18, 24};
+    const int options[] = {4, 3, 3, 5, 4, 4};
+    for (int pass = 0; pass < 6 && st == CGPU_OK; ++pass) {
+        // the thresholds only act in the persistent while-while passes
+        if (pass == 4 && best.traversal < 2) continue;
+        if (pass == 5 && best.traversal < 3) continue;
         for (int k = 0; k < options[pass] && st == CGPU_OK; ++k) {
             cgpu_tuning t = best;
             if (pass == 0) t.traversal = k;
             if (pass == 1) t.block_trace = blocks[k];
             if (pass == 2) t.block_shade = blocks[k];
             if (pass == 3) t.max_paths = caps[k];
+            if (pass == 4) t.refill_closest = refills[k];
+            if (pass == 5) t.refill_any = refills[k];
+            if (cg::refill_lanes(t.refill_closest) == cg::refill_lanes(best.refill_closest) &&
+                cg::refill_lanes(t.refill_any) == cg::refill_lanes(best.refill_any) && pass >= 4)
+                continue;
             if (std::memcmp(&t, &best, sizeof(t)) == 0) continue;
             float ms = 0.0f;
             st = time_one(t, &ms);
@@ -192,7 +213,8 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
         std::ofstream f(cache_path, std::ios::app);
         f << "{\"key\": \"" << key << "\", \"block_trace\": " << best.block_trace << ", \"block_shade\": "
           << best.block_shade << ", \"max_paths\": " << best.max_paths << ", \"traversal\": " << best.traversal
-          << ", \"reorder\": " << best.reorder << ", \"ms\": " << best_ms << "}\n";
+          << ", \"reorder\": " << best.reorder << ", \"refill_closest\": " << best.refill_closest
+          << ", \"refill_any\": " << best.refill_any << ", \"ms\": " << best_ms << "}\n";
     }
     if (out) *out = best;
     return CGPU_OK;

@@ -34,6 +34,7 @@ inline void sincospif(float x, float* s, float* c) {
 using std::max;
 using std::min;
 inline unsigned long long atomicAdd(unsigned long long* p, unsigned long long v) { unsigned long long o = *p; *p += v; return o; }
+inline unsigned atomicAdd(unsigned* p, unsigned v) { unsigned o = *p; *p += v; return o; }
 inline double atomicAdd(double* p, double v) { double o = *p; *p += v; return o; }
 // one thread is a whole warp on the host
 inline unsigned __activemask() { return 1u; }

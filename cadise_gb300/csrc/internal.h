@@ -177,7 +177,14 @@ struct RenderArgs {
     AdjBufs adj;      // wavefront adjoint only
     // reordered closest-hit queue (tuning.reorder): path | 0x80000000 for a MIS ray
     const uint32_t* sorted;
+    // persistent traversal passes: a warp refills its finished lanes once
+    // fewer than this many of its lanes still trace (cgpu_tuning)
+    int refill_closest, refill_any;
 };
+
+// The refill thresholds of a tuning, 0 replaced by the default.
+constexpr int kDefaultRefillLanes = 12;
+inline int refill_lanes(int32_t v) { return v > 0 ? v : kDefaultRefillLanes; }
 
 // Buffers of the ray reordering: keys / values ping-pong for 2 * path_cap
 // queue entries, digit counts, scan scratch, the entry count.
@@ -218,7 +225,7 @@ struct cgpu_ctx {
     std::vector<SceneSlot> scenes;
     int num_sms = 0;
     bool counting = false;
-    cgpu_tuning tuning{128, 128, 0, 0, 0};
+    cgpu_tuning tuning{128, 128, 0, 0, 0, 0, 0};
 
     // device tables (rebuilt when the scene set changes)
     cg::SceneD* d_scenes = nullptr;
@@ -247,6 +254,10 @@ struct cgpu_ctx {
     int adjoint_schedule = CGPU_MODE_WAVEFRONT;
     int bvh_builder = CGPU_BVH_BUILDER_AUTO;
     unsigned long long* d_counters = nullptr;
+    // device status word: rays whose traversal ran out of its visit budget
+    // since the last check (cg_check_status); 0 = automatic budget per scene
+    uint32_t* d_status = nullptr;
+    uint32_t visit_budget = 0;
 
     // captured wavefront graph
     cudaGraphExec_t graph = nullptr;
@@ -282,3 +293,6 @@ void cg_free_render_state(cgpu_ctx* ctx);
 cgpu_status cg_fail(cgpu_ctx* ctx, cgpu_status s, const std::string& msg);
 cgpu_status cg_cuda(cgpu_ctx* ctx, cudaError_t e, const char* what);
 cgpu_status cg_sync_tables(cgpu_ctx* ctx);
+// After the context stream is synchronised: CGPU_ERR_TIMEOUT (and a reset
+// count) if a traversal ran out of its device-side visit budget.
+cgpu_status cg_check_status(cgpu_ctx* ctx);

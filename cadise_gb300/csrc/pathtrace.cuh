@@ -68,10 +68,53 @@ CG_D void count_flush(unsigned long long* counters, const TraceCounters& cc, con
     if (ca.tris) atomicAdd(counters + 5, (unsigned long long)ca.tris);
 }
 
+// A MIS ray adds its light's term only when its closest hit is the sampled
+// light (or, for the environment, when it hits nothing).  So the shade pass
+// tests the ray against that light's own records first, as the closest-hit
+// traversal tests them (the smaller t of a rectangle's two halves; a first
+// hit must lie within the ray's tmax): a ray that misses the light adds
+// nothing whatever else it meets and is not traced.  A ray that meets it is
+// left to k_wf_mis_occl, which asks only whether a primitive comes before
+// that hit in closest-hit order - the same answer as the closest-hit pass,
+// bit for bit, with an any-hit query bounded by the light's distance.
+// Writes (t, slot, u, v) of the light's hit; slot -1 for the environment.
+CG_D bool mis_light_hit(const SceneD& S, const RayPre& r, int mlight, float4* mh) {
+    if (mlight == S.env_light) {
+        *mh = make_float4(r.tmax, __int_as_float(-1), 0.0f, 0.0f);
+        return true;
+    }
+    const LightD& L = S.lights[mlight];
+    int best = -1;
+    float bt = 0.0f, bu = 0.0f, bv = 0.0f;
+    for (int k = 0; k < 2; ++k) {
+        const int slot = L.slot[k];
+        if (slot < 0) continue;
+        const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
+        const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+        float t, u, v;
+        // the closest-hit pass's rule between the halves (closer_hit): the
+        // smaller t, on a tie (the diagonal) the lower record slot
+        if (tri_test(r, f3(a), f3(b), f3(c), r.tmax * 1.00000036f, &t, &u, &v) && t <= r.tmax &&
+            (best < 0 || t < bt || (t == bt && slot < best))) {
+            best = slot;
+            bt = t;
+            bu = u;
+            bv = v;
+        }
+    }
+    *mh = make_float4(bt, __int_as_float(best), bu, bv);
+    return best >= 0;
+}
+
 // One whole path sample (PtEstimator::estimate): the megakernel body.
 // Three accumulators, as the wavefront keeps them: L (emission and the
 // BSDF-sampled half of NEE), Le (the sky seen by an escaping continuation
 // ray) and Ls (the light-sampled half of NEE); the sample is (L + Le) + Ls.
+// The same rays as the wavefront schedule: a shadow ray whose contribution
+// is zero in every channel is not traced, and a MIS ray is resolved against
+// its sampled light at the vertex (mis_light_hit) and, when it meets it,
+// traced as an any-hit query bounded by the light's hit (occluded_before)
+// instead of a closest-hit ray - the closest-hit answer bit for bit.
 template <bool COUNT, bool SPH = true>
 CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, float3* Leout, float3* Lsout,
                   TraceCounters* tc, TraceCounters* ta, uint32_t* nclosest, uint32_t* nany) {
@@ -88,7 +131,7 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
         const SurfaceD si = surface_at(S, o, d, hit);
         const VertexPlan pl = plan_vertex(S, si, T, ce, b, rng);
         L += pl.emit;
-        if (pl.shadow) {
+        if (pl.shadow && !is_zero(pl.scontrib)) {
             const RayPre sr = ray_prep(si.P, pl.sdir, kRayEps, pl.stmax);
             HitD sh;
             if (COUNT) ++*nany;
@@ -96,15 +139,25 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
         }
         if (pl.mis) {
             const RayPre mr = ray_prep(si.P, pl.mdir, kRayEps, kFloatMax);
-            HitD mh;
-            if (COUNT) ++*nclosest;
-            if (traverse<false, COUNT, SPH>(S, mr, &mh, tc)) {
-                if (light_of_slot(S, mh.slot) == pl.mlight) {
-                    const SurfaceD hs = surface_at(S, si.P, pl.mdir, mh);
-                    L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);
+            float4 mh;
+            if (mis_light_hit(S, mr, pl.mlight, &mh)) {
+                const int slot = __float_as_int(mh.y);
+                const int prim_l =
+                    slot >= 0 ? __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + slot)).w) : 0x7FFFFFFF;
+                if (COUNT) ++*nany;
+                if (!occluded_before<COUNT, SPH>(S, mr, mh.x, prim_l, ta)) {
+                    if (slot >= 0) {
+                        HitD hit;
+                        hit.t = mh.x;
+                        hit.slot = slot;
+                        hit.u = mh.z;
+                        hit.v = mh.w;
+                        const SurfaceD hs = surface_at(S, si.P, pl.mdir, hit);
+                        L += mis_resolve(S, hs, si.P, T, pl.mfactor, pl.mpdf);
+                    } else {
+                        L += mis_resolve_env(S, pl.mdir, T, pl.mfactor, pl.mpdf);
+                    }
                 }
-            } else if (pl.mlight == S.env_light) {
-                L += mis_resolve_env(S, pl.mdir, T, pl.mfactor, pl.mpdf);
             }
         }
         if (!pl.cont) break;

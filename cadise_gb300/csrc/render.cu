@@ -162,42 +162,6 @@ CG_D int extend_finish(const WfBuffers& w, const SceneD& S, int p, bool cont, fl
     return -1;
 }
 
-// A MIS ray adds its light's term only when its closest hit is the sampled
-// light (or, for the environment, when it hits nothing).  So the shade pass
-// tests the ray against that light's own records first, as the closest-hit
-// traversal tests them (the smaller t of a rectangle's two halves; a first
-// hit must lie within the ray's tmax): a ray that misses the light adds
-// nothing whatever else it meets and is not traced.  A ray that meets it is
-// left to k_wf_mis_occl, which asks only whether a primitive comes before
-// that hit in closest-hit order - the same answer as the closest-hit pass,
-// bit for bit, with an any-hit query bounded by the light's distance.
-// Writes (t, slot, u, v) of the light's hit; slot -1 for the environment.
-CG_D bool mis_light_hit(const SceneD& S, const RayPre& r, int mlight, float4* mh) {
-    if (mlight == S.env_light) {
-        *mh = make_float4(r.tmax, __int_as_float(-1), 0.0f, 0.0f);
-        return true;
-    }
-    const LightD& L = S.lights[mlight];
-    int best = -1;
-    float bt = 0.0f, bu = 0.0f, bv = 0.0f;
-    for (int k = 0; k < 2; ++k) {
-        const int slot = L.slot[k];
-        if (slot < 0) continue;
-        const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
-        const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
-        float t, u, v;
-        if (tri_test(r, f3(a), f3(b), f3(c), r.tmax * 1.00000036f, &t, &u, &v) && t <= r.tmax &&
-            (best < 0 || t < bt)) {
-            best = slot;
-            bt = t;
-            bu = u;
-            bv = v;
-        }
-    }
-    *mh = make_float4(bt, __int_as_float(best), bu, bv);
-    return best >= 0;
-}
-
 // MIS rays that meet their light (mis_light_hit): unless a primitive comes
 // before the light's hit, the MIS term of extend_finish, added to L (ADJ:
 // stored with its radiance derivative for the adjoint's gradient kernel).
@@ -434,11 +398,11 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
 
 // Persistent closest-hit pass: the while-while traversal of traverse_warp
 // with dynamic ray fetch (Aila & Laine 2009).  A lane keeps its ray across
-// rounds; after each round of leaves, once fewer than kRefillLanes lanes of
-// the warp still hold an unfinished ray, the finished lanes store their hits
-// and take the next rays of the queue, so lanes do not idle until the warp's
-// longest ray is done.  Same hits as the other extend kernels (closer_hit).
-constexpr int kRefillLanes = 12;
+// rounds; after each round of leaves, once fewer than a.refill_closest lanes
+// of the warp still hold an unfinished ray (the autotuned compaction
+// threshold), the finished lanes store their hits and take the next rays of
+// the queue, so lanes do not idle until the warp's longest ray is done.
+// Same hits as the other extend kernels (closer_hit).
 
 template <bool COUNT, bool SPH, bool SORTED = false, bool ADJ = false>
 __global__ void k_wf_extend_pww(RenderArgs a, int b) {
@@ -451,8 +415,9 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     int* const* qmat = w.q_mat;
     TraceCounters tc{0, 0};
     uint32_t nclosest = 0;
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
+    extern __shared__ uint32_t trav_stack_smem[];
+    SharedStack<true> stack;
+    stack.bind(trav_stack_smem);
     int sp = 0;
     RayPre r{};
     float tcur = 0.0f, hu = 0.0f, hv = 0.0f;
@@ -461,10 +426,11 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     int i = -1, p = -1;  // queue entry and path of this lane's ray (i < 0: none)
     bool cont = false;   // continuation ray (else MIS ray)
     bool drained = false;
+    uint32_t steps = 0, budget = 0;  // this ray's node and leaf visits, its scene's budget
     auto pop = [&]() -> uint32_t {
         while (sp > 0) {
             --sp;
-            if (stack_t[sp] <= tcur * 1.00000036f) return stack_e[sp];
+            if (stack.dist(sp) <= tcur * 1.00000036f) return stack.entry(sp);
         }
         return kNoEntry;
     };
@@ -486,6 +452,8 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 cur = 0;
                 leaf = kNoEntry;
                 sp = 0;
+                steps = 0;
+                budget = a.scenes[__ldcs(&w.meta[p].x)].visit_budget;
                 if (COUNT) ++nclosest;
             }
         }
@@ -494,7 +462,11 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
         const SceneD& S = a.scenes[__ldcs(&w.meta[p].x)];
         for (;;) {
             while (cur != kNoEntry && !entry_is_leaf(cur)) {
-                cur = visit_node<false, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, &tc);
+                if (over_budget(S, budget, steps)) {
+                    cur = leaf = kNoEntry;
+                    break;
+                }
+                cur = visit_node<false, COUNT>(S, r, cur, tcur, stack, sp, &tc);
                 if (cur == kNoEntry) cur = pop();
                 if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
@@ -508,6 +480,10 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 cur = pop();
             }
             while (leaf != kNoEntry) {
+                if (over_budget(S, budget, steps)) {
+                    cur = leaf = kNoEntry;
+                    break;
+                }
                 visit_leaf<false, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, &tc);
                 leaf = kNoEntry;
                 if (cur != kNoEntry && entry_is_leaf(cur)) {
@@ -516,7 +492,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 }
             }
             if (cur == kNoEntry) break;  // the ray is done
-            if (__popc(__activemask()) < kRefillLanes) break;
+            if (__popc(__activemask()) < a.refill_closest) break;
         }
         if (cur == kNoEntry && leaf == kNoEntry) {
             HitD hit;
@@ -533,8 +509,8 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
 }
 
 // Persistent any-hit pass: k_wf_extend_pww's while-while traversal with
-// dynamic ray fetch for the shadow rays; a ray ends at its first hit.
-constexpr int kRefillLanesAny = 12;
+// dynamic ray fetch for the shadow rays; a ray ends at its first hit.  The
+// refill threshold is a.refill_any.
 
 template <bool COUNT, bool SPH, bool ADJ = false>
 __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
@@ -544,8 +520,9 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
     const int* q = w.q_shadow[b & 1];
     TraceCounters tc{0, 0};
     uint32_t nany = 0;
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
+    extern __shared__ uint32_t trav_stack_smem[];
+    SharedStack<false> stack;
+    stack.bind(trav_stack_smem);
     int sp = 0;
     RayPre r{};
     float tcur = 0.0f, hu = 0.0f, hv = 0.0f;
@@ -553,8 +530,9 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
     uint32_t cur = kNoEntry, leaf = kNoEntry;
     int i = -1, p = -1;
     bool occluded = false, drained = false;
+    uint32_t steps = 0, budget = 0;  // this ray's node and leaf visits, its scene's budget
     auto pop = [&]() -> uint32_t {
-        if (sp > 0) return stack_e[--sp];
+        if (sp > 0) return stack.entry(--sp);
         return kNoEntry;
     };
     for (;;) {
@@ -574,6 +552,8 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
                 leaf = kNoEntry;
                 sp = 0;
                 occluded = false;
+                steps = 0;
+                budget = a.scenes[__ldcs(&w.meta[p].x)].visit_budget;
                 if (COUNT) ++nany;
             }
         }
@@ -582,7 +562,11 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
         const SceneD& S = a.scenes[__ldcs(&w.meta[p].x)];
         for (;;) {
             while (cur != kNoEntry && !entry_is_leaf(cur)) {
-                cur = visit_node<true, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, &tc);
+                if (over_budget(S, budget, steps)) {
+                    cur = leaf = kNoEntry;
+                    break;
+                }
+                cur = visit_node<true, COUNT>(S, r, cur, tcur, stack, sp, &tc);
                 if (cur == kNoEntry) cur = pop();
                 if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
@@ -596,6 +580,10 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
                 cur = pop();
             }
             while (leaf != kNoEntry) {
+                if (over_budget(S, budget, steps)) {
+                    cur = leaf = kNoEntry;
+                    break;
+                }
                 if (visit_leaf<true, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, &tc)) {
                     occluded = true;
                     cur = leaf = kNoEntry;
@@ -608,7 +596,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
                 }
             }
             if (cur == kNoEntry) break;  // the ray is done
-            if (__popc(__activemask()) < kRefillLanesAny) break;
+            if (__popc(__activemask()) < a.refill_any) break;
         }
         if (cur == kNoEntry && leaf == kNoEntry) {
             shadow_finish<ADJ>(w, p, occluded);
@@ -1006,6 +994,17 @@ int grid_for(cgpu_ctx* ctx, K kernel, int block, uint64_t work, size_t shared_by
     return int(std::max<uint64_t>(1, std::min<uint64_t>(full, need)));
 }
 
+// Dynamic shared memory of a traversal launch: the shared-memory part of the
+// traversal stacks of the persistent passes (0 for the other variants).  A
+// block above the default 48 KB window opts the kernel in first.
+template <typename K>
+size_t stack_smem(K kernel, bool shared_stack, bool with_t, int block) {
+    if (!shared_stack) return 0;
+    const size_t bytes = with_t ? SharedStack<true>::bytes(block) : SharedStack<false>::bytes(block);
+    if (bytes > 48 * 1024) cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+    return bytes;
+}
+
 uint32_t paths_capacity(cgpu_ctx* ctx, uint32_t max_npix) {
     uint32_t cap = ctx->tuning.max_paths ? ctx->tuning.max_paths : (1u << 21);
     if (cap < max_npix) cap = max_npix;
@@ -1081,6 +1080,8 @@ RenderArgs make_args(cgpu_ctx* ctx) {
     a.counters = ctx->d_counters;
     a.adj = AdjBufs{};
     a.sorted = nullptr;
+    a.refill_closest = refill_lanes(ctx->tuning.refill_closest);
+    a.refill_any = refill_lanes(ctx->tuning.refill_any);
     return a;
 }
 
@@ -1149,8 +1150,12 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int sort_passes = (3 + 3 * sort_bits + 7) / 8;
     if (reorder) a.sorted = ctx->sort.vals[sort_passes & 1];
     const int gkeys = grid_for(ctx, k_ray_keys, 256, uint64_t(paths) * 2);
-    const int gext = grid_for(ctx, ext_kernel, bt, paths);
-    const int gsh = grid_for(ctx, sh_kernel, bt, paths);
+    // the persistent passes keep the bottom of their traversal stacks in shared memory
+    const size_t ext_sm = stack_smem(ext_kernel, trav >= 2, true, bt);
+    const size_t ext_sorted_sm = stack_smem(ext_sorted, trav >= 2, true, bt);
+    const size_t sh_sm = stack_smem(sh_kernel, trav == 3, false, bt);
+    const int gext = grid_for(ctx, ext_kernel, bt, paths, ext_sm);
+    const int gsh = grid_for(ctx, sh_kernel, bt, paths, sh_sm);
     const int gmo = grid_for(ctx, mocc_kernel, bt, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
@@ -1165,11 +1170,11 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
                 radix_sort_pairs<uint32_t>(q.keys, q.vals, 0, q.n, q.tiles, sort_passes, q.hist, q.sums, s);
             });
             launches += 1 + sort_passes * (2 + scan_launches(q.tiles * 256));
-            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_sorted<<<gext, bt, 0, s>>>(a, b); });
+            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_sorted<<<gext, bt, ext_sorted_sm, s>>>(a, b); });
         } else {
-            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, 0, s>>>(a, b); });
+            timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, ext_sm, s>>>(a, b); });
         }
-        timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, 0, side>>>(a, b); });
+        timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, sh_sm, side>>>(a, b); });
         // the MIS rays of the vertices of bounce b - 1 that meet their light
         if (b > 0) {
             timed(ctx, CGPU_KERNEL_MIS_OCCL, side, [&] { mocc_kernel<<<gmo, bt, 0, side>>>(a, b); });
@@ -1496,7 +1501,8 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
     void (*shade[kNumBsdfKinds])(RenderArgs, int) = {k_wf_shade<0, true>, k_wf_shade<1, true>, k_wf_shade<2, true>,
                                                      k_wf_shade<3, true>, k_wf_shade<4, true>};
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
-    const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, shd, bt, paths);
+    const size_t ext_sm = stack_smem(ext, trav >= 2, true, bt), sh_sm = stack_smem(shd, trav == 3, false, bt);
+    const int gext = grid_for(ctx, ext, bt, paths, ext_sm), gsh = grid_for(ctx, shd, bt, paths, sh_sm);
     const int gmo = grid_for(ctx, mo, bt, paths);
     const int gv = grid_for(ctx, k_adj_vertex, kBlock, paths, shared_bytes);
     int gsd[kNumBsdfKinds];
@@ -1505,8 +1511,8 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
     for (int b = 0; b <= depth; ++b) {
         cudaEventRecord(fork, s);
         cudaStreamWaitEvent(side, fork, 0);
-        ext<<<gext, bt, 0, s>>>(a, b);
-        shd<<<gsh, bt, 0, side>>>(a, b);
+        ext<<<gext, bt, ext_sm, s>>>(a, b);
+        shd<<<gsh, bt, sh_sm, side>>>(a, b);
         if (b > 0) {
             mo<<<gmo, bt, 0, side>>>(a, b);
             launches += 1;
@@ -1668,15 +1674,16 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
               : trav == 3 ? (sph ? k_wf_shadow_pww<false, true> : k_wf_shadow_pww<false, false>)
                           : (sph ? k_wf_shadow<false, true> : k_wf_shadow<false, false>);
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
-    const int gext = grid_for(ctx, ext, bt, paths), gsh = grid_for(ctx, sh, bt, paths);
+    const size_t ext_sm = stack_smem(ext, trav >= 2, true, bt), sh_sm = stack_smem(sh, trav == 3, false, bt);
+    const int gext = grid_for(ctx, ext, bt, paths, ext_sm), gsh = grid_for(ctx, sh, bt, paths, sh_sm);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
                                     grid_for(ctx, k_wf_shade<4>, bs, paths)};
     auto mocc = sph ? k_wf_mis_occl<false, true> : k_wf_mis_occl<false, false>;
     const int gmo = grid_for(ctx, mocc, bt, paths);
     for (int b = 0; b <= depth; ++b) {
-        ext<<<gext, bt, 0, s>>>(a, b);
-        sh<<<gsh, bt, 0, s>>>(a, b);
+        ext<<<gext, bt, ext_sm, s>>>(a, b);
+        sh<<<gsh, bt, sh_sm, s>>>(a, b);
         if (b > 0) mocc<<<gmo, bt, 0, s>>>(a, b);
         if (b == depth) break;
         k_wf_shade<0><<<gsd[0], bs, 0, s>>>(a, b);
@@ -1728,6 +1735,8 @@ extern "C" cgpu_status cgpu_render_noalloc(cgpu_ctx* ctx, int32_t scene, uint32_
     a.films = v.films;
     a.wf = v.wf;
     a.counters = v.counters;
+    a.refill_closest = refill_lanes(ctx->tuning.refill_closest);
+    a.refill_any = refill_lanes(ctx->tuning.refill_any);
     const uint32_t n = uint32_t(npix);
     const uint32_t per = kNoAllocMaxPaths / n;  // samples per batch
     const int depth = sl.max_depth;

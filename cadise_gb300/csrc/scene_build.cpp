@@ -484,6 +484,8 @@ SceneD host_view(HostScene& hs, const cgpu_scene_desc* d) {
         }
         S.bounds_inv = make_float3(inv[0], inv[1], inv[2]);
     }
+    S.visit_budget = auto_visit_budget(hs.nodes.size());
+    S.status = nullptr;
     return S;
 }
 

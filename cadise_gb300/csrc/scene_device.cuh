@@ -210,6 +210,21 @@ struct SceneD {
     CameraD cam;
     FilterD filter;
     float3 bounds_lo, bounds_inv;  // scene bounds: lower corner, 1 / extent (0 for a flat axis)
+    // Device-side iteration budget: node and leaf visits one traversal of
+    // this scene may make before it stops (over_budget, traverse.cuh), and
+    // the context's status word that counts the rays that ran out.
+    uint32_t visit_budget;
+    uint32_t* status;
 };
+
+// The automatic visit budget of a tree of `nodes` 4-wide nodes.  A stack
+// traversal reaches every inner node and every leaf at most once (each is
+// pushed by its parent, once), and a node holds at most four leaves, so a
+// correct traversal makes fewer than 5 x nodes + 1 visits: only a corrupted
+// tree, or a budget the caller set lower, runs out.
+inline uint32_t auto_visit_budget(uint64_t nodes) {
+    const uint64_t b = 5 * nodes + 64;
+    return b > 0xFFFFFFFFull ? 0xFFFFFFFFu : uint32_t(b);
+}
 
 }  // namespace cg

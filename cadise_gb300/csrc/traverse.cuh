@@ -148,24 +148,99 @@ CG_D void child_hits(const RayPre& r, const float4 (&q)[4], float tcur, float (&
 
 constexpr uint32_t kNoEntry = 0xFFFFFFFFu;  // never a node or leaf entry (28-bit triangle range)
 
+// Device-side iteration budget of one ray: `steps` counts its node and leaf
+// visits; past `budget` (SceneD::visit_budget) the traversal stops, reports
+// the hit it holds so far (or none) and counts the ray in S.status.  The
+// host reads that count at its next synchronising call and returns
+// CGPU_ERR_TIMEOUT, so a corrupted tree ends in an error status instead of a
+// kernel that never returns.
+CG_D bool over_budget(const SceneD& S, uint32_t budget, uint32_t& steps) {
+    if (++steps <= budget) return false;
+    if (S.status) atomicAdd(S.status, 1u);
+    return true;
+}
+
 // Which of two hits a closest-hit query keeps: the smaller distance, and on
 // an exact tie (a ray through an edge shared by two triangles hits both at
 // the same t) the lower primitive index, so that the answer depends neither
 // on the order in which the traversal met them nor on the BVH (which builder,
-// which leaf order).  The two halves of a rectangle share a primitive and give
-// the same hit point, so between them either will do.  `prim` is the
-// candidate's primitive; the kept hit's is loaded only on a tie.
-CG_D bool closer_hit(const SceneD& S, float t, int prim, float tcur, int hslot) {
+// which leaf order).  The two halves of a rectangle share a primitive; on a
+// tie between them (a ray through the diagonal) the lower record slot, the
+// rule mis_light_hit applies to a light's halves too.  Either half gives the
+// same hit point (hit_point recomputes t and the edge coordinates from the
+// rectangle's own frame), so the answer does not depend on the half.
+// `prim` / `slot` are the candidate's; the kept hit's primitive is loaded
+// only on a tie.
+CG_D bool closer_hit(const SceneD& S, float t, int prim, int slot, float tcur, int hslot) {
     if (hslot < 0) return t <= tcur;
     if (t != tcur) return t < tcur;
-    return prim < __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + hslot)).w);
+    const int kept = __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + hslot)).w);
+    return prim < kept || (prim == kept && slot < hslot);
 }
+
+// Traversal stacks: kStackSize entries of (child entry, entry distance),
+// enough for any tree the upload accepts (3 x depth + 1 entries).
+// LocalStack keeps them in per-thread arrays (local memory on the GPU): the
+// megakernel, the per-ray loops and the host build of these headers.
+struct LocalStack {
+    uint32_t e[kStackSize];
+    float t[kStackSize];
+    CG_HD void push(int sp, uint32_t ee, float tt) { e[sp] = ee; t[sp] = tt; }
+    CG_HD uint32_t entry(int sp) const { return e[sp]; }
+    CG_HD float dist(int sp) const { return t[sp]; }
+};
+
+#ifdef __CUDACC__
+// The persistent traversal passes keep the bottom kSmemStack entries of each
+// lane in shared memory and only deeper ones in local memory: on the 1 M-
+// triangle field a closest-hit ray's stack reaches 4 entries at the median,
+// 10 at the 99th percentile and more than 16 for 2 rays in 100,000.  Entry k
+// of thread i sits at word k * stride + i (stride = threads per block, a
+// multiple of 32), so the lanes of a warp always hit 32 different banks,
+// whatever depth each one is at.  WITH_T = false (any-hit) keeps no
+// distances: an any-hit pass pops without the distance test.
+constexpr int kSmemStack = 16;
+
+template <bool WITH_T>
+struct SharedStack {
+    uint32_t* e;  // this thread's column of the block's entry array
+    float* t;     // ... of the distance array (WITH_T)
+    int stride;
+    uint32_t oe[kStackSize - kSmemStack];
+    float ot[WITH_T ? kStackSize - kSmemStack : 1];
+
+    // Shared memory per block for `threads` threads.
+    static constexpr size_t bytes(int threads) {
+        return size_t(threads) * kSmemStack * (WITH_T ? 8u : 4u);
+    }
+    // `base`: the block's dynamic shared memory.
+    CG_D void bind(uint32_t* base) {
+        stride = int(blockDim.x);
+        e = base + threadIdx.x;
+        t = WITH_T ? reinterpret_cast<float*>(base + size_t(kSmemStack) * blockDim.x) + threadIdx.x : nullptr;
+    }
+    CG_D void push(int sp, uint32_t ee, float tt) {
+        if (sp < kSmemStack) {
+            e[sp * stride] = ee;
+            if (WITH_T) t[sp * stride] = tt;
+        } else {
+            oe[sp - kSmemStack] = ee;
+            if (WITH_T) ot[sp - kSmemStack] = tt;
+        }
+    }
+    CG_D uint32_t entry(int sp) const { return sp < kSmemStack ? e[sp * stride] : oe[sp - kSmemStack]; }
+    CG_D float dist(int sp) const {
+        if (!WITH_T) return 0.0f;
+        return sp < kSmemStack ? t[sp * stride] : ot[sp - kSmemStack];
+    }
+};
+#endif
 
 // Visits inner node `e`: pushes the children the ray enters, farthest first,
 // except the nearest, which it returns (kNoEntry when the ray misses all four).
-template <bool ANY, bool COUNT>
-CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcur, uint32_t (&stack_e)[kStackSize],
-                         float (&stack_t)[kStackSize], int& sp, TraceCounters* cnt) {
+template <bool ANY, bool COUNT, typename Stack>
+CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcur, Stack& stack, int& sp,
+                         TraceCounters* cnt) {
     const float kInf = __int_as_float(0x7f800000);
     float4 q[4];
     load_node(S.nodes, e, r, q);
@@ -190,8 +265,7 @@ CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcu
     for (int i = 3; i >= 0; --i) {
         if (tn[i] < kInf) {
             if (nearest != kNoEntry && sp < kStackSize) {
-                stack_e[sp] = nearest;
-                stack_t[sp] = nearest_t;
+                stack.push(sp, nearest, nearest_t);
                 ++sp;
             }
             nearest = ce[i];
@@ -251,7 +325,7 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
                 tcur = t;
                 return true;
             }
-            if (closer_hit(S, t, __float_as_int(a.w), tcur, hslot)) {
+            if (closer_hit(S, t, __float_as_int(a.w), slot, tcur, hslot)) {
                 hslot = slot;
                 tcur = t;
                 hu = u;
@@ -268,14 +342,16 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
 // gain from holding leaves back).
 template <bool ANY, bool COUNT, bool SPH = true>
 CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
+    LocalStack stack;
     int sp = 0;
     float tcur = r.tmax;
     int hslot = -1;
     float hu = 0.0f, hv = 0.0f;
     uint32_t cur = 0;  // root first (always an inner node)
+    const uint32_t budget = S.visit_budget;
+    uint32_t steps = 0;
     for (;;) {
+        if (over_budget(S, budget, steps)) break;
         uint32_t next = kNoEntry;
         if (entry_is_leaf(cur)) {
             if (visit_leaf<ANY, COUNT, SPH>(S, r, cur, tcur, hslot, hu, hv, cnt)) {
@@ -284,12 +360,12 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
                 return true;
             }
         } else {
-            next = visit_node<ANY, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, cnt);
+            next = visit_node<ANY, COUNT>(S, r, cur, tcur, stack, sp, cnt);
         }
         // else the next stack entry that can still hold a closer hit
         while (next == kNoEntry && sp > 0) {
             --sp;
-            if (ANY || stack_t[sp] <= tcur * 1.00000036f) next = stack_e[sp];
+            if (ANY || stack.dist(sp) <= tcur * 1.00000036f) next = stack.entry(sp);
         }
         if (next == kNoEntry) break;
         cur = next;
@@ -328,18 +404,20 @@ CG_D bool visit_leaf_before(const SceneD& S, const RayPre& r, uint32_t e, float 
 
 template <bool COUNT, bool SPH = true>
 CG_D bool occluded_before(const SceneD& S, const RayPre& r, float t_l, int prim_l, TraceCounters* cnt) {
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
+    LocalStack stack;
     int sp = 0;
     uint32_t cur = 0;
+    const uint32_t budget = S.visit_budget;
+    uint32_t steps = 0;
     for (;;) {
+        if (over_budget(S, budget, steps)) return false;
         uint32_t next = kNoEntry;
         if (entry_is_leaf(cur)) {
             if (visit_leaf_before<COUNT, SPH>(S, r, cur, t_l, prim_l, cnt)) return true;
         } else {
-            next = visit_node<true, COUNT>(S, r, cur, t_l, stack_e, stack_t, sp, cnt);
+            next = visit_node<true, COUNT>(S, r, cur, t_l, stack, sp, cnt);
         }
-        if (next == kNoEntry && sp > 0) next = stack_e[--sp];
+        if (next == kNoEntry && sp > 0) next = stack.entry(--sp);
         if (next == kNoEntry) return false;
         cur = next;
     }
@@ -355,25 +433,30 @@ CG_D bool occluded_before(const SceneD& S, const RayPre& r, float t_l, int prim_
 // visiting order).
 template <bool COUNT, bool SPH = true>
 CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* cnt) {
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
+    LocalStack stack;
     int sp = 0;
     float tcur = r.tmax;
     int hslot = -1;
     float hu = 0.0f, hv = 0.0f;
     uint32_t cur = 0;          // root first (always an inner node)
     uint32_t leaf = kNoEntry;  // postponed leaf
+    const uint32_t budget = S.visit_budget;
+    uint32_t steps = 0;
     // next stack entry that can still hold a closer hit
     auto pop = [&]() -> uint32_t {
         while (sp > 0) {
             --sp;
-            if (stack_t[sp] <= tcur * 1.00000036f) return stack_e[sp];
+            if (stack.dist(sp) <= tcur * 1.00000036f) return stack.entry(sp);
         }
         return kNoEntry;
     };
     while (cur != kNoEntry || leaf != kNoEntry) {
         while (cur != kNoEntry && !entry_is_leaf(cur)) {
-            cur = visit_node<false, COUNT>(S, r, cur, tcur, stack_e, stack_t, sp, cnt);
+            if (over_budget(S, budget, steps)) {
+                cur = leaf = kNoEntry;
+                break;
+            }
+            cur = visit_node<false, COUNT>(S, r, cur, tcur, stack, sp, cnt);
             if (cur == kNoEntry) cur = pop();
             if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
                 leaf = cur;
@@ -387,6 +470,10 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
             cur = pop();
         }
         while (leaf != kNoEntry) {
+            if (over_budget(S, budget, steps)) {
+                cur = leaf = kNoEntry;
+                break;
+            }
             visit_leaf<false, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, cnt);
             leaf = kNoEntry;
             if (cur != kNoEntry && entry_is_leaf(cur)) {
@@ -409,17 +496,18 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
 // node visit or one leaf test and finds the same hit as traverse() (the
 // closest-hit rule does not depend on the visiting order).
 struct TravState {
-    uint32_t stack_e[kStackSize];
-    float stack_t[kStackSize];
+    LocalStack stack;
     int sp;
     uint32_t cur;
     float tcur;
     int hslot;
     float hu, hv;
     bool done;
+    uint32_t steps;  // node and leaf visits so far (over_budget)
 };
 
 CG_D void trav_begin(TravState& st, const RayPre& r) {
+    st.steps = 0;
     st.sp = 0;
     st.cur = 0;
     st.tcur = r.tmax;
@@ -430,13 +518,17 @@ CG_D void trav_begin(TravState& st, const RayPre& r) {
 
 template <bool ANY, bool COUNT, bool SPH = true>
 CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounters* cnt) {
+    if (over_budget(S, S.visit_budget, st.steps)) {
+        st.done = true;
+        return;
+    }
     if (entry_is_leaf(st.cur)) {
         if (visit_leaf<ANY, COUNT, SPH>(S, r, st.cur, st.tcur, st.hslot, st.hu, st.hv, cnt)) {
             st.done = true;
             return;
         }
     } else {
-        const uint32_t next = visit_node<ANY, COUNT>(S, r, st.cur, st.tcur, st.stack_e, st.stack_t, st.sp, cnt);
+        const uint32_t next = visit_node<ANY, COUNT>(S, r, st.cur, st.tcur, st.stack, st.sp, cnt);
         if (next != kNoEntry) {
             st.cur = next;
             return;
@@ -444,8 +536,8 @@ CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounte
     }
     while (st.sp > 0) {
         --st.sp;
-        if (ANY || st.stack_t[st.sp] <= st.tcur * 1.00000036f) {
-            st.cur = st.stack_e[st.sp];
+        if (ANY || st.stack.dist(st.sp) <= st.tcur * 1.00000036f) {
+            st.cur = st.stack.entry(st.sp);
             return;
         }
     }

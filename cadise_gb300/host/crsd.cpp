@@ -173,9 +173,10 @@ bool read_pfm(const std::string& path, int* w, int* h, std::vector<float>* rgb) 
     std::vector<float> raw(size_t(*w) * *h * 3);
     f.read(reinterpret_cast<char*>(raw.data()), std::streamsize(raw.size() * 4));
     if (!f) return false;
-    rgb->resize(raw.size());
-    for (int y = 0; y < *h; ++y)  // flip to row 0 = top
-        std::memcpy(&(*rgb)[size_t(y) * *w * 3], &raw[size_t(*h - 1 - y) * *w * 3], size_t(*w) * 12);
+    // rows in file order: a PFM stores the picture's bottom row first, and
+    // row 0 is v = 0, the bottom row, as the reference lays pictures out
+    // (file-io/pictureLoader.cpp flips them vertically on load)
+    *rgb = std::move(raw);
     return true;
 }
 

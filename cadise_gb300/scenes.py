@@ -105,9 +105,19 @@ class AreaLight:
 
 @dataclass
 class ImageTexture:
-    """RGB float texture, nearest lookup with repeat wrap."""
+    """RGB float texture, nearest lookup with repeat wrap.  Row 0 of
+    `texels` is v = 0, the picture's bottom row (the reference lays every
+    picture out that way: its loader flips images vertically)."""
     name: str
     texels: np.ndarray  # (h, w, 3) float32
+
+    def write_pfm(self, path: str) -> None:
+        """Portable float map: rows in file order from the bottom row up,
+        which is the order of `texels`."""
+        h, w, _ = self.texels.shape
+        with open(path, "wb") as f:
+            f.write(b"PF\n%d %d\n-1.0\n" % (w, h))
+            f.write(np.ascontiguousarray(self.texels, dtype="<f4").tobytes())
 
 
 @dataclass
@@ -175,14 +185,16 @@ class SceneSpec:
         return n
 
     # ------------------------------------------------------------------- CRSD
-    def write_crsd(self, path: str, sidecar_min_triangles: int = 4096) -> None:
+    def write_crsd(self, path: str, sidecar_min_triangles: int = 4096, header: str = "") -> None:
         """Write the scene as a CRSD file; meshes with at least
         `sidecar_min_triangles` triangles go to binary float32 sidecar files
-        next to it (`[positions-file string ...]`) instead of text arrays."""
+        next to it (`[positions-file string ...]`) instead of text arrays, and
+        image textures to PFM files next to it."""
         import os
         base = os.path.dirname(os.path.abspath(path))
         stem = os.path.splitext(os.path.basename(path))[0]
         with open(path, "w") as f:
+            f.write(header)
             f.write(self.to_crsd(sidecar=(base, stem, sidecar_min_triangles)))
 
     def to_crsd(self, with_header: bool = True, sidecar=None) -> str:
@@ -217,6 +229,18 @@ class SceneSpec:
           "    [max-depth int32 \"%d\"]\n}\n" % (self.spp, self.max_depth))
         w("accelerator {\n    [type string \"bvh\"]\n}\n")
         w("light-cluster {\n    [type string \"%s\"]\n}\n" % self.light_cluster)
+        for t in self.textures:
+            if t.name == self.environment:
+                continue
+            if sidecar is None:
+                raise ValueError("image texture '%s' needs a PFM file next to the CRSD: use write_crsd" % t.name)
+            import os
+            base, stem, _ = sidecar
+            fn = "%s.%s.pfm" % (stem, t.name)
+            t.write_pfm(os.path.join(base, fn))
+            w("texture-spectrum {\n    [type string \"image\"]\n    [name string \"%s\"]\n"
+              "    [filename string \"%s\"]\n    [sample-mode string \"nearest\"]\n"
+              "    [wrap-mode string \"repeat\"]\n}\n" % (t.name, fn))
         for m in self.materials:
             w("material {\n    [type string \"%s\"]\n    [name string \"%s\"]\n" % (m.type, m.name))
             if m.type == LAMBERT:
@@ -548,6 +572,48 @@ def diff_scene(width: int = 512, height: int = 512, spp: int = 32, max_depth: in
         s.primitives.append(Rectangle(name, "lightBase", (cx + h, 14.0, cz - h), (cx - h, 14.0, cz - h),
                                       (cx - h, 14.0, cz + h)))
         s.lights.append(AreaLight(name, col, _quad_light_watt(col, (2 * h) ** 2)))
+    return s
+
+
+def texture_scene(width: int = 48, height: int = 40, spp: int = 16, max_depth: int = 6, seed: int = 17,
+                  tex_w: int = 16, tex_h: int = 12) -> SceneSpec:
+    """Image-texture scene: a floor and a back wall (two-triangle meshes) and
+    a smooth icosphere share one RGB albedo texture of `tex_w` x `tex_h`
+    distinct seeded texels, looked up nearest with repeat wrap.  The floor's
+    uvs run from -1.5 to 2.25 and from -0.75 to 2.5 (negative coordinates
+    and several wraps), the wall's from 0 to 3 and 0 to 2 (texel borders on
+    its edges), the sphere's are spherical; a plain Lambert sphere and a
+    rectangle light overhead."""
+    rng = np.random.default_rng(seed)
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(0.0, 7.0, -20.0), cam_direction=(0.0, -0.3, 1.0),
+                  cam_up=(0.0, 1.0, 0.0), fov=55.0)
+    s.textures.append(ImageTexture("albedoTex", rng.uniform(0.05, 0.95, (tex_h, tex_w, 3)).astype(np.float32)))
+    s.materials = [Material("tex", LAMBERT, albedo_texture="albedoTex"),
+                   Material("clay", LAMBERT, albedo=(0.7, 0.4, 0.3)),
+                   Material("emitterBase", LAMBERT, albedo=(0.2, 0.2, 0.2))]
+    f = 14.0
+    floor = np.array([[[-f, 0, -f], [f, 0, f], [f, 0, -f]], [[-f, 0, -f], [-f, 0, f], [f, 0, f]]], np.float32)
+    fuv = np.zeros_like(floor)
+    fuv[..., 0] = -1.5 + (floor[..., 0] + f) / (2 * f) * 3.75
+    fuv[..., 1] = -0.75 + (floor[..., 2] + f) / (2 * f) * 3.25
+    s.primitives.append(TriangleMesh("floor", "tex", floor, uvws=fuv.astype(np.float32)))
+    wall = np.array([[[-f, 0, 10], [f, 16, 10], [f, 0, 10]], [[-f, 0, 10], [-f, 16, 10], [f, 16, 10]]], np.float32)
+    wuv = np.zeros_like(wall)
+    wuv[..., 0] = (wall[..., 0] + f) / (2 * f) * 3.0
+    wuv[..., 1] = wall[..., 1] / 16.0 * 2.0
+    s.primitives.append(TriangleMesh("wall", "tex", wall, uvws=wuv.astype(np.float32)))
+    unit = icosphere(2)
+    n = unit / np.linalg.norm(unit, axis=2, keepdims=True)
+    uv = np.zeros_like(unit)
+    uv[..., 0] = 0.5 + np.arctan2(n[..., 0], n[..., 2]) / (2 * math.pi)
+    uv[..., 1] = 0.5 + np.arcsin(np.clip(n[..., 1], -1, 1)) / math.pi
+    s.primitives.append(TriangleMesh("ball", "tex", (unit * 3.0 + [-4.0, 3.0, 2.0]).astype(np.float32),
+                                     uvws=uv.astype(np.float32)))
+    s.primitives.append(TriangleMesh("plain", "clay", (unit * 2.0 + [5.0, 2.0, -1.0]).astype(np.float32)))
+    s.primitives.append(Rectangle("light", "emitterBase", (3, 12, -2), (-3, 12, -2), (-3, 12, 4)))
+    emission = (9.0, 8.0, 7.0)
+    s.lights = [AreaLight("light", emission, _quad_light_watt(emission, 36.0))]
     return s
 
 

@@ -48,14 +48,14 @@
 extern "C" {
 #endif
 
-#define CGPU_ABI_VERSION 3
+#define CGPU_ABI_VERSION 4
 
 typedef enum cgpu_status {
     CGPU_OK = 0,
     CGPU_ERR_INVALID_ARGUMENT = 1,
     CGPU_ERR_CUDA = 2,
     CGPU_ERR_OUT_OF_MEMORY = 3,
-    CGPU_ERR_TIMEOUT = 4, /* a device-side iteration budget ran out */
+    CGPU_ERR_TIMEOUT = 4, /* a device-side iteration budget ran out (cgpu_set_visit_budget) */
     CGPU_ERR_UNSUPPORTED = 5,
     CGPU_ERR_NOT_FOUND = 6,
     CGPU_ERR_PARSE = 7,
@@ -105,7 +105,9 @@ typedef struct cgpu_material {
 typedef struct cgpu_texture {
     int32_t width;
     int32_t height;
-    const float* texels; /* width * height * 3, row-major, row 0 first */
+    const float* texels; /* width * height * 3, row-major; row y holds v in [y / height, (y + 1) / height),
+                            so row 0 is the picture's bottom row (the reference lays pictures out
+                            bottom-up: its loader flips them vertically, file-io/pictureLoader.cpp) */
 } cgpu_texture;
 
 /* One-sided area emitter on a primitive (singleAreaLight.cpp:20-37):
@@ -230,7 +232,25 @@ void cgpu_destroy(cgpu_ctx* ctx);
 const char* cgpu_last_error(const cgpu_ctx* ctx);
 const char* cgpu_status_string(cgpu_status status);
 int32_t cgpu_abi_version(void);
+/* Waits for the context stream; CGPU_ERR_TIMEOUT if a traversal since the
+ * last check ran out of its visit budget (below). */
 cgpu_status cgpu_synchronize(cgpu_ctx* ctx);
+
+/* Device-side iteration budget of every BVH traversal (no counterpart in the
+ * reference, whose accelerator asserts and aborts on a broken tree,
+ * fundamental/assertion.cpp:14-25): a ray that makes more than `visits` node
+ * and leaf visits stops, keeps the hit it holds (or none) and is counted on
+ * the device, so a corrupted tree cannot keep a kernel running.  0 (the
+ * default) is 5 x the scene's nodes + 64 per ray, which a correct traversal
+ * never reaches: it reaches every inner node and every leaf at most once.
+ * Asynchronous calls (cgpu_render, cgpu_trace_*_device) do not wait for the
+ * count; the next call that synchronises the context - cgpu_synchronize,
+ * cgpu_film_read, cgpu_trace_closest / _any, cgpu_path_radiance,
+ * cgpu_render_paths, cgpu_adjoint_forward / _backward - returns
+ * CGPU_ERR_TIMEOUT with the number of rays in cgpu_last_error and resets the
+ * count; results computed since the previous check are then not valid, and
+ * the context stays usable. */
+cgpu_status cgpu_set_visit_budget(cgpu_ctx* ctx, uint32_t visits);
 
 cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder);
 cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* desc, int32_t* out_scene);
@@ -312,7 +332,11 @@ cgpu_status cgpu_film_read(cgpu_ctx* ctx, int32_t scene, double* sum_rgb, double
  * one call before relying on the no-allocation property.  One scratch per
  * device and process: calls that overlap in time (any contexts, streams or
  * threads on one device) race on it and must be serialised by the caller.
- * Asynchronous on the context stream, like cgpu_render. */
+ * Asynchronous on the context stream, like cgpu_render.  Counting
+ * (cgpu_set_counting) and per-kernel timing (cgpu_set_profiling) do not
+ * apply to this call: afterwards cgpu_render_stats_get reports its paths,
+ * batches and kernel launches, and zero for the ray, node and triangle
+ * counters and for h2d_bytes (it copies nothing). */
 cgpu_status cgpu_render_noalloc(cgpu_ctx* ctx, int32_t scene, uint32_t first_sample, uint32_t num_samples,
                                 uint64_t seed);
 
@@ -349,19 +373,26 @@ typedef struct cgpu_tuning {
     uint32_t max_paths;    /* paths in flight per wavefront batch; 0 = automatic (2^21, at least one frame) */
     int32_t traversal;     /* 0: one ray per thread per grid-stride step; 1: persistent warps that hand a
                               finished lane the next ray at once; 2: persistent while-while closest-hit
-                              pass that refills a warp's finished lanes once 20 of them are done;
-                              3: 2 plus the same persistent while-while form for the any-hit pass */
+                              pass that refills a warp's finished lanes once fewer than refill_closest
+                              of its lanes still trace; 3: 2 plus the same persistent while-while form
+                              for the any-hit pass (refill_any) */
     int32_t reorder;       /* 1, 2, 3: before each closest-hit pass after the first, sort its rays by
                               direction octant and origin (Morton order of 9, 7 or 4 bits per axis in the
                               scene bounds; 4, 3 or 2 radix passes), so that a warp traces neighbouring
                               rays (traversal 0 and 2); 0: queue order (default; cgpu_autotune does not
                               search it: on the 1 M-triangle field the sort costs about what it saves) */
+    int32_t refill_closest;/* queue compaction of the persistent closest-hit pass (traversal 2 and 3):
+                              after each round of leaves a warp whose unfinished rays number fewer than
+                              this stores its finished lanes' hits and takes the next rays of the queue
+                              for them; 1..32, 0 = 12 */
+    int32_t refill_any;    /* the same threshold for the persistent any-hit pass (traversal 3); 0 = 12 */
 } cgpu_tuning;
 cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out_tuning);
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* tuning);
 /* Times wavefront passes of `scenes` (`samples` samples each) over a small
- * search of cgpu_tuning values (traversal variant, block sizes, 2^20..2^24
- * paths in flight) and applies the fastest.  With a cache path, a result
+ * search of cgpu_tuning values (traversal variant, block sizes, the refill
+ * thresholds of the persistent passes, 2^20..2^24 paths in flight) and
+ * applies the fastest.  With a cache path, a result
  * stored for the same GPU, scene sizes and sample count is reused without
  * timing and new results are appended (one JSON object per line). */
 cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t num_scenes, uint32_t samples,

@@ -19,6 +19,10 @@
 // Commands (binary little-endian I/O, see tests/golden/make_golden.py):
 //   camera <scene.crsd> <in: N x {f64 fx, f64 fy}>           <out: N x 6 f32 (o, d)>
 //   trace  <scene.crsd> <in: N x 8 f32 {o, tmin, d, tmax}>    <out: N x {i32 bvh_prim, f32 bvh_t, i32 bf_prim, f32 bf_t, i32 occluded}>
+//   trace-bvh  the same without the brute-force query (bf_prim / bf_t repeat
+//          the BVH's answer), for scenes too large for a brute-force loop
+//   texel  <scene.crsd> <texture name> <in: N x 3 f32 uvw>    <out: N x 3 f32 rgb>
+//          RgbImageTexture::evaluate (core/texture/category/rgbImageTexture.cpp:8-15)
 //   paths  <scene.crsd> <in: N x {f64 fx, f64 fy, u64 key}>   <out: N x {f32 r, g, b, u32 draws}>
 //   render <scene.crsd> <out: H x W x 7 f64> <spp> <seed> <threads>
 //          (sum r,g,b, sum of squares r,g,b, accepted sample count)
@@ -31,6 +35,15 @@
 //          the render loop above with the scene's film filter: every pass of up
 //          to 256 samples per pixel goes through a fresh FilmTile per tile, whose
 //          sensors are then added in FP64 (sum w r,g,b, zeros, sum w)
+//
+// Image textures: the reference reads pictures through stb
+// (file-io/pictureLoader.cpp), which has no float RGB format.  A
+// texture-spectrum block of type "image" whose filename ends in .pfm is built
+// here in memory instead - the reference's own TImage and RgbImageTexture
+// (core/texture/category/tImageTexture.ipp:11-27) with the block's sample and
+// wrap modes - from the PFM's rows in file order, so that row 0 is the
+// picture's bottom row, as the reference's loader lays out every picture
+// (stbi_set_flip_vertically_on_load: uv starts at the lower-left corner).
 
 #include "core/camera/camera.h"
 #include "core/estimator/energyEstimator.h"
@@ -53,6 +66,10 @@
 #include "core/spectrum/spectrum.h"
 #include "core/surface/bsdf/bsdf.h"
 #include "core/texture/tTexture.h"
+#include "core/texture/category/rgbImageTexture.h"
+#include "core/texture/eTextureSampleMode.h"
+#include "core/texture/eTextureWrapMode.h"
+#include "math/type/imageType.h"
 #include "file-io/scene-description/eSdClassType.h"
 #include "file-io/scene-description/sdData.h"
 #include "file-io/scene-description/tokenizer.h"
@@ -140,6 +157,37 @@ std::string readStripped(const char* path) {
     return s;
 }
 
+std::string dirOf(const char* path) {
+    const std::string p(path);
+    const std::size_t k = p.find_last_of('/');
+    return k == std::string::npos ? std::string() : p.substr(0, k + 1);
+}
+
+// PFM ("PF", width, height, scale, then float RGB rows) into the reference's
+// RgbImageTexture, rows in file order (row 0 = the picture's bottom row).
+std::shared_ptr<TTexture<Spectrum>> pfmTexture(const std::string& file, const std::string_view& wrap) {
+    std::ifstream f(file, std::ios::binary);
+    std::string magic;
+    int w = 0, h = 0;
+    float scale = 0.0f;
+    f >> magic >> w >> h >> scale;
+    f.get();
+    if (!f || magic != "PF" || w <= 0 || h <= 0) {
+        std::fprintf(stderr, "cannot read PFM %s\n", file.c_str());
+        std::exit(2);
+    }
+    std::vector<float> raw(static_cast<std::size_t>(w) * h * 3);
+    f.read(reinterpret_cast<char*>(raw.data()), static_cast<std::streamsize>(raw.size() * sizeof(float)));
+    HdrImage image(w, h);
+    for (int y = 0; y < h; ++y)
+        for (int x = 0; x < w; ++x) {
+            const float* px = &raw[(static_cast<std::size_t>(y) * w + x) * 3];
+            image.setPixelValue(x, y, Vector3R(px[0], px[1], px[2]));
+        }
+    const ETextureWrapMode mode = wrap == "clamp" ? ETextureWrapMode::CLAMP : ETextureWrapMode::REPEAT;
+    return std::make_shared<RgbImageTexture>(image, ETextureSampleMode::NEAREST, mode);
+}
+
 std::unique_ptr<LoadedScene> load(const char* path) {
     auto ls = std::make_unique<LoadedScene>();
     ls->text = readStripped(path);
@@ -159,10 +207,16 @@ std::unique_ptr<LoadedScene> load(const char* path) {
                 ls->realTextures.insert({std::string(data->findString("name")),
                                          instantiator::makeRealTexture(data, ls->realTextures, ls->spectrumTextures)});
                 break;
-            case ESdClassType::TEXTURE_SPECTRUM:
-                ls->spectrumTextures.insert({std::string(data->findString("name")),
-                                             instantiator::makeSpectrumTexture(data, ls->realTextures, ls->spectrumTextures)});
+            case ESdClassType::TEXTURE_SPECTRUM: {
+                const std::string fn(data->findString("filename"));
+                const bool pfm = data->findString("type") == "image" && fn.size() > 4 &&
+                                 fn.compare(fn.size() - 4, 4, ".pfm") == 0;
+                ls->spectrumTextures.insert(
+                    {std::string(data->findString("name")),
+                     pfm ? pfmTexture(fn[0] == '/' ? fn : dirOf(path) + fn, data->findString("wrap-mode"))
+                         : instantiator::makeSpectrumTexture(data, ls->realTextures, ls->spectrumTextures)});
                 break;
+            }
             case ESdClassType::MATERIAL:
                 ls->bsdfs.insert({std::string(data->findString("name")),
                                   instantiator::makeBsdf(data, ls->realTextures, ls->spectrumTextures, ls->bsdfs)});
@@ -235,7 +289,7 @@ int cmdCamera(const LoadedScene& ls, const char* in, const char* out) {
     return 0;
 }
 
-int cmdTrace(const LoadedScene& ls, const char* in, const char* out) {
+int cmdTrace(const LoadedScene& ls, const char* in, const char* out, bool bruteForce) {
     const auto rays = readAll<float>(in);
     const std::size_t n = rays.size() / 8;
     struct Rec { int32_t bvhPrim; float bvhT; int32_t bfPrim; float bfT; int32_t occluded; };
@@ -250,17 +304,42 @@ int cmdTrace(const LoadedScene& ls, const char* in, const char* out) {
             rec.bvhPrim = primOf(ls, pa);
             rec.bvhT = a.maxT();
         }
-        Ray b(o, d, r[3], r[7]);
-        PrimitiveInfo pb;
-        if (ls.bruteForce->isIntersecting(b, pb)) {
-            rec.bfPrim = primOf(ls, pb);
-            rec.bfT = b.maxT();
+        if (bruteForce) {
+            Ray b(o, d, r[3], r[7]);
+            PrimitiveInfo pb;
+            if (ls.bruteForce->isIntersecting(b, pb)) {
+                rec.bfPrim = primOf(ls, pb);
+                rec.bfT = b.maxT();
+            }
+        } else {
+            rec.bfPrim = rec.bvhPrim;
+            rec.bfT = rec.bvhT;
         }
         Ray c(o, d, r[3], r[7]);
         rec.occluded = ls.accelerator->isOccluded(c) ? 1 : 0;
         res[i] = rec;
     }
     writeAll(out, res.data(), res.size() * sizeof(Rec));
+    return 0;
+}
+
+int cmdTexel(const LoadedScene& ls, const char* name, const char* in, const char* out) {
+    const auto it = ls.spectrumTextures.find(std::string(name));
+    if (it == ls.spectrumTextures.end()) {
+        std::fprintf(stderr, "no texture %s\n", name);
+        return 2;
+    }
+    const auto uvw = readAll<float>(in);
+    const std::size_t n = uvw.size() / 3;
+    std::vector<float> res(n * 3);
+    for (std::size_t i = 0; i < n; ++i) {
+        Spectrum v;
+        it->second->evaluate(Vector3R(uvw[3 * i], uvw[3 * i + 1], uvw[3 * i + 2]), &v);
+        Vector3R rgb;
+        v.transformToRgb(&rgb);
+        for (int k = 0; k < 3; ++k) res[3 * i + k] = rgb[k];
+    }
+    writeAll(out, res.data(), res.size() * sizeof(float));
     return 0;
 }
 
@@ -463,7 +542,9 @@ int main(int argc, char** argv) {
     const std::string cmd = argv[1];
     auto ls = load(argv[2]);
     if (cmd == "camera" && argc >= 5) return cmdCamera(*ls, argv[3], argv[4]);
-    if (cmd == "trace" && argc >= 5) return cmdTrace(*ls, argv[3], argv[4]);
+    if (cmd == "trace" && argc >= 5) return cmdTrace(*ls, argv[3], argv[4], true);
+    if (cmd == "trace-bvh" && argc >= 5) return cmdTrace(*ls, argv[3], argv[4], false);
+    if (cmd == "texel" && argc >= 6) return cmdTexel(*ls, argv[3], argv[4], argv[5]);
     if (cmd == "paths" && argc >= 5) return cmdPaths(*ls, argv[3], argv[4]);
     if (cmd == "filmtile" && argc >= 5) return cmdFilmTile(*ls, argv[3], argv[4]);
     if (cmd == "render-tiles" && argc >= 7) {

@@ -33,6 +33,9 @@ FILTER_CASES = [
 def specs():
     return {
         "cornell": scenes.cornell_box(64, 64, 16, 6),
+        # the first configuration itself: 256 x 256, 16 spp, depth 6
+        "cornell256": scenes.cornell_box(),
+        "textured": scenes.texture_scene(),
         "field": scenes.icosphere_field(n_spheres=10, subdivision=2, n_lights=3, seed=3, width=48, height=36,
                                         spp=16, max_depth=8, dielectric=scenes.GLASS, box=30.0,
                                         radius_range=(2.0, 6.0)),
@@ -43,12 +46,79 @@ def specs():
     }
 
 
+def field1m_spec(width=1920, height=1080):
+    """The second configuration's 1,024,000-triangle field with the GGX
+    dielectric replaced by the reference's smooth glass (the reference has no
+    rough dielectric); same geometry, lights and camera."""
+    return scenes.icosphere_field(dielectric=scenes.GLASS, width=width, height=height)
+
+
 def vectors(name):
     return dict(np.load(os.path.join(GOLDEN, name + "_vectors.npz")))
 
 
 def image(name):
     return dict(np.load(os.path.join(GOLDEN, name + "_image.npz")))
+
+
+def image_mean_var(name):
+    """Per pixel the reference render's mean and the variance of that mean,
+    from either golden film layout (FP64 sums, or FP32 mean / sample variance)."""
+    ref = image(name)
+    if "mean" in ref:
+        n = ref["count"][..., None].astype(np.float64)
+        return ref["mean"].astype(np.float64), ref["var"].astype(np.float64) / n
+    n = ref["count"][..., None]
+    mean = ref["sum"] / n
+    return mean, (ref["sum_sq"] / n - mean ** 2) / n
+
+
+def scene_digest(flat) -> str:
+    """SHA-1 of a flattened scene's arrays (geometry, materials, lights,
+    textures), as tests/golden/make_golden.py records it for a large golden
+    scene that is rebuilt rather than committed."""
+    import hashlib
+    h = hashlib.sha1()
+    for a in (flat.kind, flat.vertices, flat.material):
+        h.update(np.ascontiguousarray(a).tobytes())
+    h.update(bytes(flat.materials))
+    h.update(bytes(flat.lights))
+    for t in flat.texture_arrays:
+        h.update(t.tobytes())
+    return h.hexdigest()
+
+
+def exact_rays(spec, n, seed):
+    """Seeded rays from exactly rounded operations only (uniform draws,
+    +, *, /, sqrt), so that every platform regenerates the same bits: 40 %
+    from the camera towards points in the sphere cube, 60 % from points in
+    the cube in uniform directions (half of those with a finite t_max)."""
+    rng = np.random.default_rng(seed)
+    box = 100.0
+    o = rng.random((n, 3)) * box
+    nc = (2 * n) // 5
+    cam = np.array(spec.cam_position, np.float64)
+    o[:nc] = cam
+    tgt = rng.random((nc, 3)) * box
+    d = np.empty((n, 3))
+    d[:nc] = tgt - cam
+    m = n - nc
+    got = 0
+    while got < m:
+        c = rng.random((2 * m, 3)) * 2.0 - 1.0
+        r2 = c[:, 0] * c[:, 0] + c[:, 1] * c[:, 1] + c[:, 2] * c[:, 2]
+        c = c[(r2 > 1e-4) & (r2 <= 1.0)][:m - got]
+        d[nc + got:nc + got + len(c)] = c
+        got += len(c)
+    d /= np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])[:, None]
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = o
+    rays[:, 3] = 1e-3
+    rays[:, 4:7] = d
+    finite = rng.random(n) < 0.5
+    finite[:nc] = False
+    rays[:, 7] = np.where(finite, (0.1 + 0.9 * rng.random(n)) * box, 3.4028235e38)
+    return rays
 
 
 def crsd_text(name):

@@ -46,6 +46,26 @@ void* khc_create(const cgpu_scene_desc* d, char* err, int errlen) {
 
 void khc_destroy(void* p) { delete static_cast<Check*>(p); }
 
+// The kernels' texel lookup (texture_rgb: nearest, repeat wrap) of texture
+// `tex` at n uvws (3 floats each); 3 floats out per uvw.
+void khc_texel(void* p, int tex, const float* uvw, uint32_t n, float* rgb) {
+    const Check& c = *static_cast<Check*>(p);
+    for (uint32_t i = 0; i < n; ++i) {
+        const float3 v = cg::texture_rgb(c.S.textures[tex], cg::mk(uvw[3 * i], uvw[3 * i + 1], uvw[3 * i + 2]));
+        rgb[3 * i + 0] = v.x;
+        rgb[3 * i + 1] = v.y;
+        rgb[3 * i + 2] = v.z;
+    }
+}
+
+// Device-side iteration budget of the traversals (0: the automatic one) and
+// the word that counts the rays that ran out of it.
+void khc_set_budget(void* p, uint32_t visits, uint32_t* status) {
+    Check& c = *static_cast<Check*>(p);
+    c.S.visit_budget = visits ? visits : cg::auto_visit_budget(c.hs.nodes.size());
+    c.S.status = status;
+}
+
 // rays: 8 floats (org, t_min, dir, t_max); dyn 1 uses the resumable stepper, 2 the warp traversal
 void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, float* t, float* u, float* v,
                int32_t* occ) {

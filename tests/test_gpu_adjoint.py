@@ -193,8 +193,7 @@ def test_wavefront_and_megakernel_schedules_agree(gpu_ctx, diff, name):
             for a, b in zip(wf, mk):
                 scale = np.abs(b).max() if b.size else 0.0
                 np.testing.assert_allclose(a, b, rtol=1e-7, atol=1e-10 * scale + 1e-30)
-        gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], base["traversal"],
-                           base["reorder"])
+        gpu_ctx.set_tuning_dict(base)
     finally:
         gpu_ctx.set_adjoint_mode(CGPU_MODE_WAVEFRONT)
         if release:

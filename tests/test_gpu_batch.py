@@ -80,9 +80,12 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
     gpu_ctx.render(sids, 0, 4, seed=5)
     ref = films(gpu_ctx, sids)
     # small batches; persistent ray replacement (1) and persistent while-while (2);
-    # closest-hit queues sorted by direction octant and origin (reorder) with traversals 0 and 2
-    for traversal, reorder in ((1, 0), (2, 0), (3, 0), (0, 1), (2, 2), (3, 3)):
-        gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal, reorder=reorder)
+    # closest-hit queues sorted by direction octant and origin (reorder) with traversals 0 and 2;
+    # the queue-compaction (refill) thresholds of the persistent passes at their extremes
+    for traversal, reorder, rc, ra in ((1, 0, 0, 0), (2, 0, 0, 0), (3, 0, 0, 0), (0, 1, 0, 0), (2, 2, 0, 0),
+                                       (3, 3, 0, 0), (3, 0, 1, 32), (3, 0, 32, 1), (2, 0, 20, 0), (3, 0, 6, 24)):
+        gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal, reorder=reorder, refill_closest=rc,
+                           refill_any=ra)
         for s in sids:
             gpu_ctx.film_clear(s)
         gpu_ctx.render(sids, 0, 4, seed=5)
@@ -91,7 +94,7 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
         for a, b in zip(ref, got):
             for x, y in zip(a, b):
                 assert np.array_equal(x, y)
-    gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], base["traversal"], base["reorder"])
+    gpu_ctx.set_tuning_dict(base)
 
 
 def test_autotune_picks_and_caches(gpu_ctx, uneven, tmp_path):
@@ -107,3 +110,5 @@ def test_autotune_picks_and_caches(gpu_ctx, uneven, tmp_path):
     assert gpu_ctx.tuning() == t1
     with pytest.raises(cg.CgpuError):
         gpu_ctx.set_tuning(100, 128)
+    with pytest.raises(cg.CgpuError):
+        gpu_ctx.set_tuning(128, 128, refill_closest=33)

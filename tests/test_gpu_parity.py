@@ -4,12 +4,13 @@ outputs (tests/golden/) and against the oracle restatement.
 Tolerances (FP32 path tracer):
   * camera rays: 2e-6 absolute per component;
   * closest hits: identical hit/miss and primitive id except rays whose hit
-    point lies within 1e-5 (relative barycentric / edge coordinate) of a
+    point lies within 1e-6 (relative barycentric / edge coordinate) of a
     primitive edge, where the reference's non-watertight test and the
-    watertight one may legitimately disagree, and equal-t ties (another
-    primitive at the same distance, e.g. coplanar faces); where the
-    primitive agrees, t is the reference's to the bit (the kernels compute
-    it with the reference's own formula and no contracted multiply-adds);
+    watertight one may legitimately disagree, and ties between coplanar
+    primitives at the same distance (tests/parity_util.py), at most 0.5 %
+    of a scene's rays; where the primitive agrees, t is the reference's to
+    the bit (the kernels compute it with the reference's own formula and no
+    contracted multiply-adds);
   * per-path radiance: the GPU evaluates transcendental functions
     differently from the host, so a path may branch differently after a
     near-tie; >= 99 % of paths within 1e-3 relative (+1e-5 absolute) and the
@@ -23,11 +24,12 @@ import pytest
 
 import oracle
 from cadise_gb300 import CGPU_MODE_MEGAKERNEL, CGPU_MODE_WAVEFRONT, CgpuError, abi, scenes
-from golden_scenes import FILTER_CASES, image, specs, vectors
+from golden_scenes import FILTER_CASES, image, image_mean_var, specs, vectors
+from parity_util import EDGE, check_hits, edge_margin
 
 pytestmark = pytest.mark.gpu
 
-NAMES = ["cornell", "field", "features", "power", "spheres"]
+NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres"]
 
 
 @pytest.fixture(scope="module")
@@ -37,36 +39,6 @@ def uploaded(gpu_ctx):
         flat = abi.flatten(spec)
         out[name] = (spec, flat, gpu_ctx.upload(flat))
     return out
-
-
-def edge_margin(flat, prim, P):
-    """Smallest relative distance of points P (n, 3) to the edges of their
-    primitives (barycentric for triangles, edge coordinates for rectangles)."""
-    m = np.full(len(prim), np.inf)
-    for i, (p, x) in enumerate(zip(prim, P)):
-        if p < 0:
-            continue
-        v = flat.vertices[p].reshape(3, 3).astype(np.float64)
-        if flat.kind[p] == abi.CGPU_PRIM_SPHERE:
-            continue  # no edges: the sphere test is the reference's own formula
-        if flat.kind[p] == abi.CGPU_PRIM_TRIANGLE:
-            e0, e1, w = v[1] - v[0], v[2] - v[0], x - v[0]
-            d00, d01, d11 = e0 @ e0, e0 @ e1, e1 @ e1
-            d20, d21 = w @ e0, w @ e1
-            den = d00 * d11 - d01 * d01
-            if den == 0:
-                m[i] = 0
-                continue
-            b1 = (d11 * d20 - d01 * d21) / den
-            b2 = (d00 * d21 - d01 * d20) / den
-            m[i] = min(abs(b1), abs(b2), abs(1 - b1 - b2))
-        else:
-            eA, eB = v[0] - v[1], v[2] - v[1]
-            w = x - v[1]
-            a = w @ eA / (eA @ eA)
-            b = w @ eB / (eB @ eB)
-            m[i] = min(abs(a), abs(1 - a), abs(b), abs(1 - b))
-    return m
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -79,26 +51,15 @@ def test_camera_rays_match_reference(name, gpu_ctx, uploaded):
 
 @pytest.mark.parametrize("name", NAMES)
 def test_closest_hits_match_reference(name, gpu_ctx, uploaded):
+    """Primitive ids equal the reference BVH's except rays within 1e-6 of an
+    edge and ties between coplanar primitives, at most 0.5 % of the rays;
+    t bit-identical where the primitive agrees."""
     v = vectors(name)
     spec, flat, sid = uploaded[name]
     rays = v["trace_rays"]
     prim, t, u, w = gpu_ctx.trace_closest(sid, rays)
-    ref_p, ref_t = v["trace_bvh_prim"], v["trace_bvh_t"]
-    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
-    near = np.zeros(len(prim), bool)
-    diff = np.where(prim != ref_p)[0]
-    if len(diff):
-        m_ref = edge_margin(flat, ref_p[diff], o[diff] + d[diff] * ref_t[diff, None])
-        m_gpu = edge_margin(flat, prim[diff], o[diff] + d[diff] * t[diff, None])
-        near[diff] = (m_ref < 1e-5) | (m_gpu < 1e-5)
-    tie = ref_p != v["trace_bf_prim"]  # the reference's own BVH / brute-force tie
-    # equal-t ties: a different primitive hit at the same distance (coplanar faces)
-    tie |= (prim != ref_p) & (prim >= 0) & (ref_p >= 0) & (np.abs(t - ref_t) <= 1e-5 * np.abs(ref_t))
-    keep = ~(near | tie)
-    assert np.mean(keep) > 0.98
-    assert np.array_equal(prim[keep], ref_p[keep]), np.where(prim[keep] != ref_p[keep])
-    both = (prim == ref_p) & (prim >= 0)
-    assert np.array_equal(t[both], ref_t[both]), np.abs(t - ref_t)[both].max()
+    frac = check_hits(flat, rays, prim, t, v["trace_bvh_prim"], v["trace_bvh_t"], name)
+    print("%s: %d rays, %.4f %% excluded (edge / coplanar tie)" % (name, len(rays), 100 * frac))
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -112,7 +73,8 @@ def test_any_hit_matches_reference(name, gpu_ctx, uploaded):
     o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
     m = edge_margin(flat, prim, o + d * t[:, None])
     boundary = (prim >= 0) & (np.abs(t - rays[:, 7]) <= 1e-5 * np.abs(rays[:, 7]))
-    keep = (m >= 1e-5) & ~boundary
+    keep = (m >= EDGE) & ~boundary
+    assert keep.mean() >= 0.995, keep.mean()
     assert np.array_equal(occ[keep], v["trace_occluded"][keep])
     # occlusion is consistent with the closest hit on the same rays
     assert np.array_equal(occ[keep], (prim[keep] >= 0).astype(np.int32))
@@ -208,24 +170,28 @@ def rel_mse(x, ref):
     return float(np.mean((x - ref) ** 2 / (ref ** 2 + 1e-2)))
 
 
-@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("field", 8192), ("features", 32768), ("power", 131072),
+@pytest.mark.parametrize("name,spp", [("cornell", 16384), ("cornell256", 65536), ("textured", 65536),
+                                      ("field", 8192), ("features", 32768), ("power", 131072),
                                       ("spheres", 65536), ("filtered", 65536)])
 def test_image_converges_to_reference(name, spp, gpu_ctx, uploaded):
     """Per pixel the film's mean (sum w L / sum w; w = 1 for the box filter of
     size 1) against the reference's converged render: relMSE, and for the box
     films a per-pixel Welch z-test."""
     spec, flat, sid = uploaded[name]
-    ref = image(name)
     gpu_ctx.film_clear(sid)
     gpu_ctx.render([sid], 0, spp, seed=1234, mode=CGPU_MODE_WAVEFRONT)
     s, q, n = gpu_ctx.film_read(sid)
     mean_g = s / n[..., None]
-    mean_r = ref["sum"] / ref["count"][..., None]
-    assert rel_mse(mean_g, mean_r) <= 1e-3
     if spec.film_filter is not None:
-        return  # the reference's FilmTile keeps no sums of squares
+        # the reference's FilmTile keeps no sums of squares
+        ref = image(name)
+        assert rel_mse(mean_g, ref["sum"] / ref["count"][..., None]) <= 1e-3
+        return
+    mean_r, var_r = image_mean_var(name)
+    r = rel_mse(mean_g, mean_r)
+    print("%s: relMSE %.2e" % (name, r))
+    assert r <= 1e-3
     var_g = (q / n[..., None] - mean_g ** 2) / n[..., None]
-    var_r = (ref["sum_sq"] / ref["count"][..., None] - mean_r ** 2) / ref["count"][..., None]
     z = (mean_g - mean_r) / np.sqrt(var_g + var_r + 1e-30)
     frac = float(np.mean(np.abs(z) > 2.576))
     assert frac <= 0.01 + 3 * np.sqrt(0.01 * 0.99 / z.size) + 0.005, frac
@@ -307,8 +273,11 @@ def test_environment_furnace_is_exact(gpu_ctx):
 
 
 def test_environment_paths_match_oracle(gpu_ctx):
-    """Sky light (no reference parity: see DESIGN) against the oracle's
-    restatement, and wavefront against megakernel."""
+    """Sky light against the oracle's restatement, and wavefront against
+    megakernel.  No reference parity: the reference samples the sky with a
+    z-up mapping (infiniteSphere.cpp:68-77) but looks its radiance up with a
+    y-up one (sphericalMapper.cpp:17-27), so its own NEE and BSDF-sampled sky
+    disagree; this library uses the y-up lookup mapping for both."""
     spec = scenes.env_field(n_spheres=10, subdivision=2, n_lights=2, width=32, height=24, spp=4, max_depth=6,
                             sky=(64, 32))
     flat = abi.flatten(spec)

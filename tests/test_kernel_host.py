@@ -15,6 +15,7 @@ import pytest
 import oracle
 from cadise_gb300 import abi, scenes
 from golden_scenes import FILTER_CASES, specs, vectors
+from parity_util import check_hits
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
 BUILD = os.path.join(ROOT, "tests", "native", "_build")
@@ -42,6 +43,8 @@ def khc():
     L.khc_create.restype = C.c_void_p
     L.khc_create.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     L.khc_destroy.argtypes = [C.c_void_p]
+    L.khc_set_budget.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+    L.khc_texel.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_uint32, C.c_void_p]
     L.khc_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int] + [C.c_void_p] * 5
     L.khc_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
     L.khc_render_paths.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p]
@@ -90,29 +93,18 @@ class Host:
         self.L.khc_destroy(self.h)
 
 
-NAMES = ["cornell", "field", "features", "power", "spheres"]
+NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres"]
 
 
 @pytest.mark.parametrize("name", NAMES)
 def test_kernel_traversal_matches_reference_hits(khc, name):
-    from test_gpu_parity import edge_margin
     v = vectors(name)
     flat = abi.flatten(specs()[name])
     h = Host(khc, flat)
     rays = v["trace_rays"]
     prim, t, occ = h.trace(rays)
     ref_p, ref_t = v["trace_bvh_prim"], v["trace_bvh_t"]
-    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
-    near = np.zeros(len(prim), bool)
-    diff = np.where(prim != ref_p)[0]
-    if len(diff):
-        near[diff] = (edge_margin(flat, ref_p[diff], o[diff] + d[diff] * ref_t[diff, None]) < 1e-5) | \
-                     (edge_margin(flat, prim[diff], o[diff] + d[diff] * t[diff, None]) < 1e-5)
-    # equal-t ties: a different primitive hit at the same distance (coplanar faces)
-    tie = (prim != ref_p) & (prim >= 0) & (ref_p >= 0) & (np.abs(t - ref_t) <= 1e-5 * np.abs(ref_t))
-    keep = ~(near | tie | (ref_p != v["trace_bf_prim"]))
-    assert keep.mean() > 0.98
-    assert np.array_equal(prim[keep], ref_p[keep])
+    check_hits(flat, rays, prim, t, ref_p, ref_t, name)
     both = (prim == ref_p) & (prim >= 0)
     assert np.array_equal(t[both], ref_t[both])  # the reference's own distance formula
     # the resumable stepper of the persistent kernels and the warp traversal
@@ -276,3 +268,47 @@ def test_quantized_nodes_are_conservative_and_tight(khc, scale):
         assert np.all(span <= 254.0)
         mag = np.maximum(np.abs(lo32).max(0), np.abs(hi32).max(0))
         assert np.all(step >= mag * 2.0 ** -22 * 0.999)
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_visit_budget_stops_traversals_and_counts_them(khc, variant):
+    """The device-side iteration budget, on the CPU: with 3 node and leaf
+    visits per ray every traversal variant (per-ray loop, resumable stepper
+    of the persistent kernels, warp traversal) stops early and counts its
+    rays; with the automatic budget (5 x nodes + 64) none runs out and the
+    hits are the reference's again."""
+    v = vectors("field")
+    flat = abi.flatten(specs()["field"])
+    h = Host(khc, flat)
+    status = np.zeros(1, np.uint32)
+    rays = v["trace_rays"]
+    khc.khc_set_budget(h.h, 3, _p(status))
+    prim_cut, _, _ = h.trace(rays, dyn=variant)
+    assert status[0] > 0
+    assert not np.array_equal(prim_cut, v["trace_bvh_prim"])
+    status[0] = 0
+    khc.khc_set_budget(h.h, 0, _p(status))
+    prim, t, occ = h.trace(rays, dyn=variant)
+    assert status[0] == 0
+    assert np.array_equal(prim, v["trace_bvh_prim"])
+    h.close()
+
+
+def test_kernel_texel_lookup_matches_reference_texture(khc):
+    """The kernels' nearest / repeat texel lookup (texture_rgb) against the
+    reference's RgbImageTexture::evaluate (rgbImageTexture.cpp:8-15,
+    tNearestPixelSampler.ipp:14-31, repeatUvwWrapper.cpp:9-15) on uvws on
+    texel borders, just below them, negative, at 1 and far outside:
+    bit-identical texels."""
+    v = dict(np.load(os.path.join(ROOT, "tests", "golden", "texel_vectors.npz")))
+    h = Host(khc, abi.flatten(specs()["textured"]))
+    uvw = np.ascontiguousarray(v["uvw"], np.float32)
+    out = np.zeros_like(uvw)
+    khc.khc_texel(h.h, 0, _p(uvw), uvw.shape[0], _p(out))
+    assert np.array_equal(out, v["rgb"]), np.where(np.any(out != v["rgb"], axis=1))[0][:10]
+    # the border cases are there: u = k / width exactly, negative and >= 1
+    w = specs()["textured"].textures[0].texels.shape[1]
+    borders = np.arange(-2 * w, 3 * w + 1, dtype=np.float64) / w
+    assert np.isin(uvw[:, 0], borders.astype(np.float32)).sum() >= 20
+    assert (uvw[:, 0] < 0).any() and (uvw[:, 0] >= 1).any()
+    h.close()

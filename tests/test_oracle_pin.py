@@ -13,11 +13,11 @@ import numpy as np
 import pytest
 
 import oracle
-from cadise_gb300 import abi
+from cadise_gb300 import abi, scenes
 from golden_scenes import crsd_text, specs, vectors
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
-NAMES = ["cornell", "field", "features", "power", "spheres"]
+NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres"]
 
 
 @pytest.fixture(scope="module")
@@ -29,10 +29,19 @@ def ports():
 
 
 @pytest.mark.parametrize("name", NAMES)
-def test_golden_scene_is_reproducible(name):
-    """The committed CRSD is exactly what the scene generator writes."""
+def test_golden_scene_is_reproducible(name, tmp_path):
+    """The committed CRSD (and its PFM textures) is exactly what the scene
+    generator writes."""
+    import os
+    from golden_scenes import GOLDEN
+    spec = specs()[name]
+    path = str(tmp_path / (name + ".crsd"))
+    spec.write_crsd(path, sidecar_min_triangles=1 << 62)
     body = crsd_text(name).split("\n", 1)[1]
-    assert body == specs()[name].to_crsd()
+    assert body == open(path).read()
+    for t in spec.textures:
+        fn = "%s.%s.pfm" % (name, t.name)
+        assert open(os.path.join(GOLDEN, fn), "rb").read() == open(str(tmp_path / fn), "rb").read()
 
 
 @pytest.mark.parametrize("name", NAMES)

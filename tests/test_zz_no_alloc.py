@@ -21,13 +21,26 @@ def films_close(a, b):
     np.testing.assert_allclose(q1, q2, rtol=1e-12, atol=1e-300)
 
 
+def filtered_spheres():
+    s = scenes.sphere_box(64, 48, 16, 8)
+    s.film_filter = scenes.FilmFilter("gaussian")
+    return s
+
+
+@pytest.mark.parametrize("traversal", [0, 1, 2, 3])
 @pytest.mark.parametrize("make", [
     lambda: scenes.cornell_box(96, 64, 16, 6),
     lambda: scenes.feature_scene(width=48, height=40, spp=16, max_depth=16),
-])
-def test_noalloc_render_matches_render_on_two_calls(gpu_ctx, make):
+    # analytic spheres (the kernels with the sphere test) and a Gaussian film filter (the gathering splat)
+    filtered_spheres,
+], ids=["cornell", "features", "spheres_gaussian"])
+def test_noalloc_render_matches_render_on_two_calls(gpu_ctx, make, traversal):
+    """Each traversal variant of the tuning: the no-alloc call launches its
+    own serial list of the same kernels."""
     spec = make()
     sid = gpu_ctx.upload(spec)
+    base = gpu_ctx.tuning()
+    gpu_ctx.set_tuning(base["block_trace"], base["block_shade"], base["max_paths"], traversal=traversal)
     try:
         npix = spec.width * spec.height
         per = (1 << 18) // npix  # samples per batch of the 262144-path scratch
@@ -51,6 +64,7 @@ def test_noalloc_render_matches_render_on_two_calls(gpu_ctx, make):
         gpu_ctx.render([sid], 300, 60, seed=7)
         films_close(alone, gpu_ctx.film_read(sid))
     finally:
+        gpu_ctx.set_tuning_dict(base)
         gpu_ctx.release(sid)
 
 
