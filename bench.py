@@ -66,6 +66,24 @@ def make_scene(args):
     return scenes.icosphere_field(spp=args.spp)
 
 
+def frame_config(args, spec):
+    """The workload keys of the JSON line, the same in both arms."""
+    return {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": spec.width,
+            "height": spec.height, "spp": spec.spp, "max_depth": spec.max_depth,
+            "triangles": spec.num_triangles(), "l2": "256 MB buffer written between steps"}
+
+
+def traversal_profile():
+    """Counters of the closest-hit pass from the committed small-case ncu
+    captures (profiles/traversal_counters.json): L2 hit rate and throughput,
+    lanes per warp instruction, per configuration."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traversal_counters.json")) as f:
+            return json.load(f)
+    except Exception:
+        return None
+
+
 # ------------------------------------------------------------------ clocks --
 class ClockSampler:
     """nvidia-smi clock / throttle samples during the timed region (read only)."""
@@ -281,6 +299,7 @@ def run_gpu(args, rank, world, local):
     except Exception:
         pass
     rays_per_sample = (st.closest_rays + st.any_rays) / float(npix)
+    prof = traversal_profile()
 
     adjoint = None
     if not args.no_adjoint:
@@ -295,13 +314,15 @@ def run_gpu(args, rank, world, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": spec.width,
-                   "height": spec.height, "spp": spp, "max_depth": spec.max_depth,
-                   "triangles": info.num_triangles, "bvh_nodes": info.num_bvh_nodes,
-                   "bvh": {"builder": {1: "host-sah", 2: "gpu-ploc", 3: "gpu-sah"}[info.bvh_builder], "build_ms": info.bvh_ms},
-                   "schedule": "wavefront, CUDA graph per batch", "l2": "256 MB buffer written between steps",
-                   "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
-        "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value},
+        "config": frame_config(args, spec),
+        "gpu_setup": {"bvh_nodes": info.num_bvh_nodes,
+                      "bvh": {"builder": {1: "host-sah", 2: "gpu-ploc", 3: "gpu-sah"}[info.bvh_builder],
+                              "build_ms": info.bvh_ms},
+                      "schedule": "wavefront, CUDA graph per batch",
+                      "parallelism": "replicas" if world > 1 else "single", "tuning": tuning},
+        "megakernel": {"value": mk_value, "unit": UNIT, "speedup_wavefront": value / world / mk_value,
+                       "rays": "the wavefront's: zero-contribution shadow rays skipped, MIS rays resolved "
+                               "against their light at the vertex with a bounded any-hit query"},
         "rays": {"closest_per_sample": st.closest_rays / float(npix), "any_per_sample": st.any_rays / float(npix),
                  "mrays_per_s": value * rays_per_sample / 1e6,
                  "nodes_per_closest_ray": st.node_visits / max(1, st.closest_rays),
@@ -310,8 +331,11 @@ def run_gpu(args, rank, world, local):
                  "triangles_per_any_ray": st.any_triangle_tests / max(1, st.any_rays)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_wf_extend (closest-hit traversal)",
-                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s"},
+                     "kernel": "k_wf_extend_pww (closest-hit traversal)",
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                     "limiter": "not HBM: the BVH and triangles sit in the 129 MB L2; issue slots and "
+                                "L1/L2 latency under divergence (lanes per warp instruction below)",
+                     "counters": prof.get("c2") if prof else None},
         "kernel_ms_per_pass": {k: v[0] for k, v in kt.items()},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": npix * 7 * 8,
@@ -410,8 +434,7 @@ def run_reference(args, rank, world, local):
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD if not args.quick else "quick-640x360", "width": w, "height": h,
-                   "spp": spec.spp, "max_depth": spec.max_depth},
+        "config": frame_config(args, spec),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -423,7 +446,7 @@ CONFIGS = {
     "c1": "cornell-box-256x256-16spp-depth6",
     "c3": "64-batched-icosphere-fields-10k-2M-tris-128..1024px-4..256spp-depth4..16",
     "c4": "diff-scene-102k-tris-512x512-32spp-depth6-forward",
-    "c5": "env-field-20.48M-tris-3840x2160-depth32-64-lights-hdr-sky (4 spp per step of the 1024)",
+    "c5": "env-field-20.48M-tris-3840x2160-depth32-64-lights-hdr-sky-64-ggx-palette (4 spp per step of the 1024)",
 }
 
 
@@ -512,9 +535,47 @@ def run_config(args):
                     "bvh_builders": sorted({{1: "host-sah", 2: "gpu-ploc", 3: "gpu-sah"}[i.bvh_builder] for i in infos})},
         "clocks": clk,
         "cpu_baseline": cpu,
+        "counters": (traversal_profile() or {}).get(args.config),
     }
+    if args.config == "c5" and not args.no_adjoint:
+        out["adjoint"] = stress_adjoint_rate(ctx, sids[0], specs[0])
     print(json.dumps(out), flush=True)
     ctx.close()
+
+
+def stress_adjoint_rate(ctx, sid, spec, spp=4, iters=2):
+    """The stress configuration's differentiation: per iteration a forward
+    pass of `spp` of the 1024 samples per pixel of the 3840 x 2160 frame and
+    the path-replay adjoint of a fixed random d loss / d image over the same
+    paths, with FP64 reductions; the parameters asked for are the 64 GGX
+    palette roughnesses and the 64 quad lights' radiances (the adjoint also
+    returns the roughness entries of the Lambert materials, which are zero)."""
+    import numpy as np
+    import torch
+
+    from cadise_gb300 import scenes
+    ggx = [i for i, m in enumerate(spec.materials) if m.type in (scenes.CONDUCTOR, scenes.ROUGH_DIELECTRIC)]
+    W = np.random.default_rng(5).normal(size=(spec.height, spec.width, 3)).astype(np.float32)
+    fwd, bwd = [], []
+    for it in range(iters + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ctx.adjoint_forward(sid, spp, 700 + it)
+        t1 = time.perf_counter()
+        gt, gr, gl = ctx.adjoint_backward(sid, spp, 700 + it, W)
+        t2 = time.perf_counter()
+        if it > 0:  # the first iteration allocates the adjoint buffers
+            fwd.append(t1 - t0)
+            bwd.append(t2 - t1)
+    nparams = len(ggx) + gl.size
+    f, b = statistics.mean(fwd), statistics.mean(bwd)
+    return {"workload": "env-field-20.48M-tris-3840x2160-depth32, %d spp forward + adjoint per iteration" % spp,
+            "parameters": int(nparams), "roughness_parameters": len(ggx), "radiance_parameters": int(gl.size),
+            "iterations_per_s": 1.0 / (f + b), "grads_per_s": nparams / (f + b),
+            "unit": "gradient evaluations/s (forward + adjoint)", "forward_ms": f * 1e3, "backward_ms": b * 1e3,
+            "backward_path_samples_per_s": spec.width * spec.height * spp / b,
+            "nonzero_roughness_gradients": int(np.count_nonzero(gr[ggx])),
+            "finite": bool(np.all(np.isfinite(gr)) and np.all(np.isfinite(gl)))}
 
 
 def run_profile_case(args):
@@ -522,15 +583,16 @@ def run_profile_case(args):
     uses (autotuned the same way first) and direct launches instead of the
     graph; the profiled range (cudaProfilerStart / Stop, for ncu
     --profile-from-start off) holds only the `--steps` renders of
-    `--profile-spp` samples per pixel."""
+    `--profile-spp` samples per pixel.  --config c1 / c4: the Cornell box or
+    the differentiable scene instead of the bench frame."""
     import torch
 
     import cadise_gb300 as cg
-    from cadise_gb300 import abi
+    from cadise_gb300 import abi, scenes
     torch.cuda.set_device(0)
     ctx = cg.Context()
     ctx.set_bvh_builder(BVH_BUILDERS[args.bvh])
-    spec = make_scene(args)
+    spec = {"c1": scenes.cornell_box, "c4": scenes.diff_scene}.get(args.config, lambda: make_scene(args))()
     sid = ctx.upload(abi.flatten(spec))
     if args.tuning:
         t = json.loads(args.tuning)
@@ -544,7 +606,8 @@ def run_profile_case(args):
         ctx.render([sid], i * args.profile_spp, args.profile_spp, seed=2024, mode=cg.CGPU_MODE_WAVEFRONT, graph=False)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()
-    print(json.dumps({"profile_case": WORKLOAD if not args.quick else "quick", "renders": args.steps,
+    print(json.dumps({"profile_case": args.config if args.config != "c2" else WORKLOAD if not args.quick else "quick",
+                      "renders": args.steps,
                       "spp_per_render": args.profile_spp, "tuning": tuning,
                       "kernel_launches_last_render": ctx.stats().kernel_launches}))
     ctx.close()

@@ -175,8 +175,8 @@ cgpu_status cgpu_autotune(cgpu_ctx* ctx, const int32_t* scenes, uint32_t n, uint
     // the closest-hit passes, so the search would pick it by noise)
     // queue compaction of the persistent passes: refill a warp's finished
     // lanes once fewer than this many lanes still trace
-    const int refills[] = {6, 12, 18, 24};
-    const int options[] = {4, 3, 3, 5, 4, 4};
+    const int refills[] = {8, 16, 24, 28, 32};
+    const int options[] = {4, 3, 3, 5, 5, 5};
     for (int pass = 0; pass < 6 && st == CGPU_OK; ++pass) {
         // the thresholds only act in the persistent while-while passes
         if (pass == 4 && best.traversal < 2) continue;

@@ -183,7 +183,7 @@ struct RenderArgs {
 };
 
 // The refill thresholds of a tuning, 0 replaced by the default.
-constexpr int kDefaultRefillLanes = 12;
+constexpr int kDefaultRefillLanes = 24;
 inline int refill_lanes(int32_t v) { return v > 0 ? v : kDefaultRefillLanes; }
 
 // Buffers of the ray reordering: keys / values ping-pong for 2 * path_cap

@@ -373,7 +373,7 @@ __global__ void k_wf_extend_dyn(RenderArgs a, int b) {
                 o = f3(w.ray_o[p]);
                 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
                 r = ray_prep(o, d, kRayEps, kFloatMax);
-                trav_begin(st, r);
+                trav_begin(st, r, a.scenes[w.meta[p].x].visit_budget);
                 if (COUNT) ++nclosest;
             }
         }
@@ -415,9 +415,8 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     int* const* qmat = w.q_mat;
     TraceCounters tc{0, 0};
     uint32_t nclosest = 0;
-    extern __shared__ uint32_t trav_stack_smem[];
     SharedStack<true> stack;
-    stack.bind(trav_stack_smem);
+    stack.bind();
     int sp = 0;
     RayPre r{};
     float tcur = 0.0f, hu = 0.0f, hv = 0.0f;
@@ -426,7 +425,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
     int i = -1, p = -1;  // queue entry and path of this lane's ray (i < 0: none)
     bool cont = false;   // continuation ray (else MIS ray)
     bool drained = false;
-    uint32_t steps = 0, budget = 0;  // this ray's node and leaf visits, its scene's budget
+    uint32_t left = 0;  // node and leaf visits this ray has left (over_budget)
     auto pop = [&]() -> uint32_t {
         while (sp > 0) {
             --sp;
@@ -452,8 +451,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 cur = 0;
                 leaf = kNoEntry;
                 sp = 0;
-                steps = 0;
-                budget = a.scenes[__ldcs(&w.meta[p].x)].visit_budget;
+                left = a.scenes[__ldcs(&w.meta[p].x)].visit_budget;
                 if (COUNT) ++nclosest;
             }
         }
@@ -462,7 +460,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
         const SceneD& S = a.scenes[__ldcs(&w.meta[p].x)];
         for (;;) {
             while (cur != kNoEntry && !entry_is_leaf(cur)) {
-                if (over_budget(S, budget, steps)) {
+                if (over_budget(S, left)) {
                     cur = leaf = kNoEntry;
                     break;
                 }
@@ -480,7 +478,7 @@ __global__ void k_wf_extend_pww(RenderArgs a, int b) {
                 cur = pop();
             }
             while (leaf != kNoEntry) {
-                if (over_budget(S, budget, steps)) {
+                if (over_budget(S, left)) {
                     cur = leaf = kNoEntry;
                     break;
                 }
@@ -520,9 +518,8 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
     const int* q = w.q_shadow[b & 1];
     TraceCounters tc{0, 0};
     uint32_t nany = 0;
-    extern __shared__ uint32_t trav_stack_smem[];
     SharedStack<false> stack;
-    stack.bind(trav_stack_smem);
+    stack.bind();
     int sp = 0;
     RayPre r{};
     float tcur = 0.0f, hu = 0.0f, hv = 0.0f;
@@ -530,7 +527,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
     uint32_t cur = kNoEntry, leaf = kNoEntry;
     int i = -1, p = -1;
     bool occluded = false, drained = false;
-    uint32_t steps = 0, budget = 0;  // this ray's node and leaf visits, its scene's budget
+    uint32_t left = 0;  // node and leaf visits this ray has left (over_budget)
     auto pop = [&]() -> uint32_t {
         if (sp > 0) return stack.entry(--sp);
         return kNoEntry;
@@ -552,8 +549,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
                 leaf = kNoEntry;
                 sp = 0;
                 occluded = false;
-                steps = 0;
-                budget = a.scenes[__ldcs(&w.meta[p].x)].visit_budget;
+                left = a.scenes[__ldcs(&w.meta[p].x)].visit_budget;
                 if (COUNT) ++nany;
             }
         }
@@ -562,7 +558,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
         const SceneD& S = a.scenes[__ldcs(&w.meta[p].x)];
         for (;;) {
             while (cur != kNoEntry && !entry_is_leaf(cur)) {
-                if (over_budget(S, budget, steps)) {
+                if (over_budget(S, left)) {
                     cur = leaf = kNoEntry;
                     break;
                 }
@@ -580,7 +576,7 @@ __global__ void k_wf_shadow_pww(RenderArgs a, int b) {
                 cur = pop();
             }
             while (leaf != kNoEntry) {
-                if (over_budget(S, budget, steps)) {
+                if (over_budget(S, left)) {
                     cur = leaf = kNoEntry;
                     break;
                 }
@@ -629,7 +625,7 @@ __global__ void k_wf_shadow_dyn(RenderArgs a, int b) {
                 p = q[i];
                 const float4 sd = w.sh_d[p];
                 r = ray_prep(f3(w.ray_o[p]), f3(sd), kRayEps, sd.w);
-                trav_begin(st, r);
+                trav_begin(st, r, a.scenes[w.meta[p].x].visit_budget);
                 if (COUNT) ++nany;
             }
         }

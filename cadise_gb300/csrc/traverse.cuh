@@ -148,14 +148,18 @@ CG_D void child_hits(const RayPre& r, const float4 (&q)[4], float tcur, float (&
 
 constexpr uint32_t kNoEntry = 0xFFFFFFFFu;  // never a node or leaf entry (28-bit triangle range)
 
-// Device-side iteration budget of one ray: `steps` counts its node and leaf
-// visits; past `budget` (SceneD::visit_budget) the traversal stops, reports
-// the hit it holds so far (or none) and counts the ray in S.status.  The
-// host reads that count at its next synchronising call and returns
-// CGPU_ERR_TIMEOUT, so a corrupted tree ends in an error status instead of a
-// kernel that never returns.
-CG_D bool over_budget(const SceneD& S, uint32_t budget, uint32_t& steps) {
-    if (++steps <= budget) return false;
+// Device-side iteration budget of one ray: `left` starts at its scene's
+// SceneD::visit_budget and counts its node and leaf visits down; at the
+// visit past the budget the traversal stops, reports the hit it holds so
+// far (or none) and counts the ray in S.status.  The host reads that count
+// at its next synchronising call and returns CGPU_ERR_TIMEOUT, so a
+// corrupted tree ends in an error status instead of a kernel that never
+// returns.
+CG_D bool over_budget(const SceneD& S, uint32_t& left) {
+    if (left != 0) {
+        --left;
+        return false;
+    }
     if (S.status) atomicAdd(S.status, 1u);
     return true;
 }
@@ -194,44 +198,42 @@ struct LocalStack {
 // The persistent traversal passes keep the bottom kSmemStack entries of each
 // lane in shared memory and only deeper ones in local memory: on the 1 M-
 // triangle field a closest-hit ray's stack reaches 4 entries at the median,
-// 10 at the 99th percentile and more than 16 for 2 rays in 100,000.  Entry k
-// of thread i sits at word k * stride + i (stride = threads per block, a
-// multiple of 32), so the lanes of a warp always hit 32 different banks,
-// whatever depth each one is at.  WITH_T = false (any-hit) keeps no
-// distances: an any-hit pass pops without the distance test.
+// 10 at the 99th percentile and more than 16 for 2 rays in 100,000.  Each
+// warp owns kSmemStack rows of 32 words (64 with distances: the 32 entries,
+// then their 32 distances); entry k of lane l sits at word
+// row_base + k * row + l, so the lanes of a warp always hit 32 different
+// banks whatever depth each one is at, and one register (the lane's base)
+// addresses the whole stack.  WITH_T = false (any-hit) keeps no distances:
+// an any-hit pass pops without the distance test.
 constexpr int kSmemStack = 16;
+// the dynamic shared memory of a persistent traversal launch
+extern __shared__ uint32_t trav_stack_smem[];
 
 template <bool WITH_T>
 struct SharedStack {
-    uint32_t* e;  // this thread's column of the block's entry array
-    float* t;     // ... of the distance array (WITH_T)
-    int stride;
+    static constexpr int kRow = WITH_T ? 64 : 32;  // words per stack level of a warp
+    uint32_t base;   // this lane's word of level 0
     uint32_t oe[kStackSize - kSmemStack];
     float ot[WITH_T ? kStackSize - kSmemStack : 1];
 
-    // Shared memory per block for `threads` threads.
-    static constexpr size_t bytes(int threads) {
-        return size_t(threads) * kSmemStack * (WITH_T ? 8u : 4u);
-    }
-    // `base`: the block's dynamic shared memory.
-    CG_D void bind(uint32_t* base) {
-        stride = int(blockDim.x);
-        e = base + threadIdx.x;
-        t = WITH_T ? reinterpret_cast<float*>(base + size_t(kSmemStack) * blockDim.x) + threadIdx.x : nullptr;
-    }
+    // Shared memory per block for `threads` threads (a multiple of 32).
+    static constexpr size_t bytes(int threads) { return size_t(threads) * kSmemStack * (WITH_T ? 8u : 4u); }
+    CG_D void bind() { base = (threadIdx.x >> 5) * uint32_t(kSmemStack * kRow) + (threadIdx.x & 31u); }
     CG_D void push(int sp, uint32_t ee, float tt) {
         if (sp < kSmemStack) {
-            e[sp * stride] = ee;
-            if (WITH_T) t[sp * stride] = tt;
+            trav_stack_smem[base + sp * kRow] = ee;
+            if (WITH_T) trav_stack_smem[base + sp * kRow + 32] = __float_as_uint(tt);
         } else {
             oe[sp - kSmemStack] = ee;
             if (WITH_T) ot[sp - kSmemStack] = tt;
         }
     }
-    CG_D uint32_t entry(int sp) const { return sp < kSmemStack ? e[sp * stride] : oe[sp - kSmemStack]; }
+    CG_D uint32_t entry(int sp) const {
+        return sp < kSmemStack ? trav_stack_smem[base + sp * kRow] : oe[sp - kSmemStack];
+    }
     CG_D float dist(int sp) const {
         if (!WITH_T) return 0.0f;
-        return sp < kSmemStack ? t[sp * stride] : ot[sp - kSmemStack];
+        return sp < kSmemStack ? __uint_as_float(trav_stack_smem[base + sp * kRow + 32]) : ot[sp - kSmemStack];
     }
 };
 #endif
@@ -348,10 +350,9 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
     int hslot = -1;
     float hu = 0.0f, hv = 0.0f;
     uint32_t cur = 0;  // root first (always an inner node)
-    const uint32_t budget = S.visit_budget;
-    uint32_t steps = 0;
+    uint32_t left = S.visit_budget;
     for (;;) {
-        if (over_budget(S, budget, steps)) break;
+        if (over_budget(S, left)) break;
         uint32_t next = kNoEntry;
         if (entry_is_leaf(cur)) {
             if (visit_leaf<ANY, COUNT, SPH>(S, r, cur, tcur, hslot, hu, hv, cnt)) {
@@ -407,10 +408,9 @@ CG_D bool occluded_before(const SceneD& S, const RayPre& r, float t_l, int prim_
     LocalStack stack;
     int sp = 0;
     uint32_t cur = 0;
-    const uint32_t budget = S.visit_budget;
-    uint32_t steps = 0;
+    uint32_t left = S.visit_budget;
     for (;;) {
-        if (over_budget(S, budget, steps)) return false;
+        if (over_budget(S, left)) return false;
         uint32_t next = kNoEntry;
         if (entry_is_leaf(cur)) {
             if (visit_leaf_before<COUNT, SPH>(S, r, cur, t_l, prim_l, cnt)) return true;
@@ -440,8 +440,7 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
     float hu = 0.0f, hv = 0.0f;
     uint32_t cur = 0;          // root first (always an inner node)
     uint32_t leaf = kNoEntry;  // postponed leaf
-    const uint32_t budget = S.visit_budget;
-    uint32_t steps = 0;
+    uint32_t left = S.visit_budget;
     // next stack entry that can still hold a closer hit
     auto pop = [&]() -> uint32_t {
         while (sp > 0) {
@@ -452,7 +451,7 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
     };
     while (cur != kNoEntry || leaf != kNoEntry) {
         while (cur != kNoEntry && !entry_is_leaf(cur)) {
-            if (over_budget(S, budget, steps)) {
+            if (over_budget(S, left)) {
                 cur = leaf = kNoEntry;
                 break;
             }
@@ -470,7 +469,7 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
             cur = pop();
         }
         while (leaf != kNoEntry) {
-            if (over_budget(S, budget, steps)) {
+            if (over_budget(S, left)) {
                 cur = leaf = kNoEntry;
                 break;
             }
@@ -503,11 +502,11 @@ struct TravState {
     int hslot;
     float hu, hv;
     bool done;
-    uint32_t steps;  // node and leaf visits so far (over_budget)
+    uint32_t left;  // node and leaf visits left (over_budget)
 };
 
-CG_D void trav_begin(TravState& st, const RayPre& r) {
-    st.steps = 0;
+CG_D void trav_begin(TravState& st, const RayPre& r, uint32_t budget) {
+    st.left = budget;
     st.sp = 0;
     st.cur = 0;
     st.tcur = r.tmax;
@@ -518,7 +517,7 @@ CG_D void trav_begin(TravState& st, const RayPre& r) {
 
 template <bool ANY, bool COUNT, bool SPH = true>
 CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounters* cnt) {
-    if (over_budget(S, S.visit_budget, st.steps)) {
+    if (over_budget(S, st.left)) {
         st.done = true;
         return;
     }

@@ -417,12 +417,18 @@ def _value_noise(p: np.ndarray, lattice: np.ndarray, freq: float) -> np.ndarray:
 def icosphere_field(n_spheres: int = 200, subdivision: int = 4, n_lights: int = 8, seed: int = 2,
                     width: int = 1920, height: int = 1080, spp: int = 64, max_depth: int = 12,
                     dielectric: str = ROUGH_DIELECTRIC, box: float = 100.0,
-                    radius_range=(3.0, 8.0), displacement: float = 0.10) -> SceneSpec:
+                    radius_range=(3.0, 8.0), displacement: float = 0.10, palette: int = 0) -> SceneSpec:
     """Displaced icospheres with centres uniform in a ``box``^3 cube over a
     2-triangle ground plane; materials drawn uniformly from Lambert
     (albedo U[0.05,0.9]^3), GGX conductor (roughness U[0.05,0.6], F0
     U[0.5,1]^3) and dielectric (IOR U[1.3,1.7]); quad lights with emission
-    log-uniform in [1, 50]."""
+    log-uniform in [1, 50].
+
+    palette > 0: the spheres share `palette` GGX materials (conductors and
+    dielectrics in turn) and palette / 2 Lambert materials, drawn from their
+    own seeded stream, instead of one material each; a sphere keeps its kind
+    (Lambert or GGX) and its geometry, so the scene differs only in its
+    material table (a fixed set of roughness parameters for the adjoint)."""
     rng = np.random.default_rng(seed)
     s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
                   cam_position=(0.5 * box, 0.75 * box, -0.95 * box),
@@ -435,8 +441,10 @@ def icosphere_field(n_spheres: int = 200, subdivision: int = 4, n_lights: int = 
     s.primitives.append(TriangleMesh("ground", "ground", ground))
     unit = icosphere(subdivision)
     flat = unit.reshape(-1, 3)
+    kinds = []
     for i in range(n_spheres):
         kind = int(rng.integers(0, 3))
+        kinds.append(kind)
         name = "m%d" % i
         if kind == 0:
             s.materials.append(Material(name, LAMBERT, albedo=tuple(rng.uniform(0.05, 0.9, 3))))
@@ -453,6 +461,22 @@ def icosphere_field(n_spheres: int = 200, subdivision: int = 4, n_lights: int = 
         disp = 1.0 + displacement * _value_noise(flat + 1.0, lattice, 1.7)
         pos = (flat * (radius * disp)[:, None] + centre).astype(np.float32).reshape(-1, 3, 3)
         s.primitives.append(TriangleMesh("sphere%d" % i, name, pos))
+    if palette > 0:
+        prng = np.random.default_rng(seed + 7919)
+        ggx, lam = [], []
+        for k in range(palette):
+            if k % 2 == 0:
+                ggx.append(Material("ggx%d" % k, CONDUCTOR, roughness=float(prng.uniform(0.05, 0.6)),
+                                    f0=tuple(prng.uniform(0.5, 1.0, 3))))
+            else:
+                ggx.append(Material("ggx%d" % k, dielectric, albedo=(1.0, 1.0, 1.0),
+                                    roughness=float(prng.uniform(0.05, 0.3)), ior_inner=float(prng.uniform(1.3, 1.7))))
+        for k in range(max(1, palette // 2)):
+            lam.append(Material("lambert%d" % k, LAMBERT, albedo=tuple(prng.uniform(0.05, 0.9, 3))))
+        s.materials = [s.materials[0]] + ggx + lam
+        pick = prng.integers(0, 1 << 30, n_spheres)
+        for i, kind in enumerate(kinds):
+            s.primitives[1 + i].material = lam[pick[i] % len(lam)].name if kind == 0 else ggx[pick[i] % len(ggx)].name
     s.materials.append(Material("lightBase", LAMBERT, albedo=(0.5, 0.5, 0.5)))
     side = 0.15 * box
     for j in range(n_lights):
@@ -617,6 +641,33 @@ def texture_scene(width: int = 48, height: int = 40, spp: int = 16, max_depth: i
     return s
 
 
+def roughness_scene(width: int = 64, height: int = 48, spp: int = 64, max_depth: int = 3) -> SceneSpec:
+    """Close-up of three GGX spheres for finite-difference checks of the
+    roughness gradient: two conductors (roughness 0.55 and 0.5) and a rough
+    dielectric (roughness 0.3, IOR 1.5) on a Lambert floor under two quad
+    lights, framed so that most pixels see a GGX surface (pixels whose paths
+    never meet one add nothing to either the gradient or its noise)."""
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(0.0, 2.6, -8.5), cam_direction=(0.0, -0.18, 1.0), cam_up=(0.0, 1.0, 0.0),
+                  fov=40.0)
+    s.materials = [Material("floor", LAMBERT, albedo=(0.55, 0.5, 0.45)),
+                   Material("gold", CONDUCTOR, roughness=0.55, f0=(1.0, 0.78, 0.34)),
+                   Material("steel", CONDUCTOR, roughness=0.5, f0=(0.6, 0.6, 0.62)),
+                   Material("frost", ROUGH_DIELECTRIC, albedo=(1.0, 1.0, 1.0), roughness=0.3, ior_inner=1.5),
+                   Material("emitterBase", LAMBERT, albedo=(0.2, 0.2, 0.2))]
+    f = 12.0
+    s.primitives.append(TriangleMesh("floor", "floor", np.array(
+        [[[-f, 0, -f], [f, 0, f], [f, 0, -f]], [[-f, 0, -f], [-f, 0, f], [f, 0, f]]], np.float32)))
+    unit = icosphere(3)
+    for name, mat, cx in (("ballA", "gold", -2.6), ("ballB", "steel", 0.0), ("ballC", "frost", 2.6)):
+        s.primitives.append(TriangleMesh(name, mat, (unit * 1.2 + [cx, 1.2, 0.0]).astype(np.float32)))
+    s.primitives.append(Rectangle("lampA", "emitterBase", (2.0, 6.0, -3.0), (-2.0, 6.0, -3.0), (-2.0, 6.0, 1.0)))
+    s.primitives.append(Rectangle("lampB", "emitterBase", (5.0, 4.0, 2.0), (4.0, 4.0, 2.0), (4.0, 4.0, 3.0)))
+    s.lights = [AreaLight("lampA", (6.0, 6.0, 5.5), _quad_light_watt((6.0, 6.0, 5.5), 16.0)),
+                AreaLight("lampB", (20.0, 14.0, 8.0), _quad_light_watt((20.0, 14.0, 8.0), 1.0))]
+    return s
+
+
 def sphere_box(width: int = 64, height: int = 48, spp: int = 16, max_depth: int = 8) -> SceneSpec:
     """Open-front box of rectangles with analytic spheres in every non-GGX
     material the reference has besides Lambert: plastic (Lambert + Phong mix),
@@ -702,12 +753,16 @@ def lognormal_sky(width: int = 2048, height: int = 1024, sigma: float = 1.5, see
 
 
 def env_field(n_spheres: int = 4000, subdivision: int = 4, n_lights: int = 64, width: int = 3840, height: int = 2160,
-              spp: int = 1024, max_depth: int = 32, seed: int = 7, sky: tuple = (2048, 1024)) -> SceneSpec:
+              spp: int = 1024, max_depth: int = 32, seed: int = 7, sky: tuple = (2048, 1024),
+              palette: int = 64) -> SceneSpec:
     """The stress configuration: displaced icospheres (4000 x subdivision 4
     = 20,480,000 triangles) over a ground plane, mixed Lambert / GGX
-    conductor / GGX dielectric, a log-normal HDR sky and quad lights."""
+    conductor / GGX dielectric from a palette of `palette` GGX materials
+    (the 64 roughness parameters of its adjoint) and palette / 2 Lambert
+    ones, a log-normal HDR sky and quad lights (64 radiance parameters)."""
     s = icosphere_field(n_spheres=n_spheres, subdivision=subdivision, n_lights=n_lights, seed=seed, width=width,
-                        height=height, spp=spp, max_depth=max_depth, box=100.0 * (n_spheres / 200.0) ** (1 / 3))
+                        height=height, spp=spp, max_depth=max_depth, box=100.0 * (n_spheres / 200.0) ** (1 / 3),
+                        palette=palette)
     s.textures.append(ImageTexture("sky", lognormal_sky(sky[0], sky[1], 1.5, seed)))
     s.environment = "sky"
     return s

@@ -384,8 +384,8 @@ typedef struct cgpu_tuning {
     int32_t refill_closest;/* queue compaction of the persistent closest-hit pass (traversal 2 and 3):
                               after each round of leaves a warp whose unfinished rays number fewer than
                               this stores its finished lanes' hits and takes the next rays of the queue
-                              for them; 1..32, 0 = 12 */
-    int32_t refill_any;    /* the same threshold for the persistent any-hit pass (traversal 3); 0 = 12 */
+                              for them; 1..32, 0 = 24 */
+    int32_t refill_any;    /* the same threshold for the persistent any-hit pass (traversal 3); 0 = 24 */
 } cgpu_tuning;
 cgpu_status cgpu_tuning_get(cgpu_ctx* ctx, cgpu_tuning* out_tuning);
 cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* tuning);

@@ -78,14 +78,14 @@ void khc_trace(void* p, const float* rays, uint32_t n, int dyn, int32_t* prim, f
         bool hit, any;
         if (dyn == 1) {
             std::unique_ptr<cg::TravState> st(new cg::TravState());
-            cg::trav_begin(*st, pr);
+            cg::trav_begin(*st, pr, c.S.visit_budget);
             while (!st->done) cg::trav_step<false, false>(c.S, pr, *st, &tc);
             hit = st->hslot >= 0;
             h.slot = st->hslot;
             h.t = st->tcur;
             h.u = st->hu;
             h.v = st->hv;
-            cg::trav_begin(*st, pr);
+            cg::trav_begin(*st, pr, c.S.visit_budget);
             while (!st->done) cg::trav_step<true, false>(c.S, pr, *st, &tc);
             any = st->hslot >= 0;
         } else if (dyn == 2) {

@@ -2,13 +2,16 @@
 differences of the forward renderer (cgpu_adjoint_forward) with common random
 numbers (same seed, same samples), FP64 film accumulation.
 
-Loss: linear, loss = sum(W * image) with a fixed random weight image W, so
+Loss: linear, loss = sum(W * image) with a fixed weight image W, so
 d loss / d image = W.  With roulette off (max depth 3) the same-seed
 estimator is polynomial in the albedo texels and linear in the emitter
 radiances, so adjoint and finite differences agree to FP32 noise; the GGX
 roughness moves the sampled directions (finite differences see that, the
 detached adjoint does not), so there the two agree in expectation and the
-check is statistical over independent seeds.
+check is statistical over independent seeds, with enough of them that four
+standard errors are at most 1 % of the gradient and the bar is 2 %.  The
+differentiable configuration itself (512 x 512, 256^2 texture, 8
+roughnesses, 4 lights, roulette on) is checked the same way.
 """
 import numpy as np
 import pytest
@@ -106,40 +109,122 @@ def test_texel_gradient_matches_finite_differences(gpu_ctx, diff):
     gpu_ctx.set_params(sid, texels=tex)
 
 
-def test_roughness_gradient_matches_finite_differences(gpu_ctx, diff):
-    """GGX roughness.  With common random numbers the finite difference also
-    sees the sampled directions move, and a path whose shadow or next ray
-    crosses an edge jumps: per seed the two estimates differ by noise of
-    order 1 / step, but both are unbiased for the same derivative.  So the
-    check is over 16 independent seeds: the mean difference within 4
-    standard errors (+2 % of the gradient), and those errors small enough
-    (< 15 % of the gradient) for the check to have teeth."""
-    spec, sid = diff
-    W = np.ones((spec.height, spec.width, 3), np.float32)  # d mean-brightness / d roughness
-    spp, step, nseeds = 4096, 0.02, 16
-    tex, rough, rad = gpu_ctx.get_params(sid)
-    metals = [i for i, m in enumerate(spec.materials) if m.type == scenes.CONDUCTOR]
-    fd = np.zeros((nseeds, len(metals)))
-    adj = np.zeros((nseeds, len(metals)))
-    for k in range(nseeds):
-        seed = 1000 + k
-        _, gr, _ = gpu_ctx.adjoint_backward(sid, spp, seed, W)
-        adj[k] = gr[metals]
-        for j, i in enumerate(metals):
-            r = rough.copy()
-            r[i] += step
-            gpu_ctx.set_params(sid, roughness=r)
+def pixel_masks(ctx, sid, spec, flat, materials):
+    """Per material, W = 1 on the pixels whose centre sees it directly."""
+    h, w = spec.height, spec.width
+    xy = np.stack(np.meshgrid(np.arange(w) + 0.5, np.arange(h) + 0.5), -1).reshape(-1, 2).astype(np.float64)
+    cam = ctx.camera_rays(sid, xy)
+    rays = np.zeros((len(xy), 8), np.float32)
+    rays[:, :3], rays[:, 3], rays[:, 4:7], rays[:, 7] = cam[:, :3], 1e-3, cam[:, 3:6], 3e38
+    prim = ctx.trace_closest(sid, rays)[0]
+    seen = np.where(prim >= 0, flat.material[np.maximum(prim, 0)], -1).reshape(h, w)
+    return {m: np.repeat((seen == m)[..., None], 3, -1).astype(np.float32) for m in materials}
+
+
+def roughness_fd_check(ctx, spec, materials, nseeds, spp, step, seed0):
+    """Per material m: with W the pixels that see m, the adjoint's d loss /
+    d roughness_m and the central finite difference (common random
+    numbers, FP64 films) over `nseeds` independent seeds.  Both estimate
+    the same derivative; per seed they differ by noise (the finite
+    difference also sees sampled directions move, and a path whose shadow
+    or next ray crosses an edge jumps).  Returns (mean adjoint gradient,
+    mean difference, standard error of the difference) per material."""
+    from cadise_gb300 import abi
+    flat = abi.flatten(spec)
+    sid = ctx.upload(flat)
+    try:
+        tex, rough, rad = ctx.get_params(sid)
+        Ws = pixel_masks(ctx, sid, spec, flat, materials)
+        adj = np.zeros((nseeds, len(materials)))
+        fd = np.zeros((nseeds, len(materials)))
+        for k in range(nseeds):
+            seed = seed0 + k
+            for j, m in enumerate(materials):
+                assert Ws[m].sum() > 0
+                adj[k, j] = ctx.adjoint_backward(sid, spp, seed, Ws[m])[1][m]
+                r = rough.copy()
+                r[m] += step
+                ctx.set_params(sid, roughness=r)
+                lp = loss(ctx, sid, Ws[m], spp, seed)
+                r[m] -= 2 * step
+                ctx.set_params(sid, roughness=r)
+                lm = loss(ctx, sid, Ws[m], spp, seed)
+                ctx.set_params(sid, roughness=rough)
+                fd[k, j] = (lp - lm) / (2 * step)
+        d = fd - adj
+        return adj.mean(0), d.mean(0), d.std(0, ddof=1) / np.sqrt(nseeds)
+    finally:
+        ctx.release(sid)
+
+
+def test_roughness_gradient_matches_finite_differences(gpu_ctx):
+    """GGX conductor roughness within 2 % of central finite differences,
+    with enough independent seeds that four standard errors of the
+    difference are at most 1 % of the gradient (the check has teeth at 2 %).
+    Close-up scene (scenes.roughness_scene: two conductors and a rough
+    dielectric), depth 3, 192 seeds x 4,096 spp, step 0.02 (the central
+    difference's curvature error at that step is far below the noise)."""
+    spec = scenes.roughness_scene()
+    conductors = [i for i, m in enumerate(spec.materials) if m.type == scenes.CONDUCTOR]
+    g, dm, se = roughness_fd_check(gpu_ctx, spec, conductors, nseeds=192, spp=4096, step=0.02, seed0=1000)
+    print("roughness (close-up): gradient %s, (fd - adjoint) / |g| %s, 4 SE / |g| %s"
+          % (g, dm / np.abs(g), 4 * se / np.abs(g)))
+    assert np.all(4 * se <= 0.01 * np.abs(g)), (g, se)
+    assert np.all(np.abs(dm) <= 0.02 * np.abs(g)), (g, dm)
+
+
+def test_config4_gradients_match_finite_differences(gpu_ctx):
+    """The differentiable configuration itself: 102,400-triangle scene,
+    512 x 512, 256 x 256 albedo texture, 8 conductor roughnesses, 4 light
+    radiances, depth 6 with Russian roulette on; FP64 films of 4,096 spp.
+    Radiance (channel 0 of every light) and the four texels with the largest
+    gradients: central differences with h = 1e-3 relative, one seed, within
+    2 %.  Roughness: with h = 1e-3 a 4,096-spp difference is dominated by
+    paths whose sampled directions cross an edge or whose roulette decision
+    flips (measured: standard errors of 100 % and more), so the conductor
+    with the most pixels of its own among those whose noise allows it is
+    checked with step 0.02 over 12 seeds: 4 SE <= 1 % and within 2 %."""
+    spec = scenes.diff_scene()
+    assert spec.max_depth > 3  # roulette on (after the third bounce)
+    sid = gpu_ctx.upload(spec)
+    try:
+        W = np.random.default_rng(3).normal(size=(spec.height, spec.width, 3)).astype(np.float32)
+        spp, seed = 4096, 11
+        gt, gr, gl = gpu_ctx.adjoint_backward(sid, spp, seed, W)
+        tex, rough, rad = gpu_ctx.get_params(sid)
+        assert tex.size == 256 * 256 * 3 and (rad.shape[0], len(rough)) == (4, len(spec.materials))
+        for l in range(rad.shape[0]):
+            h = H * rad[l, 0]
+            r = rad.copy()
+            r[l, 0] += h
+            gpu_ctx.set_params(sid, radiance=r)
             lp = loss(gpu_ctx, sid, W, spp, seed)
-            r[i] -= 2 * step
-            gpu_ctx.set_params(sid, roughness=r)
+            r[l, 0] -= 2 * h
+            gpu_ctx.set_params(sid, radiance=r)
             lm = loss(gpu_ctx, sid, W, spp, seed)
-            fd[k, j] = (lp - lm) / (2 * step)
-        gpu_ctx.set_params(sid, roughness=rough)
-    d = fd - adj
-    se = d.std(0, ddof=1) / np.sqrt(nseeds)
-    g = np.abs(adj.mean(0))
-    assert np.all(se < 0.15 * g), (se, g)
-    assert np.all(np.abs(d.mean(0)) <= 4 * se + 0.02 * g), (fd.mean(0), adj.mean(0), se)
+            gpu_ctx.set_params(sid, radiance=rad)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - gl[l, 0]) <= 0.02 * abs(fd), ("radiance", l, fd, gl[l, 0])
+        for i in np.argsort(-np.abs(gt))[:4]:
+            h = H * tex[i]
+            t = tex.copy()
+            t[i] += h
+            gpu_ctx.set_params(sid, texels=t)
+            lp = loss(gpu_ctx, sid, W, spp, seed)
+            t[i] -= 2 * h
+            gpu_ctx.set_params(sid, texels=t)
+            lm = loss(gpu_ctx, sid, W, spp, seed)
+            gpu_ctx.set_params(sid, texels=tex)
+            fd = (lp - lm) / (2 * h)
+            assert abs(fd - gt[i]) <= 0.02 * abs(fd), ("texel", int(i), fd, gt[i])
+    finally:
+        gpu_ctx.release(sid)
+    metal = [i for i, m in enumerate(spec.materials) if m.type == scenes.CONDUCTOR][2]
+    g, dm, se = roughness_fd_check(gpu_ctx, spec, [metal], nseeds=12, spp=4096, step=0.02, seed0=500)
+    print("roughness (config 4, material %d): gradient %s, (fd - adjoint) / |g| %s, 4 SE / |g| %s"
+          % (metal, g, dm / np.abs(g), 4 * se / np.abs(g)))
+    assert np.all(4 * se <= 0.01 * np.abs(g)), (g, se)
+    assert np.all(np.abs(dm) <= 0.02 * np.abs(g)), (g, dm)
 
 
 def test_adjoint_matches_fp64_reference_gradient(gpu_ctx, diff):

@@ -7,7 +7,7 @@
   frame's): 100,000 seeded rays against the reference BVH's closest hits and
   occlusion, 10,000 path radiances at full-resolution film positions against
   the reference estimator, and the same geometry and camera rendered at
-  192 x 108 against the reference's converged render.  The scene (100 MB as
+  96 x 54 against the reference's converged render (131,072 spp).  The scene (100 MB as
   CRSD text) is rebuilt by the scene generator and must match the SHA-1 of
   the arrays the reference was given; the rays too.
 * The first configuration (the 256 x 256 Cornell box) is in
@@ -25,7 +25,7 @@ import pytest
 
 from cadise_gb300 import CGPU_MODE_WAVEFRONT, abi
 from golden_scenes import exact_rays, field1m_spec, image_mean_var, scene_digest, vectors
-from parity_util import EDGE, check_hits, edge_margin
+from parity_util import check_hits, near_edge
 
 pytestmark = pytest.mark.gpu
 
@@ -68,11 +68,8 @@ def test_field1m_any_hit_matches_reference(gpu_ctx, field1m, rays):
     spec, flat, sid, v = field1m
     occ = gpu_ctx.trace_any(sid, rays).astype(np.int32)
     prim, t, _, _ = gpu_ctx.trace_closest(sid, rays)
-    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
-    d /= np.linalg.norm(d, axis=1, keepdims=True)
-    m = edge_margin(flat, prim, o + d * t[:, None])
     boundary = (prim >= 0) & (np.abs(t - rays[:, 7]) <= 1e-5 * np.abs(rays[:, 7]))
-    keep = (m >= EDGE) & ~boundary
+    keep = ~near_edge(flat, prim, rays, t) & ~boundary
     assert keep.mean() >= 0.995, keep.mean()
     ref = v["trace_occluded"].astype(np.int32)
     assert np.array_equal(occ[keep], ref[keep]), np.where(occ[keep] != ref[keep])[0][:10]
@@ -82,7 +79,7 @@ def test_field1m_path_radiance_matches_reference(gpu_ctx, field1m):
     spec, flat, sid, v = field1m
     rgb = gpu_ctx.path_radiance(sid, v["paths_xy"], v["paths_keys"])
     ref = v["paths_rgb"]
-    assert len(ref) == 10000 and (ref.sum(1) > 0).mean() > 0.3
+    assert len(ref) == 10000 and (ref.sum(1) > 0).mean() > 0.2  # the rest see the black sky
     close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
     assert close.mean() >= 0.99, close.mean()
     assert abs(rgb.mean() - ref.mean()) <= 0.01 * abs(ref.mean()) + 1e-6
@@ -93,21 +90,24 @@ def rel_mse(x, ref):
 
 
 def test_field1m_image_converges_to_reference(gpu_ctx):
-    """The bench frame's geometry and camera at 192 x 108 (same aspect, same
-    view), rendered to convergence on the GPU against the reference."""
-    spec = field1m_spec(192, 108)
+    """The bench frame's geometry and camera at 96 x 54 (same aspect, same
+    view), rendered to convergence on the GPU (524,288 spp) against the
+    reference's 131,072-spp render: the glass caustics and small bright
+    lights make this frame's per-pixel variance high, so both sides need that
+    many samples for relMSE 1e-3 to measure bias rather than noise."""
+    spec = field1m_spec(96, 54)
     sid = gpu_ctx.upload(spec)
     try:
         mean_r, var_r = image_mean_var("field1m")
         gpu_ctx.film_clear(sid)
-        gpu_ctx.render([sid], 0, 32768, seed=1234, mode=CGPU_MODE_WAVEFRONT)
+        gpu_ctx.render([sid], 0, 524288, seed=1234, mode=CGPU_MODE_WAVEFRONT)
         s, q, n = gpu_ctx.film_read(sid)
         mean_g = s / n[..., None]
         var_g = (q / n[..., None] - mean_g ** 2) / n[..., None]
         r = rel_mse(mean_g, mean_r)
         z = (mean_g - mean_r) / np.sqrt(var_g + var_r + 1e-30)
         frac = float(np.mean(np.abs(z) > 2.576))
-        print("field1m 192x108: relMSE %.2e, z-test failures %.4f" % (r, frac))
+        print("field1m 96x54: relMSE %.2e, z-test failures %.4f" % (r, frac))
         assert r <= 1e-3
         assert frac <= 0.01 + 3 * np.sqrt(0.01 * 0.99 / z.size) + 0.005, frac
     finally:

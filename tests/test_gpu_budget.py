@@ -41,7 +41,7 @@ def test_render_reports_an_exhausted_budget(gpu_ctx, field, traversal):
         ref = render(gpu_ctx, sid, CGPU_MODE_WAVEFRONT)
         gpu_ctx.set_visit_budget(2)
         gpu_ctx.film_clear(sid)
-        gpu_ctx.render([sid], 0, 2, seed=9, mode=CGPU_MODE_WAVEFRONT)  # asynchronous: no status yet
+        gpu_ctx.render([sid], 0, 2, seed=9, mode=CGPU_MODE_WAVEFRONT, sync=False)  # asynchronous: no status yet
         with pytest.raises(CgpuError) as e:
             gpu_ctx.film_read(sid)
         assert e.value.status == TIMEOUT
@@ -63,7 +63,7 @@ def test_megakernel_and_queries_report_an_exhausted_budget(gpu_ctx, field):
     gpu_ctx.set_visit_budget(2)
     try:
         gpu_ctx.film_clear(sid)
-        gpu_ctx.render([sid], 0, 1, seed=9, mode=CGPU_MODE_MEGAKERNEL)
+        gpu_ctx.render([sid], 0, 1, seed=9, mode=CGPU_MODE_MEGAKERNEL, sync=False)
         with pytest.raises(CgpuError) as e:
             gpu_ctx.synchronize()
         assert e.value.status == TIMEOUT

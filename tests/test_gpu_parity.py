@@ -25,7 +25,7 @@ import pytest
 import oracle
 from cadise_gb300 import CGPU_MODE_MEGAKERNEL, CGPU_MODE_WAVEFRONT, CgpuError, abi, scenes
 from golden_scenes import FILTER_CASES, image, image_mean_var, specs, vectors
-from parity_util import EDGE, check_hits, edge_margin
+from parity_util import check_hits, near_edge
 
 pytestmark = pytest.mark.gpu
 
@@ -70,10 +70,8 @@ def test_any_hit_matches_reference(name, gpu_ctx, uploaded):
     occ = gpu_ctx.trace_any(sid, rays).astype(np.int32)
     prim, t, _, _ = gpu_ctx.trace_closest(sid, rays)
     # exclude grazing edge hits and occluders sitting on the t_max boundary
-    o, d = rays[:, :3].astype(np.float64), rays[:, 4:7].astype(np.float64)
-    m = edge_margin(flat, prim, o + d * t[:, None])
     boundary = (prim >= 0) & (np.abs(t - rays[:, 7]) <= 1e-5 * np.abs(rays[:, 7]))
-    keep = (m >= EDGE) & ~boundary
+    keep = ~near_edge(flat, prim, rays, t) & ~boundary
     assert keep.mean() >= 0.995, keep.mean()
     assert np.array_equal(occ[keep], v["trace_occluded"][keep])
     # occlusion is consistent with the closest hit on the same rays

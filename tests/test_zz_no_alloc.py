@@ -5,7 +5,7 @@ Collected last on purpose: it must pass alone and after every other GPU test
 has used the context.  Same paths (keyed by seed, scene, pixel, sample) and
 the same kernels, so the films agree; they may differ in the last FP64 bits
 because the two entry points split the samples into batches differently:
-rtol 1e-12 on the sums, the sample counts exactly."""
+rtol 1e-12 on the sums (and on a filtered film's sums of weights)."""
 import numpy as np
 import pytest
 
@@ -16,7 +16,8 @@ pytestmark = pytest.mark.gpu
 
 def films_close(a, b):
     (s1, q1, n1), (s2, q2, n2) = a, b
-    assert np.array_equal(n1, n2)
+    # sample counts exactly; a filtered film's sums of weights to FP64 order
+    np.testing.assert_allclose(n1, n2, rtol=1e-12, atol=0)
     np.testing.assert_allclose(s1, s2, rtol=1e-12, atol=1e-300)
     np.testing.assert_allclose(q1, q2, rtol=1e-12, atol=1e-300)
 
@@ -54,7 +55,8 @@ def test_noalloc_render_matches_render_on_two_calls(gpu_ctx, make, traversal):
         assert gpu_ctx.stats().batches == -(-300 // per) > 1
         gpu_ctx.render_noalloc(sid, 300, 60, seed=7)
         got = gpu_ctx.film_read(sid)
-        assert got[2].max() == 360
+        if spec.film_filter is None:
+            assert got[2].max() == 360  # sample counts (a filtered film holds sums of weights)
         films_close(got, ref)
         # and once more on its own: nothing carried over from the previous call
         gpu_ctx.film_clear(sid)
