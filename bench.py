@@ -290,16 +290,12 @@ def run_gpu(args, rank, world, local):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     achieved = ext_bytes / (ext_ms / 1e3) / 1e9 if ext_ms > 0 else None
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "extend_traffic.json")) as f:
-            tr = json.load(f)
-        # scale the captured per-launch traffic to this frame by closest rays
-        traffic = tr["dram_bytes_per_closest_ray"] * st.closest_rays / max(1, ext_launches)
-    except Exception:
-        pass
     rays_per_sample = (st.closest_rays + st.any_rays) / float(npix)
     prof = traversal_profile()
+    traffic = None
+    if prof and "c2" in prof:
+        # the DRAM bytes per closest-hit ray of the small-case capture, scaled to one launch of this frame
+        traffic = prof["c2"]["dram_bytes_per_closest_ray"] * st.closest_rays / max(1, ext_launches)
 
     adjoint = None
     if not args.no_adjoint:

@@ -39,7 +39,7 @@ The BASELINE-size scenes:
   rays through the reference BVH (closest hit and occlusion; no brute-force
   pass at this size), 10,000 path radiances at full-resolution film
   positions, and a converged render of the same geometry and camera at
-  96 x 54 (131,072 spp).  Its CRSD (100 MB of text) is not committed: the tests rebuild
+  96 x 54 (262,144 spp).  Its CRSD (100 MB of text) is not committed: the tests rebuild
   the scene with cadise_gb300.scenes and check it against the SHA-1 of its
   flattened arrays stored here; the rays are regenerated from their seed with
   exactly rounded operations only and checked against a stored SHA-1 too.
@@ -77,8 +77,8 @@ def big_scenes():
     return {
         "cornell256": (scenes.cornell_box(), None, 16384, 3000, 4000, True),
         # the image: the frame's camera and geometry at 96 x 54 (same aspect); its glass caustics and
-        # small bright lights need 131,072 spp for the reference's own noise to fall to relMSE ~2.5e-4
-        "field1m": (field1m_spec(), field1m_spec(96, 54), 131072, 100000, 10000, False),
+        # small bright lights need 262,144 spp for the reference's own noise to fall to relMSE ~1.5e-4
+        "field1m": (field1m_spec(), field1m_spec(96, 54), 262144, 100000, 10000, False),
     }
 
 

@@ -7,7 +7,7 @@
   frame's): 100,000 seeded rays against the reference BVH's closest hits and
   occlusion, 10,000 path radiances at full-resolution film positions against
   the reference estimator, and the same geometry and camera rendered at
-  96 x 54 against the reference's converged render (131,072 spp).  The scene (100 MB as
+  96 x 54 against the reference's converged render (262,144 spp).  The scene (100 MB as
   CRSD text) is rebuilt by the scene generator and must match the SHA-1 of
   the arrays the reference was given; the rays too.
 * The first configuration (the 256 x 256 Cornell box) is in
@@ -91,16 +91,19 @@ def rel_mse(x, ref):
 
 def test_field1m_image_converges_to_reference(gpu_ctx):
     """The bench frame's geometry and camera at 96 x 54 (same aspect, same
-    view), rendered to convergence on the GPU (524,288 spp) against the
-    reference's 131,072-spp render: the glass caustics and small bright
-    lights make this frame's per-pixel variance high, so both sides need that
-    many samples for relMSE 1e-3 to measure bias rather than noise."""
+    view), rendered on the GPU with as many samples per pixel as the
+    reference's converged render (262,144).  The glass caustics and small
+    bright lights give this frame heavy-tailed per-pixel radiance: with
+    unequal sample counts the rarer bright samples skew the two means and
+    the two variance estimates differently and the Welch z-test over-rejects
+    (measured: 2.7 % of pixels at a 4 : 1 ratio of samples; two GPU renders
+    of equal counts, 0.8 %), so the counts are equal."""
     spec = field1m_spec(96, 54)
     sid = gpu_ctx.upload(spec)
     try:
         mean_r, var_r = image_mean_var("field1m")
         gpu_ctx.film_clear(sid)
-        gpu_ctx.render([sid], 0, 524288, seed=1234, mode=CGPU_MODE_WAVEFRONT)
+        gpu_ctx.render([sid], 0, 262144, seed=1234, mode=CGPU_MODE_WAVEFRONT)
         s, q, n = gpu_ctx.film_read(sid)
         mean_g = s / n[..., None]
         var_g = (q / n[..., None] - mean_g ** 2) / n[..., None]

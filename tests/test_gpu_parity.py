@@ -297,3 +297,36 @@ def furnace_mask(spec):
     r = f * math.tan(math.asin(0.95 / 6.0)) - 1.5
     y, x = np.mgrid[0:spec.height, 0:spec.width] + 0.5
     return (x - spec.width / 2) ** 2 + (y - spec.height / 2) ** 2 <= r * r
+
+
+def test_rough_dielectric_smooth_limit_converges_to_reference_glass(gpu_ctx):
+    """The GGX dielectric has no reference counterpart; in its smooth limit
+    (roughness 0, alpha at its 1e-3 floor) it must render what the
+    reference's smooth glass renders.  The golden icosphere field with its
+    glass materials switched to the GGX dielectric at roughness 0, against
+    the reference's converged render of the glass field: relMSE and the
+    per-pixel z-test of the image tests."""
+    spec = specs()["field"]
+    n = 0
+    for m in spec.materials:
+        if m.type == scenes.GLASS:
+            m.type = scenes.ROUGH_DIELECTRIC
+            m.roughness = 0.0
+            n += 1
+    assert n > 0
+    sid = gpu_ctx.upload(spec)
+    try:
+        gpu_ctx.film_clear(sid)
+        gpu_ctx.render([sid], 0, 8192, seed=4321, mode=CGPU_MODE_WAVEFRONT)
+        s, q, cnt = gpu_ctx.film_read(sid)
+        mean_g = s / cnt[..., None]
+        var_g = (q / cnt[..., None] - mean_g ** 2) / cnt[..., None]
+        mean_r, var_r = image_mean_var("field")
+        r = rel_mse(mean_g, mean_r)
+        z = (mean_g - mean_r) / np.sqrt(var_g + var_r + 1e-30)
+        frac = float(np.mean(np.abs(z) > 2.576))
+        print("rough dielectric at roughness 0 vs reference glass: relMSE %.2e, z-test failures %.4f" % (r, frac))
+        assert r <= 1e-3
+        assert frac <= 0.01 + 3 * np.sqrt(0.01 * 0.99 / z.size) + 0.005, frac
+    finally:
+        gpu_ctx.release(sid)
