@@ -16,7 +16,7 @@ namespace {
 bool valid_tuning(const cgpu_tuning& t) {
     auto ok_block = [](int b) { return b >= 32 && b <= 1024 && b % 32 == 0; };
     return ok_block(t.block_trace) && ok_block(t.block_shade) && (t.traversal >= 0 && t.traversal <= 3) &&
-           (t.reorder >= 0 && t.reorder <= 3) && (t.refill_closest >= 0 && t.refill_closest <= 32) &&
+           (t.reorder >= 0 && t.reorder <= 4) && (t.refill_closest >= 0 && t.refill_closest <= 32) &&
            (t.refill_any >= 0 && t.refill_any <= 32);
 }
 
@@ -104,7 +104,7 @@ cgpu_status cgpu_tuning_set(cgpu_ctx* ctx, const cgpu_tuning* t) {
     if (!ctx || !t) return CGPU_ERR_INVALID_ARGUMENT;
     if (!valid_tuning(*t))
         return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT,
-                       "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0 to 3, reorder 0 to 3, "
+                       "tuning: block sizes must be multiples of 32 in [32, 1024], traversal 0 to 3, reorder 0 to 4, "
                        "refill thresholds 0 to 32");
     cudaStreamSynchronize(ctx->stream);
     apply(ctx, *t);

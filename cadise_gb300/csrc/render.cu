@@ -1145,9 +1145,9 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     auto ext_sorted = sph ? (counting ? CG_PICK_SORTED(true, true) : CG_PICK_SORTED(false, true))
                           : (counting ? CG_PICK_SORTED(true, false) : CG_PICK_SORTED(false, false));
 #undef CG_PICK_SORTED
-    // reorder 1 / 2 / 3: 9 / 7 / 4 Morton bits per axis, 4 / 3 / 2 sort passes of 8 bits; an odd
-    // pass count leaves the sorted values in the second buffer
-    const int sort_bits = ctx->tuning.reorder == 1 ? 9 : ctx->tuning.reorder == 2 ? 7 : 4;
+    // reorder 1 / 2 / 3 / 4: 9 / 7 / 4 / 0 Morton bits per axis, 4 / 3 / 2 / 1 sort passes of 8 bits
+    // (4: the direction octant alone); an odd pass count leaves the sorted values in the second buffer
+    const int sort_bits = ctx->tuning.reorder == 1 ? 9 : ctx->tuning.reorder == 2 ? 7 : ctx->tuning.reorder == 3 ? 4 : 0;
     const int sort_passes = (3 + 3 * sort_bits + 7) / 8;
     if (reorder) a.sorted = ctx->sort.vals[sort_passes & 1];
     const int gkeys = grid_for(ctx, k_ray_keys, 256, uint64_t(paths) * 2);

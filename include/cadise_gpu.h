@@ -379,8 +379,9 @@ typedef struct cgpu_tuning {
     int32_t reorder;       /* 1, 2, 3: before each closest-hit pass after the first, sort its rays by
                               direction octant and origin (Morton order of 9, 7 or 4 bits per axis in the
                               scene bounds; 4, 3 or 2 radix passes), so that a warp traces neighbouring
-                              rays (traversal 0 and 2); 0: queue order (default; cgpu_autotune does not
-                              search it: on the 1 M-triangle field the sort costs about what it saves) */
+                              rays (traversal 0, 2 and 3); 4: by direction octant alone (one radix pass);
+                              0: queue order (default; cgpu_autotune does not search it: on the
+                              1 M-triangle field the sort costs about what it saves) */
     int32_t refill_closest;/* queue compaction of the persistent closest-hit pass (traversal 2 and 3):
                               after each round of leaves a warp whose unfinished rays number fewer than
                               this stores its finished lanes' hits and takes the next rays of the queue

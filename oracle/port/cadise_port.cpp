@@ -1450,6 +1450,29 @@ D3 bsdfDual(const Scene& s, int mi, const Surface& si, const V3& L) {
         const V3 F = schlick(m.f0, L.dot(H));
         return d3(F) * (ggxDG(s, mi, m, V, L, N, H) * (1.0 / (4.0 * std::abs(double(VdotN) * LdotN))));
     }
+    if (m.type == CGPU_BSDF_DIELECTRIC_GGX) {
+        // the FP32 value of the path, times d ln(D G) / d theta: roughness
+        // enters the Walter et al. BRDF / BTDF only through D and G, at the
+        // reflection or refraction half vector of roughDielectric
+        V3 f;
+        float pdf;
+        roughDielectric(m, albedoAt(m, si.uvw), V, L, N, &f, &pdf);
+        if (f.isZero()) return d3(V3(0.0f));
+        const float cv = V.dot(N), cl = L.dot(N);
+        const V3 Nv = cv > 0.0f ? N : -N;
+        V3 H;
+        if (cv * cl > 0.0f) {
+            H = (V + L).normalize();
+        } else {
+            const float etaV = cv > 0.0f ? m.iorOuter : m.iorInner;
+            const float etaL = cv > 0.0f ? m.iorInner : m.iorOuter;
+            H = (V + L * (etaL / etaV)).normalize();
+            if (H.dot(Nv) < 0.0f) H = -H;
+        }
+        const Dual dg = ggxDG(s, mi, m, V, L, Nv, H);
+        if (dg.v == 0.0) return d3(f);
+        return d3(f) * (dg * (1.0 / dg.v));
+    }
     return d3(bsdfEval(m, si, L));  // no differentiable parameter of this BSDF here
 }
 
@@ -1510,7 +1533,7 @@ D3 estimateDual(const Scene& s, Ray ray, Rng& rng) {
         if (!bs.valid()) break;
         const float LdotN = bs.L.absDot(si.Ns);
         Tf *= bs.f * LdotN / bs.pdf;
-        if (m.type == CGPU_BSDF_LAMBERTIAN || m.type == CGPU_BSDF_CONDUCTOR_GGX)
+        if (m.type == CGPU_BSDF_LAMBERTIAN || m.type == CGPU_BSDF_CONDUCTOR_GGX || m.type == CGPU_BSDF_DIELECTRIC_GGX)
             T = T * (bsdfDual(s, pr.material, si, bs.L) * (double(LdotN) / bs.pdf));
         else
             T = T * d3(bs.f * LdotN / bs.pdf);

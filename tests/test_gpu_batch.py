@@ -83,7 +83,7 @@ def test_tuning_does_not_change_results(gpu_ctx, uneven):
     # closest-hit queues sorted by direction octant and origin (reorder) with traversals 0 and 2;
     # the queue-compaction (refill) thresholds of the persistent passes at their extremes
     for traversal, reorder, rc, ra in ((1, 0, 0, 0), (2, 0, 0, 0), (3, 0, 0, 0), (0, 1, 0, 0), (2, 2, 0, 0),
-                                       (3, 3, 0, 0), (3, 0, 1, 32), (3, 0, 32, 1), (2, 0, 20, 0), (3, 0, 6, 24)):
+                                       (3, 3, 0, 0), (3, 4, 0, 0), (3, 0, 1, 32), (3, 0, 32, 1), (2, 0, 20, 0), (3, 0, 6, 24)):
         gpu_ctx.set_tuning(64, 256, 1 << 14, traversal=traversal, reorder=reorder, refill_closest=rc,
                            refill_any=ra)
         for s in sids:

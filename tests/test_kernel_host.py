@@ -175,6 +175,26 @@ def test_kernel_adjoint_matches_fp64_reference(khc):
     assert np.all(np.abs(got - ref) <= 1e-3 * np.abs(ref) + 1e-4 * np.abs(ref).max()), np.stack([got, ref])
 
 
+def test_kernel_adjoint_roughness_of_every_ggx_bsdf_matches_fp64_reference(khc):
+    """The same on the close-up of two GGX conductors and a GGX (rough)
+    dielectric: d loss / d roughness of each, reflection and refraction
+    half vectors, against the oracle's FP64 forward mode."""
+    spec = scenes.roughness_scene(width=32, height=24)
+    flat = abi.flatten(spec)
+    h = Host(khc, flat)
+    W = np.random.default_rng(8).normal(size=(spec.height, spec.width, 3)).astype(np.float32)
+    spp, seed, scene_index = 16, 31, 0
+    gt, gr, gl = np.zeros(1), np.zeros(len(spec.materials)), np.zeros((len(spec.lights), 3))
+    khc.khc_adjoint(h.h, seed, scene_index, spp, _p(W), _p(gt), _p(gr), _p(gl))
+    h.close()
+    ggx = [i for i, m in enumerate(spec.materials) if m.type in (scenes.CONDUCTOR, scenes.ROUGH_DIELECTRIC)]
+    assert any(spec.materials[i].type == scenes.ROUGH_DIELECTRIC for i in ggx)
+    ref = oracle.PortScene(flat).adjoint_fp64(seed, spp, W, [(1, i, 0) for i in ggx], scene_index=scene_index)
+    got = gr[ggx]
+    assert np.all(ref != 0)
+    assert np.all(np.abs(got - ref) <= 1e-3 * np.abs(ref) + 1e-4 * np.abs(ref).max()), np.stack([got, ref])
+
+
 @pytest.mark.parametrize("cap", [1, 63, 20000, 1 << 14, 2073600, (1 << 21) + 5])
 def test_wavefront_buffer_layout_fits(khc, cap):
     """The path-state arrays of the wavefront stay inside the block they are
