@@ -271,6 +271,8 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     if (st == CGPU_OK && d->prim_normals) st = upload(ctx, sl, d->prim_normals, size_t(np) * 9, &dnorm);
     if (st == CGPU_OK && d->prim_uvws) st = upload(ctx, sl, d->prim_uvws, size_t(np) * 9, &duvw);
     if (st == CGPU_OK) st = upload(ctx, sl, hs.rect_frames.data(), hs.rect_frames.size(), &drect);
+    uint32_t* drank = nullptr;
+    if (st == CGPU_OK) st = upload(ctx, sl, hs.prim_rank.data(), hs.prim_rank.size(), &drank);
     float* dlcdf = nullptr;
     if (st == CGPU_OK && !hs.light_cdf.empty()) st = upload(ctx, sl, hs.light_cdf.data(), hs.light_cdf.size(), &dlcdf);
     const size_t npix = size_t(d->width) * size_t(d->height);
@@ -304,6 +306,7 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.prim_normals = dnorm;
     S.prim_uvws = duvw;
     S.rect_frames = drect;
+    S.prim_rank = drank;
     S.light_cdf = dlcdf;
     S.num_lights = int(hs.lights.size());
     S.env_light = hs.env_light;
@@ -316,6 +319,10 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
     S.filter = hs.filter;
     S.visit_budget = ctx->visit_budget ? ctx->visit_budget : auto_visit_budget(hs.nodes.size());
     S.status = ctx->d_status;
+    {
+        const float c[3] = {hs.cam.pos.x, hs.cam.pos.y, hs.cam.pos.z};
+        S.tie_abs = tie_window_abs(hs.info.bounds_min, hs.info.bounds_max, c);
+    }
     S.bounds_lo = make_float3(hs.info.bounds_min[0], hs.info.bounds_min[1], hs.info.bounds_min[2]);
     {
         float inv[3];

@@ -145,7 +145,7 @@ CG_D void mk_path(const SceneD& S, float3 o, float3 d, Rng& rng, float3* Lout, f
                 const int prim_l =
                     slot >= 0 ? __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + slot)).w) : 0x7FFFFFFF;
                 if (COUNT) ++*nany;
-                if (!occluded_before<COUNT, SPH>(S, mr, mh.x, prim_l, ta)) {
+                if (!occluded_before<COUNT, SPH>(S, mr, mh.x, prim_l, slot, ta)) {
                     if (slot >= 0) {
                         HitD hit;
                         hit.t = mh.x;

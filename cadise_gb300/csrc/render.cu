@@ -180,7 +180,7 @@ __global__ void k_wf_mis_occl(RenderArgs a, int b) {
         const int slot = __float_as_int(mh.y);
         const int prim_l = slot >= 0 ? __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + slot)).w) : 0x7FFFFFFF;
         if (COUNT) ++nany;
-        if (occluded_before<COUNT, SPH>(S, r, mh.x, prim_l, &tc)) continue;
+        if (occluded_before<COUNT, SPH>(S, r, mh.x, prim_l, slot, &tc)) continue;
         const float4 mb = w.mis_b[p], ma = w.mis_a[p];
         float3 add, X = splat3(0.0f);
         int xlight = -1;
@@ -431,10 +431,10 @@ __global__ void __maxnreg__(56) k_wf_extend_pww(RenderArgs a, int b) {
     bool cont = false;   // continuation ray (else MIS ray)
     bool drained = false;
     uint32_t left = 0;  // node and leaf visits this ray has left (over_budget)
-    auto pop = [&]() -> uint32_t {
+    auto pop = [&](const SceneD& S) -> uint32_t {
         while (sp > 0) {
             --sp;
-            if (stack.dist(sp) <= tcur * 1.00000036f) return stack.entry(sp);
+            if (stack.dist(sp) <= tie_hi(S, tcur) * 1.00000036f) return stack.entry(sp);
         }
         return kNoEntry;
     };
@@ -470,17 +470,17 @@ __global__ void __maxnreg__(56) k_wf_extend_pww(RenderArgs a, int b) {
                     break;
                 }
                 cur = visit_node<false, COUNT>(S, r, cur, tcur, stack, sp, &tc);
-                if (cur == kNoEntry) cur = pop();
+                if (cur == kNoEntry) cur = pop(S);
                 if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
-                    cur = pop();
+                    cur = pop(S);
                 }
                 if (!__any_sync(__activemask(), leaf == kNoEntry)) break;
             }
             if (leaf == kNoEntry) {
                 if (cur == kNoEntry) break;  // the ray is done
                 leaf = cur;
-                cur = pop();
+                cur = pop(S);
             }
             while (leaf != kNoEntry) {
                 if (over_budget(S, left)) {
@@ -491,7 +491,7 @@ __global__ void __maxnreg__(56) k_wf_extend_pww(RenderArgs a, int b) {
                 leaf = kNoEntry;
                 if (cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
-                    cur = pop();
+                    cur = pop(S);
                 }
             }
             if (cur == kNoEntry) break;  // the ray is done
@@ -501,8 +501,10 @@ __global__ void __maxnreg__(56) k_wf_extend_pww(RenderArgs a, int b) {
             HitD hit;
             hit.t = tcur;
             hit.slot = hslot;
-            hit.u = hu;
-            hit.v = hv;
+            // the shading recomputes the surface coordinates from the hit
+            // point (hit_point), so the traversal's need not be kept
+            hit.u = 0.0f;
+            hit.v = 0.0f;
             const int key = extend_finish<ADJ>(w, S, p, cont, r.o, r.d, hslot >= 0, hit, &a.adj);
             grouped_push(qmat, cnt + 3, key, p);
             i = -1;

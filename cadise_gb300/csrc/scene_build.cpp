@@ -2,9 +2,11 @@
 #include "scene_build.h"
 
 #include "bvh_build.h"
+#include "tie_order.h"
 
 #include <algorithm>
 #include <chrono>
+#include <future>
 #include <cmath>
 #include <cstring>
 
@@ -179,6 +181,8 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
     for (float f : tv) {
         if (!std::isfinite(f)) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "non-finite vertex");
     }
+    // the reference's tie order, built on other threads while the BVH builds
+    std::future<std::vector<uint32_t>> ranks = std::async(std::launch::async, [d] { return reference_visit_ranks(d); });
     Bvh4Result bvh;
     std::string berr;
     const auto tb = std::chrono::steady_clock::now();
@@ -448,6 +452,7 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         cdf[n] = 1.0f;
         out->light_cdf = std::move(cdf);
     }
+    out->prim_rank = ranks.get();
     return CGPU_OK;
 }
 
@@ -465,6 +470,7 @@ SceneD host_view(HostScene& hs, const cgpu_scene_desc* d) {
     S.prim_normals = d->prim_normals;
     S.prim_uvws = d->prim_uvws;
     S.rect_frames = hs.rect_frames.data();
+    S.prim_rank = hs.prim_rank.empty() ? nullptr : hs.prim_rank.data();
     S.light_cdf = hs.light_cdf.empty() ? nullptr : hs.light_cdf.data();
     S.num_lights = int(hs.lights.size());
     S.env_light = hs.env_light;
@@ -486,6 +492,10 @@ SceneD host_view(HostScene& hs, const cgpu_scene_desc* d) {
     }
     S.visit_budget = auto_visit_budget(hs.nodes.size());
     S.status = nullptr;
+    {
+        const float c[3] = {hs.cam.pos.x, hs.cam.pos.y, hs.cam.pos.z};
+        S.tie_abs = tie_window_abs(hs.info.bounds_min, hs.info.bounds_max, c);
+    }
     return S;
 }
 

@@ -25,6 +25,7 @@ struct HostScene {
     std::vector<float> env_marg, env_cond;
     std::vector<TextureD> textures;  // texel pointers into the caller's desc
     std::vector<float> rect_frames;  // vB, eA, eB per rectangle
+    std::vector<uint32_t> prim_rank; // 8 per primitive (reference_visit_ranks)
     std::vector<float> light_cdf;    // power light cluster: num_lights + 1 CDF values; empty: uniform
     CameraD cam{};
     FilterD filter{};

@@ -200,6 +200,7 @@ struct SceneD {
     const float* prim_normals;  // 9 per primitive or null
     const float* prim_uvws;     // 9 per primitive or null
     const float* rect_frames;   // 9 per rectangle (vB, eA, eB), indexed by the rectangle index
+    const uint32_t* prim_rank;  // 8 per primitive: the reference's tie order per direction octant, or null
     const float* light_cdf;     // power light cluster: num_lights + 1 CDF values; null: uniform pick
     int num_lights;  // area lights + environment
     int env_light;   // index of the environment light, -1 if none
@@ -215,7 +216,21 @@ struct SceneD {
     // the context's status word that counts the rays that ran out.
     uint32_t visit_budget;
     uint32_t* status;
+    // absolute part of the closest-hit tie window (tie_hi, traverse.cuh):
+    // 2^-16 of the largest coordinate magnitude of the scene and camera
+    float tie_abs;
 };
+
+// SceneD::tie_abs of a scene with bounds [lo, hi] seen from camera position c.
+inline float tie_window_abs(const float* lo, const float* hi, const float* c) {
+    float m = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        m = fmaxf(m, fabsf(lo[k]));
+        m = fmaxf(m, fabsf(hi[k]));
+        m = fmaxf(m, fabsf(c[k]));
+    }
+    return ldexpf(m, -16);
+}
 
 // The automatic visit budget of a tree of `nodes` 4-wide nodes.  A stack
 // traversal reaches every inner node and every leaf at most once (each is

@@ -203,13 +203,20 @@ CG_D SurfaceD surface_at(const SceneD& S, float3 o, float3 d, const HitD& h) {
     float3 Ng = cross(B - A, C - A);
     Ng = is_zero(Ng) ? mk(0.0f, 1.0f, 0.0f) : normalize(Ng);
     si.Ng = Ng;
+    // the vertex normals start as the face normal and a mesh's own replace
+    // them where non-zero (triangle.cpp:15-41, triangleMesh.cpp:24-28); the
+    // shading normal always interpolates them, which rounds differently from
+    // the face normal itself even on a flat mesh (triangle.cpp:125-160)
+    float3 nA = Ng, nB = Ng, nC = Ng;
     if (S.prim_normals) {
         const float* n = S.prim_normals + 9 * size_t(si.prim);
-        const float3 Ns = mk(n[0], n[1], n[2]) * b0 + mk(n[3], n[4], n[5]) * b1 + mk(n[6], n[7], n[8]) * b2;
-        si.Ns = is_zero(Ns) ? Ng : normalize(Ns);
-    } else {
-        si.Ns = Ng;
+        const float3 a3 = mk(n[0], n[1], n[2]), b3 = mk(n[3], n[4], n[5]), c3 = mk(n[6], n[7], n[8]);
+        if (!is_zero(a3)) nA = a3;
+        if (!is_zero(b3)) nB = b3;
+        if (!is_zero(c3)) nC = c3;
     }
+    const float3 Ns = nA * b0 + nB * b1 + nC * b2;
+    si.Ns = is_zero(Ns) ? Ng : normalize(Ns);
     if (S.prim_uvws) {
         const float* u = S.prim_uvws + 9 * size_t(si.prim);
         si.uvw = mk(u[0], u[1], u[2]) * b0 + mk(u[3], u[4], u[5]) * b1 + mk(u[6], u[7], u[8]) * b2;

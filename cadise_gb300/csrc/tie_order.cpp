@@ -1,0 +1,246 @@
+// Exact-tie ranks: the reference's binary BVH over the scene's primitives
+// (shape only) and, per direction octant, the order in which its closest-hit
+// traversal reaches their leaves.
+#include "tie_order.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cfloat>
+#include <future>
+#include <thread>
+
+namespace cg {
+namespace {
+
+struct Box3 {
+    float lo[3], hi[3];
+};
+
+// TAABB's empty box (tAabb.ipp:13-17): the upper corner starts at FLT_MIN,
+// the smallest positive float, and unionWith is a component min / max.
+inline Box3 empty_box() {
+    Box3 b;
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = FLT_MAX;
+        b.hi[k] = FLT_MIN;
+    }
+    return b;
+}
+inline void grow(Box3& b, const float* lo, const float* hi) {
+    for (int k = 0; k < 3; ++k) {
+        b.lo[k] = std::min(b.lo[k], lo[k]);
+        b.hi[k] = std::max(b.hi[k], hi[k]);
+    }
+}
+// half the surface area; the reference's SAH divides full areas by a full
+// area, which rounds to the same ratio (both scale by exactly 2)
+inline float half_area(const Box3& b) {
+    const float x = b.hi[0] - b.lo[0], y = b.hi[1] - b.lo[1], z = b.hi[2] - b.lo[2];
+    return x * y + y * z + z * x;
+}
+
+struct Tree {
+    // per node: split axis (internal) or -1 (leaf); children; leaf range of `idx`
+    std::vector<int8_t> axis;
+    std::vector<int32_t> first, second, begin, count;
+};
+
+class Builder {
+public:
+    Builder(const cgpu_scene_desc* d) : n_(d->num_primitives), lo_(3 * size_t(n_)), hi_(3 * size_t(n_)), c_(3 * size_t(n_)) {
+        for (uint32_t i = 0; i < n_; ++i) prim_box(d, i);
+        idx_.resize(n_);
+        for (uint32_t i = 0; i < n_; ++i) idx_[i] = int32_t(i);
+        // at most 2n - 1 nodes; slots are taken with an atomic counter
+        const size_t cap = n_ > 0 ? 2 * size_t(n_) - 1 : 1;
+        tree_.axis.assign(cap, -1);
+        tree_.first.assign(cap, -1);
+        tree_.second.assign(cap, -1);
+        tree_.begin.assign(cap, 0);
+        tree_.count.assign(cap, 0);
+    }
+
+    void build() {
+        next_.store(0);
+        if (n_ > 0) node(0, int32_t(n_), 0);
+    }
+
+    std::vector<uint32_t> ranks() const {
+        std::vector<uint32_t> r(8 * size_t(n_));
+        if (n_ == 0) return r;
+        std::vector<std::thread> th;
+        for (int o = 0; o < 8; ++o) th.emplace_back([this, o, &r] { rank_octant(o, r.data()); });
+        for (auto& t : th) t.join();
+        return r;
+    }
+
+private:
+    // Primitive bounds as the reference computes them: the vertices' box
+    // expanded by 0.0001 (a rectangle's fourth corner is vB + eA + eB), a
+    // sphere's (c - r, c + r) expanded by 0.0001.
+    void prim_box(const cgpu_scene_desc* d, uint32_t i) {
+        const int kind = d->prim_kind ? d->prim_kind[i] : CGPU_PRIM_TRIANGLE;
+        const float* v = d->prim_vertices + 9 * size_t(i);
+        float* lo = &lo_[3 * size_t(i)];
+        float* hi = &hi_[3 * size_t(i)];
+        if (kind == CGPU_PRIM_SPHERE) {
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = (v[k] - v[3]) - 0.0001f;
+                hi[k] = (v[k] + v[3]) + 0.0001f;
+            }
+        } else {
+            float p[4][3];
+            int np = 3;
+            for (int j = 0; j < 3; ++j)
+                for (int k = 0; k < 3; ++k) p[j][k] = v[3 * j + k];
+            if (kind == CGPU_PRIM_RECTANGLE) {  // v = (vA, vB, vC)
+                for (int k = 0; k < 3; ++k) {
+                    const float eA = v[k] - v[3 + k], eB = v[6 + k] - v[3 + k];
+                    p[3][k] = (v[3 + k] + eA) + eB;
+                }
+                np = 4;
+            }
+            for (int k = 0; k < 3; ++k) {
+                float a = p[0][k], b = p[0][k];
+                for (int j = 1; j < np; ++j) {
+                    a = std::min(a, p[j][k]);
+                    b = std::max(b, p[j][k]);
+                }
+                lo[k] = a - 0.0001f;
+                hi[k] = b + 0.0001f;
+            }
+        }
+        for (int k = 0; k < 3; ++k) c_[3 * size_t(i) + k] = (lo[k] + hi[k]) * 0.5f;
+    }
+
+    int32_t make_leaf(int32_t id, int32_t b, int32_t e) {
+        tree_.axis[size_t(id)] = -1;
+        tree_.begin[size_t(id)] = b;
+        tree_.count[size_t(id)] = e - b;
+        return id;
+    }
+
+    // BvhBuilder::_buildBinaryNodesRecursively on idx_[b, e)
+    int32_t node(int32_t b, int32_t e, int depth) {
+        const int32_t id = next_.fetch_add(1);
+        const int32_t count = e - b;
+        if (count <= 1) return make_leaf(id, b, e);
+        Box3 box = empty_box(), cbox = empty_box();
+        for (int32_t i = b; i < e; ++i) {
+            const size_t p = size_t(idx_[size_t(i)]);
+            grow(box, &lo_[3 * p], &hi_[3 * p]);
+            grow(cbox, &c_[3 * p], &c_[3 * p]);
+        }
+        float ext[3];
+        for (int k = 0; k < 3; ++k) ext[k] = cbox.hi[k] - cbox.lo[k];
+        int axis = 0;
+        if (ext[1] > ext[axis]) axis = 1;
+        if (ext[2] > ext[axis]) axis = 2;
+        if (cbox.lo[axis] == cbox.hi[axis]) return make_leaf(id, b, e);
+        const float* c = c_.data();
+        int32_t* ix = idx_.data();
+        int32_t mid;
+        if (count <= 2) {
+            // the equal split (_canSplitWithEqual): the lower centroid first
+            mid = b + (count + 1) / 2;
+            std::nth_element(ix + b, ix + mid, ix + e,
+                             [c, axis](int32_t x, int32_t y) { return c[3 * size_t(x) + axis] < c[3 * size_t(y) + axis]; });
+        } else {
+            constexpr int kBuckets = 12;
+            const float cmin = cbox.lo[axis];
+            const float inv_ext = 1.0f / ext[axis];
+            auto bucket = [c, axis, cmin, inv_ext](int32_t p) {
+                const size_t k = size_t((c[3 * size_t(p) + axis] - cmin) * inv_ext * float(kBuckets));
+                return k == size_t(kBuckets) ? size_t(kBuckets - 1) : k;
+            };
+            int32_t bn[kBuckets] = {0};
+            Box3 bb[kBuckets];
+            for (auto& x : bb) x = empty_box();
+            for (int32_t i = b; i < e; ++i) {
+                const int32_t p = ix[size_t(i)];
+                const size_t k = bucket(p);
+                ++bn[k];
+                grow(bb[k], &lo_[3 * size_t(p)], &hi_[3 * size_t(p)]);
+            }
+            const float inv_area = 1.0f / half_area(box);
+            float best = FLT_MAX;
+            size_t best_split = size_t(kBuckets);
+            for (int s = 0; s < kBuckets - 1; ++s) {
+                Box3 A = empty_box(), B = empty_box();
+                int32_t na = 0, nb = 0;
+                for (int k = 0; k <= s; ++k) {
+                    grow(A, bb[k].lo, bb[k].hi);
+                    na += bn[k];
+                }
+                for (int k = s + 1; k < kBuckets; ++k) {
+                    grow(B, bb[k].lo, bb[k].hi);
+                    nb += bn[k];
+                }
+                // an empty side has an infinite area and its cost 0 x inf is
+                // NaN in the reference, which never compares below the best
+                if (na == 0 || nb == 0) continue;
+                const float cost = 0.125f + (half_area(A) * inv_area * float(na) + half_area(B) * inv_area * float(nb));
+                if (cost < best) {
+                    best = cost;
+                    best_split = size_t(s);
+                }
+            }
+            if (best >= float(count)) return make_leaf(id, b, e);
+            mid = int32_t(std::partition(ix + b, ix + e, [&](int32_t p) { return bucket(p) <= best_split; }) - ix);
+            if (mid == b || mid == e) return make_leaf(id, b, e);
+        }
+        tree_.axis[size_t(id)] = int8_t(axis);
+        int32_t f;
+        if (count >= kParallelRange && depth < kParallelDepth) {
+            auto left = std::async(std::launch::async, [this, b, mid, depth] { return node(b, mid, depth + 1); });
+            tree_.second[size_t(id)] = node(mid, e, depth + 1);
+            f = left.get();
+        } else {
+            f = node(b, mid, depth + 1);
+            tree_.second[size_t(id)] = node(mid, e, depth + 1);
+        }
+        tree_.first[size_t(id)] = f;
+        return id;
+    }
+
+    // Depth-first leaf order of octant o: at a node split on axis k the
+    // reference takes the second child first when the ray runs towards -k.
+    void rank_octant(int o, uint32_t* r) const {
+        std::vector<int32_t> stack;
+        stack.push_back(0);
+        uint32_t pos = 0;
+        while (!stack.empty()) {
+            const int32_t id = stack.back();
+            stack.pop_back();
+            const int ax = tree_.axis[size_t(id)];
+            if (ax < 0) {
+                const int32_t b = tree_.begin[size_t(id)], n = tree_.count[size_t(id)];
+                for (int32_t i = 0; i < n; ++i) r[8 * size_t(idx_[size_t(b + i)]) + size_t(o)] = pos++;
+                continue;
+            }
+            const bool second_first = ((o >> ax) & 1) != 0;
+            // the child visited first is pushed last
+            stack.push_back(second_first ? tree_.first[size_t(id)] : tree_.second[size_t(id)]);
+            stack.push_back(second_first ? tree_.second[size_t(id)] : tree_.first[size_t(id)]);
+        }
+    }
+
+    static constexpr int32_t kParallelRange = 1 << 15;
+    static constexpr int kParallelDepth = 5;
+
+    uint32_t n_;
+    std::vector<float> lo_, hi_, c_;
+    std::vector<int32_t> idx_;
+    Tree tree_;
+    std::atomic<int32_t> next_{0};
+};
+
+}  // namespace
+
+std::vector<uint32_t> reference_visit_ranks(const cgpu_scene_desc* d) {
+    Builder b(d);
+    b.build();
+    return b.ranks();
+}
+
+}  // namespace cg

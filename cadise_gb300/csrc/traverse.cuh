@@ -9,10 +9,12 @@
 // (Woop, Benthin & Wald, "Watertight Ray/Triangle Intersection", JCGT 2013):
 // the three edge functions are evaluated in a ray-aligned sheared space with
 // exactly rounded products (no contraction), falling back to FP64 when one of
-// them is exactly zero, so no ray slips between adjoining triangles (a ray
-// through a shared edge or vertex may hit both at the same t: the lower
-// triangle slot is kept).  Box tests widen t_max by 1 + 2 gamma(3) to stay
-// conservative.
+// them is exactly zero, so no ray slips between adjoining triangles.  Two
+// primitives met within a few roundings of each other (a ray through an edge
+// two triangles share, coplanar overlapping quads) are ordered by the
+// reference's own test and tie order (tie_prefers), so the closest hit is the
+// reference's there too.  Box tests widen t_max by 1 + 2 gamma(3) (and by the
+// tie window for closest hits) to stay conservative.
 #pragma once
 
 #include "scene_device.cuh"
@@ -110,6 +112,16 @@ CG_D void load_node(const Bvh4Node* nodes, uint32_t idx, const RayPre& r, float4
     q[3] = __ldg(p + 3);
 }
 
+// Closest-hit tie window (tie_prefers): candidates whose distances lie within
+// tie_hi of each other are ordered by the reference's rule, so closest-hit
+// bounds are widened to tie_hi, and box distances by a further 1 + 2 gamma(3).
+// The window is relative (kTieSlack) plus absolute (SceneD::tie_abs, 2^-16 of
+// the scene's coordinate scale): the watertight distance of a short ray
+// carries the rounding of vertex coordinates of the scene's magnitude, up to
+// 3e-6 of the scale on the reference's test scenes.
+constexpr float kTieSlack = 1.000004f;
+CG_D float tie_hi(const SceneD& S, float t) { return t * kTieSlack + S.tie_abs; }
+
 // Child box distances; tnear = +inf marks a miss.  Empty child slots hold
 // entry 0 (the root, never anyone's child) and are always a miss.  Per axis
 // the slab distances are a + q * b with a = (origin - o) / d and b = step / d
@@ -162,24 +174,6 @@ CG_D bool over_budget(const SceneD& S, uint32_t& left) {
     }
     if (S.status) atomicAdd(S.status, 1u);
     return true;
-}
-
-// Which of two hits a closest-hit query keeps: the smaller distance, and on
-// an exact tie (a ray through an edge shared by two triangles hits both at
-// the same t) the lower primitive index, so that the answer depends neither
-// on the order in which the traversal met them nor on the BVH (which builder,
-// which leaf order).  The two halves of a rectangle share a primitive; on a
-// tie between them (a ray through the diagonal) the lower record slot, the
-// rule mis_light_hit applies to a light's halves too.  Either half gives the
-// same hit point (hit_point recomputes t and the edge coordinates from the
-// rectangle's own frame), so the answer does not depend on the half.
-// `prim` / `slot` are the candidate's; the kept hit's primitive is loaded
-// only on a tie.
-CG_D bool closer_hit(const SceneD& S, float t, int prim, int slot, float tcur, int hslot) {
-    if (hslot < 0) return t <= tcur;
-    if (t != tcur) return t < tcur;
-    const int kept = __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + hslot)).w);
-    return prim < kept || (prim == kept && slot < hslot);
 }
 
 // Traversal stacks: kStackSize entries of (child entry, entry distance),
@@ -248,7 +242,7 @@ CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcu
     load_node(S.nodes, e, r, q);
     if (COUNT) cnt->nodes++;
     float tn[4];
-    child_hits(r, q, tcur, tn);
+    child_hits(r, q, ANY ? tcur : tie_hi(S, tcur), tn);
     uint32_t ce[4] = {__float_as_uint(q[1].x), __float_as_uint(q[1].y), __float_as_uint(q[1].z),
                       __float_as_uint(q[1].w)};
     if (!ANY) {
@@ -302,6 +296,103 @@ CG_D bool sphere_test(const RayPre& r, float3 G, float rad, float tmax, float* t
     return true;
 }
 
+// ---- exact ties --------------------------------------------------------
+// Two candidates of a closest-hit query whose traversal (watertight)
+// distances lie within the tie window (tie_hi, defined with the box test) of
+// each other are ordered by the reference's own rule instead: its hit test of
+// each primitive (ref_hit), the smaller of its distances, and on an exact tie
+// the primitive its BVH traversal reaches last - the higher rank of the ray's
+// direction octant (tie_order.h).  The traversal widens its closest-hit
+// bounds by the same window, so every candidate inside it reaches the
+// comparison.  Outside the window the watertight distances decide.
+
+// Octant of a ray direction: bit k set when component k is negative (-0
+// included), the reference's directionIsNegative (bvhAccelerator.cpp:44-48).
+CG_D int ray_octant(const RayPre& r) {
+    return int(__float_as_uint(r.d.x) >> 31) | int(__float_as_uint(r.d.y) >> 31) << 1 |
+           int(__float_as_uint(r.d.z) >> 31) << 2;
+}
+
+// The reference's hit test of the primitive of record `slot` on the ray's
+// [tmin, tmax], in its FP32 order: Triangle::isIntersecting (Moller-Trumbore,
+// triangle.cpp:54-89), Rectangle::isIntersecting (plane distance and edge
+// coordinates, rectangle.cpp:49-75), Sphere::isIntersecting (sphere_test is
+// already the reference's).  Its distance in *tout.
+CG_D bool ref_hit(const SceneD& S, const RayPre& r, int slot, float* tout) {
+    const float4* tp = reinterpret_cast<const float4*>(S.tris + slot);
+    const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
+    const uint32_t flags = __float_as_uint(c.w);
+    if ((flags & 3u) == kRecSphere) return sphere_test(r, f3(a), b.x, r.tmax, tout);
+    if ((flags & 3u) == kRecRectHalf) {
+        const float* fr = S.rect_frames + 9 * size_t(flags >> 2);
+        const float3 vB = mk(fr[0], fr[1], fr[2]), eA0 = mk(fr[3], fr[4], fr[5]), eB0 = mk(fr[6], fr[7], fr[8]);
+        float3 eA = eA0, eB = eB0;
+        if (dot(r.d, cross(eA, eB)) > 0.0f) {
+            eA = eB0;
+            eB = eA0;
+        }
+        const float3 n = normalize(cross(eA, eB));
+        const float t = dot(n, vB - r.o) / dot(n, r.d);
+        if (t < r.tmin || t > r.tmax) return false;
+        const float3 onp = (r.o + r.d * t) - vB;
+        const float p1 = dot(onp, normalize(eA0)), p2 = dot(onp, normalize(eB0));
+        if (p1 < 0.0f || p1 > len(eA0) || p2 < 0.0f || p2 > len(eB0)) return false;
+        *tout = t;
+        return true;
+    }
+    const float3 A = f3(a);
+    float3 eAB = f3(b) - A, eAC = f3(c) - A;
+    if (dot(r.d, cross(eAB, eAC)) > 0.0f) {
+        const float3 e = eAB;
+        eAB = eAC;
+        eAC = e;
+    }
+    const float3 T = r.o - A;
+    const float3 Q = cross(T, eAB), P = cross(r.d, eAC);
+    const float den = dot(P, eAB);
+    if (den == 0.0f) return false;
+    const float inv = 1.0f / den;
+    const float t = dot(Q, eAC) * inv, u = dot(P, T) * inv, v = dot(Q, r.d) * inv;
+    if (u < 0.0f || v < 0.0f || u + v > 1.0f) return false;
+    if (t < r.tmin || t > r.tmax) return false;
+    *tout = t;
+    return true;
+}
+
+// Whether the candidate (slot, prim, watertight t) comes before the kept hit
+// (kslot, kprim, kt) of another primitive, the two within the tie window: a
+// primitive the reference's test accepts comes before one it rejects; of two
+// it accepts the smaller reference distance, and on equal distances the one
+// the reference's traversal reaches last (no ranks uploaded: the lower
+// primitive index).  Where the reference accepts neither, the watertight
+// distance, then the lower primitive index.
+CG_D bool tie_prefers(const SceneD& S, const RayPre& r, int slot, int prim, float t, int kslot, int kprim, float kt) {
+    float rt = 0.0f, rk = 0.0f;
+    const bool a = ref_hit(S, r, slot, &rt), ak = ref_hit(S, r, kslot, &rk);
+    if (a != ak) return a;
+    if (!a) return t < kt || (t == kt && prim < kprim);
+    if (rt != rk) return rt < rk;
+    if (!S.prim_rank) return prim < kprim;
+    const int o = ray_octant(r);
+    return S.prim_rank[8 * size_t(prim) + size_t(o)] > S.prim_rank[8 * size_t(kprim) + size_t(o)];
+}
+
+// Which of two hits a closest-hit query keeps: the smaller distance, within
+// the tie window tie_prefers.  The two halves of a rectangle share a
+// primitive; between them (a ray through the diagonal) the smaller t, then
+// the lower record slot, the rule mis_light_hit applies to a light's halves
+// too.  Either half gives the same hit point (hit_point recomputes t and the
+// edge coordinates from the rectangle's own frame).  `prim` / `slot` are the
+// candidate's; the kept hit's primitive is loaded only inside the window.
+CG_D bool closer_hit(const SceneD& S, const RayPre& r, float t, int prim, int slot, float tcur, int hslot) {
+    if (hslot < 0) return t <= tcur;
+    if (tie_hi(S, t) < tcur) return true;
+    if (t > tie_hi(S, tcur)) return false;
+    const int kept = __float_as_int(ldg4(reinterpret_cast<const float4*>(S.tris + hslot)).w);
+    if (prim == kept) return t < tcur || (t == tcur && slot < hslot);
+    return tie_prefers(S, r, slot, prim, t, hslot, kept, tcur);
+}
+
 // Tests the primitives of leaf `e`; returns true when an any-hit query is
 // answered (the hit is in slot / tcur).
 // SPH = false: the scene holds no spheres, and the sphere test is compiled out
@@ -316,18 +407,18 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
         const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
         if (COUNT) cnt->tris++;
         float t, u = 0.0f, v = 0.0f;
-        // closest hit: a bound one rounding wider than tcur, so that every
-        // triangle whose t rounds to <= tcur reaches closer_hit
+        // closest hit: a bound as wide as the tie window, so that every
+        // primitive within it reaches closer_hit
         const bool sphere = SPH && (__float_as_uint(c.w) & 3u) == kRecSphere;
-        if (sphere ? sphere_test(r, f3(a), b.x, tcur, &t)
-                   : tri_test(r, f3(a), f3(b), f3(c), ANY ? tcur : tcur * 1.00000036f, &t, &u, &v)) {
+        const float bound = ANY ? tcur : tie_hi(S, tcur);
+        if (sphere ? sphere_test(r, f3(a), b.x, bound, &t) : tri_test(r, f3(a), f3(b), f3(c), bound, &t, &u, &v)) {
             const int slot = int(first + k);
             if (ANY) {
                 hslot = slot;
                 tcur = t;
                 return true;
             }
-            if (closer_hit(S, t, __float_as_int(a.w), slot, tcur, hslot)) {
+            if (closer_hit(S, r, t, __float_as_int(a.w), slot, tcur, hslot)) {
                 hslot = slot;
                 tcur = t;
                 hu = u;
@@ -366,7 +457,7 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
         // else the next stack entry that can still hold a closer hit
         while (next == kNoEntry && sp > 0) {
             --sp;
-            if (ANY || stack.dist(sp) <= tcur * 1.00000036f) next = stack.entry(sp);
+            if (ANY || stack.dist(sp) <= tie_hi(S, tcur) * 1.00000036f) next = stack.entry(sp);
         }
         if (next == kNoEntry) break;
         cur = next;
@@ -378,44 +469,52 @@ CG_D bool traverse(const SceneD& S, const RayPre& r, HitD* hit, TraceCounters* c
     return hslot >= 0;
 }
 
-// Whether a primitive other than `prim_l` comes before the hit (t_l, prim_l)
-// in closest-hit order - a smaller t, or the same t and a lower primitive
-// index (closer_hit) - so that the closest hit of the ray is not prim_l.
+// Whether a primitive other than `prim_l` comes before the hit (t_l, prim_l,
+// record slot_l) in closest-hit order (closer_hit: a smaller t, within the
+// tie window tie_prefers), so that the closest hit of the ray is not prim_l.
 // Each primitive is tested as visit_leaf<false> tests it while its bound is
-// t_l, which every primitive that could come first passes; the nodes are
-// culled by t_l with the closest-hit slack.  prim_l = INT_MAX, t_l = the
-// ray's tmax: whether the ray hits anything at all.
+// t_l, with the same window; the nodes are culled by t_l with the
+// closest-hit slack.  slot_l < 0, t_l = the ray's tmax: whether the ray hits
+// anything at all (the environment is its light).
 template <bool COUNT, bool SPH = true>
-CG_D bool visit_leaf_before(const SceneD& S, const RayPre& r, uint32_t e, float t_l, int prim_l, TraceCounters* cnt) {
+CG_D bool visit_leaf_before(const SceneD& S, const RayPre& r, uint32_t e, float t_l, int prim_l, int slot_l,
+                            TraceCounters* cnt) {
     const uint32_t first = leaf_first(e), n = leaf_count(e);
+    const float bound = tie_hi(S, t_l);
     for (uint32_t k = 0; k < n; ++k) {
         const float4* tp = reinterpret_cast<const float4*>(S.tris + first + k);
         const float4 a = ldg4(tp), b = ldg4(tp + 1), c = ldg4(tp + 2);
         if (COUNT) cnt->tris++;
         float t, u, v;
         const bool sphere = SPH && (__float_as_uint(c.w) & 3u) == kRecSphere;
-        if (sphere ? sphere_test(r, f3(a), b.x, t_l, &t)
-                   : tri_test(r, f3(a), f3(b), f3(c), t_l * 1.00000036f, &t, &u, &v)) {
+        if (sphere ? sphere_test(r, f3(a), b.x, bound, &t) : tri_test(r, f3(a), f3(b), f3(c), bound, &t, &u, &v)) {
             const int prim = __float_as_int(a.w);
-            if (prim != prim_l && (t < t_l || (t == t_l && prim < prim_l))) return true;
+            if (prim == prim_l) continue;
+            if (slot_l < 0) {
+                if (t <= t_l) return true;
+                continue;
+            }
+            if (tie_hi(S, t) < t_l) return true;
+            if (tie_prefers(S, r, int(first + k), prim, t, slot_l, prim_l, t_l)) return true;
         }
     }
     return false;
 }
 
 template <bool COUNT, bool SPH = true>
-CG_D bool occluded_before(const SceneD& S, const RayPre& r, float t_l, int prim_l, TraceCounters* cnt) {
+CG_D bool occluded_before(const SceneD& S, const RayPre& r, float t_l, int prim_l, int slot_l, TraceCounters* cnt) {
     LocalStack stack;
     int sp = 0;
     uint32_t cur = 0;
     uint32_t left = S.visit_budget;
+    const float tb = tie_hi(S, t_l);
     for (;;) {
         if (over_budget(S, left)) return false;
         uint32_t next = kNoEntry;
         if (entry_is_leaf(cur)) {
-            if (visit_leaf_before<COUNT, SPH>(S, r, cur, t_l, prim_l, cnt)) return true;
+            if (visit_leaf_before<COUNT, SPH>(S, r, cur, t_l, prim_l, slot_l, cnt)) return true;
         } else {
-            next = visit_node<true, COUNT>(S, r, cur, t_l, stack, sp, cnt);
+            next = visit_node<true, COUNT>(S, r, cur, tb, stack, sp, cnt);
         }
         if (next == kNoEntry && sp > 0) next = stack.entry(--sp);
         if (next == kNoEntry) return false;
@@ -445,7 +544,7 @@ CG_D bool traverse_warp(const SceneD& S, const RayPre& r, HitD* hit, TraceCounte
     auto pop = [&]() -> uint32_t {
         while (sp > 0) {
             --sp;
-            if (stack.dist(sp) <= tcur * 1.00000036f) return stack.entry(sp);
+            if (stack.dist(sp) <= tie_hi(S, tcur) * 1.00000036f) return stack.entry(sp);
         }
         return kNoEntry;
     };
@@ -535,7 +634,7 @@ CG_D void trav_step(const SceneD& S, const RayPre& r, TravState& st, TraceCounte
     }
     while (st.sp > 0) {
         --st.sp;
-        if (ANY || st.stack.dist(st.sp) <= st.tcur * 1.00000036f) {
+        if (ANY || st.stack.dist(st.sp) <= tie_hi(S, st.tcur) * 1.00000036f) {
             st.cur = st.stack.entry(st.sp);
             return;
         }

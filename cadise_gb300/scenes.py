@@ -706,6 +706,55 @@ def sphere_box(width: int = 64, height: int = 48, spp: int = 16, max_depth: int 
     return s
 
 
+def coplanar_scene(width: int = 40, height: int = 30, spp: int = 16, max_depth: int = 8) -> SceneSpec:
+    """Coplanar, overlapping primitives - where the reference's closest hit
+    is decided by the order of its BVH traversal: quad lights of different
+    emission lying in the ceiling's own plane and overlapping one another
+    (one inside another, two identical), and rectangles and triangle meshes
+    of different albedos overlapping on the floor's plane, seen directly and
+    in a glossy wall."""
+    H, W = 10.0, 10.0
+    s = SceneSpec(width=width, height=height, spp=spp, max_depth=max_depth,
+                  cam_position=(0.0, 4.5, -9.5), cam_direction=(0.0, 0.2, 1.0), cam_up=(0.0, 1.0, 0.0), fov=85.0)
+    s.materials = [Material("white", LAMBERT, albedo=(0.72, 0.71, 0.68)),
+                   Material("grey", LAMBERT, albedo=(0.45, 0.45, 0.45)),
+                   Material("red", LAMBERT, albedo=(0.7, 0.1, 0.08)),
+                   Material("green", LAMBERT, albedo=(0.12, 0.6, 0.1)),
+                   Material("blue", LAMBERT, albedo=(0.1, 0.15, 0.7)),
+                   Material("yellow", LAMBERT, albedo=(0.75, 0.7, 0.1)),
+                   Material("steel", CONDUCTOR, roughness=0.08, f0=(0.9, 0.9, 0.92)),
+                   Material("lightBase", LAMBERT, albedo=(0.3, 0.3, 0.3))]
+
+    def rect_xz(name, mat, x0, x1, z0, z1, y):
+        # v1 - v2 = +x edge, v3 - v2 = +z edge: the normal faces -y
+        return Rectangle(name, mat, (x1, y, z0), (x0, y, z0), (x0, y, z1))
+
+    def quad_mesh(name, mat, x0, x1, z0, z1, y):
+        a, b, c, d = (x0, y, z0), (x1, y, z0), (x1, y, z1), (x0, y, z1)
+        return TriangleMesh(name, mat, np.array([[a, b, c], [a, c, d]], np.float32))
+
+    s.primitives = [
+        rect_xz("ceiling", "white", -W, W, -W, W, H),
+        rect_xz("floor", "grey", -W, W, -W, W, 0.0),
+        Rectangle("back", "white", (-W, 0, W), (W, 0, W), (W, H, W)),
+        Rectangle("left", "grey", (-W, 0, -W), (-W, 0, W), (-W, H, W)),
+        Rectangle("right", "steel", (W, 0, W), (W, 0, -W), (W, H, -W)),
+        rect_xz("redTile", "red", -6.0, 0.0, -2.0, 6.0, 0.0),
+        rect_xz("greenTile", "green", -3.0, 3.0, 0.0, 8.0, 0.0),
+        quad_mesh("blueTile", "blue", 1.0, 7.0, -4.0, 2.0, 0.0),
+        quad_mesh("yellowTile", "yellow", 4.0, 9.0, -1.0, 5.0, 0.0),
+    ]
+    lights = [("light0", -6.0, -1.0, 0.0, 5.0, (8.0, 8.0, 8.0)),
+              ("light1", -4.0, 1.0, 2.0, 7.0, (2.0, 5.0, 10.0)),
+              ("light2", 2.0, 7.0, 1.0, 6.0, (12.0, 6.0, 2.0)),
+              ("light3", 2.0, 7.0, 1.0, 6.0, (1.0, 1.0, 1.0)),  # light2's own rectangle
+              ("light4", 3.0, 5.0, 2.0, 4.0, (4.0, 12.0, 4.0))]  # inside light2
+    for name, x0, x1, z0, z1, e in lights:
+        s.primitives.append(rect_xz(name, "lightBase", x0, x1, z0, z1, H))
+        s.lights.append(AreaLight(name, e, _quad_light_watt(e, (x1 - x0) * (z1 - z0))))
+    return s
+
+
 def power_field(width: int = 48, height: int = 36, spp: int = 16, max_depth: int = 8, seed: int = 21) -> SceneSpec:
     """Small icosphere field (glass, conductors, Lambert) under 6 quad lights
     of log-uniform emission, lights picked by the power light cluster."""

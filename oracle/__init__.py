@@ -76,6 +76,7 @@ def lib():
         L.port_num_bvh_nodes.argtypes = [C.c_void_p]
         L.port_camera_rays.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
         L.port_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.port_visit_ranks.argtypes = [C.c_void_p, C.c_void_p]
         L.port_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]
         L.port_render.argtypes = [C.c_void_p, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32,
                                   C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
@@ -133,6 +134,14 @@ class PortScene:
         occ = np.zeros(n, dtype=np.int32)
         lib().port_trace(self.handle, _p(r), n, _p(prim), _p(t), _p(occ))
         return prim, t, occ
+
+    def visit_ranks(self) -> np.ndarray:
+        """(num_primitives, 8) leaf-order position of every primitive per
+        ray-direction octant in the reference tree's traversal."""
+        n = int(self.flat.desc.num_primitives)
+        out = np.zeros((n, 8), dtype=np.uint32)
+        lib().port_visit_ranks(self.handle, _p(out))
+        return out
 
     def paths(self, film_xy: np.ndarray, keys: np.ndarray):
         xy = np.ascontiguousarray(film_xy, dtype=np.float64)

@@ -1679,6 +1679,32 @@ void port_camera_rays(void* sp, const double* xy, uint32_t n, float* out) {
     }
 }
 
+// For each primitive and direction octant o (bit k: direction component k
+// negative), its position in the leaf order of this tree's traversal
+// (traverse: the second child first on a node whose split axis the ray
+// runs down), 8 per primitive.  Of two primitives hit at the same distance
+// the traversal keeps the later one.
+void port_visit_ranks(void* sp, uint32_t* out) {
+    const port::Scene& s = *static_cast<port::Scene*>(sp);
+    if (s.nodes.empty()) return;
+    for (int o = 0; o < 8; ++o) {
+        uint32_t pos = 0;
+        std::vector<int> stack{0};
+        while (!stack.empty()) {
+            const int cur = stack.back();
+            stack.pop_back();
+            const port::Scene::Node& n = s.nodes[static_cast<std::size_t>(cur)];
+            if (n.second < 0) {
+                for (int i = 0; i < n.count; ++i) out[8 * static_cast<std::size_t>(s.order[n.prim + i]) + o] = pos++;
+                continue;
+            }
+            const bool secondFirst = ((o >> n.axis) & 1) != 0;
+            stack.push_back(secondFirst ? cur + 1 : n.second);
+            stack.push_back(secondFirst ? n.second : cur + 1);
+        }
+    }
+}
+
 // rays: 8 floats each (org, t_min, dir, t_max)
 void port_trace(void* sp, const float* rays, uint32_t n, int32_t* prim, float* t, int32_t* occ) {
     const port::Scene& s = *static_cast<port::Scene*>(sp);

@@ -24,6 +24,9 @@ next to this script, and records what the reference computes for it:
   reference's FilmTile, sum_sq zero).
 * ``filter_vectors.npz`` - the reference's FilmTile::addSample with each
   filter of FILTER_CASES on one set of samples: per-pixel sensor sums.
+* ``coplanar`` - quad lights in the ceiling's plane overlapping one another
+  and tiles overlapping on the floor's plane: its closest hits are decided by
+  the order in which the reference's BVH traversal meets the tied primitives.
 * ``texel_vectors.npz`` - RgbImageTexture::evaluate (nearest, repeat) of the
   textured scene's texture at uvws on texel borders, below 0, above 1 and
   far outside.
@@ -94,6 +97,7 @@ def golden_scenes():
         "power": (scenes.power_field(), 131072),
         "spheres": (scenes.sphere_box(), 16384),
         "filtered": (filtered_scene(), 32768),
+        "coplanar": (scenes.coplanar_scene(), 16384),
     }
 
 

@@ -43,6 +43,8 @@ def specs():
         "power": scenes.power_field(),
         "spheres": scenes.sphere_box(),
         "filtered": filtered_scene(),
+        # coplanar, overlapping primitives: the reference's tie order
+        "coplanar": scenes.coplanar_scene(),
     }
 
 
@@ -51,6 +53,17 @@ def field1m_spec(width=1920, height=1080):
     dielectric replaced by the reference's smooth glass (the reference has no
     rough dielectric); same geometry, lights and camera."""
     return scenes.icosphere_field(dielectric=scenes.GLASS, width=width, height=height)
+
+
+# Fraction of the golden paths whose radiance must match the reference's to
+# 1e-3: 99 %, except in the coplanar scene, where a rectangle and a triangle
+# mesh share a plane: their reference distances come from two different
+# formulas and differ by a rounding, so a bounce perturbed by an ulp upstream
+# (a transcendental of another libm) meets them in either order - about 1 %
+# of its paths end on the other tile.  Its exact rays (the trace vectors) tie
+# bit for bit.
+def path_close_fraction(name):
+    return 0.98 if name == "coplanar" else 0.99
 
 
 def vectors(name):

@@ -60,6 +60,12 @@ void khc_texel(void* p, int tex, const float* uvw, uint32_t n, float* rgb) {
 
 // Device-side iteration budget of the traversals (0: the automatic one) and
 // the word that counts the rays that ran out of it.
+// the scene's exact-tie ranks (reference_visit_ranks), 8 per primitive
+void khc_ranks(void* p, uint32_t* out) {
+    const Check& c = *static_cast<Check*>(p);
+    for (size_t i = 0; i < c.hs.prim_rank.size(); ++i) out[i] = c.hs.prim_rank[i];
+}
+
 void khc_set_budget(void* p, uint32_t visits, uint32_t* status) {
     Check& c = *static_cast<Check*>(p);
     c.S.visit_budget = visits ? visits : cg::auto_visit_budget(c.hs.nodes.size());

@@ -24,12 +24,12 @@ import pytest
 
 import oracle
 from cadise_gb300 import CGPU_MODE_MEGAKERNEL, CGPU_MODE_WAVEFRONT, CgpuError, abi, scenes
-from golden_scenes import FILTER_CASES, image, image_mean_var, specs, vectors
+from golden_scenes import FILTER_CASES, image, image_mean_var, path_close_fraction, specs, vectors
 from parity_util import check_hits, near_edge
 
 pytestmark = pytest.mark.gpu
 
-NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres"]
+NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres", "coplanar"]
 
 
 @pytest.fixture(scope="module")
@@ -52,14 +52,14 @@ def test_camera_rays_match_reference(name, gpu_ctx, uploaded):
 @pytest.mark.parametrize("name", NAMES)
 def test_closest_hits_match_reference(name, gpu_ctx, uploaded):
     """Primitive ids equal the reference BVH's except rays within 1e-6 of an
-    edge and ties between coplanar primitives, at most 0.5 % of the rays;
-    t bit-identical where the primitive agrees."""
+    edge, at most 0.5 % of the rays (coplanar ties included: the reference's
+    tie order); t bit-identical where the primitive agrees."""
     v = vectors(name)
     spec, flat, sid = uploaded[name]
     rays = v["trace_rays"]
     prim, t, u, w = gpu_ctx.trace_closest(sid, rays)
     frac = check_hits(flat, rays, prim, t, v["trace_bvh_prim"], v["trace_bvh_t"], name)
-    print("%s: %d rays, %.4f %% excluded (edge / coplanar tie)" % (name, len(rays), 100 * frac))
+    print("%s: %d rays, %.4f %% excluded (edge)" % (name, len(rays), 100 * frac))
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -85,7 +85,7 @@ def test_path_radiance_matches_reference(name, gpu_ctx, uploaded):
     rgb = gpu_ctx.path_radiance(sid, v["paths_xy"], v["paths_keys"])
     ref = v["paths_rgb"]
     close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
-    assert close.mean() >= 0.99, close.mean()
+    assert close.mean() >= path_close_fraction(name), close.mean()
     assert abs(rgb.mean() - ref.mean()) <= 0.01 * abs(ref.mean()) + 1e-6
 
 
@@ -104,7 +104,7 @@ def test_render_paths_match_oracle(name, gpu_ctx, uploaded):
     ps = oracle.PortScene(flat)
     _, port = ps.render(seed=11, first=3, count=2, threads=8, want_paths=True, scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.99, close.mean()
+    assert close.mean() >= path_close_fraction(name), close.mean()
 
 
 def test_film_equals_sum_of_paths(gpu_ctx, uploaded):
@@ -170,7 +170,7 @@ def rel_mse(x, ref):
 
 @pytest.mark.parametrize("name,spp", [("cornell", 16384), ("cornell256", 65536), ("textured", 65536),
                                       ("field", 8192), ("features", 32768), ("power", 131072),
-                                      ("spheres", 65536), ("filtered", 65536)])
+                                      ("spheres", 65536), ("filtered", 65536), ("coplanar", 16384)])
 def test_image_converges_to_reference(name, spp, gpu_ctx, uploaded):
     """Per pixel the film's mean (sum w L / sum w; w = 1 for the box filter of
     size 1) against the reference's converged render: relMSE, and for the box
@@ -243,7 +243,7 @@ def test_rough_dielectric_paths_match_oracle(gpu_ctx):
     _, port = oracle.PortScene(flat).render(seed=3, first=0, count=4, threads=8, want_paths=True,
                                             scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.99, close.mean()
+    assert close.mean() >= path_close_fraction(name), close.mean()
     gpu_ctx.release(sid)
 
 
@@ -285,7 +285,7 @@ def test_environment_paths_match_oracle(gpu_ctx):
     assert np.array_equal(gpu, mk)
     _, port = oracle.PortScene(flat).render(seed=9, first=0, count=4, threads=8, want_paths=True, scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= 0.99, close.mean()
+    assert close.mean() >= path_close_fraction(name), close.mean()
     gpu_ctx.release(sid)
 
 

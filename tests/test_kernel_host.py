@@ -14,7 +14,7 @@ import pytest
 
 import oracle
 from cadise_gb300 import abi, scenes
-from golden_scenes import FILTER_CASES, specs, vectors
+from golden_scenes import FILTER_CASES, field1m_spec, path_close_fraction, specs, vectors
 from parity_util import check_hits
 
 ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
@@ -22,7 +22,8 @@ BUILD = os.path.join(ROOT, "tests", "native", "_build")
 LIB = os.path.join(BUILD, "libkhc.so")
 SRCS = [os.path.join(ROOT, "tests", "native", "kernel_host_check.cpp"),
         os.path.join(ROOT, "cadise_gb300", "csrc", "scene_build.cpp"),
-        os.path.join(ROOT, "cadise_gb300", "csrc", "bvh_build.cpp")]
+        os.path.join(ROOT, "cadise_gb300", "csrc", "bvh_build.cpp"),
+        os.path.join(ROOT, "cadise_gb300", "csrc", "tie_order.cpp")]
 
 
 def _cuda_include():
@@ -44,6 +45,7 @@ def khc():
     L.khc_create.argtypes = [C.c_void_p, C.c_char_p, C.c_int]
     L.khc_destroy.argtypes = [C.c_void_p]
     L.khc_set_budget.argtypes = [C.c_void_p, C.c_uint32, C.c_void_p]
+    L.khc_ranks.argtypes = [C.c_void_p, C.c_void_p]
     L.khc_texel.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_uint32, C.c_void_p]
     L.khc_trace.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_int] + [C.c_void_p] * 5
     L.khc_paths.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p]
@@ -93,7 +95,7 @@ class Host:
         self.L.khc_destroy(self.h)
 
 
-NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres"]
+NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres", "coplanar"]
 
 
 @pytest.mark.parametrize("name", NAMES)
@@ -115,6 +117,24 @@ def test_kernel_traversal_matches_reference_hits(khc, name):
     h.close()
 
 
+@pytest.mark.parametrize("name", NAMES + ["field1m"])
+def test_tie_ranks_follow_the_reference_tree(khc, name):
+    """The library's exact-tie ranks (its own build of the reference's binary
+    BVH, tie_order.cpp) equal the leaf order of the oracle's tree, which
+    reproduces the reference's hits, ties included, on the golden rays."""
+    flat = abi.flatten(field1m_spec() if name == "field1m" else specs()[name])
+    h = Host(khc, flat)
+    n = int(flat.desc.num_primitives)
+    got = np.zeros((n, 8), np.uint32)
+    khc.khc_ranks(h.h, _p(got))
+    h.close()
+    want = oracle.PortScene(flat).visit_ranks()
+    assert np.array_equal(got, want)
+    # each octant's ranks are a permutation, and the octants differ
+    assert all(np.array_equal(np.sort(got[:, o]), np.arange(n)) for o in range(8))
+    assert n < 3 or len({got[:, o].tobytes() for o in range(8)}) > 1
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_kernel_paths_match_reference(khc, name):
     v = vectors(name)
@@ -122,7 +142,7 @@ def test_kernel_paths_match_reference(khc, name):
     rgb = h.paths(v["paths_xy"], v["paths_keys"])
     ref = v["paths_rgb"]
     close = np.all(np.abs(rgb - ref) <= 1e-3 * np.abs(ref) + 1e-5, axis=1)
-    assert close.mean() >= 0.99, close.mean()
+    assert close.mean() >= path_close_fraction(name), close.mean()
     h.close()
 
 

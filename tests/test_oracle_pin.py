@@ -17,7 +17,7 @@ from cadise_gb300 import abi, scenes
 from golden_scenes import crsd_text, specs, vectors
 
 EXACT = platform.machine() in ("x86_64", "AMD64")
-NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres"]
+NAMES = ["cornell", "cornell256", "textured", "field", "features", "power", "spheres", "coplanar"]
 
 
 @pytest.fixture(scope="module")
@@ -67,8 +67,15 @@ def test_bvh_hits_match_reference(name, ports):
         assert np.array_equal(occ, v["trace_occluded"])
     else:
         assert np.mean(prim == v["trace_bvh_prim"]) > 0.999
-    # the reference BVH agrees with its own brute-force accelerator on non-tie rays
-    assert np.mean(v["trace_bvh_prim"] == v["trace_bf_prim"]) > 0.99
+    # the reference BVH agrees with its own brute-force accelerator on non-tie
+    # rays; where they differ both hit at the same distance (a tie, which each
+    # accelerator breaks by its own visiting order) - in the coplanar scene
+    # the ceiling's lights and the floor's tiles make those common
+    diff = v["trace_bvh_prim"] != v["trace_bf_prim"]
+    if name != "coplanar":
+        assert np.mean(diff) < 0.01
+    assert np.all(v["trace_bvh_prim"][diff] >= 0)
+    assert np.allclose(v["trace_bvh_t"][diff], v["trace_bf_t"][diff], rtol=1e-5, atol=1e-5)
 
 
 @pytest.mark.parametrize("name", NAMES)
