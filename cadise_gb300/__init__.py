@@ -25,7 +25,7 @@ LIB_PATH = os.path.join(HERE, "_build", "libcadise_gpu.so")
 # Every symbol include/cadise_gpu.h declares.
 EXPORTED = [
     "cgpu_create", "cgpu_destroy", "cgpu_last_error", "cgpu_status_string", "cgpu_abi_version",
-    "cgpu_synchronize", "cgpu_set_visit_budget", "cgpu_set_bvh_builder", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
+    "cgpu_synchronize", "cgpu_set_visit_budget", "cgpu_set_tie_order", "cgpu_set_bvh_builder", "cgpu_scene_upload", "cgpu_scene_release", "cgpu_scene_info_get",
     "cgpu_trace_closest", "cgpu_trace_any", "cgpu_trace_closest_device", "cgpu_trace_any_device",
     "cgpu_camera_rays", "cgpu_render", "cgpu_render_noalloc", "cgpu_film_clear", "cgpu_film_read", "cgpu_path_radiance",
     "cgpu_render_paths", "cgpu_render_stats_get", "cgpu_set_counting", "cgpu_set_profiling",
@@ -36,7 +36,7 @@ EXPORTED = [
     "cgpu_crsd_primitive_index", "cgpu_crsd_free",
 ]
 
-KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel", "reorder", "mis_occl"]
+KERNEL_CLASSES = ["generate", "extend", "shadow", "shade", "splat", "megakernel", "reorder", "mis_occl", "ties"]
 
 _lib = None
 
@@ -73,6 +73,7 @@ def load(path: Optional[str] = None):
     L.cgpu_abi_version.restype = C.c_int32
     L.cgpu_synchronize.argtypes = [vp]
     L.cgpu_set_visit_budget.argtypes = [vp, C.c_uint32]
+    L.cgpu_set_tie_order.argtypes = [vp, C.c_int32]
     L.cgpu_scene_upload.argtypes = [vp, vp, C.POINTER(C.c_int32)]
     L.cgpu_scene_release.argtypes = [vp, C.c_int32]
     L.cgpu_scene_info_get.argtypes = [vp, C.c_int32, C.POINTER(cgpu_scene_info)]
@@ -272,6 +273,12 @@ class Context:
     def set_visit_budget(self, visits: int):
         """Node and leaf visits per ray before a traversal stops (0: automatic)."""
         self._check(self.L.cgpu_set_visit_budget(self.h, visits))
+
+    def set_tie_order(self, order: int):
+        """Exact-tie rule of closest hits for scenes uploaded afterwards:
+        CGPU_TIE_ORDER_REFERENCE (default; the reference BVH's visiting
+        order, built at upload) or CGPU_TIE_ORDER_INDEX (lower primitive)."""
+        self._check(self.L.cgpu_set_tie_order(self.h, order))
 
     def set_counting(self, on: bool):
         self._check(self.L.cgpu_set_counting(self.h, 1 if on else 0))

@@ -118,9 +118,13 @@ CGPU_BVH_BUILDER_AUTO = 0
 CGPU_BVH_BUILDER_HOST_SAH = 1
 CGPU_BVH_BUILDER_GPU_PLOC = 2
 CGPU_BVH_BUILDER_GPU_SAH = 3
+
 CGPU_BVH_GPU_MIN_PRIMITIVES = 1000000
 CGPU_BVH_GPU_MIN_PRIMS_PER_SAMPLE = 0.01
 CGPU_BVH_GPU_SAH_MIN_PRIMITIVES = 65536
+
+CGPU_TIE_ORDER_REFERENCE = 0
+CGPU_TIE_ORDER_INDEX = 1
 
 
 class cgpu_options(C.Structure):
@@ -166,7 +170,7 @@ class cgpu_param_counts(C.Structure):
 
 
 class cgpu_kernel_times(C.Structure):
-    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_uint32 * 8)]
+    _fields_ = [("ms", C.c_double * 9), ("launches", C.c_uint32 * 9)]
 
 
 def _fptr(a: np.ndarray):

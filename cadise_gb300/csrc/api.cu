@@ -198,6 +198,14 @@ cgpu_status cgpu_set_visit_budget(cgpu_ctx* ctx, uint32_t visits) {
     return CGPU_OK;
 }
 
+cgpu_status cgpu_set_tie_order(cgpu_ctx* ctx, int32_t order) {
+    if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
+    if (order != CGPU_TIE_ORDER_REFERENCE && order != CGPU_TIE_ORDER_INDEX)
+        return cg_fail(ctx, CGPU_ERR_INVALID_ARGUMENT, "set_tie_order: unknown order");
+    ctx->tie_order = order;
+    return CGPU_OK;
+}
+
 cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder) {
     if (!check_ctx(ctx)) return CGPU_ERR_INVALID_ARGUMENT;
     if (builder < CGPU_BVH_BUILDER_AUTO || builder > CGPU_BVH_BUILDER_GPU_SAH)
@@ -233,9 +241,10 @@ cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* d, int32_t* 
                       ? CGPU_BVH_BUILDER_GPU_PLOC
                   : d->num_primitives >= CGPU_BVH_GPU_SAH_MIN_PRIMITIVES ? CGPU_BVH_BUILDER_GPU_SAH
                                                                          : CGPU_BVH_BUILDER_HOST_SAH;
-    cgpu_status st = builder == CGPU_BVH_BUILDER_GPU_PLOC  ? build_host_scene(d, &hs, &err, gpu_ploc_builder, ctx)
-                     : builder == CGPU_BVH_BUILDER_GPU_SAH ? build_host_scene(d, &hs, &err, gpu_sah_builder, ctx)
-                                                           : build_host_scene(d, &hs, &err);
+    const bool ranks = ctx->tie_order == CGPU_TIE_ORDER_REFERENCE;
+    cgpu_status st = builder == CGPU_BVH_BUILDER_GPU_PLOC  ? build_host_scene(d, &hs, &err, gpu_ploc_builder, ctx, ranks)
+                     : builder == CGPU_BVH_BUILDER_GPU_SAH ? build_host_scene(d, &hs, &err, gpu_sah_builder, ctx, ranks)
+                                                           : build_host_scene(d, &hs, &err, nullptr, nullptr, ranks);
     if (st != CGPU_OK) return cg_fail(ctx, st, "scene_upload: " + err);
     hs.info.bvh_builder = builder;
     if (3 * hs.wide_depth + 1 > kStackSize)

@@ -46,7 +46,8 @@ struct FilmD {
 //   8 / 9: rays handed out so far by the persistent extend / shadow kernels,
 //   10: adjoint vertices of bounce b - 1 (the wavefront adjoint's gradient kernel),
 //   11: MIS rays whose direction meets the sampled light's primitive (or that
-//       sampled the environment), left for the MIS occlusion pass.
+//       sampled the environment), left for the MIS occlusion pass,
+//   12: closest-hit rays of the persistent pass left for k_wf_ties (q_tie).
 constexpr int kCntStride = 16;
 
 struct WfBuffers {
@@ -66,6 +67,10 @@ struct WfBuffers {
     int* q_shadow[2];
     int* q_mocc[2];   // MIS occlusion queries, ping-pong on the bounce
     int* q_mat[kNumBsdfKinds];
+    // closest-hit rays whose persistent traversal met two primitives within
+    // the tie window (k_wf_extend_pww), for k_wf_ties: path, | 0x80000000 for
+    // a MIS ray; room for every ray of a pass (2 per path)
+    int* q_tie;
     int* cnt;
     int cnt_depth;    // bounces the counter array covers
 };
@@ -92,6 +97,7 @@ inline size_t wf_layout(char* base, size_t cap, int cnt_rows, WfBuffers* w) {
         w->q_mocc[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
     }
     for (int k = 0; k < kNumBsdfKinds; ++k) w->q_mat[k] = reinterpret_cast<int*>(take(cap * sizeof(int)));
+    w->q_tie = reinterpret_cast<int*>(take(2 * cap * sizeof(int)));
     w->cnt = reinterpret_cast<int*>(take(size_t(cnt_rows) * kCntStride * sizeof(int)));
     w->cnt_depth = cnt_rows;
     return off;
@@ -253,6 +259,7 @@ struct cgpu_ctx {
     void* adj_block = nullptr;
     int adjoint_schedule = CGPU_MODE_WAVEFRONT;
     int bvh_builder = CGPU_BVH_BUILDER_AUTO;
+    int tie_order = CGPU_TIE_ORDER_REFERENCE;
     unsigned long long* d_counters = nullptr;
     // device status word: rays whose traversal ran out of its visit budget
     // since the last check (cg_check_status); 0 = automatic budget per scene

@@ -431,10 +431,10 @@ __global__ void __maxnreg__(56) k_wf_extend_pww(RenderArgs a, int b) {
     bool cont = false;   // continuation ray (else MIS ray)
     bool drained = false;
     uint32_t left = 0;  // node and leaf visits this ray has left (over_budget)
-    auto pop = [&](const SceneD& S) -> uint32_t {
+    auto pop = [&]() -> uint32_t {
         while (sp > 0) {
             --sp;
-            if (stack.dist(sp) <= tie_hi(S, tcur) * 1.00000036f) return stack.entry(sp);
+            if (stack.dist(sp) <= tcur * 1.00000036f) return stack.entry(sp);
         }
         return kNoEntry;
     };
@@ -469,48 +469,86 @@ __global__ void __maxnreg__(56) k_wf_extend_pww(RenderArgs a, int b) {
                     cur = leaf = kNoEntry;
                     break;
                 }
-                cur = visit_node<false, COUNT>(S, r, cur, tcur, stack, sp, &tc);
-                if (cur == kNoEntry) cur = pop(S);
+                cur = visit_node<false, COUNT, false>(S, r, cur, tcur, stack, sp, &tc);
+                if (cur == kNoEntry) cur = pop();
                 if (leaf == kNoEntry && cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
-                    cur = pop(S);
+                    cur = pop();
                 }
                 if (!__any_sync(__activemask(), leaf == kNoEntry)) break;
             }
             if (leaf == kNoEntry) {
                 if (cur == kNoEntry) break;  // the ray is done
                 leaf = cur;
-                cur = pop(S);
+                cur = pop();
             }
             while (leaf != kNoEntry) {
                 if (over_budget(S, left)) {
                     cur = leaf = kNoEntry;
                     break;
                 }
-                visit_leaf<false, COUNT, SPH>(S, r, leaf, tcur, hslot, hu, hv, &tc);
+                visit_leaf<false, COUNT, SPH, true>(S, r, leaf, tcur, hslot, hu, hv, &tc);
                 leaf = kNoEntry;
                 if (cur != kNoEntry && entry_is_leaf(cur)) {
                     leaf = cur;
-                    cur = pop(S);
+                    cur = pop();
                 }
             }
             if (cur == kNoEntry) break;  // the ray is done
             if (__popc(__activemask()) < a.refill_closest) break;
         }
         if (cur == kNoEntry && leaf == kNoEntry) {
-            HitD hit;
-            hit.t = tcur;
-            hit.slot = hslot;
-            // the shading recomputes the surface coordinates from the hit
-            // point (hit_point), so the traversal's need not be kept
-            hit.u = 0.0f;
-            hit.v = 0.0f;
-            const int key = extend_finish<ADJ>(w, S, p, cont, r.o, r.d, hslot >= 0, hit, &a.adj);
-            grouped_push(qmat, cnt + 3, key, p);
+            if (hu != 0.0f) {
+                // two primitives within the tie window: k_wf_ties decides
+                w.q_tie[atomicAdd(cnt + 12, 1)] = cont ? p : int(uint32_t(p) | 0x80000000u);
+            } else {
+                HitD hit;
+                hit.t = tcur;
+                hit.slot = hslot;
+                // the shading recomputes the surface coordinates from the hit
+                // point (hit_point), so the traversal's need not be kept
+                hit.u = 0.0f;
+                hit.v = 0.0f;
+                const int key = extend_finish<ADJ>(w, S, p, cont, r.o, r.d, hslot >= 0, hit, &a.adj);
+                grouped_push(qmat, cnt + 3, key, p);
+            }
             i = -1;
         }
     }
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, nclosest, 0);
+}
+
+constexpr int kTieBlock = 64;
+
+// Closest-hit rays the persistent pass left to this kernel (q_tie): two
+// primitives within the tie window of each other, which tie_prefers orders
+// by the reference's own test and tie order.  Traced again with the per-ray
+// traversal (closer_hit / tie_prefers, wide culling), then finished as the
+// persistent pass finishes its other rays.  It runs beside the any-hit pass
+// (on the other stream), and its grid strides over however few rays it got.
+template <bool COUNT, bool SPH, bool ADJ = false>
+__global__ void k_wf_ties(RenderArgs a, int b) {
+    const WfBuffers& w = a.wf;
+    int* cnt = w.cnt + b * kCntStride;
+    const int n = cnt[12];
+    int* const* qmat = w.q_mat;
+    TraceCounters tc{0, 0};
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int e = w.q_tie[i];
+        const bool cont = e >= 0;
+        const int p = e & 0x7FFFFFFF;
+        const SceneD& S = a.scenes[w.meta[p].x];
+        const float3 o = f3(w.ray_o[p]);
+        const float3 d = cont ? f3(w.ray_d[p]) : f3(w.mis_d[p]);
+        const RayPre r = ray_prep(o, d, kRayEps, kFloatMax);
+        HitD hit;
+        const bool hitp = traverse<false, COUNT, SPH>(S, r, &hit, &tc);
+        hit.u = 0.0f;
+        hit.v = 0.0f;
+        const int key = extend_finish<ADJ>(w, S, p, cont, o, d, hitp, hit, &a.adj);
+        grouped_push(qmat, cnt + 3, key, p);
+    }
+    count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, 0, 0);
 }
 
 // Persistent any-hit pass: k_wf_extend_pww's while-while traversal with
@@ -1140,6 +1178,7 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
                       : (trav == 2 || trav == 3) ? CG_PICK(k_wf_extend_pww) : CG_PICK(k_wf_extend);
     auto sh_kernel = trav == 1 ? CG_PICK(k_wf_shadow_dyn) : trav == 3 ? CG_PICK(k_wf_shadow_pww) : CG_PICK(k_wf_shadow);
     auto mocc_kernel = CG_PICK(k_wf_mis_occl);
+    auto ties_kernel = CG_PICK(k_wf_ties);
 #undef CG_PICK
     // reordered closest-hit passes after the first (the primary rays are in pixel order already)
     const bool reorder = ctx->tuning.reorder != 0 && trav != 1 && ctx->sort_block != nullptr;
@@ -1160,6 +1199,7 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
     const int gext = grid_for(ctx, ext_kernel, bt, paths, ext_sm);
     const int gsh = grid_for(ctx, sh_kernel, bt, paths, sh_sm);
     const int gmo = grid_for(ctx, mocc_kernel, bt, paths);
+    const int gties = grid_for(ctx, ties_kernel, kTieBlock, paths);
     const int gsd[kNumBsdfKinds] = {grid_for(ctx, k_wf_shade<0>, bs, paths), grid_for(ctx, k_wf_shade<1>, bs, paths),
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
                                     grid_for(ctx, k_wf_shade<4>, bs, paths)};
@@ -1176,6 +1216,11 @@ cgpu_status enqueue_wavefront(cgpu_ctx* ctx, int depth, uint32_t paths, bool spl
             timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_sorted<<<gext, bt, ext_sorted_sm, s>>>(a, b); });
         } else {
             timed(ctx, CGPU_KERNEL_EXTEND, s, [&] { ext_kernel<<<gext, bt, ext_sm, s>>>(a, b); });
+        }
+        if (trav >= 2) {
+            // the persistent pass's rays within the tie window
+            timed(ctx, CGPU_KERNEL_TIES, s, [&] { ties_kernel<<<gties, kTieBlock, 0, s>>>(a, b); });
+            launches += 1;
         }
         timed(ctx, CGPU_KERNEL_SHADOW, side, [&] { sh_kernel<<<gsh, bt, sh_sm, side>>>(a, b); });
         // the MIS rays of the vertices of bounce b - 1 that meet their light
@@ -1501,12 +1546,13 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
     auto shd = trav == 3 ? (sph ? k_wf_shadow_pww<false, true, true> : k_wf_shadow_pww<false, false, true>)
                          : (sph ? k_wf_shadow<false, true, true> : k_wf_shadow<false, false, true>);
     auto mo = sph ? k_wf_mis_occl<false, true, true> : k_wf_mis_occl<false, false, true>;
+    auto ties = sph ? k_wf_ties<false, true, true> : k_wf_ties<false, false, true>;
     void (*shade[kNumBsdfKinds])(RenderArgs, int) = {k_wf_shade<0, true>, k_wf_shade<1, true>, k_wf_shade<2, true>,
                                                      k_wf_shade<3, true>, k_wf_shade<4, true>};
     k_wf_generate<<<grid_for(ctx, k_wf_generate, kBlock, paths), kBlock, 0, s>>>(a);
     const size_t ext_sm = stack_smem(ext, trav >= 2, true, bt), sh_sm = stack_smem(shd, trav == 3, false, bt);
     const int gext = grid_for(ctx, ext, bt, paths, ext_sm), gsh = grid_for(ctx, shd, bt, paths, sh_sm);
-    const int gmo = grid_for(ctx, mo, bt, paths);
+    const int gmo = grid_for(ctx, mo, bt, paths), gties = grid_for(ctx, ties, kTieBlock, paths);
     const int gv = grid_for(ctx, k_adj_vertex, kBlock, paths, shared_bytes);
     int gsd[kNumBsdfKinds];
     for (int k = 0; k < kNumBsdfKinds; ++k) gsd[k] = grid_for(ctx, shade[k], bs, paths, shared_bytes);
@@ -1515,6 +1561,10 @@ void enqueue_adjoint_pass(cgpu_ctx* ctx, const RenderArgs& a, int depth, uint32_
         cudaEventRecord(fork, s);
         cudaStreamWaitEvent(side, fork, 0);
         ext<<<gext, bt, ext_sm, s>>>(a, b);
+        if (trav >= 2) {
+            ties<<<gties, kTieBlock, 0, s>>>(a, b);
+            launches += 1;
+        }
         shd<<<gsh, bt, sh_sm, side>>>(a, b);
         if (b > 0) {
             mo<<<gmo, bt, 0, side>>>(a, b);
@@ -1683,9 +1733,12 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
                                     grid_for(ctx, k_wf_shade<2>, bs, paths), grid_for(ctx, k_wf_shade<3>, bs, paths),
                                     grid_for(ctx, k_wf_shade<4>, bs, paths)};
     auto mocc = sph ? k_wf_mis_occl<false, true> : k_wf_mis_occl<false, false>;
+    auto ties = sph ? k_wf_ties<false, true> : k_wf_ties<false, false>;
     const int gmo = grid_for(ctx, mocc, bt, paths);
+    const int gties = grid_for(ctx, ties, kTieBlock, paths);
     for (int b = 0; b <= depth; ++b) {
         ext<<<gext, bt, ext_sm, s>>>(a, b);
+        if (trav >= 2) ties<<<gties, kTieBlock, 0, s>>>(a, b);
         sh<<<gsh, bt, sh_sm, s>>>(a, b);
         if (b > 0) mocc<<<gmo, bt, 0, s>>>(a, b);
         if (b == depth) break;
@@ -1696,7 +1749,8 @@ void enqueue_wavefront_serial(cgpu_ctx* ctx, const RenderArgs& a, int depth, uin
         k_wf_shade<4><<<gsd[4], bs, 0, s>>>(a, b);
     }
     k_splat<<<grid_for(ctx, k_splat, 256, npix), 256, 0, s>>>(a);
-    ctx->stats.kernel_launches += uint32_t(3 + 2 * (depth + 1) + depth + kNumBsdfKinds * depth);
+    ctx->stats.kernel_launches +=
+        uint32_t(3 + 2 * (depth + 1) + depth + kNumBsdfKinds * depth + (trav >= 2 ? depth + 1 : 0));
 }
 
 }  // namespace

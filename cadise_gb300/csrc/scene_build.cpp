@@ -77,7 +77,7 @@ cgpu_status resolve_filter(const cgpu_film_filter& f, FilterD* out, std::string*
 }
 
 cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err, BvhBuildFn bvh_builder,
-                             void* bvh_user) {
+                             void* bvh_user, bool tie_ranks) {
     if (!d) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "null scene description");
     {
         const cgpu_status fs = resolve_filter(d->filter, &out->filter, err);
@@ -182,7 +182,8 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         if (!std::isfinite(f)) return fail(err, CGPU_ERR_INVALID_ARGUMENT, "non-finite vertex");
     }
     // the reference's tie order, built on other threads while the BVH builds
-    std::future<std::vector<uint32_t>> ranks = std::async(std::launch::async, [d] { return reference_visit_ranks(d); });
+    std::future<std::vector<uint32_t>> ranks;
+    if (tie_ranks) ranks = std::async(std::launch::async, [d] { return reference_visit_ranks(d); });
     Bvh4Result bvh;
     std::string berr;
     const auto tb = std::chrono::steady_clock::now();
@@ -452,7 +453,7 @@ cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::stri
         cdf[n] = 1.0f;
         out->light_cdf = std::move(cdf);
     }
-    out->prim_rank = ranks.get();
+    if (tie_ranks) out->prim_rank = ranks.get();
     return CGPU_OK;
 }
 

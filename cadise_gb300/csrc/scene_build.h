@@ -39,9 +39,10 @@ struct HostScene {
 cgpu_status resolve_filter(const cgpu_film_filter& f, FilterD* out, std::string* err);
 
 // Returns CGPU_OK or an error status with a message in *err.  `bvh_builder`
-// (optional) builds the BVH in place of the host builder.
+// (optional) builds the BVH in place of the host builder.  `tie_ranks`:
+// also build the reference's tie order (prim_rank, tie_order.h).
 cgpu_status build_host_scene(const cgpu_scene_desc* d, HostScene* out, std::string* err,
-                             BvhBuildFn bvh_builder = nullptr, void* bvh_user = nullptr);
+                             BvhBuildFn bvh_builder = nullptr, void* bvh_user = nullptr, bool tie_ranks = true);
 
 // A SceneD whose pointers are the host arrays (for running the kernel logic on the CPU).
 SceneD host_view(HostScene& hs, const cgpu_scene_desc* d);

@@ -40,17 +40,23 @@ inline float half_area(const Box3& b) {
 }
 
 struct Tree {
-    // per node: split axis (internal) or -1 (leaf); children; leaf range of `idx`
+    // per node: split axis (internal) or -1 (leaf); children; leaf range of `items`
     std::vector<int8_t> axis;
     std::vector<int32_t> first, second, begin, count;
 };
 
+// One primitive's box, centroid and index; the build partitions these in
+// place (contiguous, as the reference's vectors of bound infos are), which
+// gives the same orders as the reference's copies.
+struct Item {
+    float lo[3], hi[3], c[3];
+    int32_t idx;
+};
+
 class Builder {
 public:
-    Builder(const cgpu_scene_desc* d) : n_(d->num_primitives), lo_(3 * size_t(n_)), hi_(3 * size_t(n_)), c_(3 * size_t(n_)) {
+    Builder(const cgpu_scene_desc* d) : n_(d->num_primitives), items_(n_) {
         for (uint32_t i = 0; i < n_; ++i) prim_box(d, i);
-        idx_.resize(n_);
-        for (uint32_t i = 0; i < n_; ++i) idx_[i] = int32_t(i);
         // at most 2n - 1 nodes; slots are taken with an atomic counter
         const size_t cap = n_ > 0 ? 2 * size_t(n_) - 1 : 1;
         tree_.axis.assign(cap, -1);
@@ -81,8 +87,10 @@ private:
     void prim_box(const cgpu_scene_desc* d, uint32_t i) {
         const int kind = d->prim_kind ? d->prim_kind[i] : CGPU_PRIM_TRIANGLE;
         const float* v = d->prim_vertices + 9 * size_t(i);
-        float* lo = &lo_[3 * size_t(i)];
-        float* hi = &hi_[3 * size_t(i)];
+        Item& it = items_[i];
+        it.idx = int32_t(i);
+        float* lo = it.lo;
+        float* hi = it.hi;
         if (kind == CGPU_PRIM_SPHERE) {
             for (int k = 0; k < 3; ++k) {
                 lo[k] = (v[k] - v[3]) - 0.0001f;
@@ -110,7 +118,7 @@ private:
                 hi[k] = b + 0.0001f;
             }
         }
-        for (int k = 0; k < 3; ++k) c_[3 * size_t(i) + k] = (lo[k] + hi[k]) * 0.5f;
+        for (int k = 0; k < 3; ++k) it.c[k] = (lo[k] + hi[k]) * 0.5f;
     }
 
     int32_t make_leaf(int32_t id, int32_t b, int32_t e) {
@@ -120,16 +128,16 @@ private:
         return id;
     }
 
-    // BvhBuilder::_buildBinaryNodesRecursively on idx_[b, e)
+    // BvhBuilder::_buildBinaryNodesRecursively on items_[b, e)
     int32_t node(int32_t b, int32_t e, int depth) {
         const int32_t id = next_.fetch_add(1);
         const int32_t count = e - b;
         if (count <= 1) return make_leaf(id, b, e);
         Box3 box = empty_box(), cbox = empty_box();
+        Item* it = items_.data();
         for (int32_t i = b; i < e; ++i) {
-            const size_t p = size_t(idx_[size_t(i)]);
-            grow(box, &lo_[3 * p], &hi_[3 * p]);
-            grow(cbox, &c_[3 * p], &c_[3 * p]);
+            grow(box, it[i].lo, it[i].hi);
+            grow(cbox, it[i].c, it[i].c);
         }
         float ext[3];
         for (int k = 0; k < 3; ++k) ext[k] = cbox.hi[k] - cbox.lo[k];
@@ -137,30 +145,27 @@ private:
         if (ext[1] > ext[axis]) axis = 1;
         if (ext[2] > ext[axis]) axis = 2;
         if (cbox.lo[axis] == cbox.hi[axis]) return make_leaf(id, b, e);
-        const float* c = c_.data();
-        int32_t* ix = idx_.data();
         int32_t mid;
         if (count <= 2) {
             // the equal split (_canSplitWithEqual): the lower centroid first
             mid = b + (count + 1) / 2;
-            std::nth_element(ix + b, ix + mid, ix + e,
-                             [c, axis](int32_t x, int32_t y) { return c[3 * size_t(x) + axis] < c[3 * size_t(y) + axis]; });
+            std::nth_element(it + b, it + mid, it + e,
+                             [axis](const Item& x, const Item& y) { return x.c[axis] < y.c[axis]; });
         } else {
             constexpr int kBuckets = 12;
             const float cmin = cbox.lo[axis];
             const float inv_ext = 1.0f / ext[axis];
-            auto bucket = [c, axis, cmin, inv_ext](int32_t p) {
-                const size_t k = size_t((c[3 * size_t(p) + axis] - cmin) * inv_ext * float(kBuckets));
+            auto bucket = [axis, cmin, inv_ext](const Item& x) {
+                const size_t k = size_t((x.c[axis] - cmin) * inv_ext * float(kBuckets));
                 return k == size_t(kBuckets) ? size_t(kBuckets - 1) : k;
             };
             int32_t bn[kBuckets] = {0};
             Box3 bb[kBuckets];
             for (auto& x : bb) x = empty_box();
             for (int32_t i = b; i < e; ++i) {
-                const int32_t p = ix[size_t(i)];
-                const size_t k = bucket(p);
+                const size_t k = bucket(it[i]);
                 ++bn[k];
-                grow(bb[k], &lo_[3 * size_t(p)], &hi_[3 * size_t(p)]);
+                grow(bb[k], it[i].lo, it[i].hi);
             }
             const float inv_area = 1.0f / half_area(box);
             float best = FLT_MAX;
@@ -186,7 +191,7 @@ private:
                 }
             }
             if (best >= float(count)) return make_leaf(id, b, e);
-            mid = int32_t(std::partition(ix + b, ix + e, [&](int32_t p) { return bucket(p) <= best_split; }) - ix);
+            mid = int32_t(std::partition(it + b, it + e, [&](const Item& x) { return bucket(x) <= best_split; }) - it);
             if (mid == b || mid == e) return make_leaf(id, b, e);
         }
         tree_.axis[size_t(id)] = int8_t(axis);
@@ -215,7 +220,7 @@ private:
             const int ax = tree_.axis[size_t(id)];
             if (ax < 0) {
                 const int32_t b = tree_.begin[size_t(id)], n = tree_.count[size_t(id)];
-                for (int32_t i = 0; i < n; ++i) r[8 * size_t(idx_[size_t(b + i)]) + size_t(o)] = pos++;
+                for (int32_t i = 0; i < n; ++i) r[8 * size_t(items_[size_t(b + i)].idx) + size_t(o)] = pos++;
                 continue;
             }
             const bool second_first = ((o >> ax) & 1) != 0;
@@ -229,8 +234,7 @@ private:
     static constexpr int kParallelDepth = 5;
 
     uint32_t n_;
-    std::vector<float> lo_, hi_, c_;
-    std::vector<int32_t> idx_;
+    std::vector<Item> items_;
     Tree tree_;
     std::atomic<int32_t> next_{0};
 };

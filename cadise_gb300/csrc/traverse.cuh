@@ -234,7 +234,9 @@ struct SharedStack {
 
 // Visits inner node `e`: pushes the children the ray enters, farthest first,
 // except the nearest, which it returns (kNoEntry when the ray misses all four).
-template <bool ANY, bool COUNT, typename Stack>
+// WIDE = false (the persistent closest-hit pass, which leaves ties to
+// k_wf_ties): children culled by tcur itself, not by the tie window.
+template <bool ANY, bool COUNT, bool WIDE = true, typename Stack>
 CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcur, Stack& stack, int& sp,
                          TraceCounters* cnt) {
     const float kInf = __int_as_float(0x7f800000);
@@ -242,7 +244,7 @@ CG_D uint32_t visit_node(const SceneD& S, const RayPre& r, uint32_t e, float tcu
     load_node(S.nodes, e, r, q);
     if (COUNT) cnt->nodes++;
     float tn[4];
-    child_hits(r, q, ANY ? tcur : tie_hi(S, tcur), tn);
+    child_hits(r, q, (ANY || !WIDE) ? tcur : tie_hi(S, tcur), tn);
     uint32_t ce[4] = {__float_as_uint(q[1].x), __float_as_uint(q[1].y), __float_as_uint(q[1].z),
                       __float_as_uint(q[1].w)};
     if (!ANY) {
@@ -398,7 +400,12 @@ CG_D bool closer_hit(const SceneD& S, const RayPre& r, float t, int prim, int sl
 // SPH = false: the scene holds no spheres, and the sphere test is compiled out
 // of the hot kernels (a sphere record would then be misread as a triangle, so
 // the host picks SPH from the scenes it renders).
-template <bool ANY, bool COUNT, bool SPH = true>
+// DEFER (the persistent closest-hit pass): the watertight rule alone, and hu
+// set to 1 when a candidate lies within the tie window of the kept hit - the
+// ray is then traced again by k_wf_ties with tie_prefers - so that the rare
+// tie code stays out of that register-capped kernel.  hu / hv are not the
+// hit's coordinates there.
+template <bool ANY, bool COUNT, bool SPH = true, bool DEFER = false>
 CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, int& hslot, float& hu, float& hv,
                      TraceCounters* cnt) {
     const uint32_t first = leaf_first(e), n = leaf_count(e);
@@ -418,7 +425,13 @@ CG_D bool visit_leaf(const SceneD& S, const RayPre& r, uint32_t e, float& tcur, 
                 tcur = t;
                 return true;
             }
-            if (closer_hit(S, r, t, __float_as_int(a.w), slot, tcur, hslot)) {
+            if (DEFER) {
+                if (hslot >= 0 && tie_hi(S, t) >= tcur) hu = 1.0f;
+                if (hslot < 0 ? t <= tcur : (t < tcur || (t == tcur && slot < hslot))) {
+                    hslot = slot;
+                    tcur = t;
+                }
+            } else if (closer_hit(S, r, t, __float_as_int(a.w), slot, tcur, hslot)) {
                 hslot = slot;
                 tcur = t;
                 hu = u;

@@ -48,7 +48,7 @@
 extern "C" {
 #endif
 
-#define CGPU_ABI_VERSION 4
+#define CGPU_ABI_VERSION 5
 
 typedef enum cgpu_status {
     CGPU_OK = 0,
@@ -253,6 +253,19 @@ cgpu_status cgpu_synchronize(cgpu_ctx* ctx);
 cgpu_status cgpu_set_visit_budget(cgpu_ctx* ctx, uint32_t visits);
 
 cgpu_status cgpu_set_bvh_builder(cgpu_ctx* ctx, int32_t builder);
+
+/* Which of two primitives a closest-hit query keeps when the reference's own
+ * test meets both at the same distance (coplanar overlapping primitives; a
+ * ray through an edge two triangles share).  CGPU_TIE_ORDER_REFERENCE (the
+ * default): the one the reference's BVH traversal reaches last
+ * (bvhAccelerator.cpp:40-97 with triangle.cpp:81-86) - each upload builds the
+ * reference's binary SAH tree on host threads beside the BVH build (about
+ * 0.4 s per million primitives on 8 cores) and keeps 32 bytes per primitive
+ * on the device.  CGPU_TIE_ORDER_INDEX: the lower primitive index, without
+ * that build.  Applies to scenes uploaded afterwards. */
+enum { CGPU_TIE_ORDER_REFERENCE = 0, CGPU_TIE_ORDER_INDEX = 1 };
+cgpu_status cgpu_set_tie_order(cgpu_ctx* ctx, int32_t order);
+
 cgpu_status cgpu_scene_upload(cgpu_ctx* ctx, const cgpu_scene_desc* desc, int32_t* out_scene);
 cgpu_status cgpu_scene_release(cgpu_ctx* ctx, int32_t scene);
 cgpu_status cgpu_scene_info_get(cgpu_ctx* ctx, int32_t scene, cgpu_scene_info* out_info);
@@ -442,7 +455,8 @@ enum {
     CGPU_KERNEL_MEGAKERNEL = 5,
     CGPU_KERNEL_REORDER = 6,    /* sort keys + radix sort of a closest-hit queue (tuning.reorder) */
     CGPU_KERNEL_MIS_OCCL = 7,   /* MIS rays that meet their light: is a primitive before the light's hit */
-    CGPU_KERNEL_CLASSES = 8
+    CGPU_KERNEL_TIES = 8,       /* closest-hit rays the persistent pass left to the tie rule (cgpu_set_tie_order) */
+    CGPU_KERNEL_CLASSES = 9
 };
 typedef struct cgpu_kernel_times {
     double ms[CGPU_KERNEL_CLASSES];

@@ -36,7 +36,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.cgpu_abi_version() == 4
+    assert lib.cgpu_abi_version() == 5
     for code, name in abi.STATUS_NAMES.items():
         assert lib.cgpu_status_string(code).decode() == name
 

@@ -62,6 +62,29 @@ def test_closest_hits_match_reference(name, gpu_ctx, uploaded):
     print("%s: %d rays, %.4f %% excluded (edge)" % (name, len(rays), 100 * frac))
 
 
+def test_index_tie_order_keeps_the_lower_primitive(gpu_ctx):
+    """CGPU_TIE_ORDER_INDEX skips the reference's tie order: on the coplanar
+    scene's exact ties the lower primitive index, everywhere else the
+    reference's hits; unknown orders are rejected."""
+    spec = specs()["coplanar"]
+    flat = abi.flatten(spec)
+    v = vectors("coplanar")
+    with pytest.raises(CgpuError):
+        gpu_ctx.set_tie_order(7)
+    gpu_ctx.set_tie_order(abi.CGPU_TIE_ORDER_INDEX)
+    try:
+        sid = gpu_ctx.upload(flat)
+    finally:
+        gpu_ctx.set_tie_order(abi.CGPU_TIE_ORDER_REFERENCE)
+    prim, t, _, _ = gpu_ctx.trace_closest(sid, v["trace_rays"])
+    gpu_ctx.release(sid)
+    ref_p, ref_t = v["trace_bvh_prim"], v["trace_bvh_t"]
+    diff = prim != ref_p
+    assert 0 < diff.sum() < 0.2 * len(prim)
+    assert np.all((prim[diff] >= 0) & (prim[diff] < ref_p[diff]))
+    assert np.array_equal(t[diff], ref_t[diff])
+
+
 @pytest.mark.parametrize("name", NAMES)
 def test_any_hit_matches_reference(name, gpu_ctx, uploaded):
     v = vectors(name)
@@ -243,7 +266,7 @@ def test_rough_dielectric_paths_match_oracle(gpu_ctx):
     _, port = oracle.PortScene(flat).render(seed=3, first=0, count=4, threads=8, want_paths=True,
                                             scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= path_close_fraction(name), close.mean()
+    assert close.mean() >= 0.99, close.mean()
     gpu_ctx.release(sid)
 
 
@@ -285,7 +308,7 @@ def test_environment_paths_match_oracle(gpu_ctx):
     assert np.array_equal(gpu, mk)
     _, port = oracle.PortScene(flat).render(seed=9, first=0, count=4, threads=8, want_paths=True, scene_index=sid)
     close = np.all(np.abs(gpu - port) <= 1e-3 * np.abs(port) + 1e-5, axis=-1)
-    assert close.mean() >= path_close_fraction(name), close.mean()
+    assert close.mean() >= 0.99, close.mean()
     gpu_ctx.release(sid)
 
 
