@@ -324,7 +324,8 @@ def run_gpu(args, rank, world, local):
                  "nodes_per_closest_ray": st.node_visits / max(1, st.closest_rays),
                  "triangles_per_closest_ray": st.triangle_tests / max(1, st.closest_rays),
                  "nodes_per_any_ray": st.any_node_visits / max(1, st.any_rays),
-                 "triangles_per_any_ray": st.any_triangle_tests / max(1, st.any_rays)},
+                 "triangles_per_any_ray": st.any_triangle_tests / max(1, st.any_rays),
+                 "tie_rule_fraction_of_closest": st.tie_rays / max(1, st.closest_rays)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                      "kernel": "k_wf_extend_pww (closest-hit traversal)",

@@ -150,7 +150,8 @@ class cgpu_render_stats(C.Structure):
     _fields_ = [("paths", C.c_uint64), ("closest_rays", C.c_uint64), ("any_rays", C.c_uint64),
                 ("node_visits", C.c_uint64), ("triangle_tests", C.c_uint64),
                 ("any_node_visits", C.c_uint64), ("any_triangle_tests", C.c_uint64),
-                ("h2d_bytes", C.c_uint64), ("kernel_launches", C.c_uint32), ("batches", C.c_uint32)]
+                ("h2d_bytes", C.c_uint64), ("kernel_launches", C.c_uint32), ("batches", C.c_uint32),
+                ("tie_rays", C.c_uint64)]
 
 
 class cgpu_crsd_settings(C.Structure):

@@ -55,7 +55,8 @@ CG_D int material_of_slot(const SceneD& S, int slot) {
 }
 
 // Counting replay: [0] closest rays, [1] any-hit rays, [2] / [3] 4-wide
-// nodes / triangles fetched by closest-hit rays, [4] / [5] by any-hit rays.
+// nodes / triangles fetched by closest-hit rays, [4] / [5] by any-hit rays,
+// [6] closest-hit rays traced again by the tie rule (k_wf_ties).
 template <bool COUNT>
 CG_D void count_flush(unsigned long long* counters, const TraceCounters& cc, const TraceCounters& ca, uint32_t closest,
                       uint32_t any) {

@@ -533,7 +533,9 @@ __global__ void k_wf_ties(RenderArgs a, int b) {
     const int n = cnt[12];
     int* const* qmat = w.q_mat;
     TraceCounters tc{0, 0};
+    uint32_t nties = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        if (COUNT) ++nties;
         const int e = w.q_tie[i];
         const bool cont = e >= 0;
         const int p = e & 0x7FFFFFFF;
@@ -549,6 +551,7 @@ __global__ void k_wf_ties(RenderArgs a, int b) {
         grouped_push(qmat, cnt + 3, key, p);
     }
     count_flush<COUNT>(a.counters, tc, TraceCounters{0, 0}, 0, 0);
+    if (COUNT && nties) atomicAdd(a.counters + 6, (unsigned long long)nties);
 }
 
 // Persistent any-hit pass: k_wf_extend_pww's while-while traversal with
@@ -1421,6 +1424,7 @@ cgpu_status cg_render_batches(cgpu_ctx* ctx, const cgpu_render_params* p) {
         ctx->stats.triangle_tests = c[3];
         ctx->stats.any_node_visits = c[4];
         ctx->stats.any_triangle_tests = c[5];
+        ctx->stats.tie_rays = c[6];
     }
     return cg_cuda(ctx, cudaGetLastError(), "render");
 }

@@ -374,6 +374,7 @@ typedef struct cgpu_render_stats {
     uint64_t h2d_bytes;           /* host->device bytes the last cgpu_render copied (batch tables) */
     uint32_t kernel_launches;     /* kernels this library launched in the last cgpu_render */
     uint32_t batches;             /* path batches the last cgpu_render ran */
+    uint64_t tie_rays;            /* counting renders: closest-hit rays the persistent pass left to the tie rule */
 } cgpu_render_stats;
 cgpu_status cgpu_render_stats_get(cgpu_ctx* ctx, cgpu_render_stats* out_stats);
 /* Count rays, node fetches and triangle tests in every following render (slower). */
